@@ -1,0 +1,318 @@
+"""Band-detection throughput benchmark (one JSON line on stdout).
+
+Workload (the batched configuration): 1,000,000 synthetic 80x80 uint8 EBSD patterns, Radon
+nTheta=180 x nRho=120, LoG sigma 1.0 px, rhoMaskFrac 0.1, nBands=9, circular detector mask;
+10% of the patterns carry no bands (background + Poisson noise only).  A step is one
+find_bands pass over the whole batch.  The patterns are a pool of seeded distinct patterns
+(pattern i uses seed BASE+i) tiled to the batch size; the 6.4 GB input is larger than L2, so
+no L2 flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--method fused16|fused|plain|plain64]
+  python bench.py --impl reference     # the CPU restatement of the reference on the host cores
+
+Under torchrun (N > 1) every rank runs its own replica of the batch (weak scaling, no
+collective in the data path); value = patterns processed by all ranks / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "band-detect patterns/sec on 1 GB300: batched FP16 vs plain FP32, at <=1e-3 px error"
+H = W = 80
+NRHO, NTHETA, NBANDS = 120, 180, 9
+BYTES_PER_PATTERN = H * W * 1 + 41 * NBANDS   # algorithmic bytes: pattern in, band fields out
+SEED = 1_000_000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default=None)
+    ap.add_argument("--patterns", type=int, default=1_000_000)
+    ap.add_argument("--pool", type=int, default=2048)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=0, help="patterns in the timed CPU sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_plan():
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300 import synthetic as syn
+    bd = pg.BandDetect(nTheta=NTHETA, nRho=NRHO, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=NBANDS)
+    bd.band_detect_setup(patDim=(H, W), patternmask=syn.circular_mask(H, W))
+    return bd
+
+
+def make_pool(n):
+    from pyebsdindex_gb300 import synthetic as syn
+    out = []
+    for s in range(0, n, 256):
+        out.append(syn.make_patterns(min(256, n - s), H, W, seed=SEED, start=s, noise_frac=0.1)[0])
+    return np.concatenate(out)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                r = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                    "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if r.returncode == 0 and r.stdout.strip():
+                    self.samples.append([x.strip() for x in r.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(pool, sample, impl_kind):
+    """Time the CPU restatement of the reference find_bands on a bounded sample."""
+    from oracle import cport
+    try:
+        cport.build()
+        fn = cport.find_bands
+        kind, cores = "port", os.cpu_count()
+    except Exception:
+        fn, kind, cores = None, None, 1
+    plan = None
+    from oracle import band_oracle as bo
+    from pyebsdindex_gb300 import synthetic as syn
+    plan = bo.Plan((H, W), NTHETA, NRHO, 1.0, 1.0, 0.1, NBANDS, mask=syn.circular_mask(H, W))
+    pats = pool[:sample]
+    if fn is not None:
+        fn(plan, pats[: min(8, len(pats))], threads=cores)  # warm-up
+        t0 = time.perf_counter()
+        fn(plan, pats, threads=cores)
+        dt = time.perf_counter() - t0
+        desc = f"C/OpenMP restatement of find_bands, {len(pats)} patterns of the bench pool, {cores} threads"
+    else:
+        bo.find_bands(plan, pats[:4])
+        t0 = time.perf_counter()
+        bo.find_bands(plan, pats)
+        dt = time.perf_counter() - t0
+        desc = f"numpy restatement of find_bands, {len(pats)} patterns, 1 process"
+    return {"value": len(pats) / dt, "unit": "patterns/s", "cores": cores, "kind": "port", "sample": desc}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sample = args.cpu_sample or 4096
+    pool = make_pool(min(args.pool, sample))
+    pool = np.concatenate([pool] * ((sample + len(pool) - 1) // len(pool)))[:sample]
+    vals = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        b = cpu_baseline(pool, sample, "port")
+        if i >= args.warmup:
+            vals.append(b["value"])
+        base = b
+    v = float(np.median(vals)) if vals else base["value"]
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "patterns/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sample / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "find_bands, 80x80 uint8, nTheta 180, nRho 120, nBands 9, host CPU sample",
+                   "patterns_per_step": sample},
+        "cpu_baseline": dict(base, value=v),
+        "e2e": {"value": v, "unit": "patterns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    bd = make_plan()
+    plan = bd._device_plan(local)
+    method = args.method
+    if method is None:
+        method = "fused16" if plan.supported("fused16") else "plain"
+    if method.startswith("fused") and not plan.supported(method):
+        method = "plain"
+    from pyebsdindex_gb300 import _lib
+
+    N = args.patterns
+    pool = make_pool(args.pool)
+    pool_d = torch.from_numpy(pool).to(dev)
+    reps = (N + len(pool) - 1) // len(pool)
+    pats_d = pool_d.repeat(reps, 1, 1)[:N].contiguous()
+    del pool_d
+    nB = NBANDS
+    outs = {
+        "max": torch.empty((N, nB), dtype=torch.float32, device=dev),
+        "normmax": torch.empty((N, nB), dtype=torch.float32, device=dev),
+        "maxloc": torch.empty((N, nB, 2), dtype=torch.float32, device=dev),
+        "avemax": torch.empty((N, nB), dtype=torch.float32, device=dev),
+        "aveloc": torch.empty((N, nB, 2), dtype=torch.float32, device=dev),
+        "width": torch.empty((N, nB), dtype=torch.float32, device=dev),
+        "theta": torch.empty((N, nB), dtype=torch.float32, device=dev),
+        "rho": torch.empty((N, nB), dtype=torch.float32, device=dev),
+        "valid": torch.empty((N, nB), dtype=torch.int8, device=dev),
+    }
+    ptrs = {k: v.data_ptr() for k, v in outs.items()}
+    stream = torch.cuda.current_stream(dev)
+    plan.reserve(method, N if method.startswith("fused") else 16384)
+
+    def step():
+        plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, N, ptrs, method, stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    launches_per_step = plan.last_launches()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step_ms = []
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        step_ms.append((a, b))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total_ms = ev0.elapsed_time(ev1)
+    per_step = [a.elapsed_time(b) for a, b in step_ms]
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * N * args.steps / (total_ms / 1000.0)
+
+    # roofline: the dominant kernel (one fused launch per chunk, or the per-stage sequence)
+    hbm = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+        hbm, peak_src = float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        hbm, peak_src = 6800.0, "fallback"
+    launch_ms = float(np.mean(per_step)) / max(launches_per_step, 1) if method.startswith("fused") else float(np.mean(per_step))
+    units_per_launch = N / max(launches_per_step, 1) if method.startswith("fused") else N
+    achieved = BYTES_PER_PATTERN * units_per_launch / (launch_ms / 1000.0) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "peak_source": peak_src,
+            "kernel": "ebsd fused kernel" if method.startswith("fused") else "per-stage sequence (7 kernels/chunk)"}
+
+    # end to end through the C ABI with pinned host buffers (H2D + D2H inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty((N, H, W), dtype=torch.uint8, pin_memory=True)
+        host.copy_(pats_d.cpu())
+        hout = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in outs.items()}
+        hb = _lib.Bands(**{k: _lib.C.c_void_p(v.data_ptr()) for k, v in hout.items()})
+        lib = _lib.load()
+
+        def e2e_step():
+            _lib.check(lib.ebsd_find_bands_host(plan.handle, _lib.method_id(method), _lib.EBSD_U8,
+                                                _lib.C.c_void_p(host.data_ptr()), N, _lib.C.byref(hb), 0))
+        e2e_step()
+        t0 = time.perf_counter()
+        e2e_steps = max(1, min(args.steps, 3))
+        for _ in range(e2e_steps):
+            e2e_step()
+        dt = time.perf_counter() - t0
+        e2e = {"value": N * e2e_steps / dt * world, "unit": "patterns/s", "h2d_bytes_per_step": N * H * W,
+               "d2h_bytes_per_step": N * nB * 41}
+        del host, hout
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            cpu = cpu_baseline(pool, args.cpu_sample or min(len(pool), 2048), "port")
+        except Exception as e:  # reported, never silently replaced
+            cpu = {"value": None, "error": str(e)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "patterns/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8 in, f16 Radon storage, f32 accumulate" if method == "fused16" else
+                     ("u8 in, f32" if method in ("plain", "fused") else "u8 in, f64"),
+            "data": "synthetic",
+            "config": {"workload": "find_bands on 1,000,000 80x80 uint8 patterns, nTheta 180, nRho 120, "
+                                   "nBands 9, LoG sigma 1, rhoMaskFrac 0.1, circular mask, 10% noise-only",
+                       "method": method, "patterns_per_step": N, "distinct_patterns": len(pool),
+                       "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

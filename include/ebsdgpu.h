@@ -1,0 +1,136 @@
+/*
+ * ebsdgpu.h -- C ABI of the GB300 band-detection library (libebsdgpu.so).
+ *
+ * The library replaces the hot path behind PyEBSDIndex's BandDetect.find_bands:
+ *   background subtraction + lookup-table Radon  (radon_fast.py:242-310)
+ *   theta/rho padding + LoG convolution + stats  (band_detect.py:562-637)
+ *   11x11 max-filter peak search + Radon mask    (band_detect.py:639-664, :811-843)
+ *   top-N band labelling + 3x3 sub-pixel fit     (band_detect.py:667-809)
+ *   normmax / theta / rho epilogue               (band_detect.py:457-460, :519-524)
+ * and its OpenCL dispatch (opencl/band_detect_cl.py:51-199).
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success or a negative EBSD_E* code; ebsd_strerror()
+ *     turns a code into text.  Nothing falls back to the CPU.
+ *   - Device pointers are plain CUDA device addresses; streams are cudaStream_t passed as
+ *     void*.  Plans own their device tables; callers own pattern and output buffers.
+ *   - A plan may be used from one host thread at a time.  Calls on one plan with different
+ *     streams are serialised by the plan's internal workspace lock.
+ */
+#ifndef EBSDGPU_H
+#define EBSDGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define EBSD_OK 0
+#define EBSD_E_ARG (-1)        /* bad argument (null pointer, size, shape)              */
+#define EBSD_E_DTYPE (-2)      /* unsupported pattern data type                          */
+#define EBSD_E_NOMEM (-3)      /* device or pinned-host allocation failed                 */
+#define EBSD_E_LAUNCH (-4)     /* a kernel launch or CUDA runtime call failed            */
+#define EBSD_E_UNSUPPORTED (-5)/* plan shape outside what a method supports              */
+#define EBSD_E_DEVICE (-6)     /* no usable CUDA device / wrong device                    */
+#define EBSD_E_TIMEOUT (-7)    /* a bounded device-side wait gave up                      */
+
+/* ---- pattern element types (BandDetect.find_bands accepts uint8, uint16, float32) ---- */
+#define EBSD_U8 0
+#define EBSD_U16 1
+#define EBSD_F32 2
+
+/* ---- methods --------------------------------------------------------------------------
+ * EBSD_PLAIN_F32  per-stage kernels, FP32 intermediates in HBM (the structure of the
+ *                 reference's OpenCL path, opencl/band_detect_cl.py:51-199).
+ * EBSD_PLAIN_F64  the same pipeline in FP64 end to end: the FP64 GPU oracle.
+ * EBSD_FUSED_F32  one persistent fused kernel per chunk, Radon image stored FP32 on chip.
+ * EBSD_FUSED_F16  the fused kernel with the Radon image stored FP16 (FP32 accumulation). */
+#define EBSD_PLAIN_F32 0
+#define EBSD_PLAIN_F64 1
+#define EBSD_FUSED_F32 2
+#define EBSD_FUSED_F16 3
+
+typedef struct ebsd_plan_s* ebsd_plan_t;
+
+/* Everything BandDetect.band_detect_setup (band_detect.py:138-294) derives for one pattern
+ * size.  All pointers are HOST pointers, copied during ebsd_plan_create. */
+typedef struct {
+    int32_t H, W;                 /* pattern rows, columns                                  */
+    int32_t nTheta, nRho;         /* Radon samples (radonPlan.nTheta / .nRho)              */
+    int32_t nBands;               /* bands per pattern, 1..32                              */
+    int32_t pad_rho, pad_theta;   /* BandDetect.padding                                    */
+    int32_t peak_rho, peak_theta; /* BandDetect.peakPad (odd max-filter window sizes)      */
+    int32_t ksz_rho, ksz_theta;   /* LoG kernel shape (BandDetect.kernel[0].shape)         */
+    const float* kernel;          /* [ksz_rho*ksz_theta] LoG taps, row-major                */
+    int32_t lut_len;              /* third extent of radonPlan.indexPlan (max(H, W))       */
+    const int64_t* lut;           /* radonPlan.indexPlan [nRho][nTheta][lut_len], each ray
+                                     sorted ascending; entries >= H*W end the ray           */
+    const uint8_t* rdnmask;       /* BandDetect.rdnmask [nRho][nTheta] (0/1)               */
+    const float* theta;           /* radonPlan.theta [nTheta], degrees                     */
+    const float* rho;             /* radonPlan.rho [nRho]                                  */
+    const double* background;     /* BandDetect.backgroundsub [H][W] or NULL               */
+    int32_t background_f32;       /* 1: background was float32 (subtract in float32)      */
+} ebsd_plan_desc;
+
+/* Structure-of-arrays band output; n patterns x nBands, row-major.  All nine arrays are
+ * required.  Device pointers for ebsd_find_bands, host pointers for ebsd_find_bands_host.
+ * maxloc/aveloc are (rho, theta) pairs in the un-padded Radon frame, as in the record. */
+typedef struct {
+    float* max;      /* 'max'      */
+    float* normmax;  /* 'normmax'  */
+    float* maxloc;   /* 'maxloc'   [..][2] */
+    float* avemax;   /* 'avemax'   */
+    float* aveloc;   /* 'aveloc'   [..][2] */
+    float* width;    /* 'width'    */
+    float* theta;    /* 'theta'    radians */
+    float* rho;      /* 'rho'      */
+    int8_t* valid;   /* 'valid'    */
+} ebsd_bands;
+
+/* Replaces BandDetect.band_detect_setup's products (band_detect.py:138-294) and the
+ * radon_fast.Radon lookup table (radon_fast.py:64-165) on the device.  The LUT is
+ * re-encoded for the GPU (ray-interleaved for the per-stage kernels, ray-major packed for
+ * the fused kernel).  `device` is the CUDA ordinal the plan lives on. */
+int ebsd_plan_create(const ebsd_plan_desc* desc, int device, ebsd_plan_t* out);
+
+/* Frees the plan's device tables and workspaces. */
+int ebsd_plan_destroy(ebsd_plan_t plan);
+
+/* Whether `method` can run this plan (the fused kernels need the plan's on-chip tile to fit
+ * in shared memory).  Returns 1 / 0, or a negative code. */
+int ebsd_method_supported(ebsd_plan_t plan, int method);
+
+/* Reserves the per-plan workspace for chunks of up to max_chunk patterns so that later
+ * calls allocate nothing.  Optional: find_bands reserves on first use. */
+int ebsd_plan_reserve(ebsd_plan_t plan, int method, int64_t max_chunk);
+
+/* BandDetect.find_bands (band_detect.py:411-526) on device-resident patterns:
+ * d_pats [n][H][W] of `dtype`, outputs into device arrays.  Asynchronous on `stream`.
+ * `chunk` <= 0 picks the plan's default chunk size. */
+int ebsd_find_bands(ebsd_plan_t plan, int method, int dtype, const void* d_pats, int64_t n,
+                    const ebsd_bands* d_out, int64_t chunk, void* stream);
+
+/* The same on HOST buffers: copies each chunk in, runs it and copies the bands out, with
+ * two streams so copies overlap compute.  Pinned host memory gives overlapped copies;
+ * pageable memory works but serialises.  Synchronous: returns when the outputs are
+ * written. */
+int ebsd_find_bands_host(ebsd_plan_t plan, int method, int dtype, const void* h_pats,
+                         int64_t n, const ebsd_bands* h_out, int64_t chunk);
+
+/* Number of kernel launches the last ebsd_find_bands / ebsd_find_bands_host call on this
+ * plan issued (for launch accounting by benchmarks). */
+int64_t ebsd_last_launch_count(ebsd_plan_t plan);
+
+/* Text for a status code. */
+const char* ebsd_strerror(int code);
+
+/* Library version string. */
+const char* ebsd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EBSDGPU_H */

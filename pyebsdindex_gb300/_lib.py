@@ -1,0 +1,200 @@
+"""ctypes binding of libebsdgpu.so (the C ABI declared in include/ebsdgpu.h).
+
+The shared library is built in-tree (``pyebsdindex_gb300/libebsdgpu.so``) by
+``pyebsdindex_gb300/_build.py``.  There is no CPU fallback: if the library or a CUDA device is
+missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libebsdgpu.so")
+
+EBSD_U8, EBSD_U16, EBSD_F32 = 0, 1, 2
+EBSD_PLAIN_F32, EBSD_PLAIN_F64, EBSD_FUSED_F32, EBSD_FUSED_F16 = 0, 1, 2, 3
+
+METHODS = {
+    "plain": EBSD_PLAIN_F32, "plain32": EBSD_PLAIN_F32, "plain_f32": EBSD_PLAIN_F32,
+    "plain64": EBSD_PLAIN_F64, "fp64": EBSD_PLAIN_F64, "plain_f64": EBSD_PLAIN_F64,
+    "fused": EBSD_FUSED_F32, "fused32": EBSD_FUSED_F32, "fused_f32": EBSD_FUSED_F32,
+    "fused16": EBSD_FUSED_F16, "fused_f16": EBSD_FUSED_F16,
+}
+
+DTYPES = {np.dtype(np.uint8): EBSD_U8, np.dtype(np.uint16): EBSD_U16, np.dtype(np.float32): EBSD_F32}
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [
+        ("H", C.c_int32), ("W", C.c_int32), ("nTheta", C.c_int32), ("nRho", C.c_int32),
+        ("nBands", C.c_int32), ("pad_rho", C.c_int32), ("pad_theta", C.c_int32),
+        ("peak_rho", C.c_int32), ("peak_theta", C.c_int32), ("ksz_rho", C.c_int32),
+        ("ksz_theta", C.c_int32), ("kernel", C.POINTER(C.c_float)), ("lut_len", C.c_int32),
+        ("lut", C.POINTER(C.c_int64)), ("rdnmask", C.POINTER(C.c_uint8)),
+        ("theta", C.POINTER(C.c_float)), ("rho", C.POINTER(C.c_float)),
+        ("background", C.POINTER(C.c_double)), ("background_f32", C.c_int32),
+    ]
+
+
+class Bands(C.Structure):
+    _fields_ = [
+        ("max", C.c_void_p), ("normmax", C.c_void_p), ("maxloc", C.c_void_p), ("avemax", C.c_void_p),
+        ("aveloc", C.c_void_p), ("width", C.c_void_p), ("theta", C.c_void_p), ("rho", C.c_void_p),
+        ("valid", C.c_void_p),
+    ]
+
+
+BAND_FIELDS = ("max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid")
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"libebsdgpu.so not found at {LIB_PATH}; build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'` or "
+                "`python pyebsdindex_gb300/_build.py`")
+        lib = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        lib.ebsd_plan_create.argtypes = [C.POINTER(PlanDesc), C.c_int, C.POINTER(P)]
+        lib.ebsd_plan_create.restype = C.c_int
+        lib.ebsd_plan_destroy.argtypes = [P]
+        lib.ebsd_plan_destroy.restype = C.c_int
+        lib.ebsd_method_supported.argtypes = [P, C.c_int]
+        lib.ebsd_method_supported.restype = C.c_int
+        lib.ebsd_plan_reserve.argtypes = [P, C.c_int, C.c_int64]
+        lib.ebsd_plan_reserve.restype = C.c_int
+        lib.ebsd_find_bands.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, C.POINTER(Bands), C.c_int64, P]
+        lib.ebsd_find_bands.restype = C.c_int
+        lib.ebsd_find_bands_host.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, C.POINTER(Bands), C.c_int64]
+        lib.ebsd_find_bands_host.restype = C.c_int
+        lib.ebsd_last_launch_count.argtypes = [P]
+        lib.ebsd_last_launch_count.restype = C.c_int64
+        lib.ebsd_strerror.argtypes = [C.c_int]
+        lib.ebsd_strerror.restype = C.c_char_p
+        lib.ebsd_version.argtypes = []
+        lib.ebsd_version.restype = C.c_char_p
+        _lib = lib
+        return lib
+
+
+def check(code: int, what: str = "ebsdgpu"):
+    if code != 0:
+        msg = load().ebsd_strerror(code).decode()
+        raise RuntimeError(f"{what} failed: {msg} (code {code})")
+    return code
+
+
+def method_id(method) -> int:
+    if isinstance(method, int):
+        return method
+    try:
+        return METHODS[str(method).lower()]
+    except KeyError:
+        raise ValueError(f"unknown method {method!r}; choose from {sorted(METHODS)}") from None
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class DevicePlan:
+    """Owns one ``ebsd_plan_t`` built from a band-detect plan's host arrays."""
+
+    def __init__(self, *, H, W, nTheta, nRho, nBands, padding, peakPad, kernel, lut, rdnmask, theta,
+                 rho, background=None, device=0):
+        lib = load()
+        self._lib = lib
+        kernel = np.ascontiguousarray(kernel, dtype=np.float32)
+        lut = np.ascontiguousarray(lut, dtype=np.int64)
+        rdnmask = np.ascontiguousarray(rdnmask, dtype=np.uint8)
+        theta = np.ascontiguousarray(theta, dtype=np.float32)
+        rho = np.ascontiguousarray(rho, dtype=np.float32)
+        bg_f32 = 0
+        if background is not None:
+            bg_f32 = 1 if np.asarray(background).dtype == np.float32 else 0
+            background = np.ascontiguousarray(np.broadcast_to(np.asarray(background, dtype=np.float64),
+                                                              (H, W)))
+        d = PlanDesc()
+        d.H, d.W, d.nTheta, d.nRho, d.nBands = int(H), int(W), int(nTheta), int(nRho), int(nBands)
+        d.pad_rho, d.pad_theta = int(padding[0]), int(padding[1])
+        d.peak_rho, d.peak_theta = int(peakPad[0]), int(peakPad[1])
+        d.ksz_rho, d.ksz_theta = int(kernel.shape[-2]), int(kernel.shape[-1])
+        d.kernel = _fptr(kernel)
+        d.lut_len = int(lut.shape[-1])
+        d.lut = lut.ctypes.data_as(C.POINTER(C.c_int64))
+        d.rdnmask = rdnmask.ctypes.data_as(C.POINTER(C.c_uint8))
+        d.theta = _fptr(theta)
+        d.rho = _fptr(rho)
+        d.background = background.ctypes.data_as(C.POINTER(C.c_double)) if background is not None else None
+        d.background_f32 = bg_f32
+        h = C.c_void_p()
+        check(lib.ebsd_plan_create(C.byref(d), int(device), C.byref(h)), "ebsd_plan_create")
+        self.handle = h
+        self.H, self.W, self.nBands = int(H), int(W), int(nBands)
+        self.device = int(device)
+
+    def supported(self, method) -> bool:
+        return self._lib.ebsd_method_supported(self.handle, method_id(method)) == 1
+
+    def reserve(self, method, max_chunk):
+        check(self._lib.ebsd_plan_reserve(self.handle, method_id(method), int(max_chunk)), "ebsd_plan_reserve")
+
+    def last_launches(self) -> int:
+        return int(self._lib.ebsd_last_launch_count(self.handle))
+
+    def find_bands_host(self, pats: np.ndarray, method, chunk=0):
+        """Host patterns [n,H,W] -> dict of host SoA band arrays (C ABI with host buffers)."""
+        dt = DTYPES.get(pats.dtype)
+        if dt is None:
+            raise TypeError(f"unsupported pattern dtype {pats.dtype}")
+        pats = np.ascontiguousarray(pats)
+        n = pats.shape[0]
+        out = alloc_host_bands(n, self.nBands)
+        b = bands_struct(out)
+        check(self._lib.ebsd_find_bands_host(self.handle, method_id(method), dt, C.c_void_p(pats.ctypes.data),
+                                             n, C.byref(b), int(chunk)), "ebsd_find_bands_host")
+        return out
+
+    def find_bands_device(self, pats_ptr: int, dtype: int, n: int, out_ptrs: dict, method, chunk=0, stream=0):
+        """Device patterns -> device SoA outputs (raw pointers), asynchronous on `stream`."""
+        b = Bands(**{k: C.c_void_p(int(out_ptrs[k])) for k in BAND_FIELDS})
+        check(self._lib.ebsd_find_bands(self.handle, method_id(method), int(dtype), C.c_void_p(int(pats_ptr)),
+                                        int(n), C.byref(b), int(chunk), C.c_void_p(int(stream))),
+              "ebsd_find_bands")
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self._lib.ebsd_plan_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def alloc_host_bands(n, nB):
+    return {
+        "max": np.empty((n, nB), np.float32), "normmax": np.empty((n, nB), np.float32),
+        "maxloc": np.empty((n, nB, 2), np.float32), "avemax": np.empty((n, nB), np.float32),
+        "aveloc": np.empty((n, nB, 2), np.float32), "width": np.empty((n, nB), np.float32),
+        "theta": np.empty((n, nB), np.float32), "rho": np.empty((n, nB), np.float32),
+        "valid": np.empty((n, nB), np.int8),
+    }
+
+
+def bands_struct(arrs):
+    return Bands(**{k: C.c_void_p(arrs[k].ctypes.data) for k in BAND_FIELDS})

@@ -1,0 +1,364 @@
+"""GPU band detection behind the reference ``BandDetect`` interface.
+
+``BandDetect`` here has the constructor, attributes and methods of the reference's
+``band_detect.BandDetect`` (band_detect.py:67-933) that ``EBSDIndexer``, ``pcopt`` and user code
+touch -- ``band_detect_setup``, ``collect_background``, ``backsub_fit``, ``find_bands``,
+``radonPlan``, ``rdnmask``, ``kernel``, ``peakPad``, ``padding``, ``dataType`` ... -- but
+``find_bands`` runs on the GPU through libebsdgpu.so.  There is no CPU fallback: without the
+library or a CUDA device, ``find_bands`` raises.
+
+``GPUFindBands`` is the find_bands implementation on its own, usable as a mixin over any class
+that carries the reference's plan attributes; ``pyebsdindex_gb300.plugin`` uses it to subclass
+the reference's own ``BandDetect`` when PyEBSDIndex is installed.
+"""
+from __future__ import annotations
+
+import hashlib
+from timeit import default_timer as timer
+
+import numpy as np
+import scipy.ndimage as ndi
+import scipy.optimize as opt
+
+from . import _lib
+from .radon_fast import Radon
+
+RADEG = 180.0 / np.pi
+
+__all__ = ["BandDetect", "GPUFindBands", "getopenclparam", "record_dtype"]
+
+
+def record_dtype(nPhases=10):
+    """The band record (band_detect.py:110-115)."""
+    return np.dtype([('id', np.int32), ('max', np.float32), ('normmax', np.float32),
+                     ('maxloc', np.float32, (2)), ('avemax', np.float32), ('aveloc', np.float32, (2)),
+                     ('pqmax', np.float32), ('width', np.float32), ('theta', np.float32),
+                     ('rho', np.float32), ('valid', np.int8),
+                     ('band_match_index', np.int64, (nPhases,)),
+                     ('bandfit', np.float64, (nPhases,))])
+
+
+def getopenclparam(**kwargs):
+    """Compatibility stub for callers of band_detect.getopenclparam (band_detect.py:932-933)."""
+    return None
+
+
+def _digest(*arrays):
+    h = hashlib.sha1()
+    for a in arrays:
+        if a is None:
+            h.update(b"none")
+        else:
+            a = np.ascontiguousarray(a)
+            h.update(str(a.dtype).encode() + str(a.shape).encode())
+            h.update(a.tobytes())
+    return h.hexdigest()
+
+
+class GPUFindBands:
+    """``find_bands`` on the GPU, reading the plan attributes the reference defines."""
+
+    default_method = "fused"
+    gpu_id = 0
+
+    def _device_plan(self, gpu_id=None):
+        dev = self.gpu_id if gpu_id is None else int(gpu_id)
+        rp = self.radonPlan
+        bg = self.backgroundsub
+        key = (dev, tuple(np.asarray(self.patDim).tolist()), int(rp.nTheta), int(rp.nRho), int(self.nBands),
+               tuple(np.asarray(self.padding).tolist()), tuple(np.asarray(self.peakPad).tolist()),
+               _digest(rp.indexPlan, self.kernel, self.rdnmask, rp.theta, rp.rho, bg))
+        cache = getattr(self, "_gpu_plan_cache", None)
+        if cache is not None and cache[0] == key:
+            return cache[1]
+        bgarr = None
+        if bg is not None:
+            bgarr = np.asarray(bg)
+            if bgarr.dtype != np.float32:
+                bgarr = bgarr.astype(np.float64)
+        plan = _lib.DevicePlan(
+            H=int(rp.imDim[0]), W=int(rp.imDim[1]), nTheta=int(rp.nTheta), nRho=int(rp.nRho),
+            nBands=int(self.nBands), padding=np.asarray(self.padding), peakPad=np.asarray(self.peakPad),
+            kernel=np.asarray(self.kernel, dtype=np.float32).reshape(np.asarray(self.kernel).shape[-2:]),
+            lut=rp.indexPlan, rdnmask=np.asarray(self.rdnmask).astype(np.uint8), theta=rp.theta,
+            rho=rp.rho, background=bgarr, device=dev)
+        self._gpu_plan_cache = (key, plan)
+        return plan
+
+    def _pick_method(self, plan, method):
+        m = self.default_method if method is None else method
+        if m in ("fused", "fused32", "fused16") and not plan.supported(m):
+            m = "plain"
+        return m
+
+    def find_bands(self, patternsIn, verbose=0, chunksize=528, clparams=None, gpu_id=None, useCPU=None,
+                   method=None, **kwargs):
+        """BandDetect.find_bands (band_detect.py:411-526) on the GPU.
+
+        patternsIn: [n, H, W] or [H, W] array (numpy, or a torch tensor on the plan's device) of
+        uint8, uint16 or float32 (other numeric types are converted to float32 first).
+        ``chunksize`` is the number of patterns per device chunk for the per-stage method (the
+        fused method streams at its own chunk size); ``clparams``/``useCPU`` are accepted for
+        interface compatibility and ignored.  ``method``: "fused" (default), "fused16",
+        "plain" or "plain64".  Returns the (nPats, nBands) record array of ``self.dataType``.
+        """
+        tic0 = timer()
+        is_torch = type(patternsIn).__module__.startswith("torch")
+        pats = patternsIn
+        if pats.ndim == 2:
+            pats = pats[None]
+        nP = int(pats.shape[0])
+        if self.patDim is None or tuple(np.asarray(self.patDim)[-2:]) != tuple(pats.shape[-2:]):
+            self.band_detect_setup(patDim=pats.shape[-2:])
+        plan = self._device_plan(gpu_id)
+        m = self._pick_method(plan, method)
+        chunk = int(chunksize) if (chunksize is not None and chunksize > 0) else 0
+        if m.startswith("fused"):
+            chunk = 0
+        if is_torch:
+            import torch
+            t = pats
+            u16 = getattr(torch, "uint16", None)
+            if t.dtype == torch.uint8:
+                dt = _lib.EBSD_U8
+            elif u16 is not None and t.dtype == u16:
+                dt = _lib.EBSD_U16
+            else:
+                t = t.to(torch.float32)
+                dt = _lib.EBSD_F32
+            t = t.contiguous()
+            nB = int(self.nBands)
+            dev_out = {
+                "max": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
+                "normmax": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
+                "maxloc": torch.empty((nP, nB, 2), dtype=torch.float32, device=t.device),
+                "avemax": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
+                "aveloc": torch.empty((nP, nB, 2), dtype=torch.float32, device=t.device),
+                "width": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
+                "theta": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
+                "rho": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
+                "valid": torch.empty((nP, nB), dtype=torch.int8, device=t.device),
+            }
+            stream = torch.cuda.current_stream(t.device).cuda_stream
+            plan.find_bands_device(t.data_ptr(), dt, nP, {k: v.data_ptr() for k, v in dev_out.items()}, m,
+                                   chunk=chunk, stream=stream)
+            soa = {k: v.cpu().numpy() for k, v in dev_out.items()}
+        else:
+            arr = np.asarray(pats)
+            if arr.dtype not in (np.uint8, np.uint16, np.float32):
+                arr = arr.astype(np.float32)
+            soa = plan.find_bands_host(arr, m, chunk=chunk)
+        bandData = self._records(soa, nP)
+        if verbose > 0:
+            print('Band Find Time (GPU, %s):' % m, timer() - tic0)
+        return bandData
+
+    def _records(self, soa, nP):
+        out = np.zeros((nP, int(self.nBands)), dtype=self.dataType)
+        for f in _lib.BAND_FIELDS:
+            out[f] = soa[f]
+        return out
+
+
+class BandDetect(GPUFindBands):
+    """Band-detection plan with the reference BandDetect's interface (band_detect.py:67-136)."""
+
+    def __init__(self, patterns=None, patDim=None, nTheta=180, nRho=90, tSigma=None, rSigma=None,
+                 rhoMaskFrac=0.1, nBands=9, nPhases=10, **kwargs):
+        self.patDim = None
+        self.nTheta = nTheta
+        self.nRho = nRho
+        self.dTheta = None
+        self.dRho = None
+        self.rhoMax = None
+        self.radonPlan = Radon()
+        self.rdnNorm = None
+        self.tSigma = tSigma
+        self.rSigma = rSigma
+        self.kernel = None
+        self.peakPad = np.array([11, 11])
+        self.padding = np.array([11, 11])
+        self.rhoMaskFrac = rhoMaskFrac
+        self.rhomask1thresh = None
+        self.rhomask1 = None
+        self.nBands = nBands
+        self.nPhases = 10 if nPhases is None else nPhases
+        self.EDAXIQ = False
+        self.backgroundsub = None
+        self.useCPU = False
+        self.gpu_id = int(kwargs.get("gpu_id", 0) or 0)
+        if "method" in kwargs and kwargs["method"] is not None:
+            self.default_method = kwargs["method"]
+        self.dataType = record_dtype(self.nPhases)
+        if patterns is not None or patDim is not None:
+            self.patDim = np.asarray(patterns.shape[-2:] if patterns is not None else patDim)
+            if 'patternmask' in kwargs:
+                self.radonPlan.mask = kwargs.get('patternmask')
+            if 'patternmaskindex' in kwargs:
+                self.radonPlan.maskindex = kwargs.get('patternmaskindex')
+            self.band_detect_setup(patterns, self.patDim, self.nTheta, self.nRho, self.tSigma, self.rSigma,
+                                   self.rhoMaskFrac, self.nBands, patternmask=self.radonPlan.mask,
+                                   patternmaskindex=self.radonPlan.maskindex)
+
+    def band_detect_setup(self, patterns=None, patDim=None, nTheta=None, nRho=None, tSigma=None, rSigma=None,
+                          rhoMaskFrac=None, nBands=None, patternmask=None, patternmaskindex=None, **kwargs):
+        """Plan setup (band_detect.py:138-294): rhoMax/dRho, Radon LUT, Radon-space mask,
+        LoG kernel and peak/padding windows."""
+        newdim = None
+        redo_radon = False
+        redo_masks = False
+        if patterns is None and patDim is not None:
+            newdim = np.asarray(patDim, dtype=np.int64)
+        if patterns is not None:
+            newdim = np.asarray(np.shape(patterns)[-2:])
+        if newdim is not None:
+            if self.patDim is None or np.sum(np.abs(np.asarray(self.patDim)[-2:] - newdim[-2:])) != 0:
+                redo_radon = True
+                self.patDim = newdim
+        if nTheta is not None:
+            self.nTheta = nTheta
+            redo_radon = redo_masks = True
+        if self.nTheta is not None:
+            self.dTheta = 180.0 / self.nTheta
+        if nRho is not None:
+            self.nRho = nRho
+            redo_radon = redo_masks = True
+        if self.dRho is None:
+            redo_radon = True
+        if patternmask is not None:
+            self.radonPlan.mask = patternmask
+            redo_radon = True
+        if patternmaskindex is not None:
+            self.radonPlan.maskindex = patternmaskindex
+            redo_radon = True
+
+        if redo_radon:
+            dim = np.asarray(self.patDim)
+            if 0 < self.rhoMaskFrac < 1:
+                self.rhoMax = 0.5 * np.float32(dim.min())
+            else:
+                self.rhoMax = 0.5 * np.float32(np.sqrt(np.float32(dim[-2]) ** 2 + np.float32(dim[-1]) ** 2))
+            self.rhomask1thresh = np.float32(dim.min()) * 0.1
+            self.dRho = self.rhoMax / np.float32(self.nRho)
+            self.radonPlan.radon_plan_setup(imageDim=dim, nTheta=self.nTheta, nRho=self.nRho, rhoMax=self.rhoMax,
+                                            mask=patternmask, maskindex=patternmaskindex)
+            # Radon of the mask image without normalisation = in-mask pixel count per ray
+            # (band_detect.py:203-215); its positive cells are the searchable Radon cells.
+            cnt = self.radonPlan.ray_counts()
+            self.rhomask1 = (cnt >= self.rhomask1thresh).astype(np.ubyte)
+            rmask = cnt > 0
+            if self.rhoMaskFrac >= (1 - 1.0e-12):
+                rmask = ndi.binary_erosion(rmask, structure=np.ones((3, 1)), iterations=int(self.rhoMaskFrac))
+            else:
+                limit = rmask.copy()
+                if self.rhoMaskFrac > 0:
+                    edge = max(int(self.nRho * self.rhoMaskFrac), 1)
+                    limit[0:edge, :] = 0
+                    limit[-edge:, :] = 0
+                elif self.rhoMaskFrac < 0:
+                    # rays that touch the circle of radius rhoMax*(1+rhoMaskFrac) (band_detect.py:232-238)
+                    ny, nx = int(dim[-2]), int(dim[-1])
+                    rad = np.sqrt(((np.arange(nx) - nx * 0.5) ** 2).reshape(1, nx)
+                                  + ((np.arange(ny) - ny * 0.5) ** 2).reshape(ny, 1))
+                    inside = np.concatenate(((rad < self.rhoMax * (1.0 + self.rhoMaskFrac)).ravel(), [False, False]))
+                    lut = np.minimum(self.radonPlan.indexPlan, nx * ny)
+                    limit = np.any(inside[lut], axis=-1) & (cnt > 0)
+                rmask = rmask & (limit > 0)
+            self.rdnmask = rmask > 0
+
+        if tSigma is not None:
+            self.tSigma = tSigma
+            redo_masks = True
+        if rSigma is not None:
+            self.rSigma = rSigma
+            redo_masks = True
+        if rhoMaskFrac is not None:
+            self.rhoMaskFrac = rhoMaskFrac
+        if self.rhoMaskFrac is not None:
+            redo_masks = True
+        if self.tSigma is None and self.dTheta is not None:
+            self.tSigma = 1.0 / self.dTheta
+            redo_masks = True
+        if self.rSigma is None and self.dRho is not None:
+            self.rSigma = 0.5 / np.float32(self.dRho)
+            redo_masks = True
+        if redo_masks:
+            # LoG: -d2/drho2 of a Gaussian, smoothed along theta, normalised to max 1
+            ksz = np.array([max(np.int64(4 * self.rSigma), 5), max(np.int64(4 * self.tSigma), 5)])
+            ksz = ksz + ((ksz % 2) == 0)
+            delta = np.zeros(ksz, dtype=np.float32)
+            delta[int(ksz[0] / 2), int(ksz[1] / 2)] = 1
+            k = -1.0 * ndi.gaussian_filter(delta, [self.rSigma, self.tSigma], order=[2, 0])
+            k *= 1.0 / np.max(k)
+            self.kernel = k.reshape((1, ksz[0], ksz[1]))
+            self.peakPad = np.array(np.around([2 * ksz[0], 2 * ksz[1]]), dtype=np.int64)
+            self.peakPad += 1 - np.mod(self.peakPad, 2)
+        self.padding = np.array([max(self.peakPad[0], self.padding[0]), max(self.peakPad[1], self.padding[1])])
+        if nBands is not None:
+            self.nBands = nBands
+
+    def collect_background(self, fileobj=None, patsIn=None, nsample=None, method='randomStride', sigma=None):
+        """Mean pattern -> 2-D Gaussian-on-a-plane fit (band_detect.py:297-348).  File input
+        goes through the reference's pattern-file objects (``read_data``)."""
+        back = None
+        if patsIn is not None:
+            p = np.expand_dims(patsIn, 0) if patsIn.ndim == 2 else patsIn
+            npats = p.shape[0]
+            nsample = npats if nsample is None else nsample
+            if npats <= nsample:
+                back = np.expand_dims(np.mean(p, axis=0), 0)
+            elif method.upper() == 'RANDOMSTRIDE':
+                back = np.mean(p[np.sort(np.random.choice(npats, size=nsample, replace=False)), :, :], axis=0)
+            elif method.upper() == 'EVENSTRIDE':
+                back = np.mean(p[np.arange(0, npats, int(npats / nsample)), :, :], axis=0)
+        if back is None and fileobj is not None:
+            if fileobj.version is None:
+                fileobj.read_header()
+            npats = fileobj.nPatterns
+            nsample = npats if (nsample is None or npats <= nsample) else nsample
+            if method.upper() == 'RANDOMSTRIDE':
+                stride = np.sort(np.random.choice(npats, size=nsample, replace=False))
+            else:
+                stride = np.arange(0, npats, int(npats / nsample), dtype=np.uint64)
+            acc = fileobj.read_data(convertToFloat=True, patStartCount=[stride[0], 1], returnArrayOnly=True)[0]
+            for i in stride[1:]:
+                acc += fileobj.read_data(convertToFloat=True, patStartCount=[i, 1], returnArrayOnly=True)[0]
+            back = acc / float(len(stride))
+        if back is not None:
+            back = self.backsub_fit(np.squeeze(back))
+        self.backgroundsub = back
+
+    def backsub_fit(self, back, mask=None):
+        """Least-squares fit of a 2-D Gaussian on a tilted plane to the mean pattern
+        (band_detect.py:350-408); falls back to the mean itself when the fit fails."""
+        def surface(x, y, a, x0, y0, sx, sy, c, d, e):
+            return a * np.exp(-((x - x0) ** 2) / (2.0 * sx ** 2) - ((y - y0) ** 2) / (2.0 * sy ** 2)) + c + d * x + e * y
+
+        nx, ny = back.shape[-1], back.shape[-2]
+        x = np.broadcast_to(np.arange(nx, dtype=float).reshape(1, nx), (ny, nx)).ravel()
+        y = np.broadcast_to(np.arange(ny, dtype=float), (nx, ny)).T.ravel()
+        if mask is None:
+            cx = (np.arange(nx) - nx * 0.5) ** 2
+            cy = (np.arange(ny) - ny * 0.5) ** 2
+            sel = np.sqrt(np.broadcast_to(cx.reshape(1, nx), (ny, nx)) + np.broadcast_to(cy, (nx, ny)).T) < (ny * 0.49)
+        else:
+            sel = mask
+        wh = np.nonzero(sel.ravel())[0]
+        xy = np.vstack((x[wh], y[wh]))
+        z = ndi.median_filter(np.squeeze(back), 3).ravel()[wh]
+        pk = np.unravel_index(back.argmax(), back.shape)
+        p0 = [(z.max() - z.min()) * 0.1, pk[1], pk[0], nx / 2.355, ny / 2.355, z.min(), 0, 0]
+        try:
+            popt, _ = opt.curve_fit(lambda M, *a: surface(M[0], M[1], *a), xy, z, p0)
+            fit = surface(x, y, *popt).reshape(ny, nx)
+        except RuntimeError:
+            print('Warning: no convergence on background gaussian fit ... using mean of the patterns.')
+            fit = back
+        fit -= np.mean(fit)
+        return fit
+
+    def _circmask(self, im):
+        nx, ny = im.shape[-1], im.shape[-2]
+        cx = (np.arange(nx) - nx * 0.5) ** 2
+        cy = (np.arange(ny) - ny * 0.5) ** 2
+        return np.sqrt(np.broadcast_to(cx.reshape(1, nx), (ny, nx)) + np.broadcast_to(cy, (nx, ny)).T)

@@ -1,0 +1,118 @@
+// Internal declarations shared by the libebsdgpu translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <mutex>
+#include <vector>
+
+#include "../../include/ebsdgpu.h"
+
+namespace ebsd {
+
+constexpr int kMaxBands = 32;
+
+// Fused-kernel geometry chosen at plan creation (see fused.cu).
+struct FusedGeom {
+    int ok = 0;                 // the tile fits on chip
+    int threads = 0;            // threads per block
+    int smem_f32 = 0;           // dynamic shared memory bytes, FP32 Radon storage
+    int smem_f16 = 0;           // dynamic shared memory bytes, FP16 Radon storage
+    // Radon tile = padded rows [row0, row1) x padded columns [col0, col1)
+    int row0 = 0, row1 = 0, col0 = 0, col1 = 0;
+    // conv region (rows/cols of the padded frame whose LoG value is needed)
+    int crow0 = 0, crow1 = 0, ccol0 = 0, ccol1 = 0;
+    int tile_pitch = 0;         // pattern tile row pitch (elements)
+    int nwarp_groups = 0;       // ray groups of 32 rays
+    int max_slots = 0;          // LUT slots per group (max ray length in the group)
+};
+
+struct Workspace {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace ebsd
+
+struct ebsd_plan_s {
+    int device = 0;
+    int H = 0, W = 0, nPx = 0, nTheta = 0, nRho = 0, nRays = 0, nB = 0;
+    int p0 = 0, p1 = 0;     // padding (rho, theta)
+    int pk0 = 0, pk1 = 0;   // peak windows (rho, theta)
+    int k0 = 0, k1 = 0;     // kernel shape (rho, theta)
+    int R = 0, Tp = 0;      // padded Radon extent
+    int maxCount = 0;       // longest ray
+    int bg_mode = 0;        // 0 none, 1 float64 subtraction, 2 float32 subtraction
+
+    // ---- device tables ----
+    uint16_t* d_lut16 = nullptr;   // [maxCount][nRays] entry-major, pixel index
+    int32_t* d_lut32 = nullptr;    // same when H*W >= 65535
+    int32_t* d_count = nullptr;    // [nRays]
+    uint8_t* d_rdnmask = nullptr;  // [nRays]
+    float* d_kernel = nullptr;     // [k0*k1]
+    double* d_kernel64 = nullptr;  // [k0*k1]
+    double* d_theta = nullptr;     // [nTheta] degrees (float32 values widened)
+    double* d_rho = nullptr;       // [nRho]
+    double* d_bg = nullptr;        // [nPx]
+    float* d_bgf = nullptr;        // [nPx]
+
+    // fused-kernel tables
+    ebsd::FusedGeom fg;
+    uint16_t* d_flut = nullptr;    // fused LUT (see fused.cu)
+    int32_t* d_fgroup = nullptr;   // per ray group: {lut offset, nslots, theta column, rho0}
+    float* d_fray = nullptr;       // per ray (tile order): {1/count, background mean} pairs
+    int64_t flut_entries = 0;
+
+    // ---- workspaces ----
+    std::mutex mtx;
+    ebsd::Workspace ws;            // per-stage intermediates
+    ebsd::Workspace stats;         // per-pattern min/mean
+    int64_t ws_chunk = 0;
+    int ws_method = -1;
+
+    // host-pipeline buffers (ebsd_find_bands_host)
+    cudaStream_t hstream[2] = {nullptr, nullptr};
+    cudaEvent_t hevent[2] = {nullptr, nullptr};
+    void* h_in_dev[2] = {nullptr, nullptr};
+    void* h_out_dev[2] = {nullptr, nullptr};
+    size_t h_in_bytes = 0, h_out_bytes = 0;
+
+    int64_t last_launches = 0;
+};
+
+namespace ebsd {
+
+// Error helpers -------------------------------------------------------------------------
+#define EBSD_CUDA_TRY(expr)                                                        \
+    do {                                                                           \
+        cudaError_t _e = (expr);                                                   \
+        if (_e != cudaSuccess) {                                                   \
+            return (_e == cudaErrorMemoryAllocation) ? EBSD_E_NOMEM : EBSD_E_LAUNCH; \
+        }                                                                          \
+    } while (0)
+
+inline int launch_status() {
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) return EBSD_OK;
+    return (e == cudaErrorMemoryAllocation) ? EBSD_E_NOMEM : EBSD_E_LAUNCH;
+}
+
+inline size_t elem_size(int dtype) {
+    return dtype == EBSD_U8 ? 1 : (dtype == EBSD_U16 ? 2 : 4);
+}
+
+// Per-stage (plain) path: plain.cu ------------------------------------------------------
+size_t plain_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);
+int plain_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
+                    const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches);
+
+// Fused path: fused.cu -------------------------------------------------------------------
+int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d);
+void fused_release(ebsd_plan_s* p);
+int fused_supported(const ebsd_plan_s* p, int method);
+size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);
+int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
+                    const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches);
+
+}  // namespace ebsd

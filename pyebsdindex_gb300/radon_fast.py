@@ -1,0 +1,181 @@
+"""Radon plan: the ray lookup table and the band-to-pole conversion.
+
+Mirrors the interface of the reference's ``radon_fast.Radon`` (radon_fast.py:43-397) --
+attribute names, argument meaning and errors -- so that callers that read ``radonPlan.theta``,
+``.rho``, ``.nTheta``, ``.nRho``, ``.imDim``, ``.mask``, ``.maskindex``, ``.indexPlan`` or call
+``.radon2pole`` keep working.  The table is built on the host once per pattern size (as in the
+reference) and re-encoded for the GPU by ``ebsd_plan_create``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+RADEG = 180.0 / np.pi
+DEGRAD = np.pi / 180.0
+
+
+class Radon:
+    def __init__(self, image=None, imageDim=None, nTheta=180, nRho=90, rhoMax=None, mask=None,
+                 maskindex=None, missingval=-1.0):
+        self.nTheta = nTheta
+        self.nRho = nRho
+        self.rhoMax = rhoMax
+        self.mask = mask
+        self.maskindex = maskindex
+        self.missingval = missingval
+        self.indexPlan = None
+        if image is None and imageDim is None:
+            self.theta = None
+            self.rho = None
+            self.imDim = None
+        else:
+            self.imDim = np.asarray(image.shape[-2:] if image is not None else imageDim[-2:])
+            self.radon_plan_setup()
+
+    # radon_fast.py:168-191
+    def _masksetup(self, mask=None, maskindex=None):
+        if mask is not None:
+            self.mask = np.array(mask).astype(int)
+        if maskindex is not None:
+            self.maskindex = np.array(maskindex).astype(np.int64)
+        if self.imDim is not None:
+            nPx = int(self.imDim[0]) * int(self.imDim[1])
+            if self.mask is None:
+                self.mask = np.ones(self.imDim)
+            if self.maskindex is None:
+                self.maskindex = np.arange(nPx, dtype=np.int64).reshape(self.imDim)
+            if self.maskindex.max() >= nPx:
+                raise Exception("max of index array must be less than the total number of pixel in the array")
+
+    def radon_plan_setup(self, image=None, imageDim=None, nTheta=None, nRho=None, rhoMax=None, mask=None,
+                         maskindex=None):
+        """Build ``indexPlan[nRho, nTheta, max(H, W)]`` (radon_fast.py:64-165).
+
+        Each ray at angle theta and offset rho samples one pixel per image column when
+        ``|sin theta| >= sqrt(2)/2`` (``y = round(a*x + b1)``), else one pixel per row
+        (``x = round(a*y + b1)``); rounding is half-to-even in float64.  Samples outside the
+        image, on masked pixels, or remapped to a negative maskindex become the sentinel
+        ``H*W + 1``; each ray's indices are sorted ascending.  theta and rho are float32 with
+        the reference's operation order, and sin/cos are numpy's float32 ufuncs.
+        """
+        if image is None and imageDim is not None:
+            self.imDim = np.asarray(imageDim, dtype=np.int64)
+        elif image is not None:
+            self.imDim = np.asarray(np.shape(image)[-2:])
+        if self.imDim is None:
+            return -1
+        if mask is not None:
+            self.mask = mask
+        if maskindex is not None:
+            self.maskindex = maskindex
+        self._masksetup()
+        if nTheta is not None:
+            self.nTheta = nTheta
+        if nRho is not None:
+            self.nRho = nRho
+        if rhoMax is not None:
+            self.rhoMax = rhoMax
+        if self.rhoMax is None:
+            self.rhoMax = np.linalg.norm(self.imDim) * 0.5
+        H, W = int(self.imDim[0]), int(self.imDim[1])
+        nPx = H * W
+        nT, nR = int(self.nTheta), int(self.nRho)
+
+        step = float(2 * self.rhoMax) / nR
+        self.theta = (np.arange(nT, dtype=np.float32) * np.float32(180.0)) / np.float32(nT)
+        if isinstance(self.rhoMax, np.float32):
+            offs = np.float32(self.rhoMax - np.float32(step))
+        else:
+            offs = np.float64(self.rhoMax) - step
+        self.rho = (np.arange(nR, dtype=np.float32) * np.float32(step) - offs).astype(np.float32)
+
+        ang = (self.theta * np.float32(DEGRAD)).astype(np.float32)
+        s = np.sin(ang)
+        c = np.cos(ang)
+        by_col = np.abs(s) >= (np.sqrt(2.0) * 0.5)
+        slope = (np.where(by_col, -c, -s) / np.where(by_col, s, c)).astype(np.float32)
+        x0 = -1.0 * (W - 1) * 0.5
+        y0 = -1.0 * (H - 1) * 0.5
+        off = x0 * c.astype(np.float64) + y0 * s.astype(np.float64)
+
+        sentinel = nPx + 1
+        L = max(H, W)
+        plan = np.full((nR, nT, L), sentinel, dtype=np.int64)
+        xs = np.arange(W, dtype=np.int64)
+        ys = np.arange(H, dtype=np.int64)
+        rho64 = self.rho.astype(np.float64)
+        for t in range(nT):
+            inter = rho64 - off[t]
+            if by_col[t]:
+                inter = (inter / np.float64(s[t]))[:, None]
+                yy = np.round(np.float64(slope[t]) * xs.astype(np.float64)[None, :] + inter).astype(np.int64)
+                bad = (yy < 0) | (yy >= H)
+                plan[:, t, :W] = np.where(bad, sentinel, np.clip(xs[None, :] + W * yy, 0, sentinel))
+            else:
+                inter = (inter / np.float64(c[t]))[:, None]
+                xx = np.round(np.float64(slope[t]) * ys.astype(np.float64)[None, :] + inter).astype(np.int64)
+                bad = (xx < 0) | (xx >= W)
+                plan[:, t, :H] = np.where(bad, sentinel, np.clip(xx + W * ys[None, :], 0, sentinel))
+        keep = np.concatenate((np.asarray(self.mask).ravel().astype(np.int64), [0, 0]))
+        remap = np.concatenate((np.asarray(self.maskindex).ravel().astype(np.int64), [-1, -1]))
+        flat = plan.ravel()
+        flat = np.where(keep[flat] > 0, flat, sentinel)
+        flat = np.where(remap[flat] >= 0, remap[flat], sentinel)
+        self.indexPlan = np.sort(flat.reshape(nR, nT, L), axis=-1)
+
+    def ray_counts(self):
+        """Number of in-mask pixels on each ray, [nRho, nTheta]."""
+        nPx = int(self.imDim[0]) * int(self.imDim[1])
+        return (self.indexPlan < nPx).sum(axis=-1)
+
+    def radon2pole(self, bandData, PC=None, vendor='EDAX'):
+        """Band (theta, rho) -> unit plane normal in the detector frame (radon_fast.py:314-397,
+        Krieger Lassen 1994 eq. 3.1.6): the band is the detector line through
+        ``p = rho*(cos, sin) + centre`` with direction ``(-sin, cos)``; its plane normal is
+        ``r x (p - t)`` with ``t`` the source point scaled per vendor convention."""
+        if PC is None:
+            PC = np.array([0.471659, 0.675044, 0.630139])
+        ven = str.upper(vendor)
+        nPats, nBands = bandData.shape[0], bandData.shape[1]
+        theta = bandData['theta'][:]
+        rho = bandData['rho'][:]
+        st, ct = np.sin(theta), np.cos(theta)
+        pc = np.asarray(PC, dtype=np.float32).copy()
+        if ven != 'EMSOFT':
+            if pc.ndim < 2:
+                pc = np.tile(pc, nPats).reshape(nPats, 3)
+            elif pc.shape[0] != nPats:
+                pc = np.tile(pc[0, :], nPats).reshape(nPats, 3)
+            t = pc
+        else:
+            if pc.ndim < 2:
+                pc = np.tile(pc, nPats).reshape(nPats, 4)
+            elif pc.shape[0] != nPats:
+                pc = np.tile(pc[0, :], nPats).reshape(nPats, 4)
+            t = pc[:, 0:3]
+            t[:, 2] /= pc[:, 3]
+        dimf = np.array(self.imDim, dtype=np.float32)
+        if ven == 'EDAX':
+            t *= np.array([dimf[1], dimf[0], -np.min(dimf[0:2])])
+        if ven == 'OXFORD':
+            t *= np.array([dimf[1], dimf[1], -dimf[1]])
+        if ven == 'EMSOFT':
+            t[:, 0] *= -1.0
+            t += np.array([dimf[1] / 2.0, dimf[0] / 2.0, 0.0])
+            t[:, 2] *= -1.0
+        if ven in ('KIKUCHIPY', 'BRUKER'):
+            t *= np.array([dimf[1], dimf[0], -dimf[0]])
+            t[:, 1] = dimf[0] - t[:, 1]
+        t = np.tile(t.reshape(nPats, 1, 3), (1, nBands, 1))
+        r = np.zeros((nPats, nBands, 3), dtype=np.float32)
+        r[:, :, 0] = -1 * st
+        r[:, :, 1] = ct
+        p = np.zeros((nPats, nBands, 3), dtype=np.float32)
+        p[:, :, 0] = rho * ct
+        p[:, :, 1] = rho * st
+        p[:, :, 0] += dimf[1] * 0.5
+        p[:, :, 1] += dimf[0] * 0.5
+        n = np.cross(r.reshape(nPats * nBands, 3), (p - t).reshape(nPats * nBands, 3))
+        nrm = np.linalg.norm(n, axis=1).clip(1e-12)
+        n /= nrm.reshape(nPats * nBands, 1)
+        return n.reshape(nPats, nBands, 3)

@@ -15,7 +15,7 @@ the pattern centre the reference's ``test_index_pats`` uses.
 
 Each case is written to ``tests/golden/<name>.npz``: inputs, plan parameters (JSON), the plan
 vectors the reference derived (theta, rho, rdnmask, kernel, per-ray counts, a hash of the LUT
-and, for the small cases, the LUT itself) and every field of the band record array.
+and the LUT itself, ray ends stored as H*W+1) and every field of the band record array.
 """
 from __future__ import annotations
 
@@ -89,7 +89,7 @@ def lut_hash(lut):
     return hashlib.sha256(np.ascontiguousarray(lut.astype(np.int64)).tobytes()).hexdigest()
 
 
-def run_case(ref, name, pats, params, mask=None, background=None, collect_bg=False, store_lut=False,
+def run_case(ref, name, pats, params, mask=None, background=None, collect_bg=False, store_lut=True,
              index_pc=None):
     bd = ref.band_detect.BandDetect(nTheta=params["nTheta"], nRho=params["nRho"],
                                     tSigma=params["tSigma"], rSigma=params["rSigma"],
@@ -121,7 +121,9 @@ def run_case(ref, name, pats, params, mask=None, background=None, collect_bg=Fal
     if background is not None:
         rec["background"] = np.asarray(background, dtype=np.float64)
     if store_lut:
-        rec["lut"] = rp.indexPlan.astype(np.uint16 if rp.indexPlan.max() < 65535 else np.int32)
+        # entries >= H*W all mean "end of ray"; store them as H*W+1 so uint16 holds them
+        lut = np.minimum(rp.indexPlan, pats.shape[-1] * pats.shape[-2] + 1)
+        rec["lut"] = lut.astype(np.uint16 if lut.max() < 65535 else np.int32)
     for f in FIELDS:
         rec["out_" + f] = out[f]
     if index_pc is not None:
@@ -154,7 +156,7 @@ def main():
     m60 = syn.circular_mask(60, 60)
     const = (np.full((60, 60), 50, dtype=np.uint8) * m60)
     p = np.concatenate([p, np.zeros((1, 60, 60), np.uint8), const[None]])
-    run_case(ref, "c0_60_u8", p, dict(base, nRho=90, nBands=8), mask=m60, store_lut=True)
+    run_case(ref, "c0_60_u8", p, dict(base, nRho=90, nBands=8), mask=m60)
 
     # 80x80 uint8, nRho 120, nBands 9 (the batched configuration's pattern geometry).
     p, _, _ = syn.make_patterns(12, 80, 80, seed=2000, noise_frac=0.1)
@@ -169,7 +171,7 @@ def main():
     p, _, _ = syn.make_patterns(6, 48, 64, seed=4000, mask=False)
     p = (p.astype(np.float32) / np.float32(255.0)).astype(np.float32)
     run_case(ref, "f32_rect_48x64", p, dict(nTheta=120, nRho=72, tSigma=None, rSigma=None,
-                                             rhoMaskFrac=0.15, nBands=7), store_lut=True)
+                                             rhoMaskFrac=0.15, nBands=7))
 
     # Larger LoG kernel (sigma 2 -> 9x9 taps, 19-wide peak window, padding 19).
     p, _, _ = syn.make_patterns(4, 60, 60, seed=5000)
@@ -177,9 +179,9 @@ def main():
 
     # rhoMaskFrac >= 1 (half-diagonal rhoMax, eroded mask) and < 0 (circle-limited).
     p, _, _ = syn.make_patterns(4, 40, 40, seed=6000, mask=False)
-    run_case(ref, "rmf1_40_u8", p, dict(base, nRho=60, rhoMaskFrac=1.0, nBands=6), store_lut=True)
+    run_case(ref, "rmf1_40_u8", p, dict(base, nRho=60, rhoMaskFrac=1.0, nBands=6))
     p, _, _ = syn.make_patterns(4, 40, 40, seed=6100, mask=False)
-    run_case(ref, "rmfneg_40_u8", p, dict(base, nRho=60, rhoMaskFrac=-0.1, nBands=6), store_lut=True)
+    run_case(ref, "rmfneg_40_u8", p, dict(base, nRho=60, rhoMaskFrac=-0.1, nBands=6))
 
     # The reference's own test fixture through find_bands and the full indexer
     # (EBSDIndexer defaults: tSigma 1.0, rSigma 1.2, rhoMaskFrac 0.15, nRho 90, nBands 9).

@@ -1,0 +1,52 @@
+"""GPU find_bands against the reference's golden vectors (all pattern types and plan shapes).
+
+Tolerances (the spec bar): integer peak locations identical for >= 99.9% of bands,
+sub-pixel (aveloc) within 1e-3 Radon pixels; the other float fields within the stated
+relative tolerances.  The device convolves directly while the reference uses an FFT
+convolution, so values differ at the float32 rounding level.
+"""
+import numpy as np
+import pytest
+
+from bandcmp import compare
+from conftest import golden_names, load_golden
+from gpuhelp import golden_records, plan_from_golden
+
+pytestmark = pytest.mark.gpu
+
+METHODS = ["plain", "plain64", "fused", "fused16"]
+
+
+def run(bd, pats, method):
+    if method.startswith("fused") and not bd._device_plan().supported(method):
+        pytest.skip(f"{method} does not support this plan shape")
+    return bd.find_bands(pats, method=method)
+
+
+@pytest.mark.parametrize("method", METHODS)
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_parity(cuda, name, method):
+    case = load_golden(name)
+    bd = plan_from_golden(case)
+    out = run(bd, case["patterns"], method)
+    c = compare(out, golden_records(case))
+    assert c["frac"] >= 0.999 or c["bands"] - c["matched"] == 0, c
+    assert c["aveloc"] <= 1e-3, c
+    tol_rel = 2e-2 if method == "fused16" else 1e-4
+    assert c["rel"]["max"] <= tol_rel, c
+    assert c["rel"]["avemax"] <= tol_rel, c
+    assert c["abs"]["theta"] <= 1e-3 * np.pi / case["params"]["nTheta"] + 1e-6, c
+    assert c["rel"]["width"] <= (5e-2 if method == "fused16" else 1e-3), c
+    # invalid band slots carry the reference's fill values
+    inv = out["valid"] == 0
+    assert np.all(out["max"][inv] == np.float32(-2.0e6))
+    assert np.all(out["band_match_index"] == 0)
+
+
+def test_orientation_fixture_bands(cuda):
+    """The reference's indexing fixture: GPU bands equal the bands the reference indexer used."""
+    case = load_golden("al_sim_20kv")
+    bd = plan_from_golden(case)
+    out = bd.find_bands(case["patterns"], method="plain")
+    np.testing.assert_allclose(out["theta"], case["index_band_theta"], atol=1e-5)
+    np.testing.assert_allclose(out["rho"], case["index_band_rho"], atol=1e-3)

@@ -1,0 +1,65 @@
+"""GPU vs the oracle on seeded samples at the benchmark geometries.
+
+Bar: integer peak locations identical on >= 99.9% of bands, sub-pixel aveloc within 1e-3
+Radon pixels of the FFT float32 reference arithmetic; every method's error against the FP64
+GPU oracle (method plain64) is reported and bounded the same way.
+"""
+import numpy as np
+import pytest
+
+import pyebsdindex_gb300 as pg
+from pyebsdindex_gb300 import synthetic as syn
+from oracle import band_oracle as bo
+from bandcmp import compare
+
+pytestmark = pytest.mark.gpu
+
+GEOMS = {
+    # 60x60 uint8, nRho 90, nBands 8
+    "60": dict(h=60, w=60, nRho=90, nBands=8, n=600, seed=10_000, noise=0.0),
+    # 80x80 uint8, nRho 120, nBands 9, 10% pure-noise patterns
+    "80": dict(h=80, w=80, nRho=120, nBands=9, n=600, seed=20_000, noise=0.1),
+}
+
+
+def setup(g):
+    mask = syn.circular_mask(g["h"], g["w"])
+    bd = pg.BandDetect(nTheta=180, nRho=g["nRho"], tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=g["nBands"])
+    bd.band_detect_setup(patDim=(g["h"], g["w"]), patternmask=mask)
+    plan = bo.Plan((g["h"], g["w"]), 180, g["nRho"], 1.0, 1.0, 0.1, g["nBands"], mask=mask)
+    bd.radonPlan.indexPlan = plan.lut.copy()  # the oracle's table (same host)
+    pats = syn.make_patterns(g["n"], g["h"], g["w"], seed=g["seed"], noise_frac=g["noise"])[0]
+    return bd, plan, pats
+
+
+@pytest.fixture(scope="module", params=sorted(GEOMS))
+def geom(request):
+    g = GEOMS[request.param]
+    bd, plan, pats = setup(g)
+    ref = bo.find_bands(plan, pats)
+    return g, bd, pats, ref
+
+
+@pytest.mark.parametrize("method", ["plain", "plain64", "fused", "fused16"])
+def test_matches_reference_arithmetic(cuda, geom, method):
+    g, bd, pats, ref = geom
+    if method.startswith("fused") and not bd._device_plan().supported(method):
+        pytest.skip("fused kernel does not support this geometry")
+    out = bd.find_bands(pats, method=method)
+    c = compare(out, ref)
+    print(method, g["h"], c)
+    assert c["frac"] >= 0.999, c
+    assert c["aveloc"] <= 1e-3, c
+
+
+@pytest.mark.parametrize("method", ["plain", "fused", "fused16"])
+def test_error_vs_fp64_gpu_oracle(cuda, geom, method):
+    g, bd, pats, _ = geom
+    if method.startswith("fused") and not bd._device_plan().supported(method):
+        pytest.skip("fused kernel does not support this geometry")
+    ref64 = bd.find_bands(pats, method="plain64")
+    out = bd.find_bands(pats, method=method)
+    c = compare(out, ref64)
+    print(method, "vs fp64", g["h"], c)
+    assert c["frac"] >= 0.999, c
+    assert c["aveloc"] <= 1e-3, c
