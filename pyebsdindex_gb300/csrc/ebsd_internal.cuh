@@ -15,7 +15,8 @@ constexpr int kMaxBands = 32;
 
 // Fused-kernel geometry chosen at plan creation (see fused.cu).
 struct FusedGeom {
-    int ok = 0;                 // the tile fits on chip
+    int ok = 0;                 // the tile fits on chip (FP16 Radon storage)
+    int ok_f32 = 0;             // ... and with FP32 Radon storage
     int threads = 0;            // threads per block
     int smem_f32 = 0;           // dynamic shared memory bytes, FP32 Radon storage
     int smem_f16 = 0;           // dynamic shared memory bytes, FP16 Radon storage

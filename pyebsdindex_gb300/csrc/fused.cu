@@ -1,35 +1,530 @@
-// Fused persistent band-detection kernel (one launch per chunk).  Placeholder until the
-// fused kernel lands: reports every plan as unsupported.
+// Fused persistent band-detection kernel: one launch per chunk, one CTA per SM, each CTA
+// looping over patterns.  Everything between the pattern bytes in HBM and the band fields
+// in HBM stays in shared memory:
+//
+//   1. load      pattern -> FP32 tile (background subtracted as radon_fast.py:255-259 does)
+//   2. radon     thread per ray, sequential FP32 sum over the ray's LUT entries in the
+//                reference's order (rdn_loops, radon_fast.py:299-305), mean -> Radon tile
+//                (stored FP32, or FP16 for EBSD_FUSED_F16)
+//   3. pad       theta mirror with rho flip + rho edge rows + zero rows below the array
+//                (band_detect.py:573-580; the FFT convolution's zero extension)
+//   4. conv      register-blocked direct LoG convolution into an FP32 conv tile, in the same
+//                multiply-add order as the per-stage kernel; min/sum for normmax on the fly
+//   5. peaks     per warp: 32-column strip x 8 rows; rho max in registers, theta max by warp
+//                shuffles, exact equality + rdnmask (band_detect.py:639-664); candidates go
+//                into a warp top-N list ordered by (value desc, position asc)
+//   6. merge     tree merge of the 32 warp lists
+//   7. label     lanes 0..nB-1 of warp 0 fit their band (band_detect.py:691-809) and write
+//                the record fields, normmax, theta and rho (band_detect.py:457-460, :521-524)
+//
+// Shared-memory footprint decides which plans the fused path takes (fused_supported()).
 #include "ebsd_internal.cuh"
+#include "label.cuh"
+
+#include <cuda_fp16.h>
+#include <algorithm>
+#include <cfloat>
 
 namespace ebsd {
+namespace {
+
+constexpr int kThreads = 1024;
+constexpr int kWarps = kThreads / 32;
+constexpr int kRowBlock = 8;
+
+struct FusedArgs {
+    const void* pats;
+    int64_t n;
+    int H, W, nPx, pitch;      // pattern tile pitch (W + 1); zero word at H*pitch
+    const uint4* lut;          // [chunks][nRays][8] u16 tile offsets, ray order theta-major
+    const int32_t* count;      // [nRays] theta-major
+    int nRays, nRho, nTheta;
+    int p0, p1, R, Tp;
+    int row0, col0, TR, TC;    // Radon tile origin (padded frame) and extent
+    int crow0, ccol0, CR, CC;  // conv tile origin and extent
+    int statR1;                // end row of the statistics slice (padded frame)
+    const float* kernel;       // [K0*K1]
+    const uint8_t* rdnmask;    // [nRho][nTheta]
+    int bg_mode;
+    const double* bg;
+    const float* bgf;
+    LabelConsts kc;
+    ebsd_bands out;
+    int64_t out_offset;
+};
+
+template <typename S> __device__ __forceinline__ S to_store(float v);
+template <> __device__ __forceinline__ float to_store<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half to_store<__half>(float v) { return __float2half_rn(v); }
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+
+__device__ __forceinline__ bool beats(float v, int p, float w, int q) {
+    return v > w || (v == w && p < q);
+}
+
+// Insert (v, pos) into a warp list ordered by (value desc, position asc).
+__device__ __forceinline__ void list_insert(float v, int pos, float& lv, int& lp, int nB, int lane) {
+    unsigned ahead = __ballot_sync(0xffffffffu, lane < nB && lp >= 0 && beats(lv, lp, v, pos));
+    int ins = __popc(ahead);
+    if (ins < nB) {
+        float uv = __shfl_up_sync(0xffffffffu, lv, 1);
+        int up = __shfl_up_sync(0xffffffffu, lp, 1);
+        if (lane > ins && lane < nB) { lv = uv; lp = up; }
+        if (lane == ins) { lv = v; lp = pos; }
+    }
+}
+
+struct SmemConv {
+    const float* c;
+    int crow0, ccol0, CC;
+    __device__ __forceinline__ float operator()(int r, int col) const {
+        return c[(r - crow0) * CC + (col - ccol0)];
+    }
+};
+
+template <typename InT>
+__device__ __forceinline__ float load_pixel(const InT* p, int idx, int bg_mode, const double* bg, const float* bgf) {
+    if (bg_mode == 1) return (float)((double)p[idx] - bg[idx]);
+    if (bg_mode == 2) return __fsub_rn((float)p[idx], bgf[idx]);
+    return (float)p[idx];
+}
+
+template <typename InT, typename S, int K0, int K1>
+__global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int D0 = K0;  // rho half-window of the max filter (peakPad = 2*ksz + 1)
+    constexpr int D1 = K1;  // theta half-window
+    constexpr int SW = 32 - 2 * D1;  // output columns per warp strip
+    constexpr int H0 = K0 / 2, H1 = K1 / 2;
+    constexpr int NV = kRowBlock + 2 * D0;  // conv rows a strip block reads
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    size_t off = 0;
+    S* tile = (S*)(smem + off);
+    off += ((size_t)a.TR * a.TC * sizeof(S) + 15) & ~(size_t)15;
+    float* conv = (float*)(smem + off);
+    float* pat = conv;  // aliased: the pattern tile is dead once the Radon is built
+    off += ((size_t)a.CR * a.CC * sizeof(float) + 15) & ~(size_t)15;
+    float* kern = (float*)(smem + off);
+    off += ((size_t)K0 * K1 * sizeof(float) + 15) & ~(size_t)15;
+    float* lv_s = (float*)(smem + off);
+    off += kWarps * kMaxBands * sizeof(float);
+    int* lp_s = (int*)(smem + off);
+    off += kWarps * kMaxBands * sizeof(int);
+    double* red_d = (double*)(smem + off);
+    off += 32 * sizeof(double);
+    float* red_f = (float*)(smem + off);
+
+    for (int i = tid; i < K0 * K1; i += kThreads) kern[i] = a.kernel[i];
+    const int nB = a.kc.nB;
+    const int stat_r0 = a.p0, stat_r1 = a.statR1, stat_c0 = a.p1, stat_c1 = a.p1 + a.nTheta;
+    const int stat_count = (stat_r1 - stat_r0) * (stat_c1 - stat_c0);
+
+    for (int64_t q = blockIdx.x; q < a.n; q += gridDim.x) {
+        // ---- 1. load the pattern into the FP32 tile (pitch W+1, zero word after it) ----
+        const InT* gp = (const InT*)a.pats + q * (int64_t)a.nPx;
+        for (int i = tid; i < a.nPx; i += kThreads) {
+            int y = i / a.W, x = i - (i / a.W) * a.W;
+            pat[y * a.pitch + x] = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
+        }
+        if (tid == 0) pat[a.H * a.pitch] = 0.0f;
+        __syncthreads();
+
+        // ---- 2. Radon: thread per ray, sequential FP32 sum in LUT order ----
+        for (int t = tid; t < a.nRays; t += kThreads) {
+            int cnt = a.count[t];
+            float sum = 0.0f;
+            int nch = (cnt + 7) >> 3;
+            const uint4* lp = a.lut + t;
+            for (int g = 0; g < nch; ++g) {
+                uint4 e = __ldg(lp + (size_t)g * a.nRays);
+                sum = __fadd_rn(sum, pat[e.x & 0xFFFF]);
+                sum = __fadd_rn(sum, pat[e.x >> 16]);
+                sum = __fadd_rn(sum, pat[e.y & 0xFFFF]);
+                sum = __fadd_rn(sum, pat[e.y >> 16]);
+                sum = __fadd_rn(sum, pat[e.z & 0xFFFF]);
+                sum = __fadd_rn(sum, pat[e.z >> 16]);
+                sum = __fadd_rn(sum, pat[e.w & 0xFFFF]);
+                sum = __fadd_rn(sum, pat[e.w >> 16]);
+            }
+            float v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
+            int j = t / a.nRho, i = t - (t / a.nRho) * a.nRho;
+            tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(v);
+        }
+        __syncthreads();
+
+        // ---- 3. pad the tile around the interior ----
+        for (int c = tid; c < a.TR * a.TC; c += kThreads) {
+            int tr = c / a.TC, tc = c - (c / a.TC) * a.TC;
+            int r = tr + a.row0, col = tc + a.col0;
+            int i = r - a.p0, j = col - a.p1;
+            if (i >= 0 && i < a.nRho && j >= 0 && j < a.nTheta) continue;
+            S val;
+            if (r < 0 || r >= a.R) {
+                val = to_store<S>(0.0f);
+            } else {
+                int ic = i < 0 ? 0 : (i >= a.nRho ? a.nRho - 1 : i);
+                int si = ic, sj = j;
+                if (j < 0) { si = a.nRho - 1 - ic; sj = a.nTheta + j; }
+                else if (j >= a.nTheta) { si = a.nRho - 1 - ic; sj = j - a.nTheta; }
+                val = tile[(si + a.p0 - a.row0) * a.TC + (sj + a.p1 - a.col0)];
+            }
+            tile[c] = val;
+        }
+        __syncthreads();
+
+        // ---- 4. LoG convolution, kRowBlock outputs per thread down one column ----
+        float smin = INFINITY, ssum = 0.0f;
+        {
+            const int nrb = (a.CR + kRowBlock - 1) / kRowBlock;
+            for (int task = tid; task < nrb * a.CC; task += kThreads) {
+                int cc = task % a.CC, rb = task / a.CC;
+                int cr0 = rb * kRowBlock;
+                float acc[kRowBlock];
+#pragma unroll
+                for (int o = 0; o < kRowBlock; ++o) acc[o] = 0.0f;
+                // tile row (cr0 + t) feeds output o through kernel row a = o + 2*H0 - t;
+                // descending t keeps each output's multiply-add order = ascending a.
+#pragma unroll
+                for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
+                    int tr = cr0 + t;
+                    float v[K1];
+                    if (tr < a.TR) {
+#pragma unroll
+                        for (int b = 0; b < K1; ++b) v[b] = to_f(tile[tr * a.TC + cc + 2 * H1 - b]);
+                    } else {
+#pragma unroll
+                        for (int b = 0; b < K1; ++b) v[b] = 0.0f;
+                    }
+#pragma unroll
+                    for (int o = 0; o < kRowBlock; ++o) {
+                        int ka = o + 2 * H0 - t;
+                        if (ka >= 0 && ka < K0) {
+#pragma unroll
+                            for (int b = 0; b < K1; ++b) acc[o] = fmaf(kern[ka * K1 + b], v[b], acc[o]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int o = 0; o < kRowBlock; ++o) {
+                    int cr = cr0 + o;
+                    if (cr < a.CR) {
+                        conv[cr * a.CC + cc] = acc[o];
+                        int r = cr + a.crow0, col = cc + a.ccol0;
+                        if (r >= stat_r0 && r < stat_r1 && col >= stat_c0 && col < stat_c1) {
+                            smin = fminf(smin, acc[o]);
+                            ssum += acc[o];
+                        }
+                    }
+                }
+            }
+        }
+        // block reduction of min / sum (sum in FP64 across threads)
+        {
+            double dsum = (double)ssum;
+            float m = smin;
+            for (int o = 16; o > 0; o >>= 1) {
+                dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+                m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
+            }
+            if (lane == 0) { red_d[warp] = dsum; red_f[warp] = m; }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double dsum = red_d[lane];
+            float m = red_f[lane];
+            for (int o = 16; o > 0; o >>= 1) {
+                dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+                m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
+            }
+            if (lane == 0) { red_d[0] = dsum; red_f[0] = m; }
+        }
+        // (red_d[0] / red_f[0] are read after the next barrier)
+
+        // ---- 5. peaks: strips of SW output columns x kRowBlock rows per warp task ----
+        float lv = -INFINITY;
+        int lp = -1;
+        {
+            const int nstrip = (a.nTheta + SW - 1) / SW;
+            const int nrowb = (a.nRho + kRowBlock - 1) / kRowBlock;
+            for (int task = warp; task < nstrip * nrowb; task += kWarps) {
+                int s = task % nstrip, rb = task / nstrip;
+                // lane column in the conv tile: output column p1 + SW*s + (lane - D1)
+                int cc = SW * s + lane + (a.p1 - D1 - a.ccol0);
+                int cr0 = rb * kRowBlock + (a.p0 - D0 - a.crow0);
+                bool colok = cc >= 0 && cc < a.CC;
+                float v[NV];
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    int cr = cr0 + k;
+                    v[k] = (colok && cr < a.CR) ? conv[cr * a.CC + cc] : -INFINITY;
+                }
+                // rho max over [o, o + 2*D0] for o = 0..7: suffix / core / prefix maxima
+                float suf[kRowBlock], pre[kRowBlock], core = -INFINITY;
+                suf[kRowBlock - 1] = -INFINITY;
+#pragma unroll
+                for (int o = kRowBlock - 2; o >= 0; --o) suf[o] = fmaxf(v[o], o + 1 <= kRowBlock - 2 ? suf[o + 1] : -INFINITY);
+#pragma unroll
+                for (int k = kRowBlock - 1; k <= 2 * D0; ++k) core = fmaxf(core, v[k]);
+                pre[0] = -INFINITY;
+#pragma unroll
+                for (int o = 1; o < kRowBlock; ++o) pre[o] = fmaxf(pre[o - 1], v[2 * D0 + o]);
+                int ocol = a.p1 + SW * s + (lane - D1);  // output column (padded frame)
+                bool lane_out = lane >= D1 && lane < 32 - D1 && ocol < a.p1 + a.nTheta;
+#pragma unroll
+                for (int o = 0; o < kRowBlock; ++o) {
+                    float m = fmaxf(fmaxf(suf[o], core), pre[o]);
+                    float mt = m;
+#pragma unroll
+                    for (int d = 1; d <= D1; ++d) {
+                        mt = fmaxf(mt, __shfl_up_sync(0xffffffffu, m, d));
+                        mt = fmaxf(mt, __shfl_down_sync(0xffffffffu, m, d));
+                    }
+                    int orow = a.p0 + rb * kRowBlock + o;
+                    float val = v[o + D0];
+                    bool f = lane_out && orow < a.p0 + a.nRho && val == mt &&
+                             a.rdnmask[(orow - a.p0) * a.nTheta + (ocol - a.p1)];
+                    unsigned bal = __ballot_sync(0xffffffffu, f);
+                    while (bal) {
+                        int b = __ffs(bal) - 1;
+                        bal &= bal - 1;
+                        float cv = __shfl_sync(0xffffffffu, val, b);
+                        int pos = (orow - a.p0) * a.nTheta + (a.p1 + SW * s + (b - D1) - a.p1);
+                        list_insert(cv, pos, lv, lp, nB, lane);
+                    }
+                }
+            }
+        }
+        if (lane < nB) {
+            lv_s[warp * kMaxBands + lane] = lv;
+            lp_s[warp * kMaxBands + lane] = lp;
+        }
+        __syncthreads();
+
+        // ---- 6. tree merge of the warp lists: list w absorbs list w + step ----
+        for (int step = 1; step < kWarps; step <<= 1) {
+            if ((warp % (2 * step)) == 0 && warp + step < kWarps) {
+                float av = lane < nB ? lv_s[warp * kMaxBands + lane] : -INFINITY;
+                int ap = lane < nB ? lp_s[warp * kMaxBands + lane] : -1;
+                float bv = lane < nB ? lv_s[(warp + step) * kMaxBands + lane] : -INFINITY;
+                int bp = lane < nB ? lp_s[(warp + step) * kMaxBands + lane] : -1;
+                // merged rank of each entry = own index + entries of the other list ahead of it
+                int ra = lane, rbk = lane;
+                for (int k = 0; k < nB; ++k) {
+                    float ov = __shfl_sync(0xffffffffu, bv, k);
+                    int op = __shfl_sync(0xffffffffu, bp, k);
+                    if (op >= 0 && (ap < 0 || beats(ov, op, av, ap))) ++ra;
+                    float ow = __shfl_sync(0xffffffffu, av, k);
+                    int oq = __shfl_sync(0xffffffffu, ap, k);
+                    if (oq >= 0 && (bp < 0 || beats(ow, oq, bv, bp))) ++rbk;
+                }
+                __syncwarp();
+                if (lane < nB) {
+                    lv_s[warp * kMaxBands + lane] = -INFINITY;
+                    lp_s[warp * kMaxBands + lane] = -1;
+                }
+                __syncwarp();
+                if (lane < nB && ap >= 0 && ra < nB) {
+                    lv_s[warp * kMaxBands + ra] = av;
+                    lp_s[warp * kMaxBands + ra] = ap;
+                }
+                if (lane < nB && bp >= 0 && rbk < nB) {
+                    lv_s[warp * kMaxBands + rbk] = bv;
+                    lp_s[warp * kMaxBands + rbk] = bp;
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- 7. label: warp 0, one lane per band ----
+        if (warp == 0 && lane < nB) {
+            int pos = lp_s[lane];
+            bool has = pos >= 0;
+            int r = 0, c = 0;
+            if (has) {
+                int i = pos / a.nTheta;
+                r = i + a.p0;
+                c = (pos - i * a.nTheta) + a.p1;
+            }
+            float mn = red_f[0];
+            float mean = (float)(red_d[0] / (double)stat_count);
+            SmemConv acc{conv, a.crow0, a.ccol0, a.CC};
+            band_fit_write<float>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + q) * nB + lane);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------
+size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1) {
+    size_t b = ((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store + 15) & ~(size_t)15;
+    b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
+    b += ((size_t)k0 * k1 * 4 + 15) & ~(size_t)15;
+    b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 32 * 4;
+    return b;
+}
+
+template <typename InT, typename S>
+void* kernel_ptr(int k0, int k1) {
+    if (k0 == 5 && k1 == 5) return (void*)k_fused<InT, S, 5, 5>;
+    if (k0 == 7 && k1 == 7) return (void*)k_fused<InT, S, 7, 7>;
+    if (k0 == 9 && k1 == 9) return (void*)k_fused<InT, S, 9, 9>;
+    if (k0 == 5 && k1 == 7) return (void*)k_fused<InT, S, 5, 7>;
+    if (k0 == 7 && k1 == 5) return (void*)k_fused<InT, S, 7, 5>;
+    return nullptr;
+}
+
+void* pick_kernel(int method, int dtype, int k0, int k1) {
+    bool h = method == EBSD_FUSED_F16;
+    switch (dtype) {
+        case EBSD_U8: return h ? kernel_ptr<uint8_t, __half>(k0, k1) : kernel_ptr<uint8_t, float>(k0, k1);
+        case EBSD_U16: return h ? kernel_ptr<uint16_t, __half>(k0, k1) : kernel_ptr<uint16_t, float>(k0, k1);
+        case EBSD_F32: return h ? kernel_ptr<float, __half>(k0, k1) : kernel_ptr<float, float>(k0, k1);
+    }
+    return nullptr;
+}
+
+}  // namespace
 
 int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
-    (void)d;
-    p->fg = FusedGeom{};
+    FusedGeom g;
+    const int K0 = p->k0, K1 = p->k1;
+    // the fused kernel assumes the standard windows: peakPad = 2*ksz + 1 (half-window = ksz)
+    bool shape_ok = p->pk0 == 2 * K0 + 1 && p->pk1 == 2 * K1 + 1 && 2 * K1 < 32 &&
+                    pick_kernel(EBSD_FUSED_F32, EBSD_U8, K0, K1) != nullptr &&
+                    p->p0 >= K0 + K0 / 2 && p->p1 >= K1 + K1 / 2;
+    int pitch = p->W + 1;
+    if ((int64_t)p->H * pitch + 1 >= 65535) shape_ok = false;
+    if (shape_ok) {
+        const int D0 = K0, D1 = K1, H0 = K0 / 2, H1 = K1 / 2;
+        int statR1 = std::min(p->R, p->Tp - p->p0);
+        g.crow0 = p->p0 - D0;
+        g.crow1 = std::max(p->p0 + p->nRho + D0, statR1);
+        g.ccol0 = p->p1 - D1;
+        g.ccol1 = p->p1 + p->nTheta + D1;
+        g.row0 = g.crow0 - H0;
+        g.row1 = g.crow1 + H0;
+        g.col0 = g.ccol0 - H1;
+        g.col1 = g.ccol1 + H1;
+        g.tile_pitch = pitch;
+        g.threads = kThreads;
+        g.smem_f32 = (int)smem_bytes(g, 4, K0, K1);
+        g.smem_f16 = (int)smem_bytes(g, 2, K0, K1);
+        size_t conv_cells = (size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0);
+        int dev_smem = 0;
+        cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+        g.ok = conv_cells >= (size_t)p->H * pitch + 1 && g.smem_f16 <= dev_smem && g.row0 >= 0;
+        g.ok_f32 = g.ok && g.smem_f32 <= dev_smem;
+    }
+    p->fg = g;
+    if (!g.ok) return EBSD_OK;
+
+    // LUT: rays in theta-major order, 8 entries per uint4, entry = tile offset y*pitch + x;
+    // padding entries point at the zero word after the pattern (adding +0.0 leaves a sum
+    // unchanged, so the reference's summation order is kept).
+    const int nRays = p->nRays, L = d->lut_len;
+    std::vector<int32_t> cnt(nRays);
+    int maxc = 0;
+    for (int j = 0; j < p->nTheta; ++j)
+        for (int i = 0; i < p->nRho; ++i) {
+            const int64_t* ray = d->lut + ((size_t)i * p->nTheta + j) * L;
+            int c = 0;
+            while (c < L && ray[c] >= 0 && ray[c] < p->nPx) ++c;
+            cnt[j * p->nRho + i] = c;
+            maxc = std::max(maxc, c);
+        }
+    int nch = std::max(1, (maxc + 7) / 8);
+    const uint16_t zero = (uint16_t)(p->H * pitch);
+    std::vector<uint16_t> lut((size_t)nch * nRays * 8, zero);
+    for (int j = 0; j < p->nTheta; ++j)
+        for (int i = 0; i < p->nRho; ++i) {
+            int t = j * p->nRho + i;
+            const int64_t* ray = d->lut + ((size_t)i * p->nTheta + j) * L;
+            for (int k = 0; k < cnt[t]; ++k) {
+                int idx = (int)ray[k];
+                int y = idx / p->W, x = idx - (idx / p->W) * p->W;
+                lut[((size_t)(k / 8) * nRays + t) * 8 + (k % 8)] = (uint16_t)(y * pitch + x);
+            }
+        }
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_flut, lut.size() * sizeof(uint16_t)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_flut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, nRays * sizeof(int32_t)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup, cnt.data(), nRays * sizeof(int32_t), cudaMemcpyHostToDevice));
+    p->flut_entries = (int64_t)lut.size();
     return EBSD_OK;
 }
 
-void fused_release(ebsd_plan_s* p) { (void)p; }
+void fused_release(ebsd_plan_s* p) {
+    cudaFree(p->d_flut);
+    cudaFree(p->d_fgroup);
+    cudaFree(p->d_fray);
+    p->d_flut = nullptr;
+    p->d_fgroup = nullptr;
+    p->d_fray = nullptr;
+}
 
 int fused_supported(const ebsd_plan_s* p, int method) {
-    (void)p;
-    (void)method;
-    return 0;
+    if (!p->fg.ok) return 0;
+    if (method == EBSD_FUSED_F32) return p->fg.ok_f32;
+    return method == EBSD_FUSED_F16;
 }
 
-size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk) {
-    (void)p;
-    (void)method;
-    (void)chunk;
-    return 0;
-}
+size_t fused_workspace_bytes(const ebsd_plan_s*, int, int64_t) { return 0; }
 
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
-    (void)p; (void)method; (void)dtype; (void)d_pats; (void)n; (void)out; (void)out_offset; (void)st;
-    (void)launches;
-    return EBSD_E_UNSUPPORTED;
+    if (n <= 0) return EBSD_OK;
+    void* fn = pick_kernel(method, dtype, p->k0, p->k1);
+    if (!fn) return EBSD_E_UNSUPPORTED;
+    const FusedGeom& g = p->fg;
+    int smem = method == EBSD_FUSED_F16 ? g.smem_f16 : g.smem_f32;
+    EBSD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    int sms = 0, per_sm = 0;
+    EBSD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+    EBSD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem));
+    if (per_sm < 1) return EBSD_E_UNSUPPORTED;
+    int64_t grid = std::min<int64_t>(n, (int64_t)sms * per_sm);
+
+    FusedArgs a;
+    a.pats = d_pats;
+    a.n = n;
+    a.H = p->H;
+    a.W = p->W;
+    a.nPx = p->nPx;
+    a.pitch = g.tile_pitch;
+    a.lut = (const uint4*)p->d_flut;
+    a.count = p->d_fgroup;
+    a.nRays = p->nRays;
+    a.nRho = p->nRho;
+    a.nTheta = p->nTheta;
+    a.p0 = p->p0;
+    a.p1 = p->p1;
+    a.R = p->R;
+    a.Tp = p->Tp;
+    a.row0 = g.row0;
+    a.col0 = g.col0;
+    a.TR = g.row1 - g.row0;
+    a.TC = g.col1 - g.col0;
+    a.crow0 = g.crow0;
+    a.ccol0 = g.ccol0;
+    a.CR = g.crow1 - g.crow0;
+    a.CC = g.ccol1 - g.ccol0;
+    a.statR1 = std::min(p->R, p->Tp - p->p0);
+    a.kernel = p->d_kernel;
+    a.rdnmask = p->d_rdnmask;
+    a.bg_mode = p->bg_mode;
+    a.bg = p->d_bg;
+    a.bgf = p->d_bgf;
+    a.kc = LabelConsts{p->p0, p->p1, p->nTheta, p->nRho, p->nB, p->d_theta, p->d_rho};
+    a.out = *out;
+    a.out_offset = out_offset;
+    void* args[] = {&a};
+    EBSD_CUDA_TRY(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kThreads), args, (size_t)smem, st));
+    *launches += 1;
+    return launch_status();
 }
 
 }  // namespace ebsd

@@ -297,7 +297,9 @@ int ebsd_find_bands_host(ebsd_plan_t p, int method, int dtype, const void* h_pat
     const int nB = p->nB;
     size_t es = elem_size(dtype);
     size_t in_bytes = (size_t)chunk * p->nPx * es;
-    size_t out_bytes = (size_t)chunk * nB * (4 * 9 + 1) + 256;  // 41 B per band + slack
+    // nine fields per band: eight float fields of which maxloc/aveloc are pairs (10 floats)
+    // plus the int8 'valid' = 41 bytes per band
+    size_t out_bytes = (size_t)chunk * nB * (10 * sizeof(float) + 1) + 256;
     for (int i = 0; i < 2; ++i) {
         if (!p->hstream[i]) EBSD_CUDA_TRY(cudaStreamCreateWithFlags(&p->hstream[i], cudaStreamNonBlocking));
         if (!p->hevent[i]) EBSD_CUDA_TRY(cudaEventCreateWithFlags(&p->hevent[i], cudaEventDisableTiming));

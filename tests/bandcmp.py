@@ -15,15 +15,19 @@ def as_dict(rec):
     return {f: rec[f] for f in rec.dtype.names}
 
 
-def compare(got, ref):
+def compare(got, ref, skip=()):
+    """Match bands of ``got`` to ``ref``; patterns listed in ``skip`` are left out."""
     got, ref = as_dict(got), as_dict(ref)
     n, nB = ref["valid"].shape
+    skip = set(int(s) for s in skip)
     total = matched = 0
     valid_count_equal = 0
     err = {f: 0.0 for f in FLOAT_FIELDS}
     rel = {f: 0.0 for f in ("max", "normmax", "avemax", "width")}
     loc_err = 0.0
     for q in range(n):
+        if q in skip:
+            continue
         rv = np.nonzero(ref["valid"][q] == 1)[0]
         gv = np.nonzero(got["valid"][q] == 1)[0]
         valid_count_equal += int(len(rv) == len(gv))

@@ -90,7 +90,7 @@ def lut_hash(lut):
 
 
 def run_case(ref, name, pats, params, mask=None, background=None, collect_bg=False, store_lut=True,
-             index_pc=None):
+             index_pc=None, degenerate=()):
     bd = ref.band_detect.BandDetect(nTheta=params["nTheta"], nRho=params["nRho"],
                                     tSigma=params["tSigma"], rSigma=params["rSigma"],
                                     rhoMaskFrac=params["rhoMaskFrac"], nBands=params["nBands"])
@@ -116,6 +116,9 @@ def run_case(ref, name, pats, params, mask=None, background=None, collect_bg=Fal
         "count": (rp.indexPlan < pats.shape[-1] * pats.shape[-2]).sum(-1).astype(np.int32),
         "lut_sha256": lut_hash(rp.indexPlan),
     }
+    # patterns whose reference bands are set by FFT rounding noise (all-zero / constant input):
+    # parity on them is checked against exact arithmetic instead (see the GPU tests)
+    rec["degenerate"] = np.asarray(degenerate, dtype=np.int64)
     if mask is not None:
         rec["mask"] = np.asarray(mask).astype(np.uint8)
     if background is not None:
@@ -156,7 +159,7 @@ def main():
     m60 = syn.circular_mask(60, 60)
     const = (np.full((60, 60), 50, dtype=np.uint8) * m60)
     p = np.concatenate([p, np.zeros((1, 60, 60), np.uint8), const[None]])
-    run_case(ref, "c0_60_u8", p, dict(base, nRho=90, nBands=8), mask=m60)
+    run_case(ref, "c0_60_u8", p, dict(base, nRho=90, nBands=8), mask=m60, degenerate=(20, 21))
 
     # 80x80 uint8, nRho 120, nBands 9 (the batched configuration's pattern geometry).
     p, _, _ = syn.make_patterns(12, 80, 80, seed=2000, noise_frac=0.1)

@@ -50,3 +50,20 @@ def test_oracle_fp64_close_to_reference():
     c = compare(out, ref)
     assert c["frac"] == 1.0
     assert c["aveloc"] < 1e-4
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_c_port_matches_reference(name):
+    """The C/OpenMP restatement (the timed CPU baseline) agrees with the reference: same
+    integer peaks, sub-pixel within 1e-3 Radon pixels (it convolves directly, not by FFT)."""
+    from bandcmp import compare
+    from oracle import cport
+    case = load_golden(name)
+    plan = oracle_plan(case)
+    out = cport.find_bands(plan, case["patterns"], threads=2)
+    ref = {f: case["out_" + f] for f in ["max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta",
+                                         "rho", "valid"]}
+    c = compare(out, ref, skip=case["degenerate"])
+    assert c["frac"] == 1.0, c
+    assert c["aveloc"] <= 1e-3, c
+    assert c["rel"]["max"] <= 1e-4, c
