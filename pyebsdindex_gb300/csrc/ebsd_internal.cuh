@@ -25,8 +25,7 @@ struct FusedGeom {
     // conv region (rows/cols of the padded frame whose LoG value is needed)
     int crow0 = 0, crow1 = 0, ccol0 = 0, ccol1 = 0;
     int tile_pitch = 0;         // pattern tile row pitch (elements)
-    int nwarp_groups = 0;       // ray groups of 32 rays
-    int max_slots = 0;          // LUT slots per group (max ray length in the group)
+    float ksum = 0.0f;          // sum of the LoG taps
 };
 
 struct Workspace {
@@ -61,8 +60,8 @@ struct ebsd_plan_s {
     // fused-kernel tables
     ebsd::FusedGeom fg;
     uint16_t* d_flut = nullptr;    // fused LUT (see fused.cu)
-    int32_t* d_fgroup = nullptr;   // per ray group: {lut offset, nslots, theta column, rho0}
-    float* d_fray = nullptr;       // per ray (tile order): {1/count, background mean} pairs
+    int32_t* d_fgroup = nullptr;   // per-ray entry counts, theta-major ray order
+    float* d_fray = nullptr;       // [nPx] weights: sum_px w*pixel = mean of the non-empty rays
     int64_t flut_entries = 0;
 
     // ---- workspaces ----

@@ -44,6 +44,8 @@ struct FusedArgs {
     int crow0, ccol0, CR, CC;  // conv tile origin and extent
     int statR1;                // end row of the statistics slice (padded frame)
     const float* kernel;       // [K0*K1]
+    float ksum;                // sum of the kernel taps (FP16 centring correction)
+    const float* wimg;         // [nPx] pixel weights whose dot product is the Radon mean
     const uint8_t* rdnmask;    // [nRho][nTheta]
     int bg_mode;
     const double* bg;
@@ -99,6 +101,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     constexpr int H0 = K0 / 2, H1 = K1 / 2;
     constexpr int NV = kRowBlock + 2 * D0;  // conv rows a strip block reads
 
+    constexpr bool kHalf = sizeof(S) == 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     size_t off = 0;
     S* tile = (S*)(smem + off);
@@ -114,7 +117,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     off += kWarps * kMaxBands * sizeof(int);
     double* red_d = (double*)(smem + off);
     off += 32 * sizeof(double);
-    float* red_f = (float*)(smem + off);
+    float* red_f = (float*)(smem + off);  // 66 floats
 
     for (int i = tid; i < K0 * K1; i += kThreads) kern[i] = a.kernel[i];
     const int nB = a.kc.nB;
@@ -124,12 +127,55 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     for (int64_t q = blockIdx.x; q < a.n; q += gridDim.x) {
         // ---- 1. load the pattern into the FP32 tile (pitch W+1, zero word after it) ----
         const InT* gp = (const InT*)a.pats + q * (int64_t)a.nPx;
+        float wsum = 0.0f, pmin = -1.0f, pmax = -1.0f;  // -1: value of an empty ray
         for (int i = tid; i < a.nPx; i += kThreads) {
             int y = i / a.W, x = i - (i / a.W) * a.W;
-            pat[y * a.pitch + x] = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
+            float v = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
+            pat[y * a.pitch + x] = v;
+            if (kHalf) {
+                wsum = fmaf(a.wimg[i], v, wsum);
+                pmin = fminf(pmin, v);
+                pmax = fmaxf(pmax, v);
+            }
         }
         if (tid == 0) pat[a.H * a.pitch] = 0.0f;
+        // FP16 storage keeps (value - m) * s: m = mean of the Radon interior (exact by
+        // linearity: sum_px w[px] * p[px]), s = power of two keeping |value - m| * s < 2^14.
+        float cen = 0.0f, scl = 1.0f, inv_scl = 1.0f;
+        if (kHalf) {
+            double dw = (double)wsum;
+            for (int o = 16; o > 0; o >>= 1) {
+                dw += __shfl_down_sync(0xffffffffu, dw, o);
+                pmin = fminf(pmin, __shfl_down_sync(0xffffffffu, pmin, o));
+                pmax = fmaxf(pmax, __shfl_down_sync(0xffffffffu, pmax, o));
+            }
+            if (lane == 0) { red_d[warp] = dw; red_f[warp] = pmin; red_f[32 + warp] = pmax; }
+            __syncthreads();
+            if (warp == 0) {
+                dw = red_d[lane];
+                pmin = red_f[lane];
+                pmax = red_f[32 + lane];
+                for (int o = 16; o > 0; o >>= 1) {
+                    dw += __shfl_down_sync(0xffffffffu, dw, o);
+                    pmin = fminf(pmin, __shfl_down_sync(0xffffffffu, pmin, o));
+                    pmax = fmaxf(pmax, __shfl_down_sync(0xffffffffu, pmax, o));
+                }
+                if (lane == 0) {
+                    float m = (float)dw;
+                    float amax = fmaxf(fabsf(pmax - m), fabsf(pmin - m));
+                    int e = 0;
+                    frexpf(fmaxf(amax, 1e-30f), &e);  // amax < 2^e
+                    red_f[64] = m;
+                    red_f[65] = ldexpf(1.0f, 14 - e);
+                }
+            }
+        }
         __syncthreads();
+        if (kHalf) {
+            cen = red_f[64];
+            scl = red_f[65];
+            inv_scl = 1.0f / scl;  // exact: scl is a power of two
+        }
 
         // ---- 2. Radon: thread per ray, sequential FP32 sum in LUT order ----
         for (int t = tid; t < a.nRays; t += kThreads) {
@@ -149,6 +195,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 sum = __fadd_rn(sum, pat[e.w >> 16]);
             }
             float v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
+            if (kHalf) v = (v - cen) * scl;
             int j = t / a.nRho, i = t - (t / a.nRho) * a.nRho;
             tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(v);
         }
@@ -162,7 +209,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             if (i >= 0 && i < a.nRho && j >= 0 && j < a.nTheta) continue;
             S val;
             if (r < 0 || r >= a.R) {
-                val = to_store<S>(0.0f);
+                val = to_store<S>(kHalf ? -cen * scl : 0.0f);
             } else {
                 int ic = i < 0 ? 0 : (i >= a.nRho ? a.nRho - 1 : i);
                 int si = ic, sj = j;
@@ -209,6 +256,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
                     int cr = cr0 + o;
+                    if (kHalf) acc[o] = fmaf(a.ksum, cen, acc[o] * inv_scl);
                     if (cr < a.CR) {
                         conv[cr * a.CC + cc] = acc[o];
                         int r = cr + a.crow0, col = cc + a.ccol0;
@@ -363,7 +411,7 @@ size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1) {
     size_t b = ((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store + 15) & ~(size_t)15;
     b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
     b += ((size_t)k0 * k1 * 4 + 15) & ~(size_t)15;
-    b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 32 * 4;
+    b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
     return b;
 }
 
@@ -449,6 +497,26 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
                 lut[((size_t)(k / 8) * nRays + t) * 8 + (k % 8)] = (uint16_t)(y * pitch + x);
             }
         }
+    // weight image: mean over non-empty rays of the ray means = sum_px w[px] * value[px]
+    {
+        std::vector<double> w(p->nPx, 0.0);
+        int nonempty = 0;
+        for (int t = 0; t < nRays; ++t) nonempty += cnt[t] > 0;
+        for (int j = 0; j < p->nTheta; ++j)
+            for (int i = 0; i < p->nRho; ++i) {
+                int t = j * p->nRho + i;
+                if (!cnt[t]) continue;
+                const int64_t* ray = d->lut + ((size_t)i * p->nTheta + j) * L;
+                double f = 1.0 / ((double)cnt[t] * std::max(nonempty, 1));
+                for (int k = 0; k < cnt[t]; ++k) w[ray[k]] += f;
+            }
+        std::vector<float> wf(w.begin(), w.end());
+        EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fray, wf.size() * sizeof(float)));
+        EBSD_CUDA_TRY(cudaMemcpy(p->d_fray, wf.data(), wf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        double ks = 0.0;
+        for (int k = 0; k < K0 * K1; ++k) ks += d->kernel[k];
+        p->fg.ksum = (float)ks;
+    }
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_flut, lut.size() * sizeof(uint16_t)));
     EBSD_CUDA_TRY(cudaMemcpy(p->d_flut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, nRays * sizeof(int32_t)));
@@ -514,6 +582,8 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.CC = g.ccol1 - g.ccol0;
     a.statR1 = std::min(p->R, p->Tp - p->p0);
     a.kernel = p->d_kernel;
+    a.ksum = g.ksum;
+    a.wimg = p->d_fray;
     a.rdnmask = p->d_rdnmask;
     a.bg_mode = p->bg_mode;
     a.bg = p->d_bg;

@@ -25,6 +25,7 @@ def compare(got, ref, skip=()):
     err = {f: 0.0 for f in FLOAT_FIELDS}
     rel = {f: 0.0 for f in ("max", "normmax", "avemax", "width")}
     loc_err = 0.0
+    errs = []
     for q in range(n):
         if q in skip:
             continue
@@ -39,8 +40,9 @@ def compare(got, ref, skip=()):
             if j is None:
                 continue
             matched += 1
-            loc_err = max(loc_err, float(np.abs(got["aveloc"][q, j].astype(np.float64)
-                                                 - ref["aveloc"][q, i].astype(np.float64)).max()))
+            e = float(np.abs(got["aveloc"][q, j].astype(np.float64) - ref["aveloc"][q, i].astype(np.float64)).max())
+            errs.append(e)
+            loc_err = max(loc_err, e)
             for f in FLOAT_FIELDS:
                 d = abs(float(got[f][q, j]) - float(ref[f][q, i]))
                 err[f] = max(err[f], d)
@@ -52,6 +54,9 @@ def compare(got, ref, skip=()):
         "frac": matched / total if total else 1.0,
         "valid_count_equal": valid_count_equal / max(n, 1),
         "aveloc": loc_err,
+        "aveloc_p50": float(np.median(errs)) if errs else 0.0,
+        "aveloc_p99": float(np.percentile(errs, 99)) if errs else 0.0,
+        "within_1e-3": float(np.mean(np.asarray(errs) <= 1e-3)) if errs else 1.0,
         "abs": err,
         "rel": rel,
     }
