@@ -39,7 +39,7 @@ __device__ __forceinline__ double interp_arange(double x, const double* fp, int 
     if (x >= (double)(n - 1)) return fp[n - 1];
     int j = (int)floor(x);
     if ((double)j == x) return fp[j];
-    double slope = __ddiv_rn(__dsub_rn(fp[j + 1], fp[j]), 1.0);
+    double slope = __dsub_rn(fp[j + 1], fp[j]);  // / (xp[j+1] - xp[j]) = / 1.0, exact
     return __dadd_rn(__dmul_rn(slope, __dsub_rn(x, (double)j)), fp[j]);
 }
 
