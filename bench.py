@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="patterns in the timed CPU sample")
+    ap.add_argument("--no-variants", action="store_true", help="skip timing the other methods")
     return ap.parse_args()
 
 
@@ -190,7 +191,7 @@ def main():
     plan = bd._device_plan(local)
     method = args.method
     if method is None:
-        method = "fused16" if plan.supported("fused16") else "plain"
+        method = "fused" if plan.supported("fused") else "plain"
     if method.startswith("fused") and not plan.supported(method):
         method = "plain"
     from pyebsdindex_gb300 import _lib
@@ -215,7 +216,6 @@ def main():
     }
     ptrs = {k: v.data_ptr() for k, v in outs.items()}
     stream = torch.cuda.current_stream(dev)
-    plan.reserve(method, N if method.startswith("fused") else 16384)
 
     def step():
         plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, N, ptrs, method, stream=stream.cuda_stream)
@@ -287,6 +287,25 @@ def main():
                "d2h_bytes_per_step": N * nB * 41}
         del host, hout
 
+    # the other methods on the same device-resident input, for the batched-vs-plain comparison
+    variants = {}
+    if not args.no_variants:
+        for vm, vn in (("plain", min(N, 131072)), ("fused", N), ("fused16", N)):
+            if vm == method or (vm.startswith("fused") and not plan.supported(vm)):
+                continue
+            def vstep():
+                plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, vn, ptrs, vm, stream=stream.cuda_stream)
+            vstep()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(2):
+                vstep()
+            b.record(stream)
+            torch.cuda.synchronize()
+            variants[vm] = vn * 2 / (a.elapsed_time(b) / 1000.0)
+        variants[method] = value / world
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
@@ -307,6 +326,7 @@ def main():
                        "method": method, "patterns_per_step": N, "distinct_patterns": len(pool),
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "variants_patterns_per_s": variants,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))
