@@ -36,6 +36,7 @@ extern "C" {
 #define EBSD_E_UNSUPPORTED (-5)/* plan shape outside what a method supports              */
 #define EBSD_E_DEVICE (-6)     /* no usable CUDA device / wrong device                    */
 #define EBSD_E_TIMEOUT (-7)    /* a bounded device-side wait gave up                      */
+#define EBSD_E_SCRATCH (-8)    /* request needs more scratch than the static array holds   */
 
 /* ---- pattern element types (BandDetect.find_bands accepts uint8, uint16, float32) ---- */
 #define EBSD_U8 0
@@ -123,6 +124,21 @@ int ebsd_find_bands_host(ebsd_plan_t plan, int method, int dtype, const void* h_
 /* Number of kernel launches the last ebsd_find_bands / ebsd_find_bands_host call on this
  * plan issued (for launch accounting by benchmarks). */
 int64_t ebsd_last_launch_count(ebsd_plan_t plan);
+
+/* Band detection that allocates nothing -- no counterpart in the reference, which always
+ * allocates per chunk (band_detect.py:425, band_detect_cl.py:252-286).  For callers that may
+ * not allocate device memory: applications whose device memory belongs to their framework's
+ * pool allocator, and streaming loops that must keep a fixed footprint because
+ * cudaMalloc/cudaFree can synchronise the device.  Runs the EBSD_PLAIN_F32 kernels on device
+ * buffers (same results as ebsd_find_bands with EBSD_PLAIN_F32), with their scratch in a
+ * 64 MiB file-scope device array that every GPU loading the library holds until exit.
+ * At most floor((64 MiB - 1 KiB - 4*ksz_rho*ksz_theta) / (12*(nRho+2*pad_rho)*(nTheta+
+ * 2*pad_theta) + nRho*nTheta + 8)) patterns per call (183 at 80x80, nRho 120, nTheta 180);
+ * larger n returns EBSD_E_SCRATCH.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, device current) and caches it: make that first call before
+ * any stream capture.  All calls share the array; calls that overlap on the GPU race. */
+int ebsd_find_bands_static(ebsd_plan_t plan, int dtype, const void* d_pats, int64_t n,
+                           const ebsd_bands* d_out, void* stream);
 
 /* Text for a status code. */
 const char* ebsd_strerror(int code);

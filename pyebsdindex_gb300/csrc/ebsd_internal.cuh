@@ -106,6 +106,10 @@ inline size_t elem_size(int dtype) {
 size_t plain_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);
 int plain_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches);
+// The same with an explicit workspace of plain_workspace_bytes(p, method, n) bytes.
+int plain_run_chunk_ws(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
+                       const ebsd_bands* out, int64_t out_offset, cudaStream_t st,
+                       int64_t* launches, void* workspace);
 
 // Fused path: fused.cu -------------------------------------------------------------------
 int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d);

@@ -263,9 +263,8 @@ size_t ws_bytes(const ebsd_plan_s* p, int64_t chunk) {
 
 template <typename T, typename InT>
 int run_chunk_t(ebsd_plan_s* p, const InT* d_pats, int64_t n, const ebsd_bands* out,
-                int64_t out_offset, cudaStream_t st, int64_t* launches) {
+                int64_t out_offset, cudaStream_t st, int64_t* launches, char* ws) {
     size_t cells = (size_t)p->R * p->Tp;
-    char* ws = (char*)p->ws.ptr;
     T* radon = (T*)ws;
     T* conv = radon + cells * n;
     T* tmp = conv + cells * n;
@@ -302,19 +301,27 @@ size_t plain_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk) {
 
 int plain_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
+    return plain_run_chunk_ws(p, method, dtype, d_pats, n, out, out_offset, st, launches,
+                              p->ws.ptr);
+}
+
+int plain_run_chunk_ws(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
+                       const ebsd_bands* out, int64_t out_offset, cudaStream_t st,
+                       int64_t* launches, void* workspace) {
+    char* ws = (char*)workspace;
     if (n <= 0) return EBSD_OK;
     if (n > 65535) return EBSD_E_ARG;
     if (method == EBSD_PLAIN_F64) {
         switch (dtype) {
-            case EBSD_U8: return run_chunk_t<double>(p, (const uint8_t*)d_pats, n, out, out_offset, st, launches);
-            case EBSD_U16: return run_chunk_t<double>(p, (const uint16_t*)d_pats, n, out, out_offset, st, launches);
-            case EBSD_F32: return run_chunk_t<double>(p, (const float*)d_pats, n, out, out_offset, st, launches);
+            case EBSD_U8: return run_chunk_t<double>(p, (const uint8_t*)d_pats, n, out, out_offset, st, launches, ws);
+            case EBSD_U16: return run_chunk_t<double>(p, (const uint16_t*)d_pats, n, out, out_offset, st, launches, ws);
+            case EBSD_F32: return run_chunk_t<double>(p, (const float*)d_pats, n, out, out_offset, st, launches, ws);
         }
     } else {
         switch (dtype) {
-            case EBSD_U8: return run_chunk_t<float>(p, (const uint8_t*)d_pats, n, out, out_offset, st, launches);
-            case EBSD_U16: return run_chunk_t<float>(p, (const uint16_t*)d_pats, n, out, out_offset, st, launches);
-            case EBSD_F32: return run_chunk_t<float>(p, (const float*)d_pats, n, out, out_offset, st, launches);
+            case EBSD_U8: return run_chunk_t<float>(p, (const uint8_t*)d_pats, n, out, out_offset, st, launches, ws);
+            case EBSD_U16: return run_chunk_t<float>(p, (const uint16_t*)d_pats, n, out, out_offset, st, launches, ws);
+            case EBSD_F32: return run_chunk_t<float>(p, (const float*)d_pats, n, out, out_offset, st, launches, ws);
         }
     }
     return EBSD_E_DTYPE;

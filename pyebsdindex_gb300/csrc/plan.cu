@@ -118,6 +118,7 @@ const char* ebsd_strerror(int code) {
         case EBSD_E_UNSUPPORTED: return "plan shape not supported by this method";
         case EBSD_E_DEVICE: return "no usable CUDA device";
         case EBSD_E_TIMEOUT: return "a bounded device-side wait timed out";
+        case EBSD_E_SCRATCH: return "request needs more scratch than the library's 64 MiB static device array holds";
         default: return "unknown error";
     }
 }
