@@ -140,6 +140,24 @@ int64_t ebsd_last_launch_count(ebsd_plan_t plan);
 int ebsd_find_bands_static(ebsd_plan_t plan, int dtype, const void* d_pats, int64_t n,
                            const ebsd_bands* d_out, void* stream);
 
+/* NLPAR noise estimate (NLPAR.sigma_numba, nlpar_cpu.py:753-796, nn = 1): for each of the
+ * nrows x ncols scan pixels, sqrt of the minimum over its clipped 3x3 neighbourhood of
+ * SSD / (2 n) over the masked pixels d_indices[nind] whose values are both below the
+ * saturation level (0.9961 * datamax, or datamax + 1 without saturation protection).
+ * d_data [nrows*ncols][npx] float32 (device); d_sigma [nrows*ncols] float32 (device). */
+int ebsd_nlpar_sigma(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+                     const int32_t* d_indices, int32_t nind, float datamax, int saturation_protect,
+                     float* d_sigma, void* stream);
+
+/* NLPAR weighted neighbour average (NLPAR.nlpar_nb, nlpar_cpu.py:821-936) over a
+ * (2 sr + 1)^2 search window (0 <= sr <= 10, shifted inward at the scan edges): d_out
+ * [nrows*ncols][npx] float32.  d_work: caller-provided device scratch of
+ * nrows*ncols*(2 sr + 1)^2 floats (the normalised window weights). */
+int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+               const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
+               float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
+               float* d_out, void* stream);
+
 /* Text for a status code. */
 const char* ebsd_strerror(int code);
 

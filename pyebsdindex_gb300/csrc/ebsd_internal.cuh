@@ -26,6 +26,9 @@ struct FusedGeom {
     int crow0 = 0, crow1 = 0, ccol0 = 0, ccol1 = 0;
     int tile_pitch = 0;         // pattern tile row pitch (elements)
     float ksum = 0.0f;          // sum of the LoG taps
+    int nGroups = 0;            // 32-ray groups of the fused LUT
+    int nRaysPad = 0;           // nGroups * 32
+    int gpt = 0;                // groups per theta column (ceil(nRho / 32))
 };
 
 struct Workspace {
@@ -51,6 +54,7 @@ struct ebsd_plan_s {
     int32_t* d_count = nullptr;    // [nRays]
     uint8_t* d_rdnmask = nullptr;  // [nRays]
     float* d_kernel = nullptr;     // [k0*k1]
+    std::vector<float> h_kernel;   // host copy of the taps (fused-kernel parameters)
     double* d_kernel64 = nullptr;  // [k0*k1]
     double* d_theta = nullptr;     // [nTheta] degrees (float32 values widened)
     double* d_rho = nullptr;       // [nRho]
@@ -60,7 +64,7 @@ struct ebsd_plan_s {
     // fused-kernel tables
     ebsd::FusedGeom fg;
     uint16_t* d_flut = nullptr;    // fused LUT (see fused.cu)
-    int32_t* d_fgroup = nullptr;   // per-ray entry counts, theta-major ray order
+    int32_t* d_fgroup = nullptr;   // [nRaysPad] entry counts, then [nGroups] chunks per group
     float* d_fray = nullptr;       // [nPx] weights: sum_px w*pixel = mean of the non-empty rays
     int64_t flut_entries = 0;
 

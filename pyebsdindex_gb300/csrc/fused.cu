@@ -36,14 +36,15 @@ struct FusedArgs {
     const void* pats;
     int64_t n;
     int H, W, nPx, pitch;      // pattern tile pitch (W + 1); zero word at H*pitch
-    const uint4* lut;          // [chunks][nRays][8] u16 tile offsets, ray order theta-major
-    const int32_t* count;      // [nRays] theta-major
-    int nRays, nRho, nTheta;
+    const uint4* lut;          // [chunks][nRaysPad][8] u16 tile offsets, ray order theta-major
+    const int32_t* count;      // [nRaysPad] entries per ray (group-major, lane-minor)
+    const int32_t* gchunks;    // [nGroups] chunks walked by each 32-ray group
+    int nRays, nRaysPad, nGroups, gpt, nRho, nTheta;  // gpt: 32-ray groups per theta column
     int p0, p1, R, Tp;
     int row0, col0, TR, TC;    // Radon tile origin (padded frame) and extent
     int crow0, ccol0, CR, CC;  // conv tile origin and extent
     int statR1;                // end row of the statistics slice (padded frame)
-    const float* kernel;       // [K0*K1]
+    float taps[81];            // LoG taps [K0*K1] (parameter space: FMA operands, no loads)
     float ksum;                // sum of the kernel taps (FP16 centring correction)
     const float* wimg;         // [nPx] pixel weights whose dot product is the Radon mean
     const uint8_t* rdnmask;    // [nRho][nTheta]
@@ -109,8 +110,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     float* conv = (float*)(smem + off);
     float* pat = conv;  // aliased: the pattern tile is dead once the Radon is built
     off += ((size_t)a.CR * a.CC * sizeof(float) + 15) & ~(size_t)15;
-    float* kern = (float*)(smem + off);
-    off += ((size_t)K0 * K1 * sizeof(float) + 15) & ~(size_t)15;
     float* lv_s = (float*)(smem + off);
     off += kWarps * kMaxBands * sizeof(float);
     int* lp_s = (int*)(smem + off);
@@ -118,8 +117,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     double* red_d = (double*)(smem + off);
     off += 32 * sizeof(double);
     float* red_f = (float*)(smem + off);  // 66 floats
+    off += 80 * sizeof(float);
+    int* gch_s = (int*)(smem + off);      // nGroups ints
 
-    for (int i = tid; i < K0 * K1; i += kThreads) kern[i] = a.kernel[i];
+    for (int i = tid; i < a.nGroups; i += kThreads) gch_s[i] = a.gchunks[i];
+    __syncthreads();
     const int nB = a.kc.nB;
     const int stat_r0 = a.p0, stat_r1 = a.statR1, stat_c0 = a.p1, stat_c1 = a.p1 + a.nTheta;
     const int stat_count = (stat_r1 - stat_r0) * (stat_c1 - stat_c0);
@@ -128,14 +130,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         // ---- 1. load the pattern into the FP32 tile (pitch W+1, zero word after it) ----
         const InT* gp = (const InT*)a.pats + q * (int64_t)a.nPx;
         float wsum = 0.0f, pmin = -1.0f, pmax = -1.0f;  // -1: value of an empty ray
-        for (int i = tid; i < a.nPx; i += kThreads) {
-            int y = i / a.W, x = i - (i / a.W) * a.W;
-            float v = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
-            pat[y * a.pitch + x] = v;
-            if (kHalf) {
-                wsum = fmaf(a.wimg[i], v, wsum);
-                pmin = fminf(pmin, v);
-                pmax = fmaxf(pmax, v);
+        for (int y = warp; y < a.H; y += kWarps) {
+            for (int x = lane; x < a.W; x += 32) {
+                const int i = y * a.W + x;
+                float v = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
+                pat[y * a.pitch + x] = v;
+                if (kHalf) {
+                    wsum = fmaf(a.wimg[i], v, wsum);
+                    pmin = fminf(pmin, v);
+                    pmax = fmaxf(pmax, v);
+                }
             }
         }
         if (tid == 0) pat[a.H * a.pitch] = 0.0f;
@@ -177,47 +181,89 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             inv_scl = 1.0f / scl;  // exact: scl is a power of two
         }
 
-        // ---- 2. Radon: thread per ray, sequential FP32 sum in LUT order ----
-        for (int t = tid; t < a.nRays; t += kThreads) {
-            int cnt = a.count[t];
+        // ---- 2. Radon: one ray per lane, sequential FP32 sum in LUT order ----
+        // Warp w takes ray groups w, w+32, ... (32 consecutive theta-major rays: neighbouring
+        // rho at one theta, i.e. parallel lines); every lane walks the group's chunk count,
+        // short rays being padded with zero-word entries (adding +0.0 leaves the sum as it
+        // is), so the loop is warp-uniform.  The LUT loads of the next kRing chunks are kept in
+        // flight in a register ring across ray boundaries.
+        {
+            constexpr int kRing = 8;
+            const unsigned zw = (unsigned)(a.H * a.pitch) * 0x10001u;
+            const uint4 zero4 = make_uint4(zw, zw, zw, zw);
+            int ig = warp, ic = 0, inch = ig < a.nGroups ? gch_s[ig] : 0;
+            uint4 ring[kRing];
+            auto issue = [&](uint4& slot) {
+                if (ig < a.nGroups) {
+                    slot = __ldg(a.lut + ((size_t)ic * a.nRaysPad + ig * 32 + lane));
+                    if (++ic == inch) {
+                        ig += kWarps;
+                        ic = 0;
+                        inch = ig < a.nGroups ? gch_s[ig] : 0;
+                    }
+                } else {
+                    slot = zero4;
+                }
+            };
+#pragma unroll
+            for (int k = 0; k < kRing; ++k) issue(ring[k]);
+            int pg = warp, pc = 0, pnch = pg < a.nGroups ? gch_s[pg] : 0;
+            int cnt = pg < a.nGroups ? __ldg(a.count + pg * 32 + lane) : 0;
             float sum = 0.0f;
-            int nch = (cnt + 7) >> 3;
-            const uint4* lp = a.lut + t;
-            for (int g = 0; g < nch; ++g) {
-                uint4 e = __ldg(lp + (size_t)g * a.nRays);
-                sum = __fadd_rn(sum, pat[e.x & 0xFFFF]);
-                sum = __fadd_rn(sum, pat[e.x >> 16]);
-                sum = __fadd_rn(sum, pat[e.y & 0xFFFF]);
-                sum = __fadd_rn(sum, pat[e.y >> 16]);
-                sum = __fadd_rn(sum, pat[e.z & 0xFFFF]);
-                sum = __fadd_rn(sum, pat[e.z >> 16]);
-                sum = __fadd_rn(sum, pat[e.w & 0xFFFF]);
-                sum = __fadd_rn(sum, pat[e.w >> 16]);
+            while (pg < a.nGroups) {
+#pragma unroll
+                for (int k = 0; k < kRing; ++k) {
+                    if (pg < a.nGroups) {
+                        uint4 e = ring[k];
+                        issue(ring[k]);
+                        sum = __fadd_rn(sum, pat[e.x & 0xFFFF]);
+                        sum = __fadd_rn(sum, pat[e.x >> 16]);
+                        sum = __fadd_rn(sum, pat[e.y & 0xFFFF]);
+                        sum = __fadd_rn(sum, pat[e.y >> 16]);
+                        sum = __fadd_rn(sum, pat[e.z & 0xFFFF]);
+                        sum = __fadd_rn(sum, pat[e.z >> 16]);
+                        sum = __fadd_rn(sum, pat[e.w & 0xFFFF]);
+                        sum = __fadd_rn(sum, pat[e.w >> 16]);
+                        if (++pc == pnch) {
+                            const int j = pg / a.gpt, i = (pg - j * a.gpt) * 32 + lane;
+                            if (i < a.nRho) {
+                                float v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
+                                if (kHalf) v = (v - cen) * scl;
+                                tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(v);
+                            }
+                            pg += kWarps;
+                            pc = 0;
+                            sum = 0.0f;
+                            if (pg < a.nGroups) {
+                                pnch = gch_s[pg];
+                                cnt = __ldg(a.count + pg * 32 + lane);
+                            }
+                        }
+                    }
+                }
             }
-            float v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
-            if (kHalf) v = (v - cen) * scl;
-            int j = t / a.nRho, i = t - (t / a.nRho) * a.nRho;
-            tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(v);
         }
         __syncthreads();
 
         // ---- 3. pad the tile around the interior ----
-        for (int c = tid; c < a.TR * a.TC; c += kThreads) {
-            int tr = c / a.TC, tc = c - (c / a.TC) * a.TC;
-            int r = tr + a.row0, col = tc + a.col0;
-            int i = r - a.p0, j = col - a.p1;
-            if (i >= 0 && i < a.nRho && j >= 0 && j < a.nTheta) continue;
-            S val;
-            if (r < 0 || r >= a.R) {
-                val = to_store<S>(kHalf ? -cen * scl : 0.0f);
-            } else {
-                int ic = i < 0 ? 0 : (i >= a.nRho ? a.nRho - 1 : i);
-                int si = ic, sj = j;
-                if (j < 0) { si = a.nRho - 1 - ic; sj = a.nTheta + j; }
-                else if (j >= a.nTheta) { si = a.nRho - 1 - ic; sj = j - a.nTheta; }
-                val = tile[(si + a.p0 - a.row0) * a.TC + (sj + a.p1 - a.col0)];
+        for (int tr = warp; tr < a.TR; tr += kWarps) {
+            const int r = tr + a.row0, i = r - a.p0;
+            const bool row_in = i >= 0 && i < a.nRho;
+            const int ic = i < 0 ? 0 : (i >= a.nRho ? a.nRho - 1 : i);
+            for (int tc = lane; tc < a.TC; tc += 32) {
+                const int j = tc + a.col0 - a.p1;
+                if (row_in && j >= 0 && j < a.nTheta) continue;
+                S val;
+                if (r < 0 || r >= a.R) {
+                    val = to_store<S>(kHalf ? -cen * scl : 0.0f);
+                } else {
+                    int si = ic, sj = j;
+                    if (j < 0) { si = a.nRho - 1 - ic; sj = a.nTheta + j; }
+                    else if (j >= a.nTheta) { si = a.nRho - 1 - ic; sj = j - a.nTheta; }
+                    val = tile[(si + a.p0 - a.row0) * a.TC + (sj + a.p1 - a.col0)];
+                }
+                tile[tr * a.TC + tc] = val;
             }
-            tile[c] = val;
         }
         __syncthreads();
 
@@ -249,7 +295,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                         int ka = o + 2 * H0 - t;
                         if (ka >= 0 && ka < K0) {
 #pragma unroll
-                            for (int b = 0; b < K1; ++b) acc[o] = fmaf(kern[ka * K1 + b], v[b], acc[o]);
+                            for (int b = 0; b < K1; ++b) acc[o] = fmaf(a.taps[ka * K1 + b], v[b], acc[o]);
                         }
                     }
                 }
@@ -407,11 +453,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 // ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
-size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1) {
+size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1, int ngroups) {
     size_t b = ((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store + 15) & ~(size_t)15;
     b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
-    b += ((size_t)k0 * k1 * 4 + 15) & ~(size_t)15;
     b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
+    b += (size_t)ngroups * 4;
     return b;
 }
 
@@ -459,8 +505,9 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         g.col1 = g.ccol1 + H1;
         g.tile_pitch = pitch;
         g.threads = kThreads;
-        g.smem_f32 = (int)smem_bytes(g, 4, K0, K1);
-        g.smem_f16 = (int)smem_bytes(g, 2, K0, K1);
+        int ngroups = p->nTheta * ((p->nRho + 31) / 32);  // 32-ray groups of the fused LUT
+        g.smem_f32 = (int)smem_bytes(g, 4, K0, K1, ngroups);
+        g.smem_f16 = (int)smem_bytes(g, 2, K0, K1, ngroups);
         size_t conv_cells = (size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0);
         int dev_smem = 0;
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
@@ -470,46 +517,103 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     p->fg = g;
     if (!g.ok) return EBSD_OK;
 
-    // LUT: rays in theta-major order, 8 entries per uint4, entry = tile offset y*pitch + x;
-    // padding entries point at the zero word after the pattern (adding +0.0 leaves a sum
-    // unchanged, so the reference's summation order is kept).
-    const int nRays = p->nRays, L = d->lut_len;
-    std::vector<int32_t> cnt(nRays);
-    int maxc = 0;
-    for (int j = 0; j < p->nTheta; ++j)
-        for (int i = 0; i < p->nRho; ++i) {
+    // LUT: groups of 32 consecutive rho at one theta (rho padded to a multiple of 32).  When
+    // every ray of a group has at most one pixel per image column (the sampling of rays with
+    // |sin theta| >= sqrt(2)/2, radon_fast.py:113-133), slot s of every lane is column
+    // base + s: a warp then reads one column at distinct rows of the odd-pitch tile, free of
+    // bank conflicts.  Likewise per row for the other family (radon_fast.py:134-158); a group
+    // that fits neither (a custom maskindex) keeps each ray's own sorted order.  Entries are
+    // tile offsets y*pitch + x; empty slots point at the zero word after the pattern.  Integer
+    // pixel sums are exact in float32 whatever the order; for background-subtracted or float
+    // patterns the slot order changes the ray sums at rounding level only.
+    const int L = d->lut_len;
+    const int gpt = (p->nRho + 31) / 32;  // groups per theta column
+    const int nGroups = p->nTheta * gpt;
+    const int nRaysPad = nGroups * 32;
+    const uint16_t zero = (uint16_t)(p->H * pitch);
+    std::vector<int32_t> cnt(nRaysPad, 0), gch(nGroups, 1), gaxis(nGroups, 2), gbase(nGroups, 0);
+    std::vector<char> seen((size_t)std::max(p->W, p->H));
+    int nch = 1;
+    for (int g = 0; g < nGroups; ++g) {
+        int j = g / gpt, i0 = (g % gpt) * 32;
+        bool colok = true, rowok = true;
+        int xmin = 1 << 30, xmax = -1, ymin = 1 << 30, ymax = -1, maxc = 0;
+        for (int l = 0; l < 32; ++l) {
+            int i = i0 + l;
+            if (i >= p->nRho) continue;
             const int64_t* ray = d->lut + ((size_t)i * p->nTheta + j) * L;
             int c = 0;
             while (c < L && ray[c] >= 0 && ray[c] < p->nPx) ++c;
-            cnt[j * p->nRho + i] = c;
+            cnt[g * 32 + l] = c;
             maxc = std::max(maxc, c);
+            std::fill(seen.begin(), seen.end(), 0);
+            for (int k = 0; k < c; ++k) {
+                int x = (int)(ray[k] % p->W);
+                if (seen[x]) colok = false;
+                seen[x] = 1;
+                xmin = std::min(xmin, x);
+                xmax = std::max(xmax, x);
+            }
+            std::fill(seen.begin(), seen.end(), 0);
+            for (int k = 0; k < c; ++k) {
+                int y = (int)(ray[k] / p->W);
+                if (seen[y]) rowok = false;
+                seen[y] = 1;
+                ymin = std::min(ymin, y);
+                ymax = std::max(ymax, y);
+            }
         }
-    int nch = std::max(1, (maxc + 7) / 8);
-    const uint16_t zero = (uint16_t)(p->H * pitch);
-    std::vector<uint16_t> lut((size_t)nch * nRays * 8, zero);
-    for (int j = 0; j < p->nTheta; ++j)
-        for (int i = 0; i < p->nRho; ++i) {
-            int t = j * p->nRho + i;
+        int nslot;
+        if (maxc == 0) {
+            nslot = 0;
+        } else if (colok) {
+            gaxis[g] = 0;
+            gbase[g] = xmin;
+            nslot = xmax - xmin + 1;
+        } else if (rowok) {
+            gaxis[g] = 1;
+            gbase[g] = ymin;
+            nslot = ymax - ymin + 1;
+        } else {
+            nslot = maxc;
+        }
+        gch[g] = std::max(1, (nslot + 7) / 8);
+        nch = std::max(nch, gch[g]);
+    }
+    std::vector<uint16_t> lut((size_t)nch * nRaysPad * 8, zero);
+    for (int g = 0; g < nGroups; ++g) {
+        int j = g / gpt, i0 = (g % gpt) * 32;
+        for (int l = 0; l < 32; ++l) {
+            int i = i0 + l;
+            if (i >= p->nRho) continue;
+            int t = g * 32 + l;
             const int64_t* ray = d->lut + ((size_t)i * p->nTheta + j) * L;
             for (int k = 0; k < cnt[t]; ++k) {
                 int idx = (int)ray[k];
                 int y = idx / p->W, x = idx - (idx / p->W) * p->W;
-                lut[((size_t)(k / 8) * nRays + t) * 8 + (k % 8)] = (uint16_t)(y * pitch + x);
+                int slot = gaxis[g] == 0 ? x - gbase[g] : (gaxis[g] == 1 ? y - gbase[g] : k);
+                lut[((size_t)(slot / 8) * nRaysPad + t) * 8 + (slot % 8)] = (uint16_t)(y * pitch + x);
             }
         }
+    }
+    p->fg.nGroups = nGroups;
+    p->fg.nRaysPad = nRaysPad;
+    p->fg.gpt = gpt;
     // weight image: mean over non-empty rays of the ray means = sum_px w[px] * value[px]
     {
         std::vector<double> w(p->nPx, 0.0);
         int nonempty = 0;
-        for (int t = 0; t < nRays; ++t) nonempty += cnt[t] > 0;
-        for (int j = 0; j < p->nTheta; ++j)
-            for (int i = 0; i < p->nRho; ++i) {
-                int t = j * p->nRho + i;
-                if (!cnt[t]) continue;
+        for (int t = 0; t < nRaysPad; ++t) nonempty += cnt[t] > 0;
+        for (int g = 0; g < nGroups; ++g) {
+            int j = g / gpt, i0 = (g % gpt) * 32;
+            for (int l = 0; l < 32; ++l) {
+                int i = i0 + l, t = g * 32 + l;
+                if (i >= p->nRho || !cnt[t]) continue;
                 const int64_t* ray = d->lut + ((size_t)i * p->nTheta + j) * L;
                 double f = 1.0 / ((double)cnt[t] * std::max(nonempty, 1));
                 for (int k = 0; k < cnt[t]; ++k) w[ray[k]] += f;
             }
+        }
         std::vector<float> wf(w.begin(), w.end());
         EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fray, wf.size() * sizeof(float)));
         EBSD_CUDA_TRY(cudaMemcpy(p->d_fray, wf.data(), wf.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -519,8 +623,9 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     }
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_flut, lut.size() * sizeof(uint16_t)));
     EBSD_CUDA_TRY(cudaMemcpy(p->d_flut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
-    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, nRays * sizeof(int32_t)));
-    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup, cnt.data(), nRays * sizeof(int32_t), cudaMemcpyHostToDevice));
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, (nRaysPad + nGroups) * sizeof(int32_t)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup, cnt.data(), nRaysPad * sizeof(int32_t), cudaMemcpyHostToDevice));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup + nRaysPad, gch.data(), nGroups * sizeof(int32_t), cudaMemcpyHostToDevice));
     p->flut_entries = (int64_t)lut.size();
     return EBSD_OK;
 }
@@ -565,7 +670,11 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.pitch = g.tile_pitch;
     a.lut = (const uint4*)p->d_flut;
     a.count = p->d_fgroup;
+    a.gchunks = p->d_fgroup + g.nRaysPad;
+    a.gpt = g.gpt;
     a.nRays = p->nRays;
+    a.nRaysPad = g.nRaysPad;
+    a.nGroups = g.nGroups;
     a.nRho = p->nRho;
     a.nTheta = p->nTheta;
     a.p0 = p->p0;
@@ -581,7 +690,7 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.CR = g.crow1 - g.crow0;
     a.CC = g.ccol1 - g.ccol0;
     a.statR1 = std::min(p->R, p->Tp - p->p0);
-    a.kernel = p->d_kernel;
+    for (int k = 0; k < p->k0 * p->k1 && k < 81; ++k) a.taps[k] = p->h_kernel[k];
     a.ksum = g.ksum;
     a.wimg = p->d_fray;
     a.rdnmask = p->d_rdnmask;

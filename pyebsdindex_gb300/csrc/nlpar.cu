@@ -1,0 +1,173 @@
+// NLPAR (non-local pattern averaging) on the device: the noise estimate and the weighted
+// neighbour average that run in front of band detection.
+//
+//   k_nlpar_sigma    NLPAR.sigma_numba, nlpar_cpu.py:753-796 (nn = 1): min over the clipped
+//                    3x3 scan neighbourhood of SSD / (2 n), then sqrt
+//   k_nlpar_weights  NLPAR.nlpar_nb, nlpar_cpu.py:866-927: normalised pair distance to each
+//                    pattern of the (2 sr + 1)^2 window (shifted inward at the scan edges),
+//                    weight exp(-max(d - dthresh, 0) / lam^2), centre weight 1, normalised
+//   k_nlpar_average  nlpar_cpu.py:929-934: weighted sum over the window for every pixel
+//
+// The float32 arithmetic keeps the reference's order: squared differences accumulate
+// sequentially over the masked-pixel list, window weights are summed and applied in window
+// order, and every add/mul is an explicitly rounded intrinsic (no contracted FMAs).
+#include "ebsd_internal.cuh"
+
+namespace ebsd {
+namespace {
+
+__device__ __forceinline__ void window(int i, int sr, int n, int& start, int& end) {
+    int a = i - sr > 0 ? i - sr : 0;
+    int b = i + sr - (n - 1) > 0 ? i + sr - (n - 1) : 0;
+    start = a - b;
+    int c = i + sr < n - 1 ? i + sr : n - 1;
+    int e = sr - i > 0 ? sr - i : 0;
+    end = c + e + 1;
+}
+
+// Sequential float32 SSD over the masked pixels where both values are below mxval.
+__device__ __forceinline__ void pair_ssd(const float* __restrict__ a, const float* __restrict__ b,
+                                         const int32_t* __restrict__ ind, int nind, float mxval,
+                                         float n_init, float& d2, float& n2) {
+    float d = 0.0f, n = n_init;
+    for (int q = 0; q < nind; ++q) {
+        int k = __ldg(ind + q);
+        float x = __ldg(a + k), y = __ldg(b + k);
+        if (y < mxval && x < mxval) {
+            n = __fadd_rn(n, 1.0f);
+            float t = __fsub_rn(x, y);
+            d = __fadd_rn(d, __fmul_rn(t, t));
+        }
+    }
+    d2 = d;
+    n2 = n;
+}
+
+// One warp per 4 scan pixels, 8 lanes per pixel (one neighbour each), min over the lanes.
+__global__ void k_nlpar_sigma(const float* __restrict__ data, int nrows, int ncols, int npx,
+                              const int32_t* __restrict__ ind, int nind, float mxval,
+                              float* __restrict__ sigma) {
+    int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    int pix = gt >> 3, slot = gt & 7;
+    int npix = nrows * ncols;
+    float s0 = 1e24f;
+    if (pix < npix) {
+        int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+        int k = slot < 4 ? slot : slot + 1;  // skip the centre of the 3x3 block
+        int jn = j + k / 3 - 1, inn = i + k % 3 - 1;
+        if (jn >= 0 && jn < nrows && inn >= 0 && inn < ncols) {
+            float d2, n2;
+            pair_ssd(data + (int64_t)pix * npx, data + (int64_t)(inn + ncols * jn) * npx, ind, nind, mxval,
+                     1.0e-12f, d2, n2);
+            if (d2 >= 1.e-3f) s0 = __fdiv_rn(d2, __fmul_rn(n2, 2.0f));
+        }
+    }
+    for (int o = 4; o > 0; o >>= 1) s0 = fminf(s0, __shfl_down_sync(0xffffffffu, s0, o, 8));
+    if (slot == 0 && pix < npix) sigma[pix] = sqrtf(s0);
+}
+
+// One block per scan pixel, one thread per window slot.
+__global__ void k_nlpar_weights(const float* __restrict__ data, int nrows, int ncols, int npx,
+                                const int32_t* __restrict__ ind, int nind, float mxval,
+                                const float* __restrict__ sigma, float lam2, float dthresh, int sr,
+                                float* __restrict__ wout) {
+    extern __shared__ float w_s[];
+    __shared__ float tot_s;
+    int pix = blockIdx.x;
+    int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+    int xs, xe, ys, ye;
+    window(i, sr, ncols, xs, xe);
+    window(j, sr, nrows, ys, ye);
+    int wx = xe - xs, winsz = (2 * sr + 1) * (2 * sr + 1);
+    int c = threadIdx.x;
+    if (c < winsz) {
+        int jn = ys + c / wx, inn = xs + c % wx;
+        int nb = inn + ncols * jn;
+        float w;
+        if (nb == pix) {
+            w = -1.0e6f;
+        } else {
+            float s0 = sigma[pix], s1 = sigma[nb];
+            s0 = __fmul_rn(s0, s0);
+            s1 = __fmul_rn(s1, s1);
+            float d2, n2;
+            pair_ssd(data + (int64_t)pix * npx, data + (int64_t)nb * npx, ind, nind, mxval, 0.0f, d2, n2);
+            float ss = __fadd_rn(s0, s1);
+            d2 = __fsub_rn(d2, __fmul_rn(n2, ss));
+            float dnorm = __fmul_rn(ss, sqrtf(__fmul_rn(2.0f, n2)));
+            w = dnorm > 1.e-8f ? __fdiv_rn(d2, dnorm) : __fmul_rn(1e6f, n2);
+        }
+        w = fmaxf(__fsub_rn(w, dthresh), 0.0f);
+        w = expf(__fmul_rn(__fmul_rn(-1.0f, w), lam2));
+        w_s[c] = w;
+    }
+    __syncthreads();
+    if (c == 0) {
+        float t = 0.0f;
+        for (int k = 0; k < winsz; ++k) t = __fadd_rn(t, w_s[k]);
+        tot_s = t;
+    }
+    __syncthreads();
+    if (c < winsz) wout[(int64_t)pix * winsz + c] = __fdiv_rn(w_s[c], tot_s);
+}
+
+// out[pix][k] = sum over the window, in window order, of data[nb][k] * w[pix][c].
+__global__ void k_nlpar_average(const float* __restrict__ data, int nrows, int ncols, int npx,
+                                const float* __restrict__ w, int sr, float* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int pix = blockIdx.y;
+    if (k >= npx) return;
+    int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+    int xs, xe, ys, ye;
+    window(i, sr, ncols, xs, xe);
+    window(j, sr, nrows, ys, ye);
+    int winsz = (2 * sr + 1) * (2 * sr + 1);
+    const float* wp = w + (int64_t)pix * winsz;
+    float acc = 0.0f;
+    int c = 0;
+    for (int jn = ys; jn < ye; ++jn)
+        for (int inn = xs; inn < xe; ++inn, ++c)
+            acc = __fadd_rn(acc, __fmul_rn(__ldg(data + (int64_t)(inn + ncols * jn) * npx + k), __ldg(wp + c)));
+    out[(int64_t)pix * npx + k] = acc;
+}
+
+}  // namespace
+}  // namespace ebsd
+
+using namespace ebsd;
+
+extern "C" {
+
+int ebsd_nlpar_sigma(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
+                     int32_t nind, float datamax, int saturation_protect, float* d_sigma, void* stream) {
+    if (!d_data || !d_indices || !d_sigma || nrows <= 0 || ncols <= 0 || npx <= 0 || nind < 0 || nind > npx)
+        return EBSD_E_ARG;
+    float mxval = saturation_protect ? datamax * 0.9961f : datamax + 1.0f;
+    int64_t threads = (int64_t)nrows * ncols * 8;
+    k_nlpar_sigma<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+        d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma);
+    return launch_status();
+}
+
+int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
+               int32_t nind, float datamax, float lam, int32_t sr, float dthresh, const float* d_sigma,
+               int saturation_protect, float* d_work, float* d_out, void* stream) {
+    if (!d_data || !d_indices || !d_sigma || !d_work || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 ||
+        nind < 0 || nind > npx || sr < 0 || sr > 10 || !(lam > 0.0f))
+        return EBSD_E_ARG;
+    if (2 * sr + 1 > nrows || 2 * sr + 1 > ncols) return EBSD_E_ARG;  // window must fit the scan
+    float mxval = saturation_protect ? datamax * 0.999f : datamax + 1.0f;
+    float lam2 = 1.0f / (lam * lam);
+    int winsz = (2 * sr + 1) * (2 * sr + 1);
+    int bs = ((winsz + 31) / 32) * 32;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_nlpar_weights<<<(unsigned)(nrows * ncols), bs, winsz * sizeof(float), st>>>(
+        d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma, lam2, dthresh, sr, d_work);
+    int rc = launch_status();
+    if (rc != EBSD_OK) return rc;
+    dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
+    k_nlpar_average<<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, d_out);
+    return launch_status();
+}
+
+}  // extern "C"

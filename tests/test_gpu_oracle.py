@@ -49,7 +49,7 @@ def test_matches_reference_arithmetic(cuda, geom, method):
     c = compare(out, ref)
     print(method, g["h"], c)
     if method == "fused16":
-        assert c["frac"] >= 0.98 and c["aveloc_p50"] <= 2e-3 and c["aveloc"] <= 0.1, c
+        assert c["frac"] >= 0.98 and c["aveloc_p50"] <= 2e-3 and c["aveloc_p99"] <= 3e-2, c
     else:
         assert c["frac"] >= 0.999, c
         assert c["aveloc"] <= 1e-3, c
@@ -65,7 +65,7 @@ def test_error_vs_fp64_gpu_oracle(cuda, geom, method):
     c = compare(out, ref64)
     print(method, "vs fp64", g["h"], c)
     if method == "fused16":
-        assert c["frac"] >= 0.98 and c["aveloc_p50"] <= 2e-3 and c["aveloc"] <= 0.1, c
+        assert c["frac"] >= 0.98 and c["aveloc_p50"] <= 2e-3 and c["aveloc_p99"] <= 3e-2, c
     else:
         assert c["frac"] >= 0.999, c
         assert c["aveloc"] <= 1e-3, c
