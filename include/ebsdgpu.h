@@ -55,6 +55,7 @@ extern "C" {
 #define EBSD_FUSED_F16 3
 
 typedef struct ebsd_plan_s* ebsd_plan_t;
+typedef struct ebsd_linop_s* ebsd_linop_t;
 
 /* Everything BandDetect.band_detect_setup (band_detect.py:138-294) derives for one pattern
  * size.  All pointers are HOST pointers, copied during ebsd_plan_create. */
@@ -157,6 +158,56 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
                const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
                float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
                float* d_out, void* stream);
+
+/* ---- differentiable path (no counterpart in the reference beyond the empty DIFF_NLPAR
+ * placeholder, nlpar.py:75-77) --------------------------------------------------------- */
+
+/* A sparse linear operator y = A x held on the device in CSR form (host arrays copied):
+ * rowptr[nrows+1] (int64), col[nnz] (int32, < ncols), val[nnz] (float).  Used for the
+ * Radon transform (val = 1/count over a ray's pixels, radon_fast.py:281-310), its transpose
+ * (back-projection), and the LoG-with-padding operator of band_detect.py:573-606 and its
+ * transpose.  The transpose is built on the host as its own operator, so both directions are
+ * gathers. */
+int ebsd_linop_create(int64_t nrows, int64_t ncols, const int64_t* rowptr, const int32_t* col,
+                      const float* val, int device, ebsd_linop_t* out);
+
+/* y[b] = A x[b] for b < n (n <= 65535); fp64 = 1 uses double values and double x / y. */
+int ebsd_linop_apply(ebsd_linop_t op, int fp64, const void* d_x, int64_t n, void* d_y, void* stream);
+
+int ebsd_linop_destroy(ebsd_linop_t op);
+
+/* NLPAR window weights of nlpar_nb (nlpar_cpu.py:866-927) exposed for differentiation:
+ * d_w[p][c] normalised weights, d_m[p][c] = max(d_pc - dthresh, 0) (0 for the centre), so
+ * that w_pc = exp(-m_pc / lam^2) / sum_c'.  Arrays nrows*ncols*(2 sr + 1)^2 floats. */
+int ebsd_nlpar_weights(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+                       const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
+                       float dthresh, const float* d_sigma, int saturation_protect, float* d_w,
+                       float* d_m, void* stream);
+
+/* y = W x with given window weights (the averaging step of nlpar_nb, nlpar_cpu.py:929-934). */
+int ebsd_nlpar_apply(const float* d_x, int32_t nrows, int32_t ncols, int32_t npx, const float* d_w,
+                     int32_t sr, float* d_out, void* stream);
+
+/* W^T g: the adjoint of ebsd_nlpar_apply. */
+int ebsd_nlpar_apply_t(const float* d_g, int32_t nrows, int32_t ncols, int32_t npx, const float* d_w,
+                       int32_t sr, float* d_out, void* stream);
+
+/* float64 forms of ebsd_nlpar_apply / ebsd_nlpar_apply_t (weights given as float64), for
+ * gradient checks of the differentiable path in double precision. */
+int ebsd_nlpar_apply64(const double* d_x, int32_t nrows, int32_t ncols, int32_t npx,
+                       const double* d_w, int32_t sr, double* d_out, void* stream);
+int ebsd_nlpar_apply_t64(const double* d_g, int32_t nrows, int32_t ncols, int32_t npx,
+                         const double* d_w, int32_t sr, double* d_out, void* stream);
+
+/* Per scan pixel p: sum_c dw_pc/dlambda (g_p . x_c) in float64 (d_out[nrows*ncols]); the sum
+ * over p is dL/dlambda for L with dL/dy = g. */
+int ebsd_nlpar_lambda_grad(const float* d_g, const float* d_x, int32_t nrows, int32_t ncols,
+                           int32_t npx, const float* d_w, const float* d_m, int32_t sr, float lam,
+                           double* d_out, void* stream);
+/* The same with float64 g and x. */
+int ebsd_nlpar_lambda_grad64(const double* d_g, const double* d_x, int32_t nrows, int32_t ncols,
+                             int32_t npx, const float* d_w, const float* d_m, int32_t sr, float lam,
+                             double* d_out, void* stream);
 
 /* Text for a status code. */
 const char* ebsd_strerror(int code);

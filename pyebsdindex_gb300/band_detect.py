@@ -362,3 +362,79 @@ class BandDetect(GPUFindBands):
         cx = (np.arange(nx) - nx * 0.5) ** 2
         cy = (np.arange(ny) - ny * 0.5) ** 2
         return np.sqrt(np.broadcast_to(cx.reshape(1, nx), (ny, nx)) + np.broadcast_to(cy, (nx, ny)).T)
+
+
+class MixedBandDetect:
+    """Band detection over a batch of patterns of different sizes.
+
+    The reference handles one pattern size per ``BandDetect`` plan (band_detect.py:138-155
+    rebuilds the plan when the size changes).  Here one plan is kept per size; a ragged batch is
+    split by size, every size group runs on its own plan and CUDA stream (the fused kernel where
+    its on-chip tile fits, the per-stage kernels otherwise), and the records come back in input
+    order.  uint16 patterns need a torch build with ``torch.uint16``; otherwise pass float32.  ``nRho`` for a size comes from ``nRho_for(H, W)`` (default 1.5 * min(H, W)).
+    """
+
+    def __init__(self, nTheta=180, nRho_for=None, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=10,
+                 mask_for=None, method="fused", gpu_id=0, **kwargs):
+        self.nTheta, self.tSigma, self.rSigma = nTheta, tSigma, rSigma
+        self.rhoMaskFrac, self.nBands, self.method, self.gpu_id = rhoMaskFrac, nBands, method, gpu_id
+        self.nRho_for = nRho_for or (lambda h, w: int(round(1.5 * min(h, w))))
+        self.mask_for = mask_for
+        self.kwargs = kwargs
+        self.plans = {}
+
+    def plan(self, h, w):
+        key = (int(h), int(w))
+        if key not in self.plans:
+            bd = BandDetect(nTheta=self.nTheta, nRho=self.nRho_for(h, w), tSigma=self.tSigma, rSigma=self.rSigma,
+                            rhoMaskFrac=self.rhoMaskFrac, nBands=self.nBands, gpu_id=self.gpu_id, **self.kwargs)
+            bd.band_detect_setup(patDim=key, patternmask=None if self.mask_for is None else self.mask_for(h, w))
+            self.plans[key] = bd
+        return self.plans[key]
+
+    def method_for(self, h, w):
+        bd = self.plan(h, w)
+        m = self.method
+        return m if not m.startswith("fused") or bd._device_plan().supported(m) else "plain"
+
+    def find_bands(self, patterns, method=None):
+        """patterns: sequence of [H, W] arrays (numpy or CUDA tensors), sizes mixed.
+        Returns an (n, nBands) record array in input order.  Size groups are launched on
+        separate CUDA streams without waiting for one another; results are gathered at the end."""
+        import torch
+        groups = {}
+        for k, p in enumerate(patterns):
+            groups.setdefault(tuple(p.shape[-2:]), []).append(k)
+        out = np.zeros((len(patterns), self.nBands), dtype=record_dtype(10))
+        dev = torch.device("cuda", self.gpu_id)
+        u16 = getattr(torch, "uint16", None)
+        pending = []
+        for key, idx in groups.items():
+            bd = self.plan(*key)
+            plan = bd._device_plan()
+            m = method or self.method_for(*key)
+            if m.startswith("fused") and not plan.supported(m):
+                m = "plain"
+            st = torch.cuda.Stream(device=dev)
+            with torch.cuda.stream(st):
+                batch = torch.stack([torch.as_tensor(patterns[k]) for k in idx]).to(dev, non_blocking=True)
+                if batch.dtype == torch.uint8:
+                    dt = _lib.EBSD_U8
+                elif u16 is not None and batch.dtype == u16:
+                    dt = _lib.EBSD_U16
+                else:
+                    batch = batch.to(torch.float32)
+                    dt = _lib.EBSD_F32
+                batch = batch.contiguous()
+                n, nB = len(idx), self.nBands
+                outs = {f: torch.empty((n, nB, 2) if f in ("maxloc", "aveloc") else (n, nB),
+                                       dtype=torch.int8 if f == "valid" else torch.float32, device=dev)
+                        for f in _lib.BAND_FIELDS}
+                plan.find_bands_device(batch.data_ptr(), dt, n, {f: v.data_ptr() for f, v in outs.items()}, m,
+                                       stream=st.cuda_stream)
+            pending.append((idx, outs, batch, st))
+        for idx, outs, _batch, st in pending:
+            st.synchronize()
+            for f, v in outs.items():
+                out[f][idx] = v.cpu().numpy()
+        return out

@@ -29,6 +29,7 @@ struct FusedGeom {
     int nGroups = 0;            // 32-ray groups of the fused LUT
     int nRaysPad = 0;           // nGroups * 32
     int gpt = 0;                // groups per theta column (ceil(nRho / 32))
+    int npad = 0;               // padding cells of the Radon tile
 };
 
 struct Workspace {
@@ -65,6 +66,7 @@ struct ebsd_plan_s {
     ebsd::FusedGeom fg;
     uint16_t* d_flut = nullptr;    // fused LUT (see fused.cu)
     int32_t* d_fgroup = nullptr;   // [nRaysPad] entry counts, then [nGroups] chunks per group
+    unsigned* d_fpad = nullptr;    // [npad] padding cell list of the fused Radon tile
     float* d_fray = nullptr;       // [nPx] weights: sum_px w*pixel = mean of the non-empty rays
     int64_t flut_entries = 0;
 

@@ -39,6 +39,10 @@ struct FusedArgs {
     const uint4* lut;          // [chunks][nRaysPad][8] u16 tile offsets, ray order theta-major
     const int32_t* count;      // [nRaysPad] entries per ray (group-major, lane-minor)
     const int32_t* gchunks;    // [nGroups] chunks walked by each 32-ray group
+    const int32_t* gids;       // [nGroups] group ids in per-warp stream order
+    const int32_t* wofs;       // [2*(kWarps+1)]: per-warp first group index, first chunk
+    const unsigned* padlist;   // [npad] (source tile cell << 16) | destination tile cell
+    int npad;
     int nRays, nRaysPad, nGroups, gpt, nRho, nTheta;  // gpt: 32-ray groups per theta column
     int p0, p1, R, Tp;
     int row0, col0, TR, TC;    // Radon tile origin (padded frame) and extent
@@ -105,11 +109,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     constexpr bool kHalf = sizeof(S) == 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     size_t off = 0;
-    S* tile = (S*)(smem + off);
-    off += ((size_t)a.TR * a.TC * sizeof(S) + 15) & ~(size_t)15;
+    // the conv tile comes first so that the pattern tile aliased into it starts at shared
+    // offset 0: the LUT then holds byte offsets usable directly as load addresses
     float* conv = (float*)(smem + off);
     float* pat = conv;  // aliased: the pattern tile is dead once the Radon is built
     off += ((size_t)a.CR * a.CC * sizeof(float) + 15) & ~(size_t)15;
+    S* tile = (S*)(smem + off);
+    off += ((size_t)a.TR * a.TC * sizeof(S) + 15) & ~(size_t)15;
     float* lv_s = (float*)(smem + off);
     off += kWarps * kMaxBands * sizeof(float);
     int* lp_s = (int*)(smem + off);
@@ -118,9 +124,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     off += 32 * sizeof(double);
     float* red_f = (float*)(smem + off);  // 66 floats
     off += 80 * sizeof(float);
-    int* gch_s = (int*)(smem + off);      // nGroups ints
+    int* gch_s = (int*)(smem + off);      // nGroups ints: chunks of each group
+    off += (size_t)a.nGroups * sizeof(int);
+    int* gid_s = (int*)(smem + off);      // nGroups ints: group ids, warp after warp
+    off += (size_t)a.nGroups * sizeof(int);
+    int* wofs_s = (int*)(smem + off);     // 2 * (kWarps + 1) ints: per-warp group / chunk offsets
+    off += 2 * (kWarps + 1) * sizeof(int);
+    int* rank_s = (int*)(smem + off);     // kThreads ints: candidate ranks
+    off += kThreads * sizeof(int);
+    float* fin_v = (float*)(smem + off);  // final top-N list
+    off += kMaxBands * sizeof(float);
+    int* fin_p = (int*)(smem + off);
 
-    for (int i = tid; i < a.nGroups; i += kThreads) gch_s[i] = a.gchunks[i];
+    for (int i = tid; i < a.nGroups; i += kThreads) {
+        gch_s[i] = a.gchunks[i];
+        gid_s[i] = a.gids[i];
+    }
+    for (int i = tid; i < 2 * (kWarps + 1); i += kThreads) wofs_s[i] = a.wofs[i];
     __syncthreads();
     const int nB = a.kc.nB;
     const int stat_r0 = a.p0, stat_r1 = a.statR1, stat_c0 = a.p1, stat_c1 = a.p1 + a.nTheta;
@@ -181,62 +201,60 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             inv_scl = 1.0f / scl;  // exact: scl is a power of two
         }
 
-        // ---- 2. Radon: one ray per lane, sequential FP32 sum in LUT order ----
-        // Warp w takes ray groups w, w+32, ... (32 consecutive theta-major rays: neighbouring
-        // rho at one theta, i.e. parallel lines); every lane walks the group's chunk count,
-        // short rays being padded with zero-word entries (adding +0.0 leaves the sum as it
-        // is), so the loop is warp-uniform.  The LUT loads of the next kRing chunks are kept in
-        // flight in a register ring across ray boundaries.
+        // ---- 2. Radon: one ray per lane ----
+        // Each warp walks its own stream of LUT chunks: the chunks of its groups (32
+        // neighbouring rho at one theta, one ray per lane) back to back, 16 B per lane per
+        // chunk, groups balanced across warps on the host.  The next kRing chunks are kept in
+        // flight in a register ring.  A chunk holds 8 byte offsets into the pattern tile;
+        // short rays are padded with the zero word (adding +0.0 leaves a sum as it is).
         {
-            constexpr int kRing = 8;
-            const unsigned zw = (unsigned)(a.H * a.pitch) * 0x10001u;
+            constexpr int kRing = 2;  // deeper rings cost registers without hiding more latency
+            const unsigned zw = (unsigned)(a.H * a.pitch * 4) * 0x10001u;
             const uint4 zero4 = make_uint4(zw, zw, zw, zw);
-            int ig = warp, ic = 0, inch = ig < a.nGroups ? gch_s[ig] : 0;
+            const int g0 = wofs_s[warp], g1 = wofs_s[warp + 1];
+            const int nchunk = wofs_s[kWarps + 1 + warp + 1] - wofs_s[kWarps + 1 + warp];
+            const uint4* ip = a.lut + ((size_t)wofs_s[kWarps + 1 + warp] * 32 + lane);
+            const unsigned char* pb = (const unsigned char*)pat;
             uint4 ring[kRing];
-            auto issue = [&](uint4& slot) {
-                if (ig < a.nGroups) {
-                    slot = __ldg(a.lut + ((size_t)ic * a.nRaysPad + ig * 32 + lane));
-                    if (++ic == inch) {
-                        ig += kWarps;
-                        ic = 0;
-                        inch = ig < a.nGroups ? gch_s[ig] : 0;
-                    }
-                } else {
-                    slot = zero4;
-                }
-            };
 #pragma unroll
-            for (int k = 0; k < kRing; ++k) issue(ring[k]);
-            int pg = warp, pc = 0, pnch = pg < a.nGroups ? gch_s[pg] : 0;
-            int cnt = pg < a.nGroups ? __ldg(a.count + pg * 32 + lane) : 0;
+            for (int k = 0; k < kRing; ++k) ring[k] = k < nchunk ? __ldg(ip + (size_t)k * 32) : zero4;
+            ip += (size_t)kRing * 32;
+            int left = nchunk - kRing;  // chunks not yet issued
+            int gi = g0, pc = 0;
+            int grp = gi < g1 ? gid_s[gi] : 0;
+            int pnch = gi < g1 ? gch_s[grp] : 0;
+            int cnt = gi < g1 ? __ldg(a.count + grp * 32 + lane) : 0;
             float sum = 0.0f;
-            while (pg < a.nGroups) {
+            while (gi < g1) {
 #pragma unroll
                 for (int k = 0; k < kRing; ++k) {
-                    if (pg < a.nGroups) {
-                        uint4 e = ring[k];
-                        issue(ring[k]);
-                        sum = __fadd_rn(sum, pat[e.x & 0xFFFF]);
-                        sum = __fadd_rn(sum, pat[e.x >> 16]);
-                        sum = __fadd_rn(sum, pat[e.y & 0xFFFF]);
-                        sum = __fadd_rn(sum, pat[e.y >> 16]);
-                        sum = __fadd_rn(sum, pat[e.z & 0xFFFF]);
-                        sum = __fadd_rn(sum, pat[e.z >> 16]);
-                        sum = __fadd_rn(sum, pat[e.w & 0xFFFF]);
-                        sum = __fadd_rn(sum, pat[e.w >> 16]);
+                    if (gi < g1) {
+                        const uint4 e = ring[k];
+                        ring[k] = left > 0 ? __ldg(ip) : zero4;
+                        ip += 32;
+                        --left;
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.x & 0xFFFF)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.x >> 16)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.y & 0xFFFF)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.y >> 16)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.z & 0xFFFF)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.z >> 16)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.w & 0xFFFF)));
+                        sum = __fadd_rn(sum, *(const float*)(pb + (e.w >> 16)));
                         if (++pc == pnch) {
-                            const int j = pg / a.gpt, i = (pg - j * a.gpt) * 32 + lane;
+                            const int j = grp / a.gpt, i = (grp - j * a.gpt) * 32 + lane;
                             if (i < a.nRho) {
                                 float v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
                                 if (kHalf) v = (v - cen) * scl;
                                 tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(v);
                             }
-                            pg += kWarps;
+                            ++gi;
                             pc = 0;
                             sum = 0.0f;
-                            if (pg < a.nGroups) {
-                                pnch = gch_s[pg];
-                                cnt = __ldg(a.count + pg * 32 + lane);
+                            if (gi < g1) {
+                                grp = gid_s[gi];
+                                pnch = gch_s[grp];
+                                cnt = __ldg(a.count + grp * 32 + lane);
                             }
                         }
                     }
@@ -246,24 +264,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         __syncthreads();
 
         // ---- 3. pad the tile around the interior ----
-        for (int tr = warp; tr < a.TR; tr += kWarps) {
-            const int r = tr + a.row0, i = r - a.p0;
-            const bool row_in = i >= 0 && i < a.nRho;
-            const int ic = i < 0 ? 0 : (i >= a.nRho ? a.nRho - 1 : i);
-            for (int tc = lane; tc < a.TC; tc += 32) {
-                const int j = tc + a.col0 - a.p1;
-                if (row_in && j >= 0 && j < a.nTheta) continue;
-                S val;
-                if (r < 0 || r >= a.R) {
-                    val = to_store<S>(kHalf ? -cen * scl : 0.0f);
-                } else {
-                    int si = ic, sj = j;
-                    if (j < 0) { si = a.nRho - 1 - ic; sj = a.nTheta + j; }
-                    else if (j >= a.nTheta) { si = a.nRho - 1 - ic; sj = j - a.nTheta; }
-                    val = tile[(si + a.p0 - a.row0) * a.TC + (sj + a.p1 - a.col0)];
-                }
-                tile[tr * a.TC + tc] = val;
-            }
+        // padding cell list (plan table): low half = destination tile cell, high half = source
+        // tile cell, 0xFFFF = zero (rows below the padded array, the convolution's zero fill)
+        for (int k = tid; k < a.npad; k += kThreads) {
+            const unsigned e = __ldg(a.padlist + k);
+            const unsigned src = e >> 16;
+            tile[e & 0xFFFF] = src == 0xFFFFu ? to_store<S>(kHalf ? -cen * scl : 0.0f) : tile[src];
         }
         __syncthreads();
 
@@ -394,38 +400,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             lv_s[warp * kMaxBands + lane] = lv;
             lp_s[warp * kMaxBands + lane] = lp;
         }
+        rank_s[tid] = 0;
+        if (tid < kMaxBands) fin_p[tid] = -1;
         __syncthreads();
 
-        // ---- 6. tree merge of the warp lists: list w absorbs list w + step ----
-        for (int step = 1; step < kWarps; step <<= 1) {
-            if ((warp % (2 * step)) == 0 && warp + step < kWarps) {
-                float av = lane < nB ? lv_s[warp * kMaxBands + lane] : -INFINITY;
-                int ap = lane < nB ? lp_s[warp * kMaxBands + lane] : -1;
-                float bv = lane < nB ? lv_s[(warp + step) * kMaxBands + lane] : -INFINITY;
-                int bp = lane < nB ? lp_s[(warp + step) * kMaxBands + lane] : -1;
-                // merged rank of each entry = own index + entries of the other list ahead of it
-                int ra = lane, rbk = lane;
-                for (int k = 0; k < nB; ++k) {
-                    float ov = __shfl_sync(0xffffffffu, bv, k);
-                    int op = __shfl_sync(0xffffffffu, bp, k);
-                    if (op >= 0 && (ap < 0 || beats(ov, op, av, ap))) ++ra;
-                    float ow = __shfl_sync(0xffffffffu, av, k);
-                    int oq = __shfl_sync(0xffffffffu, ap, k);
-                    if (oq >= 0 && (bp < 0 || beats(ow, oq, bv, bp))) ++rbk;
+        // ---- 6. merge the warp lists: rank of a candidate = candidates ahead of it ----
+        // (value desc, position asc is a strict total order: positions are unique).  Each
+        // candidate's rank is counted over `parts` disjoint sets of warp lists by different
+        // threads, combined with shared-memory atomics; the candidates of rank < nB form the
+        // final list.
+        {
+            const int ncand = kWarps * nB;
+            const int parts = kThreads / ncand;  // >= 1 since nB <= 32
+            const int c = tid % ncand, part = tid / ncand;
+            if (part < parts) {
+                const int cw = c / nB, ck = c - (c / nB) * nB;
+                const float cv = lv_s[cw * kMaxBands + ck];
+                const int cp = lp_s[cw * kMaxBands + ck];
+                if (cp >= 0) {
+                    int rank = 0;
+                    for (int w = part; w < kWarps; w += parts) {
+                        const float* vw = lv_s + w * kMaxBands;
+                        const int* pw = lp_s + w * kMaxBands;
+                        for (int k = 0; k < nB; ++k) {
+                            const int op = pw[k];
+                            if (op < 0) break;
+                            rank += beats(vw[k], op, cv, cp);
+                        }
+                    }
+                    if (rank) atomicAdd(rank_s + c, rank);
                 }
-                __syncwarp();
-                if (lane < nB) {
-                    lv_s[warp * kMaxBands + lane] = -INFINITY;
-                    lp_s[warp * kMaxBands + lane] = -1;
-                }
-                __syncwarp();
-                if (lane < nB && ap >= 0 && ra < nB) {
-                    lv_s[warp * kMaxBands + ra] = av;
-                    lp_s[warp * kMaxBands + ra] = ap;
-                }
-                if (lane < nB && bp >= 0 && rbk < nB) {
-                    lv_s[warp * kMaxBands + rbk] = bv;
-                    lp_s[warp * kMaxBands + rbk] = bp;
+            }
+            __syncthreads();
+            if (part == 0) {
+                const int cw = c / nB, ck = c - (c / nB) * nB;
+                const float cv = lv_s[cw * kMaxBands + ck];
+                const int cp = lp_s[cw * kMaxBands + ck];
+                const int rank = rank_s[c];
+                if (cp >= 0 && rank < nB) {
+                    fin_v[rank] = cv;
+                    fin_p[rank] = cp;
                 }
             }
             __syncthreads();
@@ -433,7 +447,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 
         // ---- 7. label: warp 0, one lane per band ----
         if (warp == 0 && lane < nB) {
-            int pos = lp_s[lane];
+            int pos = fin_p[lane];
             bool has = pos >= 0;
             int r = 0, c = 0;
             if (has) {
@@ -457,7 +471,8 @@ size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1, int ngroups)
     size_t b = ((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store + 15) & ~(size_t)15;
     b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
     b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
-    b += (size_t)ngroups * 4;
+    b += (size_t)ngroups * 8 + 2 * (kWarps + 1) * 4;
+    b += (size_t)kThreads * 4 + kMaxBands * 8;
     return b;
 }
 
@@ -491,7 +506,7 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
                     pick_kernel(EBSD_FUSED_F32, EBSD_U8, K0, K1) != nullptr &&
                     p->p0 >= K0 + K0 / 2 && p->p1 >= K1 + K1 / 2;
     int pitch = p->W + 1;
-    if ((int64_t)p->H * pitch + 1 >= 65535) shape_ok = false;
+    if (((int64_t)p->H * pitch + 1) * 4 >= 65535) shape_ok = false;  // byte offsets in 16 bits
     if (shape_ok) {
         const int D0 = K0, D1 = K1, H0 = K0 / 2, H1 = K1 / 2;
         int statR1 = std::min(p->R, p->Tp - p->p0);
@@ -511,7 +526,8 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         size_t conv_cells = (size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0);
         int dev_smem = 0;
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
-        g.ok = conv_cells >= (size_t)p->H * pitch + 1 && g.smem_f16 <= dev_smem && g.row0 >= 0;
+        g.ok = conv_cells >= (size_t)p->H * pitch + 1 && g.smem_f16 <= dev_smem && g.row0 >= 0 &&
+               (size_t)(g.row1 - g.row0) * (g.col1 - g.col0) < 65535;
         g.ok_f32 = g.ok && g.smem_f32 <= dev_smem;
     }
     p->fg = g;
@@ -580,7 +596,35 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         gch[g] = std::max(1, (nslot + 7) / 8);
         nch = std::max(nch, gch[g]);
     }
-    std::vector<uint16_t> lut((size_t)nch * nRaysPad * 8, zero);
+    // assign groups to warps, longest first, each to the warp with the fewest chunks so far
+    std::vector<int> order(nGroups);
+    for (int g = 0; g < nGroups; ++g) order[g] = g;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return gch[x] > gch[y]; });
+    std::vector<std::vector<int>> wg(kWarps);
+    std::vector<long> wload(kWarps, 0);
+    for (int g : order) {
+        int w = (int)(std::min_element(wload.begin(), wload.end()) - wload.begin());
+        wg[w].push_back(g);
+        wload[w] += gch[g];
+    }
+    std::vector<int32_t> gids, wofs(2 * (kWarps + 1), 0);
+    for (int w = 0; w < kWarps; ++w) {
+        std::sort(wg[w].begin(), wg[w].end());
+        wofs[w + 1] = wofs[w] + (int)wg[w].size();
+        wofs[kWarps + 1 + w + 1] = wofs[kWarps + 1 + w] + (int)wload[w];
+        for (int g : wg[w]) gids.push_back(g);
+    }
+    const long total_chunks = wofs[2 * kWarps + 1];
+    // stream layout: [chunk of the warp's stream][lane][8 entries], entry = byte offset
+    std::vector<uint16_t> lut((size_t)total_chunks * 32 * 8, (uint16_t)(zero * 4));
+    std::vector<long> gstart(nGroups, 0);
+    for (int w = 0; w < kWarps; ++w) {
+        long f = wofs[kWarps + 1 + w];
+        for (int g : wg[w]) {
+            gstart[g] = f;
+            f += gch[g];
+        }
+    }
     for (int g = 0; g < nGroups; ++g) {
         int j = g / gpt, i0 = (g % gpt) * 32;
         for (int l = 0; l < 32; ++l) {
@@ -592,10 +636,34 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
                 int idx = (int)ray[k];
                 int y = idx / p->W, x = idx - (idx / p->W) * p->W;
                 int slot = gaxis[g] == 0 ? x - gbase[g] : (gaxis[g] == 1 ? y - gbase[g] : k);
-                lut[((size_t)(slot / 8) * nRaysPad + t) * 8 + (slot % 8)] = (uint16_t)(y * pitch + x);
+                lut[((size_t)(gstart[g] + slot / 8) * 32 + l) * 8 + (slot % 8)] = (uint16_t)((y * pitch + x) * 4);
             }
         }
     }
+    // padding cells of the Radon tile and where each copies from (band_detect.py:573-580):
+    // theta padding = theta-wrapped interior column with rho flipped, rho padding = first /
+    // last interior row, rows at or below R = zero (the convolution's zero extension)
+    std::vector<unsigned> padlist;
+    {
+        const int TR = g.row1 - g.row0, TC = g.col1 - g.col0;
+        for (int tr = 0; tr < TR; ++tr)
+            for (int tc = 0; tc < TC; ++tc) {
+                int r = tr + g.row0, i = r - p->p0, j = tc + g.col0 - p->p1;
+                if (i >= 0 && i < p->nRho && j >= 0 && j < p->nTheta) continue;
+                unsigned src = 0xFFFFu;
+                if (r >= 0 && r < p->R) {
+                    int ic = i < 0 ? 0 : (i >= p->nRho ? p->nRho - 1 : i);
+                    int si = ic, sj = j;
+                    if (j < 0) { si = p->nRho - 1 - ic; sj = p->nTheta + j; }
+                    else if (j >= p->nTheta) { si = p->nRho - 1 - ic; sj = j - p->nTheta; }
+                    src = (unsigned)((si + p->p0 - g.row0) * TC + (sj + p->p1 - g.col0));
+                }
+                padlist.push_back((src << 16) | (unsigned)(tr * TC + tc));
+            }
+    }
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fpad, padlist.size() * sizeof(unsigned)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_fpad, padlist.data(), padlist.size() * sizeof(unsigned), cudaMemcpyHostToDevice));
+    p->fg.npad = (int)padlist.size();
     p->fg.nGroups = nGroups;
     p->fg.nRaysPad = nRaysPad;
     p->fg.gpt = gpt;
@@ -623,9 +691,12 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     }
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_flut, lut.size() * sizeof(uint16_t)));
     EBSD_CUDA_TRY(cudaMemcpy(p->d_flut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
-    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, (nRaysPad + nGroups) * sizeof(int32_t)));
-    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup, cnt.data(), nRaysPad * sizeof(int32_t), cudaMemcpyHostToDevice));
-    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup + nRaysPad, gch.data(), nGroups * sizeof(int32_t), cudaMemcpyHostToDevice));
+    std::vector<int32_t> tables(cnt);
+    tables.insert(tables.end(), gch.begin(), gch.end());
+    tables.insert(tables.end(), gids.begin(), gids.end());
+    tables.insert(tables.end(), wofs.begin(), wofs.end());
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, tables.size() * sizeof(int32_t)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup, tables.data(), tables.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     p->flut_entries = (int64_t)lut.size();
     return EBSD_OK;
 }
@@ -634,6 +705,8 @@ void fused_release(ebsd_plan_s* p) {
     cudaFree(p->d_flut);
     cudaFree(p->d_fgroup);
     cudaFree(p->d_fray);
+    cudaFree(p->d_fpad);
+    p->d_fpad = nullptr;
     p->d_flut = nullptr;
     p->d_fgroup = nullptr;
     p->d_fray = nullptr;
@@ -671,6 +744,10 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.lut = (const uint4*)p->d_flut;
     a.count = p->d_fgroup;
     a.gchunks = p->d_fgroup + g.nRaysPad;
+    a.gids = a.gchunks + g.nGroups;
+    a.wofs = a.gids + g.nGroups;
+    a.padlist = p->d_fpad;
+    a.npad = g.npad;
     a.gpt = g.gpt;
     a.nRays = p->nRays;
     a.nRaysPad = g.nRaysPad;

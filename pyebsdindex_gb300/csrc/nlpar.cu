@@ -111,9 +111,13 @@ __global__ void k_nlpar_weights(const float* __restrict__ data, int nrows, int n
     if (c < winsz) wout[(int64_t)pix * winsz + c] = __fdiv_rn(w_s[c], tot_s);
 }
 
+__device__ __forceinline__ float wadd(float acc, float x, float w) { return __fadd_rn(acc, __fmul_rn(x, w)); }
+__device__ __forceinline__ double wadd(double acc, double x, double w) { return __dadd_rn(acc, __dmul_rn(x, w)); }
+
 // out[pix][k] = sum over the window, in window order, of data[nb][k] * w[pix][c].
-__global__ void k_nlpar_average(const float* __restrict__ data, int nrows, int ncols, int npx,
-                                const float* __restrict__ w, int sr, float* __restrict__ out) {
+template <typename T>
+__global__ void k_nlpar_average(const T* __restrict__ data, int nrows, int ncols, int npx,
+                                const T* __restrict__ w, int sr, T* __restrict__ out) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     int pix = blockIdx.y;
     if (k >= npx) return;
@@ -122,12 +126,12 @@ __global__ void k_nlpar_average(const float* __restrict__ data, int nrows, int n
     window(i, sr, ncols, xs, xe);
     window(j, sr, nrows, ys, ye);
     int winsz = (2 * sr + 1) * (2 * sr + 1);
-    const float* wp = w + (int64_t)pix * winsz;
-    float acc = 0.0f;
+    const T* wp = w + (int64_t)pix * winsz;
+    T acc = (T)0;
     int c = 0;
     for (int jn = ys; jn < ye; ++jn)
         for (int inn = xs; inn < xe; ++inn, ++c)
-            acc = __fadd_rn(acc, __fmul_rn(__ldg(data + (int64_t)(inn + ncols * jn) * npx + k), __ldg(wp + c)));
+            acc = wadd(acc, __ldg(data + (int64_t)(inn + ncols * jn) * npx + k), __ldg(wp + c));
     out[(int64_t)pix * npx + k] = acc;
 }
 
@@ -166,7 +170,27 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, c
     int rc = launch_status();
     if (rc != EBSD_OK) return rc;
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
-    k_nlpar_average<<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, d_out);
+    k_nlpar_average<float><<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, d_out);
+    return launch_status();
+}
+
+int ebsd_nlpar_apply(const float* d_x, int32_t nrows, int32_t ncols, int32_t npx, const float* d_w, int32_t sr,
+                     float* d_out, void* stream) {
+    if (!d_x || !d_w || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10 || 2 * sr + 1 > nrows ||
+        2 * sr + 1 > ncols)
+        return EBSD_E_ARG;
+    dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
+    k_nlpar_average<float><<<grid, 256, 0, (cudaStream_t)stream>>>(d_x, nrows, ncols, npx, d_w, sr, d_out);
+    return launch_status();
+}
+
+int ebsd_nlpar_apply64(const double* d_x, int32_t nrows, int32_t ncols, int32_t npx, const double* d_w, int32_t sr,
+                       double* d_out, void* stream) {
+    if (!d_x || !d_w || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10 || 2 * sr + 1 > nrows ||
+        2 * sr + 1 > ncols)
+        return EBSD_E_ARG;
+    dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
+    k_nlpar_average<double><<<grid, 256, 0, (cudaStream_t)stream>>>(d_x, nrows, ncols, npx, d_w, sr, d_out);
     return launch_status();
 }
 
