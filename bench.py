@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="patterns in the timed CPU sample")
     ap.add_argument("--no-variants", action="store_true", help="skip timing the other methods")
+    ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the plan's rule-based kernel variant")
     return ap.parse_args()
 
 
@@ -217,13 +219,37 @@ def main():
     ptrs = {k: v.data_ptr() for k, v in outs.items()}
     stream = torch.cuda.current_stream(dev)
 
+    # autotune the patterns per block pass on a sample of the batch, then capture one step
+    # (the whole batch is one persistent launch per 1M-pattern chunk) in a CUDA graph
+    ppp = "rule: 2 for uint8 without background"
+    if not args.no_autotune:
+        ppp = plan.autotune(pats_d.data_ptr(), _lib.EBSD_U8, min(N, 16384), method, stream=stream.cuda_stream)
+    plan.reserve(method, N)
+
+    def launch(st):
+        plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, N, ptrs, method, stream=st.cuda_stream)
+
+    launch(stream)
+    torch.cuda.synchronize()
+    launches_per_step = plan.last_launches()
+    graph = None
+    if not args.no_graph:
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(stream)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            launch(side)
+        torch.cuda.synchronize()
+
     def step():
-        plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, N, ptrs, method, stream=stream.cuda_stream)
+        if graph is not None:
+            graph.replay()
+        else:
+            launch(stream)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    launches_per_step = plan.last_launches()
     if world > 1:
         torch.distributed.barrier()
     clk = ClockSampler(local)
@@ -324,6 +350,7 @@ def main():
             "config": {"workload": "find_bands on 1,000,000 80x80 uint8 patterns, nTheta 180, nRho 120, "
                                    "nBands 9, LoG sigma 1, rhoMaskFrac 0.1, circular mask, 10% noise-only",
                        "method": method, "patterns_per_step": N, "distinct_patterns": len(pool),
+                       "patterns_per_block_pass": ppp, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "variants_patterns_per_s": variants,

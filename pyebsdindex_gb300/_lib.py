@@ -81,6 +81,10 @@ def load():
         lib.ebsd_find_bands_host.restype = C.c_int
         lib.ebsd_last_launch_count.argtypes = [P]
         lib.ebsd_last_launch_count.restype = C.c_int64
+        lib.ebsd_plan_autotune.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, P, C.POINTER(C.c_int)]
+        lib.ebsd_plan_autotune.restype = C.c_int
+        lib.ebsd_plan_set_patterns_per_pass.argtypes = [P, C.c_int]
+        lib.ebsd_plan_set_patterns_per_pass.restype = C.c_int
         lib.ebsd_strerror.argtypes = [C.c_int]
         lib.ebsd_strerror.restype = C.c_char_p
         lib.ebsd_version.argtypes = []
@@ -153,6 +157,18 @@ class DevicePlan:
 
     def last_launches(self) -> int:
         return int(self._lib.ebsd_last_launch_count(self.handle))
+
+    def set_patterns_per_pass(self, ppp: int):
+        """Pin the fused kernel's patterns per block pass (1, 2, 4; 0 = rule)."""
+        check(self._lib.ebsd_plan_set_patterns_per_pass(self.handle, int(ppp)), "ebsd_plan_set_patterns_per_pass")
+
+    def autotune(self, pats_ptr: int, dtype: int, n: int, method, stream=0) -> int:
+        """Time the record-identical kernel variants on a device-resident sample and keep the
+        faster in the plan; returns the chosen patterns per block pass (1, 2 or 4)."""
+        ppp = C.c_int(0)
+        check(self._lib.ebsd_plan_autotune(self.handle, method_id(method), int(dtype), C.c_void_p(int(pats_ptr)),
+                                           int(n), C.c_void_p(int(stream)), C.byref(ppp)), "ebsd_plan_autotune")
+        return int(ppp.value)
 
     def find_bands_host(self, pats: np.ndarray, method, chunk=0):
         """Host patterns [n,H,W] -> dict of host SoA band arrays (C ABI with host buffers)."""

@@ -153,6 +153,30 @@ class GPUFindBands:
             print('Band Find Time (GPU, %s):' % m, timer() - tic0)
         return bandData
 
+    def autotune(self, sample, method=None, gpu_id=None):
+        """Time the record-identical variants of the fused kernel (one, two or four patterns per
+        block pass) on ``sample`` ([n, H, W] numpy or torch, uint8/uint16/float32) and keep
+        the faster in the device plan for later ``find_bands`` calls.  No counterpart in the
+        reference.  Returns the chosen patterns per pass."""
+        import torch
+        plan = self._device_plan(gpu_id)
+        m = self._pick_method(plan, method)
+        dev = torch.device("cuda", plan.device)
+        t = sample if type(sample).__module__.startswith("torch") else torch.from_numpy(np.ascontiguousarray(sample))
+        if t.ndim == 2:
+            t = t[None]
+        u16 = getattr(torch, "uint16", None)
+        if t.dtype == torch.uint8:
+            dt = _lib.EBSD_U8
+        elif u16 is not None and t.dtype == u16:
+            dt = _lib.EBSD_U16
+        else:
+            t = t.to(torch.float32)
+            dt = _lib.EBSD_F32
+        t = t.to(dev).contiguous()
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        return plan.autotune(t.data_ptr(), dt, int(t.shape[0]), m, stream=stream)
+
     def _records(self, soa, nP):
         out = np.zeros((nP, int(self.nBands)), dtype=self.dataType)
         for f in _lib.BAND_FIELDS:

@@ -10,10 +10,11 @@
 //                (band_detect.py:573-580; the FFT convolution's zero extension)
 //   4. conv      register-blocked direct LoG convolution into an FP32 conv tile, in the same
 //                multiply-add order as the per-stage kernel; min/sum for normmax on the fly
-//   5. peaks     per warp: 32-column strip x 8 rows; rho max in registers, theta max by warp
-//                shuffles, exact equality + rdnmask (band_detect.py:639-664); candidates go
-//                into a warp top-N list ordered by (value desc, position asc)
-//   6. merge     tree merge of the 32 warp lists
+//   5. peaks     separable max filter: theta max per row into the dead Radon tile, then
+//                rho max per column in registers, exact equality + rdnmask
+//                (band_detect.py:639-664); candidates go into a warp top-N list ordered
+//                by (value desc, position asc)
+//   6. merge     threshold = nB-th best warp-list head; rank the survivors among themselves
 //   7. label     lanes 0..nB-1 of warp 0 fit their band (band_detect.py:691-809) and write
 //                the record fields, normmax, theta and rho (band_detect.py:457-460, :521-524)
 //
@@ -24,6 +25,7 @@
 #include <cuda_fp16.h>
 #include <algorithm>
 #include <cfloat>
+#include <cstring>
 
 namespace ebsd {
 namespace {
@@ -31,18 +33,22 @@ namespace {
 constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
 constexpr int kRowBlock = 8;
+constexpr int kRing = 2;  // LUT chunks in flight per warp (deeper rings cost registers, not latency)
 
 struct FusedArgs {
     const void* pats;
     int64_t n;
     int H, W, nPx, pitch;      // pattern tile pitch (W + 1); zero word at H*pitch
-    const uint4* lut;          // [chunks][nRaysPad][8] u16 tile offsets, ray order theta-major
+    const uint4* lut;          // per-warp LUT streams: 8 u16 byte offsets per lane per chunk
+    const uint4* lut8;         // the same for the 8-byte pixel elements of the 4-pattern tile
     const int32_t* count;      // [nRaysPad] entries per ray (group-major, lane-minor)
-    const int32_t* gchunks;    // [nGroups] chunks walked by each 32-ray group
-    const int32_t* gids;       // [nGroups] group ids in per-warp stream order
+    const float* rcount;       // [nRaysPad] RN(1 / count) (0 for empty rays)
+    const uint32_t* gstream;   // [nGroups] per-warp stream order: group id | chunks << 16
+    const uint32_t* gtile;     // [nGroups] same order: Radon tile offset of lane 0 | rays << 16
     const int32_t* wofs;       // [2*(kWarps+1)]: per-warp first group index, first chunk
     const unsigned* padlist;   // [npad] (source tile cell << 16) | destination tile cell
     int npad;
+    float* pack_scratch;       // packed modes: [gridDim.x][kPack-1][nRaysPad] parked ray means
     int nRays, nRaysPad, nGroups, gpt, nRho, nTheta;  // gpt: 32-ray groups per theta column
     int p0, p1, R, Tp;
     int row0, col0, TR, TC;    // Radon tile origin (padded frame) and extent
@@ -65,6 +71,17 @@ template <> __device__ __forceinline__ float to_store<float>(float v) { return v
 template <> __device__ __forceinline__ __half to_store<__half>(float v) { return __float2half_rn(v); }
 __device__ __forceinline__ float to_f(float v) { return v; }
 __device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+
+// RN(s / c) for integers 0 <= s < 2^16 and 1 <= c <= 257, given r = RN(1 / c): one
+// correction step of Markstein's division (P. Markstein, IBM J. Res. Dev. 34(1), 1990):
+// q0 = RN(s r), the remainder s - q0 c is exact in one FMA, q = RN(q0 + rem r).  Checked
+// exhaustively over that domain against the correctly rounded quotient.
+__device__ __forceinline__ float div_int_exact(unsigned s, float c, float r) {
+    const float fs = (float)s;
+    const float q0 = __fmul_rn(fs, r);
+    const float rem = __fmaf_rn(-q0, c, fs);
+    return __fmaf_rn(rem, r, q0);
+}
 
 __device__ __forceinline__ bool beats(float v, int p, float w, int q) {
     return v > w || (v == w && p < q);
@@ -97,14 +114,22 @@ __device__ __forceinline__ float load_pixel(const InT* p, int idx, int bg_mode, 
     return (float)p[idx];
 }
 
-template <typename InT, typename S, int K0, int K1>
+// kPack = 2 or 4: that many uint8 patterns per pass (no background).  Pattern pixels are
+// packed as 16-bit lanes -- two per shared word, four per 8-byte element -- so one load and
+// one integer add per word gather them all; a ray sum of at most 257 uint8 values fits its
+// lane, and integer sums are exact, so the means equal the float sequential sums of the
+// single-pattern pass.  The other patterns' ray means are parked in a per-CTA global scratch
+// (L2-resident) and reloaded once the pattern before them is finished.
+template <typename InT, typename S, int K0, int K1, int kPack>
 __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
+    static_assert(kPack == 1 || (sizeof(S) == 4 && sizeof(InT) == 1), "packed modes: uint8 input, FP32 tile");
+    static_assert(kPack == 1 || kPack == 2 || kPack == 4, "1, 2 or 4 patterns per pass");
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int D0 = K0;  // rho half-window of the max filter (peakPad = 2*ksz + 1)
     constexpr int D1 = K1;  // theta half-window
-    constexpr int SW = 32 - 2 * D1;  // output columns per warp strip
+    constexpr int WIN = 2 * D1 + 1;  // theta window of the max filter
     constexpr int H0 = K0 / 2, H1 = K1 / 2;
-    constexpr int NV = kRowBlock + 2 * D0;  // conv rows a strip block reads
+    constexpr int NV = kRowBlock + 2 * D0;  // theta-max rows a peak task reads
 
     constexpr bool kHalf = sizeof(S) == 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -115,30 +140,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     float* pat = conv;  // aliased: the pattern tile is dead once the Radon is built
     off += ((size_t)a.CR * a.CC * sizeof(float) + 15) & ~(size_t)15;
     S* tile = (S*)(smem + off);
-    off += ((size_t)a.TR * a.TC * sizeof(S) + 15) & ~(size_t)15;
+    {
+        // the Radon tile region also holds the peaks' theta-max rows once the tile is dead
+        const size_t tb = (size_t)a.TR * a.TC * sizeof(S), mb = (size_t)(a.nRho + 2 * D0) * a.nTheta * sizeof(float);
+        off += ((tb > mb ? tb : mb) + 15) & ~(size_t)15;
+    }
     float* lv_s = (float*)(smem + off);
     off += kWarps * kMaxBands * sizeof(float);
     int* lp_s = (int*)(smem + off);
     off += kWarps * kMaxBands * sizeof(int);
     double* red_d = (double*)(smem + off);
     off += 32 * sizeof(double);
-    float* red_f = (float*)(smem + off);  // 66 floats
+    float* red_f = (float*)(smem + off);  // 66 floats, then the merge's scalars
+    float* thr_v = red_f + 72;            // merge threshold (value, position)
+    int* thr_p = (int*)(red_f + 73);
+    int* nsurv = (int*)(red_f + 74);      // number of merge survivors
     off += 80 * sizeof(float);
-    int* gch_s = (int*)(smem + off);      // nGroups ints: chunks of each group
-    off += (size_t)a.nGroups * sizeof(int);
-    int* gid_s = (int*)(smem + off);      // nGroups ints: group ids, warp after warp
-    off += (size_t)a.nGroups * sizeof(int);
+    unsigned* gst_s = (unsigned*)(smem + off);  // nGroups: group id | chunks << 16, stream order
+    off += (size_t)a.nGroups * sizeof(unsigned);
+    unsigned* gtb_s = (unsigned*)(smem + off);  // nGroups: tile offset | valid rays << 16
+    off += (size_t)a.nGroups * sizeof(unsigned);
     int* wofs_s = (int*)(smem + off);     // 2 * (kWarps + 1) ints: per-warp group / chunk offsets
     off += 2 * (kWarps + 1) * sizeof(int);
-    int* rank_s = (int*)(smem + off);     // kThreads ints: candidate ranks
+    int* surv = (int*)(smem + off);       // kThreads ints: surviving candidates of the merge
     off += kThreads * sizeof(int);
     float* fin_v = (float*)(smem + off);  // final top-N list
     off += kMaxBands * sizeof(float);
     int* fin_p = (int*)(smem + off);
 
     for (int i = tid; i < a.nGroups; i += kThreads) {
-        gch_s[i] = a.gchunks[i];
-        gid_s[i] = a.gids[i];
+        gst_s[i] = a.gstream[i];
+        gtb_s[i] = a.gtile[i];
     }
     for (int i = tid; i < 2 * (kWarps + 1); i += kThreads) wofs_s[i] = a.wofs[i];
     __syncthreads();
@@ -146,15 +178,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     const int stat_r0 = a.p0, stat_r1 = a.statR1, stat_c0 = a.p1, stat_c1 = a.p1 + a.nTheta;
     const int stat_count = (stat_r1 - stat_r0) * (stat_c1 - stat_c0);
 
-    for (int64_t q = blockIdx.x; q < a.n; q += gridDim.x) {
+    const int64_t nunits = (a.n + kPack - 1) / kPack;
+    float* scratch = kPack > 1 ? a.pack_scratch + (size_t)blockIdx.x * (kPack - 1) * a.nRaysPad : nullptr;
+    for (int64_t u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int64_t q0 = u * kPack;
+        const int npk = (int)(a.n - q0 < kPack ? a.n - q0 : kPack);  // patterns in this unit
         // ---- 1. load the pattern into the FP32 tile (pitch W+1, zero word after it) ----
-        const InT* gp = (const InT*)a.pats + q * (int64_t)a.nPx;
+        const InT* gp = (const InT*)a.pats + q0 * (int64_t)a.nPx;
         float wsum = 0.0f, pmin = -1.0f, pmax = -1.0f;  // -1: value of an empty ray
         for (int y = warp; y < a.H; y += kWarps) {
             for (int x = lane; x < a.W; x += 32) {
                 const int i = y * a.W + x;
-                float v = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
-                pat[y * a.pitch + x] = v;
+                float v;
+                if (kPack == 2) {
+                    const unsigned lo = (unsigned)gp[i], hi = npk > 1 ? (unsigned)gp[a.nPx + i] : 0u;
+                    ((unsigned*)pat)[y * a.pitch + x] = lo | (hi << 16);
+                    v = 0.0f;
+                } else if (kPack == 4) {
+                    unsigned w[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) w[j] = j < npk ? (unsigned)gp[(size_t)j * a.nPx + i] : 0u;
+                    ((uint2*)pat)[y * a.pitch + x] = make_uint2(w[0] | (w[1] << 16), w[2] | (w[3] << 16));
+                    v = 0.0f;
+                } else {
+                    v = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
+                    pat[y * a.pitch + x] = v;
+                }
                 if (kHalf) {
                     wsum = fmaf(a.wimg[i], v, wsum);
                     pmin = fminf(pmin, v);
@@ -162,7 +211,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 }
             }
         }
-        if (tid == 0) pat[a.H * a.pitch] = 0.0f;
+        if (tid == 0) {
+            if (kPack == 4) ((uint2*)pat)[a.H * a.pitch] = make_uint2(0u, 0u);
+            else pat[a.H * a.pitch] = 0.0f;
+        }
         // FP16 storage keeps (value - m) * s: m = mean of the Radon interior (exact by
         // linearity: sum_px w[px] * p[px]), s = power of two keeping |value - m| * s < 2^14.
         float cen = 0.0f, scl = 1.0f, inv_scl = 1.0f;
@@ -208,53 +260,83 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         // flight in a register ring.  A chunk holds 8 byte offsets into the pattern tile;
         // short rays are padded with the zero word (adding +0.0 leaves a sum as it is).
         {
-            constexpr int kRing = 2;  // deeper rings cost registers without hiding more latency
-            const unsigned zw = (unsigned)(a.H * a.pitch * 4) * 0x10001u;
-            const uint4 zero4 = make_uint4(zw, zw, zw, zw);
             const int g0 = wofs_s[warp], g1 = wofs_s[warp + 1];
-            const int nchunk = wofs_s[kWarps + 1 + warp + 1] - wofs_s[kWarps + 1 + warp];
-            const uint4* ip = a.lut + ((size_t)wofs_s[kWarps + 1 + warp] * 32 + lane);
+            // each warp stream ends with kRing zero chunks, so the ring loads unconditionally
+            const uint4* ip = (kPack == 4 ? a.lut8 : a.lut) + ((size_t)wofs_s[kWarps + 1 + warp] * 32 + lane);
             const unsigned char* pb = (const unsigned char*)pat;
             uint4 ring[kRing];
 #pragma unroll
-            for (int k = 0; k < kRing; ++k) ring[k] = k < nchunk ? __ldg(ip + (size_t)k * 32) : zero4;
+            for (int k = 0; k < kRing; ++k) ring[k] = __ldg(ip + (size_t)k * 32);
             ip += (size_t)kRing * 32;
-            int left = nchunk - kRing;  // chunks not yet issued
             int gi = g0, pc = 0;
-            int grp = gi < g1 ? gid_s[gi] : 0;
-            int pnch = gi < g1 ? gch_s[grp] : 0;
-            int cnt = gi < g1 ? __ldg(a.count + grp * 32 + lane) : 0;
+            unsigned gs = gi < g1 ? gst_s[gi] : 0u;
+            int t = (int)(gs & 0xFFFFu) * 32 + lane;  // ray slot: group * 32 + lane
+            int cnt = gi < g1 ? __ldg(a.count + t) : 0;
+            float rc = gi < g1 ? __ldg(a.rcount + t) : 0.0f;
             float sum = 0.0f;
+            unsigned isum = 0u, isum2 = 0u;  // packed modes: 16-bit lane sums
             while (gi < g1) {
 #pragma unroll
                 for (int k = 0; k < kRing; ++k) {
                     if (gi < g1) {
                         const uint4 e = ring[k];
-                        ring[k] = left > 0 ? __ldg(ip) : zero4;
+                        ring[k] = __ldg(ip);
                         ip += 32;
-                        --left;
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.x & 0xFFFF)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.x >> 16)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.y & 0xFFFF)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.y >> 16)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.z & 0xFFFF)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.z >> 16)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.w & 0xFFFF)));
-                        sum = __fadd_rn(sum, *(const float*)(pb + (e.w >> 16)));
-                        if (++pc == pnch) {
-                            const int j = grp / a.gpt, i = (grp - j * a.gpt) * 32 + lane;
-                            if (i < a.nRho) {
-                                float v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
-                                if (kHalf) v = (v - cen) * scl;
-                                tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(v);
+                        if (kPack == 4) {
+                            const unsigned o[8] = {e.x & 0xFFFF, e.x >> 16, e.y & 0xFFFF, e.y >> 16,
+                                                   e.z & 0xFFFF, e.z >> 16, e.w & 0xFFFF, e.w >> 16};
+#pragma unroll
+                            for (int k8 = 0; k8 < 8; ++k8) {
+                                const uint2 w = *(const uint2*)(pb + o[k8]);
+                                isum += w.x;
+                                isum2 += w.y;
                             }
+                        } else if (kPack == 2) {
+                            isum += *(const unsigned*)(pb + (e.x & 0xFFFF));
+                            isum += *(const unsigned*)(pb + (e.x >> 16));
+                            isum += *(const unsigned*)(pb + (e.y & 0xFFFF));
+                            isum += *(const unsigned*)(pb + (e.y >> 16));
+                            isum += *(const unsigned*)(pb + (e.z & 0xFFFF));
+                            isum += *(const unsigned*)(pb + (e.z >> 16));
+                            isum += *(const unsigned*)(pb + (e.w & 0xFFFF));
+                            isum += *(const unsigned*)(pb + (e.w >> 16));
+                        } else {
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.x & 0xFFFF)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.x >> 16)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.y & 0xFFFF)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.y >> 16)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.z & 0xFFFF)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.z >> 16)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.w & 0xFFFF)));
+                            sum = __fadd_rn(sum, *(const float*)(pb + (e.w >> 16)));
+                        }
+                        if (++pc == (int)(gs >> 16)) {
+                            // ray ends: the mean of an empty ray is -1 (radon_fast.py:265)
+                            float v;
+                            if (kPack > 1) {
+                                const float fc = (float)cnt;
+                                v = cnt > 0 ? div_int_exact(isum & 0xFFFFu, fc, rc) : -1.0f;
+                                scratch[t] = cnt > 0 ? div_int_exact(isum >> 16, fc, rc) : -1.0f;
+                                if (kPack == 4) {
+                                    scratch[a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum2 & 0xFFFFu, fc, rc) : -1.0f;
+                                    scratch[2 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum2 >> 16, fc, rc) : -1.0f;
+                                }
+                            } else {
+                                v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
+                                if (kHalf) v = (v - cen) * scl;
+                            }
+                            const unsigned tb = gtb_s[gi];
+                            if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * a.TC] = to_store<S>(v);
                             ++gi;
                             pc = 0;
                             sum = 0.0f;
+                            isum = 0u;
+                            isum2 = 0u;
                             if (gi < g1) {
-                                grp = gid_s[gi];
-                                pnch = gch_s[grp];
-                                cnt = __ldg(a.count + grp * 32 + lane);
+                                gs = gst_s[gi];
+                                t = (int)(gs & 0xFFFFu) * 32 + lane;
+                                cnt = __ldg(a.count + t);
+                                rc = __ldg(a.rcount + t);
                             }
                         }
                     }
@@ -263,6 +345,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         }
         __syncthreads();
 
+        for (int sub = 0; sub < npk; ++sub) {
+        const int64_t q = q0 + sub;
+        if (kPack > 1 && sub > 0) {
+            // the next pattern's ray means, parked by the gather, back into the tile
+            const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
+            for (int t = tid; t < a.nRaysPad; t += kThreads) {
+                const int grp = t >> 5, j = grp / a.gpt, i = (grp - j * a.gpt) * 32 + (t & 31);
+                if (i < a.nRho) tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(src[t]);
+            }
+            __syncthreads();
+        }
         // ---- 3. pad the tile around the interior ----
         // padding cell list (plan table): low half = destination tile cell, high half = source
         // tile cell, 0xFFFF = zero (rows below the padded array, the convolution's zero fill)
@@ -277,46 +370,60 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         float smin = INFINITY, ssum = 0.0f;
         {
             const int nrb = (a.CR + kRowBlock - 1) / kRowBlock;
-            for (int task = tid; task < nrb * a.CC; task += kThreads) {
-                int cc = task % a.CC, rb = task / a.CC;
-                int cr0 = rb * kRowBlock;
+            const int ntask = nrb * a.CC;
+            // task = rb * CC + cc, advanced by kThreads without a division per task
+            int cc = tid % a.CC, rb = tid / a.CC;
+            const int dcc = kThreads % a.CC, drb = kThreads / a.CC;
+            const unsigned stat_rows = (unsigned)(stat_r1 - stat_r0);
+            for (int task = tid; task < ntask; task += kThreads) {
+                const int cr0 = rb * kRowBlock;
                 float acc[kRowBlock];
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) acc[o] = 0.0f;
                 // tile row (cr0 + t) feeds output o through kernel row a = o + 2*H0 - t;
                 // descending t keeps each output's multiply-add order = ascending a.
+                const S* tcol = tile + cc + 2 * H1;
 #pragma unroll
                 for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
-                    int tr = cr0 + t;
+                    const int tr = cr0 + t;
                     float v[K1];
                     if (tr < a.TR) {
 #pragma unroll
-                        for (int b = 0; b < K1; ++b) v[b] = to_f(tile[tr * a.TC + cc + 2 * H1 - b]);
+                        for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[tr * a.TC - b]);
                     } else {
 #pragma unroll
                         for (int b = 0; b < K1; ++b) v[b] = 0.0f;
                     }
 #pragma unroll
                     for (int o = 0; o < kRowBlock; ++o) {
-                        int ka = o + 2 * H0 - t;
+                        const int ka = o + 2 * H0 - t;
                         if (ka >= 0 && ka < K0) {
 #pragma unroll
                             for (int b = 0; b < K1; ++b) acc[o] = fmaf(a.taps[ka * K1 + b], v[b], acc[o]);
                         }
                     }
                 }
+                // statistics slice: padded rows [stat_r0, stat_r1) x columns [stat_c0, stat_c1)
+                const int col = cc + a.ccol0;
+                const bool colstat = col >= stat_c0 && col < stat_c1;
+                const int rs0 = cr0 + a.crow0 - stat_r0;
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
-                    int cr = cr0 + o;
+                    const int cr = cr0 + o;
                     if (kHalf) acc[o] = fmaf(a.ksum, cen, acc[o] * inv_scl);
                     if (cr < a.CR) {
                         conv[cr * a.CC + cc] = acc[o];
-                        int r = cr + a.crow0, col = cc + a.ccol0;
-                        if (r >= stat_r0 && r < stat_r1 && col >= stat_c0 && col < stat_c1) {
+                        if (colstat && (unsigned)(rs0 + o) < stat_rows) {
                             smin = fminf(smin, acc[o]);
                             ssum += acc[o];
                         }
                     }
+                }
+                cc += dcc;
+                rb += drb;
+                if (cc >= a.CC) {
+                    cc -= a.CC;
+                    ++rb;
                 }
             }
         }
@@ -342,25 +449,61 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         }
         // (red_d[0] / red_f[0] are read after the next barrier)
 
-        // ---- 5. peaks: strips of SW output columns x kRowBlock rows per warp task ----
+        // ---- 5. peaks: separable max filter (band_detect.py:639-664, :811-843) ----
+        // 5a. theta max of every conv row the rho window needs, into the dead Radon tile:
+        //     tm[rr][j] = max(conv[p0 - D0 + rr][p1 + j - D1 .. p1 + j + D1]).  One thread per
+        //     WIN consecutive outputs: suffix maxima of the first WIN inputs and running
+        //     prefix maxima of the next WIN - 1 give every window with two max operations.
+        float* tm = (float*)tile;
+        {
+            const int NR = a.nRho + 2 * D0;
+            const int nseg = (a.nTheta + WIN - 1) / WIN;
+            for (int task = tid; task < NR * nseg; task += kThreads) {
+                const int rr = task / nseg, sg = task - rr * nseg;
+                const int j0 = sg * WIN;
+                const float* x = conv + (rr + a.p0 - D0 - a.crow0) * a.CC + (j0 + a.p1 - D1 - a.ccol0);
+                float* out = tm + rr * a.nTheta + j0;
+                const int nout = a.nTheta - j0 < WIN ? a.nTheta - j0 : WIN;
+                float xv[2 * WIN - 1];
+                if (nout == WIN) {
+#pragma unroll
+                    for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = x[k];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = k < nout + 2 * D1 ? x[k] : -INFINITY;
+                }
+#pragma unroll
+                for (int k = WIN - 2; k >= 0; --k) xv[k] = fmaxf(xv[k], xv[k + 1]);  // suffix maxima
+                float pm = -INFINITY;
+#pragma unroll
+                for (int t = 0; t < WIN; ++t) {
+                    if (t > 0) pm = fmaxf(pm, xv[WIN - 1 + t]);
+                    if (t < nout) out[t] = fmaxf(xv[t], pm);
+                }
+            }
+        }
+        __syncthreads();
+
+        // 5b. rho max of tm over [i - D0, i + D0], exact equality with the conv value and the
+        //     Radon mask; warp task = kRowBlock output rows x 32 columns (one per lane), the
+        //     flagged peaks go into the warp's top-N list ordered by (value desc, position asc)
         float lv = -INFINITY;
         int lp = -1;
         {
-            const int nstrip = (a.nTheta + SW - 1) / SW;
+            const int nstrip = (a.nTheta + 31) / 32;
             const int nrowb = (a.nRho + kRowBlock - 1) / kRowBlock;
             for (int task = warp; task < nstrip * nrowb; task += kWarps) {
-                int s = task % nstrip, rb = task / nstrip;
-                // lane column in the conv tile: output column p1 + SW*s + (lane - D1)
-                int cc = SW * s + lane + (a.p1 - D1 - a.ccol0);
-                int cr0 = rb * kRowBlock + (a.p0 - D0 - a.crow0);
-                bool colok = cc >= 0 && cc < a.CC;
+                const int s = task % nstrip, rb = task / nstrip;
+                const int j = 32 * s + lane;               // output column (0-based)
+                const bool colok = j < a.nTheta;
+                const int i0 = rb * kRowBlock;             // first output row (0-based)
                 float v[NV];
 #pragma unroll
                 for (int k = 0; k < NV; ++k) {
-                    int cr = cr0 + k;
-                    v[k] = (colok && cr < a.CR) ? conv[cr * a.CC + cc] : -INFINITY;
+                    // tm row i0 + k covers output rows up to i0 + k - D0; rows past NR are -inf
+                    v[k] = (colok && i0 + k < a.nRho + 2 * D0) ? tm[(i0 + k) * a.nTheta + j] : -INFINITY;
                 }
-                // rho max over [o, o + 2*D0] for o = 0..7: suffix / core / prefix maxima
+                // rho max over [o, o + 2*D0] for o = 0..kRowBlock-1: suffix / core / prefix maxima
                 float suf[kRowBlock], pre[kRowBlock], core = -INFINITY;
                 suf[kRowBlock - 1] = -INFINITY;
 #pragma unroll
@@ -370,28 +513,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 pre[0] = -INFINITY;
 #pragma unroll
                 for (int o = 1; o < kRowBlock; ++o) pre[o] = fmaxf(pre[o - 1], v[2 * D0 + o]);
-                int ocol = a.p1 + SW * s + (lane - D1);  // output column (padded frame)
-                bool lane_out = lane >= D1 && lane < 32 - D1 && ocol < a.p1 + a.nTheta;
+                const float* crow = conv + (i0 + a.p0 - a.crow0) * a.CC + (j + a.p1 - a.ccol0);
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
-                    float m = fmaxf(fmaxf(suf[o], core), pre[o]);
-                    float mt = m;
-#pragma unroll
-                    for (int d = 1; d <= D1; ++d) {
-                        mt = fmaxf(mt, __shfl_up_sync(0xffffffffu, m, d));
-                        mt = fmaxf(mt, __shfl_down_sync(0xffffffffu, m, d));
-                    }
-                    int orow = a.p0 + rb * kRowBlock + o;
-                    float val = v[o + D0];
-                    bool f = lane_out && orow < a.p0 + a.nRho && val == mt &&
-                             a.rdnmask[(orow - a.p0) * a.nTheta + (ocol - a.p1)];
+                    const float m = fmaxf(fmaxf(suf[o], core), pre[o]);
+                    const int i = i0 + o;
+                    const bool inside = colok && i < a.nRho;
+                    const float val = inside ? crow[o * a.CC] : 0.0f;
+                    const bool f = inside && val == m && a.rdnmask[i * a.nTheta + j];
                     unsigned bal = __ballot_sync(0xffffffffu, f);
                     while (bal) {
-                        int b = __ffs(bal) - 1;
+                        const int b = __ffs(bal) - 1;
                         bal &= bal - 1;
-                        float cv = __shfl_sync(0xffffffffu, val, b);
-                        int pos = (orow - a.p0) * a.nTheta + (a.p1 + SW * s + (b - D1) - a.p1);
-                        list_insert(cv, pos, lv, lp, nB, lane);
+                        const float cv = __shfl_sync(0xffffffffu, val, b);
+                        list_insert(cv, i * a.nTheta + 32 * s + b, lv, lp, nB, lane);
                     }
                 }
             }
@@ -400,50 +535,61 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             lv_s[warp * kMaxBands + lane] = lv;
             lp_s[warp * kMaxBands + lane] = lp;
         }
-        rank_s[tid] = 0;
         if (tid < kMaxBands) fin_p[tid] = -1;
+        if (tid == 0) {
+            thr_p[0] = -1;  // no threshold until warp 0 finds nB list heads
+            nsurv[0] = 0;
+        }
         __syncthreads();
 
-        // ---- 6. merge the warp lists: rank of a candidate = candidates ahead of it ----
-        // (value desc, position asc is a strict total order: positions are unique).  Each
-        // candidate's rank is counted over `parts` disjoint sets of warp lists by different
-        // threads, combined with shared-memory atomics; the candidates of rank < nB form the
-        // final list.
-        {
-            const int ncand = kWarps * nB;
-            const int parts = kThreads / ncand;  // >= 1 since nB <= 32
-            const int c = tid % ncand, part = tid / ncand;
-            if (part < parts) {
-                const int cw = c / nB, ck = c - (c / nB) * nB;
-                const float cv = lv_s[cw * kMaxBands + ck];
-                const int cp = lp_s[cw * kMaxBands + ck];
-                if (cp >= 0) {
-                    int rank = 0;
-                    for (int w = part; w < kWarps; w += parts) {
-                        const float* vw = lv_s + w * kMaxBands;
-                        const int* pw = lp_s + w * kMaxBands;
-                        for (int k = 0; k < nB; ++k) {
-                            const int op = pw[k];
-                            if (op < 0) break;
-                            rank += beats(vw[k], op, cv, cp);
-                        }
-                    }
-                    if (rank) atomicAdd(rank_s + c, rank);
-                }
+        // ---- 6. merge the warp lists ----
+        // (value desc, position asc) is a strict total order: positions are unique.  The
+        // threshold is the nB-th best warp-list head: a candidate it beats has nB heads ahead
+        // of it and cannot make the final list, while every member of the final list
+        // survives.  The survivors' ranks among themselves are therefore their final ranks.
+        if (warp == 0) {
+            const float hv = lane < kWarps ? lv_s[lane * kMaxBands] : 0.0f;
+            const int hp = lane < kWarps ? lp_s[lane * kMaxBands] : -1;
+            int r = 0;
+            for (int j = 0; j < kWarps; ++j) {
+                const float v = __shfl_sync(0xffffffffu, hv, j);
+                const int p = __shfl_sync(0xffffffffu, hp, j);
+                r += p >= 0 && beats(v, p, hv, hp);
             }
-            __syncthreads();
-            if (part == 0) {
-                const int cw = c / nB, ck = c - (c / nB) * nB;
-                const float cv = lv_s[cw * kMaxBands + ck];
-                const int cp = lp_s[cw * kMaxBands + ck];
-                const int rank = rank_s[c];
-                if (cp >= 0 && rank < nB) {
+            if (hp >= 0 && r == nB - 1) {  // at most one lane: ranks of valid heads are distinct
+                thr_v[0] = hv;
+                thr_p[0] = hp;
+            }
+        }
+        __syncthreads();
+        const int ncand = kWarps * nB;
+        if (tid < ncand) {
+            const int cw = tid / nB, ck = tid - cw * nB;
+            const float cv = lv_s[cw * kMaxBands + ck];
+            const int cp = lp_s[cw * kMaxBands + ck];
+            const int tp = thr_p[0];
+            if (cp >= 0 && (tp < 0 || !beats(thr_v[0], tp, cv, cp)))
+                surv[atomicAdd(nsurv, 1)] = cw * kMaxBands + ck;
+        }
+        __syncthreads();
+        {
+            const int ns = nsurv[0];
+            for (int k = tid; k < ns; k += kThreads) {
+                const int ci = surv[k];
+                const float cv = lv_s[ci];
+                const int cp = lp_s[ci];
+                int rank = 0;
+                for (int j = 0; j < ns; ++j) {
+                    const int oj = surv[j];
+                    rank += beats(lv_s[oj], lp_s[oj], cv, cp);
+                }
+                if (rank < nB) {
                     fin_v[rank] = cv;
                     fin_p[rank] = cp;
                 }
             }
-            __syncthreads();
         }
+        __syncthreads();
 
         // ---- 7. label: warp 0, one lane per band ----
         if (warp == 0 && lane < nB) {
@@ -461,14 +607,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             band_fit_write<float>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + q) * nB + lane);
         }
         __syncthreads();
+        }  // sub
     }
 }
 
 // ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
-size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1, int ngroups) {
-    size_t b = ((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store + 15) & ~(size_t)15;
+size_t smem_bytes(const FusedGeom& g, size_t store, int ngroups, size_t tm_bytes) {
+    size_t b = (std::max((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store, tm_bytes) + 15) & ~(size_t)15;
     b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
     b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
     b += (size_t)ngroups * 8 + 2 * (kWarps + 1) * 4;
@@ -476,24 +623,82 @@ size_t smem_bytes(const FusedGeom& g, size_t store, int k0, int k1, int ngroups)
     return b;
 }
 
-template <typename InT, typename S>
+template <typename InT, typename S, int P>
 void* kernel_ptr(int k0, int k1) {
-    if (k0 == 5 && k1 == 5) return (void*)k_fused<InT, S, 5, 5>;
-    if (k0 == 7 && k1 == 7) return (void*)k_fused<InT, S, 7, 7>;
-    if (k0 == 9 && k1 == 9) return (void*)k_fused<InT, S, 9, 9>;
-    if (k0 == 5 && k1 == 7) return (void*)k_fused<InT, S, 5, 7>;
-    if (k0 == 7 && k1 == 5) return (void*)k_fused<InT, S, 7, 5>;
+    if (k0 == 5 && k1 == 5) return (void*)k_fused<InT, S, 5, 5, P>;
+    if (k0 == 7 && k1 == 7) return (void*)k_fused<InT, S, 7, 7, P>;
+    if (k0 == 9 && k1 == 9) return (void*)k_fused<InT, S, 9, 9, P>;
+    if (k0 == 5 && k1 == 7) return (void*)k_fused<InT, S, 5, 7, P>;
+    if (k0 == 7 && k1 == 5) return (void*)k_fused<InT, S, 7, 5, P>;
     return nullptr;
 }
 
-void* pick_kernel(int method, int dtype, int k0, int k1) {
+void* pick_kernel(int method, int dtype, int k0, int k1, int pack) {
     bool h = method == EBSD_FUSED_F16;
     switch (dtype) {
-        case EBSD_U8: return h ? kernel_ptr<uint8_t, __half>(k0, k1) : kernel_ptr<uint8_t, float>(k0, k1);
-        case EBSD_U16: return h ? kernel_ptr<uint16_t, __half>(k0, k1) : kernel_ptr<uint16_t, float>(k0, k1);
-        case EBSD_F32: return h ? kernel_ptr<float, __half>(k0, k1) : kernel_ptr<float, float>(k0, k1);
+        case EBSD_U8:
+            if (pack == 4 && !h) return kernel_ptr<uint8_t, float, 4>(k0, k1);
+            if (pack == 2 && !h) return kernel_ptr<uint8_t, float, 2>(k0, k1);
+            return h ? kernel_ptr<uint8_t, __half, 1>(k0, k1) : kernel_ptr<uint8_t, float, 1>(k0, k1);
+        case EBSD_U16:
+            return h ? kernel_ptr<uint16_t, __half, 1>(k0, k1) : kernel_ptr<uint16_t, float, 1>(k0, k1);
+        case EBSD_F32:
+            return h ? kernel_ptr<float, __half, 1>(k0, k1) : kernel_ptr<float, float, 1>(k0, k1);
     }
     return nullptr;
+}
+
+// Packed modes apply to uint8 patterns without a background, FP32 tile, rays of <= 257
+// pixels; four per pass also needs the 8-byte-element tile and its LUT (fg.quad).  Returns
+// the largest patterns-per-pass the call may use (1, 2 or 4).
+int max_pack(const ebsd_plan_s* p, int method, int dtype, int64_t n) {
+    if (!(dtype == EBSD_U8 && method == EBSD_FUSED_F32 && p->bg_mode == 0 && p->maxCount <= 257 && n >= 2))
+        return 1;
+    return p->fg.quad && p->d_flut8 ? 4 : 2;
+}
+
+// Launch facts, set up on first use so that later launches -- also inside a CUDA-graph
+// capture -- issue nothing but the launch itself.  The opt-in shared-memory attribute is per
+// (kernel, device) and only ever raised (plans of different sizes share a kernel); resident
+// CTAs per SM are kept per (kernel, device, shared-memory size).
+struct SmemAttr {
+    const void* fn;
+    int device, smem_max;
+};
+struct LaunchCfg {
+    const void* fn;
+    int device, smem, sms, per_sm;
+};
+std::mutex g_cfg_mtx;
+std::vector<SmemAttr> g_attr;
+std::vector<LaunchCfg> g_cfg;
+
+int launch_config(const void* fn, int device, int smem, int* sms, int* per_sm) {
+    std::lock_guard<std::mutex> lk(g_cfg_mtx);
+    SmemAttr* attr = nullptr;
+    for (SmemAttr& s : g_attr)
+        if (s.fn == fn && s.device == device) attr = &s;
+    if (!attr) {
+        g_attr.push_back(SmemAttr{fn, device, 0});
+        attr = &g_attr.back();
+    }
+    if (smem > attr->smem_max) {
+        EBSD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr->smem_max = smem;
+    }
+    for (const LaunchCfg& c : g_cfg)
+        if (c.fn == fn && c.device == device && c.smem == smem) {
+            *sms = c.sms;
+            *per_sm = c.per_sm;
+            return EBSD_OK;
+        }
+    LaunchCfg c{fn, device, smem, 0, 0};
+    EBSD_CUDA_TRY(cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, device));
+    EBSD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.per_sm, fn, kThreads, smem));
+    g_cfg.push_back(c);
+    *sms = c.sms;
+    *per_sm = c.per_sm;
+    return EBSD_OK;
 }
 
 }  // namespace
@@ -503,7 +708,7 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     const int K0 = p->k0, K1 = p->k1;
     // the fused kernel assumes the standard windows: peakPad = 2*ksz + 1 (half-window = ksz)
     bool shape_ok = p->pk0 == 2 * K0 + 1 && p->pk1 == 2 * K1 + 1 && 2 * K1 < 32 &&
-                    pick_kernel(EBSD_FUSED_F32, EBSD_U8, K0, K1) != nullptr &&
+                    pick_kernel(EBSD_FUSED_F32, EBSD_U8, K0, K1, 1) != nullptr &&
                     p->p0 >= K0 + K0 / 2 && p->p1 >= K1 + K1 / 2;
     int pitch = p->W + 1;
     if (((int64_t)p->H * pitch + 1) * 4 >= 65535) shape_ok = false;  // byte offsets in 16 bits
@@ -521,14 +726,18 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         g.tile_pitch = pitch;
         g.threads = kThreads;
         int ngroups = p->nTheta * ((p->nRho + 31) / 32);  // 32-ray groups of the fused LUT
-        g.smem_f32 = (int)smem_bytes(g, 4, K0, K1, ngroups);
-        g.smem_f16 = (int)smem_bytes(g, 2, K0, K1, ngroups);
+        const size_t tm_bytes = (size_t)(p->nRho + 2 * D0) * p->nTheta * sizeof(float);
+        g.smem_f32 = (int)smem_bytes(g, 4, ngroups, tm_bytes);
+        g.smem_f16 = (int)smem_bytes(g, 2, ngroups, tm_bytes);
         size_t conv_cells = (size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0);
         int dev_smem = 0;
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
         g.ok = conv_cells >= (size_t)p->H * pitch + 1 && g.smem_f16 <= dev_smem && g.row0 >= 0 &&
                (size_t)(g.row1 - g.row0) * (g.col1 - g.col0) < 65535;
         g.ok_f32 = g.ok && g.smem_f32 <= dev_smem;
+        // four patterns per pass: 8-byte pixel elements, byte offsets still in 16 bits
+        const size_t quad_bytes = ((size_t)p->H * pitch + 1) * 8;
+        g.quad = g.ok_f32 && quad_bytes < 65535 && conv_cells * 4 >= quad_bytes;
     }
     p->fg = g;
     if (!g.ok) return EBSD_OK;
@@ -546,6 +755,10 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     const int gpt = (p->nRho + 31) / 32;  // groups per theta column
     const int nGroups = p->nTheta * gpt;
     const int nRaysPad = nGroups * 32;
+    if (nGroups > 65535) {  // group ids are packed into 16 bits
+        p->fg.ok = p->fg.ok_f32 = p->fg.quad = 0;
+        return EBSD_OK;
+    }
     const uint16_t zero = (uint16_t)(p->H * pitch);
     std::vector<int32_t> cnt(nRaysPad, 0), gch(nGroups, 1), gaxis(nGroups, 2), gbase(nGroups, 0);
     std::vector<char> seen((size_t)std::max(p->W, p->H));
@@ -607,12 +820,22 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         wg[w].push_back(g);
         wload[w] += gch[g];
     }
-    std::vector<int32_t> gids, wofs(2 * (kWarps + 1), 0);
+    // per-warp stream order: group id | chunks << 16, and the Radon tile offset of the
+    // group's lane 0 | rays inside nRho << 16; each warp's chunk stream is followed by kRing
+    // zero chunks so that the kernel's ring of prefetched chunks loads unconditionally
+    std::vector<uint32_t> gst, gtb;
+    std::vector<int32_t> wofs(2 * (kWarps + 1), 0);
+    const int TC = g.col1 - g.col0;
     for (int w = 0; w < kWarps; ++w) {
         std::sort(wg[w].begin(), wg[w].end());
         wofs[w + 1] = wofs[w] + (int)wg[w].size();
-        wofs[kWarps + 1 + w + 1] = wofs[kWarps + 1 + w] + (int)wload[w];
-        for (int g : wg[w]) gids.push_back(g);
+        wofs[kWarps + 1 + w + 1] = wofs[kWarps + 1 + w] + (int)wload[w] + kRing;
+        for (int gg : wg[w]) {
+            const int j = gg / gpt, i0 = (gg % gpt) * 32;
+            gst.push_back((uint32_t)gg | ((uint32_t)gch[gg] << 16));
+            const int base = (i0 + p->p0 - g.row0) * TC + (j + p->p1 - g.col0);
+            gtb.push_back((uint32_t)base | ((uint32_t)std::min(32, p->nRho - i0) << 16));
+        }
     }
     const long total_chunks = wofs[2 * kWarps + 1];
     // stream layout: [chunk of the warp's stream][lane][8 entries], entry = byte offset
@@ -691,9 +914,23 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     }
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_flut, lut.size() * sizeof(uint16_t)));
     EBSD_CUDA_TRY(cudaMemcpy(p->d_flut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    if (p->fg.quad) {
+        // 8-byte tile elements: every byte offset (cell * 4) doubles; fg.quad guarantees
+        // the doubled offsets, zero element included, stay below 65535
+        for (uint16_t& e : lut) e = (uint16_t)(e * 2);
+        EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_flut8, lut.size() * sizeof(uint16_t)));
+        EBSD_CUDA_TRY(cudaMemcpy(p->d_flut8, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+    // device tables: [count][RN(1/count)][stream group ids][stream tile offsets][wofs]
     std::vector<int32_t> tables(cnt);
-    tables.insert(tables.end(), gch.begin(), gch.end());
-    tables.insert(tables.end(), gids.begin(), gids.end());
+    for (int t = 0; t < nRaysPad; ++t) {
+        const float r = cnt[t] > 0 ? 1.0f / (float)cnt[t] : 0.0f;
+        int32_t bits;
+        std::memcpy(&bits, &r, sizeof(bits));
+        tables.push_back(bits);
+    }
+    tables.insert(tables.end(), gst.begin(), gst.end());
+    tables.insert(tables.end(), gtb.begin(), gtb.end());
     tables.insert(tables.end(), wofs.begin(), wofs.end());
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fgroup, tables.size() * sizeof(int32_t)));
     EBSD_CUDA_TRY(cudaMemcpy(p->d_fgroup, tables.data(), tables.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
@@ -703,6 +940,8 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
 
 void fused_release(ebsd_plan_s* p) {
     cudaFree(p->d_flut);
+    cudaFree(p->d_flut8);
+    p->d_flut8 = nullptr;
     cudaFree(p->d_fgroup);
     cudaFree(p->d_fray);
     cudaFree(p->d_fpad);
@@ -718,21 +957,37 @@ int fused_supported(const ebsd_plan_s* p, int method) {
     return method == EBSD_FUSED_F16;
 }
 
-size_t fused_workspace_bytes(const ebsd_plan_s*, int, int64_t) { return 0; }
+// packed-mode scratch: (patterns per pass - 1) rows of parked ray means per resident CTA
+size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t) {
+    if (method != EBSD_FUSED_F32 || !p->fg.ok_f32) return 0;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+    const int rows = p->fg.quad ? 3 : 1;
+    return (size_t)std::max(sms, 1) * rows * p->fg.nRaysPad * sizeof(float);
+}
+
+int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t n) {
+    int pack = max_pack(p, method, dtype, n);
+    if (pack == 1 || p->ws.ptr == nullptr || p->ws.bytes < fused_workspace_bytes(p, method, n)) return 1;
+    if (p->fused_ppp >= 1 && p->fused_ppp < pack) pack = p->fused_ppp;
+    return pack;
+}
 
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
     if (n <= 0) return EBSD_OK;
-    void* fn = pick_kernel(method, dtype, p->k0, p->k1);
+    const int pack = fused_patterns_per_pass(p, method, dtype, n);
+    void* fn = pick_kernel(method, dtype, p->k0, p->k1, pack);
     if (!fn) return EBSD_E_UNSUPPORTED;
     const FusedGeom& g = p->fg;
     int smem = method == EBSD_FUSED_F16 ? g.smem_f16 : g.smem_f32;
-    EBSD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     int sms = 0, per_sm = 0;
-    EBSD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
-    EBSD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, smem));
+    int rc = launch_config(fn, p->device, smem, &sms, &per_sm);
+    if (rc != EBSD_OK) return rc;
     if (per_sm < 1) return EBSD_E_UNSUPPORTED;
-    int64_t grid = std::min<int64_t>(n, (int64_t)sms * per_sm);
+    int64_t units = (n + pack - 1) / pack;
+    int64_t grid = std::min<int64_t>(units, (int64_t)sms * per_sm);
+    if (pack > 1 && grid > sms) grid = sms;  // the scratch holds one set of rows per SM
 
     FusedArgs a;
     a.pats = d_pats;
@@ -742,12 +997,15 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.nPx = p->nPx;
     a.pitch = g.tile_pitch;
     a.lut = (const uint4*)p->d_flut;
+    a.lut8 = (const uint4*)p->d_flut8;
     a.count = p->d_fgroup;
-    a.gchunks = p->d_fgroup + g.nRaysPad;
-    a.gids = a.gchunks + g.nGroups;
-    a.wofs = a.gids + g.nGroups;
+    a.rcount = (const float*)(p->d_fgroup + g.nRaysPad);
+    a.gstream = (const uint32_t*)(p->d_fgroup + 2 * g.nRaysPad);
+    a.gtile = a.gstream + g.nGroups;
+    a.wofs = (const int32_t*)(a.gtile + g.nGroups);
     a.padlist = p->d_fpad;
     a.npad = g.npad;
+    a.pack_scratch = pack > 1 ? (float*)p->ws.ptr : nullptr;
     a.gpt = g.gpt;
     a.nRays = p->nRays;
     a.nRaysPad = g.nRaysPad;

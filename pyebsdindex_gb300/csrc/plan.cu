@@ -372,4 +372,80 @@ int ebsd_find_bands_host(ebsd_plan_t p, int method, int dtype, const void* h_pat
     return EBSD_OK;
 }
 
+int ebsd_plan_set_patterns_per_pass(ebsd_plan_t p, int ppp) {
+    if (!p || !(ppp == 0 || ppp == 1 || ppp == 2 || ppp == 4)) return EBSD_E_ARG;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    p->fused_ppp = ppp == 0 ? -1 : ppp;
+    return EBSD_OK;
+}
+
+int ebsd_plan_autotune(ebsd_plan_t p, int method, int dtype, const void* d_pats, int64_t n,
+                       void* stream, int* patterns_per_pass) {
+    if (!p || n <= 0 || !d_pats) return EBSD_E_ARG;
+    if (dtype != EBSD_U8 && dtype != EBSD_U16 && dtype != EBSD_F32) return EBSD_E_DTYPE;
+    int rc = check_method(p, method);
+    if (rc != EBSD_OK) return rc;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!is_fused(method)) {
+        if (patterns_per_pass) *patterns_per_pass = 1;
+        return EBSD_OK;
+    }
+    rc = reserve(p, method, n);
+    if (rc != EBSD_OK) return rc;
+    p->fused_ppp = -1;
+    const int maxp = fused_patterns_per_pass(p, method, dtype, n);
+    if (maxp == 1) {  // one variant only
+        if (patterns_per_pass) *patterns_per_pass = 1;
+        return EBSD_OK;
+    }
+    // time the variants (they give identical records) on the caller's sample
+    const size_t nb = (size_t)n * p->nB;
+    char* buf = nullptr;
+    EBSD_CUDA_TRY(cudaMalloc((void**)&buf, nb * (10 * sizeof(float) + 1) + 256));
+    ebsd_bands dev;
+    dev.max = (float*)buf;
+    dev.normmax = dev.max + nb;
+    dev.maxloc = dev.normmax + nb;
+    dev.avemax = dev.maxloc + 2 * nb;
+    dev.aveloc = dev.avemax + nb;
+    dev.width = dev.aveloc + 2 * nb;
+    dev.theta = dev.width + nb;
+    dev.rho = dev.theta + nb;
+    dev.valid = (int8_t*)(dev.rho + nb);
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    float best_ms = 0.0f;
+    int best = maxp;
+    int64_t launches = 0;
+    for (int i = 0; i < 2 && rc == EBSD_OK; ++i)
+        if (cudaEventCreate(&ev[i]) != cudaSuccess) rc = EBSD_E_LAUNCH;
+    for (int ppp = maxp; ppp >= 1 && rc == EBSD_OK; ppp /= 2) {
+        p->fused_ppp = ppp;
+        float ms_min = 0.0f;
+        for (int rep = 0; rep < 3 && rc == EBSD_OK; ++rep) {  // first pass warms up
+            if (cudaEventRecord(ev[0], st) != cudaSuccess) { rc = EBSD_E_LAUNCH; break; }
+            rc = fused_run_chunk(p, method, dtype, d_pats, n, &dev, 0, st, &launches);
+            if (rc != EBSD_OK) break;
+            if (cudaEventRecord(ev[1], st) != cudaSuccess || cudaEventSynchronize(ev[1]) != cudaSuccess) {
+                rc = EBSD_E_LAUNCH;
+                break;
+            }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (rep > 0 && (rep == 1 || ms < ms_min)) ms_min = ms;
+        }
+        if (rc == EBSD_OK && (ppp == maxp || ms_min < best_ms)) {
+            best_ms = ms_min;
+            best = ppp;
+        }
+    }
+    for (int i = 0; i < 2; ++i)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    cudaFree(buf);
+    p->fused_ppp = rc == EBSD_OK ? best : -1;
+    if (rc == EBSD_OK && patterns_per_pass) *patterns_per_pass = best;
+    return rc;
+}
+
 }  // extern "C"
