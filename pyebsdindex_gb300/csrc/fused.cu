@@ -120,7 +120,8 @@ __device__ __forceinline__ float load_pixel(const InT* p, int idx, int bg_mode, 
 // lane, and integer sums are exact, so the means equal the float sequential sums of the
 // single-pattern pass.  The other patterns' ray means are parked in a per-CTA global scratch
 // (L2-resident) and reloaded once the pattern before them is finished.
-template <typename InT, typename S, int K0, int K1, int kPack>
+// kNT > 0: nTheta fixed at compile time, so every tile pitch is a constant (0: runtime).
+template <typename InT, typename S, int K0, int K1, int kPack, int kNT>
 __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     static_assert(kPack == 1 || (sizeof(S) == 4 && sizeof(InT) == 1), "packed modes: uint8 input, FP32 tile");
     static_assert(kPack == 1 || kPack == 2 || kPack == 4, "1, 2 or 4 patterns per pass");
@@ -133,6 +134,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 
     constexpr bool kHalf = sizeof(S) == 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // geometry: conv tile = padded rows [p0 - D0, ..) x columns [p1 - D1, p1 + nTheta + D1),
+    // Radon tile = the conv tile grown by the kernel half-widths (H0, H1) on each side
+    const int nT = kNT > 0 ? kNT : a.nTheta;
+    const int CC = kNT > 0 ? kNT + 2 * D1 : a.CC;
+    const int TC = kNT > 0 ? kNT + 2 * D1 + 2 * H1 : a.TC;
     size_t off = 0;
     // the conv tile comes first so that the pattern tile aliased into it starts at shared
     // offset 0: the LUT then holds byte offsets usable directly as load addresses
@@ -151,28 +157,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     off += kWarps * kMaxBands * sizeof(int);
     double* red_d = (double*)(smem + off);
     off += 32 * sizeof(double);
-    float* red_f = (float*)(smem + off);  // 66 floats, then the merge's scalars
-    float* thr_v = red_f + 72;            // merge threshold (value, position)
-    int* thr_p = (int*)(red_f + 73);
-    int* nsurv = (int*)(red_f + 74);      // number of merge survivors
+    float* red_f = (float*)(smem + off);  // 66 floats
     off += 80 * sizeof(float);
     unsigned* gst_s = (unsigned*)(smem + off);  // nGroups: group id | chunks << 16, stream order
     off += (size_t)a.nGroups * sizeof(unsigned);
     unsigned* gtb_s = (unsigned*)(smem + off);  // nGroups: tile offset | valid rays << 16
     off += (size_t)a.nGroups * sizeof(unsigned);
     int* wofs_s = (int*)(smem + off);     // 2 * (kWarps + 1) ints: per-warp group / chunk offsets
-    off += 2 * (kWarps + 1) * sizeof(int);
-    int* surv = (int*)(smem + off);       // kThreads ints: surviving candidates of the merge
-    off += kThreads * sizeof(int);
-    float* fin_v = (float*)(smem + off);  // final top-N list
-    off += kMaxBands * sizeof(float);
-    int* fin_p = (int*)(smem + off);
 
     for (int i = tid; i < a.nGroups; i += kThreads) {
         gst_s[i] = a.gstream[i];
         gtb_s[i] = a.gtile[i];
     }
     for (int i = tid; i < 2 * (kWarps + 1); i += kThreads) wofs_s[i] = a.wofs[i];
+    for (int i = tid; i < kWarps * kMaxBands; i += kThreads) lp_s[i] = -1;  // empty warp lists
     __syncthreads();
     const int nB = a.kc.nB;
     const int stat_r0 = a.p0, stat_r1 = a.statR1, stat_c0 = a.p1, stat_c1 = a.p1 + a.nTheta;
@@ -326,7 +324,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                                 if (kHalf) v = (v - cen) * scl;
                             }
                             const unsigned tb = gtb_s[gi];
-                            if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * a.TC] = to_store<S>(v);
+                            if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * TC] = to_store<S>(v);
                             ++gi;
                             pc = 0;
                             sum = 0.0f;
@@ -345,55 +343,116 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         }
         __syncthreads();
 
+        // ---- 6. merge + 7. label (warp 0), for pattern qq: a k-way merge of the sorted
+        //      warp lists -- lane l holds the head of warp l's list; each round the best head
+        //      under (value desc, position asc), a strict total order on which every lane of
+        //      the xor butterfly agrees, goes to lane k and its list advances -- then lanes
+        //      0..nB-1 fit their band (band_detect.py:691-809).  Reads the warp lists, the conv
+        //      tile and the conv statistics of qq only.
+        auto merge_label = [&](int64_t qq) {
+            int ptr = 0;
+            float hv = lane < kWarps ? lv_s[lane * kMaxBands] : -INFINITY;
+            int hp = lane < kWarps ? lp_s[lane * kMaxBands] : -1;
+            int mypos = -1;
+            for (int k = 0; k < nB; ++k) {
+                float bv = hv;
+                int bp = hp, bl = lane;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                    const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+                    const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
+                    if (op >= 0 && (bp < 0 || beats(ov, op, bv, bp))) {
+                        bv = ov;
+                        bp = op;
+                        bl = ol;
+                    }
+                }
+                if (bp < 0) break;  // every list is exhausted (the same in all lanes)
+                if (lane == k) mypos = bp;
+                if (lane == bl) {
+                    ++ptr;
+                    hp = ptr < nB ? lp_s[lane * kMaxBands + ptr] : -1;
+                    hv = ptr < nB ? lv_s[lane * kMaxBands + ptr] : -INFINITY;
+                }
+            }
+            if (lane < nB) {
+                const bool has = mypos >= 0;
+                int r = 0, c = 0;
+                if (has) {
+                    const int i = mypos / nT;
+                    r = i + a.p0;
+                    c = (mypos - i * nT) + a.p1;
+                }
+                const float mn = red_f[0];
+                const float mean = (float)(red_d[0] / (double)stat_count);
+                SmemConv acc{conv, a.p0 - D0, a.p1 - D1, CC};
+                band_fit_write<float>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + qq) * nB + lane);
+            }
+        };
+
         for (int sub = 0; sub < npk; ++sub) {
         const int64_t q = q0 + sub;
-        if (kPack > 1 && sub > 0) {
-            // the next pattern's ray means, parked by the gather, back into the tile
-            const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
-            for (int t = tid; t < a.nRaysPad; t += kThreads) {
-                const int grp = t >> 5, j = grp / a.gpt, i = (grp - j * a.gpt) * 32 + (t & 31);
-                if (i < a.nRho) tile[(i + a.p0 - a.row0) * a.TC + (j + a.p1 - a.col0)] = to_store<S>(src[t]);
-            }
-            __syncthreads();
-        }
         // ---- 3. pad the tile around the interior ----
         // padding cell list (plan table): low half = destination tile cell, high half = source
-        // tile cell, 0xFFFF = zero (rows below the padded array, the convolution's zero fill)
-        for (int k = tid; k < a.npad; k += kThreads) {
-            const unsigned e = __ldg(a.padlist + k);
-            const unsigned src = e >> 16;
-            tile[e & 0xFFFF] = src == 0xFFFFu ? to_store<S>(kHalf ? -cen * scl : 0.0f) : tile[src];
+        // tile cell, 0xFFFF = zero (rows below the padded array, the convolution's zero fill).
+        // After the first pattern of a packed unit, warp 0 merges and labels the previous
+        // pattern while warps 1.. reload this pattern's parked ray means and pad the tile.
+        if (kPack > 1 && sub > 0) {
+            if (warp == 0) {
+                merge_label(q - 1);
+            } else {
+                // parked ray means back into the tile: warp w >= 1 takes the groups at stream
+                // positions w - 1, w - 1 + (kWarps - 1), ... (one ray per lane)
+                const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
+                for (int gi = warp - 1; gi < a.nGroups; gi += kWarps - 1) {
+                    const unsigned tb = gtb_s[gi];
+                    const float v = src[(gst_s[gi] & 0xFFFFu) * 32 + lane];
+                    if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * TC] = v;
+                }
+                asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");  // warps 1.. only
+                for (int k = tid - 32; k < a.npad; k += kThreads - 32) {
+                    const unsigned e = __ldg(a.padlist + k);
+                    const unsigned src2 = e >> 16;
+                    tile[e & 0xFFFF] = src2 == 0xFFFFu ? to_store<S>(0.0f) : tile[src2];
+                }
+            }
+        } else {
+            for (int k = tid; k < a.npad; k += kThreads) {
+                const unsigned e = __ldg(a.padlist + k);
+                const unsigned src = e >> 16;
+                tile[e & 0xFFFF] = src == 0xFFFFu ? to_store<S>(kHalf ? -cen * scl : 0.0f) : tile[src];
+            }
         }
         __syncthreads();
 
-        // ---- 4. LoG convolution, kRowBlock outputs per thread down one column ----
+        // ---- 4. LoG convolution: conv[cr][cc] = sum_a sum_b tap[a][b] tile[cr+2H0-a][cc+2H1-b],
+        //      kRowBlock outputs per thread down one column.  The last row block is moved up to
+        //      end at CR, so no load leaves the tile; rows it shares with the block above are
+        //      neither stored again nor counted twice.
         float smin = INFINITY, ssum = 0.0f;
         {
-            const int nrb = (a.CR + kRowBlock - 1) / kRowBlock;
-            const int ntask = nrb * a.CC;
+            const int CR = a.CR;
+            const int nrb = (CR + kRowBlock - 1) / kRowBlock;
+            const int ntask = nrb * CC;
             // task = rb * CC + cc, advanced by kThreads without a division per task
-            int cc = tid % a.CC, rb = tid / a.CC;
-            const int dcc = kThreads % a.CC, drb = kThreads / a.CC;
+            int cc = tid % CC, rb = tid / CC;
+            const int dcc = kThreads % CC, drb = kThreads / CC;
             const unsigned stat_rows = (unsigned)(stat_r1 - stat_r0);
             for (int task = tid; task < ntask; task += kThreads) {
-                const int cr0 = rb * kRowBlock;
+                const int cr_first = rb * kRowBlock;
+                const int cr0 = cr_first < CR - kRowBlock ? cr_first : CR - kRowBlock;
                 float acc[kRowBlock];
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) acc[o] = 0.0f;
                 // tile row (cr0 + t) feeds output o through kernel row a = o + 2*H0 - t;
                 // descending t keeps each output's multiply-add order = ascending a.
-                const S* tcol = tile + cc + 2 * H1;
+                const S* tcol = tile + cr0 * TC + cc + 2 * H1;
 #pragma unroll
                 for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
-                    const int tr = cr0 + t;
                     float v[K1];
-                    if (tr < a.TR) {
 #pragma unroll
-                        for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[tr * a.TC - b]);
-                    } else {
-#pragma unroll
-                        for (int b = 0; b < K1; ++b) v[b] = 0.0f;
-                    }
+                    for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[t * TC - b]);
 #pragma unroll
                     for (int o = 0; o < kRowBlock; ++o) {
                         const int ka = o + 2 * H0 - t;
@@ -403,17 +462,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                         }
                     }
                 }
-                // statistics slice: padded rows [stat_r0, stat_r1) x columns [stat_c0, stat_c1)
-                const int col = cc + a.ccol0;
-                const bool colstat = col >= stat_c0 && col < stat_c1;
-                const int rs0 = cr0 + a.crow0 - stat_r0;
+                // statistics slice: padded rows [stat_r0, stat_r1) x columns [stat_c0, stat_c1),
+                // i.e. conv rows from D0 and conv columns [D1, D1 + nTheta)
+                const bool colstat = (unsigned)(cc - D1) < (unsigned)nT;
+                float* ccol = conv + cr0 * CC + cc;
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
-                    const int cr = cr0 + o;
                     if (kHalf) acc[o] = fmaf(a.ksum, cen, acc[o] * inv_scl);
-                    if (cr < a.CR) {
-                        conv[cr * a.CC + cc] = acc[o];
-                        if (colstat && (unsigned)(rs0 + o) < stat_rows) {
+                    if (cr0 + o >= cr_first) {
+                        ccol[o * CC] = acc[o];
+                        if (colstat && (unsigned)(cr0 + o - D0) < stat_rows) {
                             smin = fminf(smin, acc[o]);
                             ssum += acc[o];
                         }
@@ -421,8 +479,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 }
                 cc += dcc;
                 rb += drb;
-                if (cc >= a.CC) {
-                    cc -= a.CC;
+                if (cc >= CC) {
+                    cc -= CC;
                     ++rb;
                 }
             }
@@ -451,58 +509,60 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 
         // ---- 5. peaks: separable max filter (band_detect.py:639-664, :811-843) ----
         // 5a. theta max of every conv row the rho window needs, into the dead Radon tile:
-        //     tm[rr][j] = max(conv[p0 - D0 + rr][p1 + j - D1 .. p1 + j + D1]).  One thread per
-        //     WIN consecutive outputs: suffix maxima of the first WIN inputs and running
-        //     prefix maxima of the next WIN - 1 give every window with two max operations.
+        //     tm[rr][j] = max(conv[rr][j .. j + 2*D1]) for rr < nRho + 2*D0, j < nTheta (conv
+        //     row rr = padded row p0 - D0 + rr, conv column j = padded column p1 + j - D1).
+        //     One thread per WIN consecutive outputs: suffix maxima of the first WIN inputs and
+        //     running prefix maxima of the next WIN - 1 give every window with two max
+        //     operations.  The last segment is moved left to end at nTheta (its overlap is
+        //     written twice with the same values).
         float* tm = (float*)tile;
         {
             const int NR = a.nRho + 2 * D0;
-            const int nseg = (a.nTheta + WIN - 1) / WIN;
+            constexpr int kSeg = (kNT + WIN - 1) / WIN;  // segments per row when nTheta is fixed
+            const int nseg = kNT > 0 ? kSeg : (nT + WIN - 1) / WIN;
             for (int task = tid; task < NR * nseg; task += kThreads) {
                 const int rr = task / nseg, sg = task - rr * nseg;
-                const int j0 = sg * WIN;
-                const float* x = conv + (rr + a.p0 - D0 - a.crow0) * a.CC + (j0 + a.p1 - D1 - a.ccol0);
-                float* out = tm + rr * a.nTheta + j0;
-                const int nout = a.nTheta - j0 < WIN ? a.nTheta - j0 : WIN;
+                const int j0 = sg * WIN < nT - WIN ? sg * WIN : nT - WIN;
+                const float* x = conv + rr * CC + j0;
+                float* out = tm + rr * nT + j0;
                 float xv[2 * WIN - 1];
-                if (nout == WIN) {
 #pragma unroll
-                    for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = x[k];
-                } else {
-#pragma unroll
-                    for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = k < nout + 2 * D1 ? x[k] : -INFINITY;
-                }
+                for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = x[k];
 #pragma unroll
                 for (int k = WIN - 2; k >= 0; --k) xv[k] = fmaxf(xv[k], xv[k + 1]);  // suffix maxima
                 float pm = -INFINITY;
 #pragma unroll
                 for (int t = 0; t < WIN; ++t) {
                     if (t > 0) pm = fmaxf(pm, xv[WIN - 1 + t]);
-                    if (t < nout) out[t] = fmaxf(xv[t], pm);
+                    out[t] = fmaxf(xv[t], pm);
                 }
             }
         }
         __syncthreads();
 
         // 5b. rho max of tm over [i - D0, i + D0], exact equality with the conv value and the
-        //     Radon mask; warp task = kRowBlock output rows x 32 columns (one per lane), the
-        //     flagged peaks go into the warp's top-N list ordered by (value desc, position asc)
+        //     Radon mask; warp task = kRowBlock output rows x 32 columns (one per lane).  The
+        //     last row block is moved up to end at nRho and the last strip's spare lanes
+        //     repeat column nTheta - 1; only rows and columns a task owns can flag.  Flagged
+        //     peaks go into the warp's top-N list ordered by (value desc, position asc).
         float lv = -INFINITY;
         int lp = -1;
         {
-            const int nstrip = (a.nTheta + 31) / 32;
-            const int nrowb = (a.nRho + kRowBlock - 1) / kRowBlock;
+            const int nrho = a.nRho;
+            constexpr int kStrip = (kNT + 31) / 32;
+            const int nstrip = kNT > 0 ? kStrip : (nT + 31) / 32;
+            const int nrowb = (nrho + kRowBlock - 1) / kRowBlock;
             for (int task = warp; task < nstrip * nrowb; task += kWarps) {
-                const int s = task % nstrip, rb = task / nstrip;
-                const int j = 32 * s + lane;               // output column (0-based)
-                const bool colok = j < a.nTheta;
-                const int i0 = rb * kRowBlock;             // first output row (0-based)
+                const int rb = task / nstrip, st = task - rb * nstrip;
+                const int jl = 32 * st + lane;
+                const bool colok = jl < nT;
+                const int j = colok ? jl : nT - 1;
+                const int i_first = rb * kRowBlock;
+                const int i0 = i_first < nrho - kRowBlock ? i_first : nrho - kRowBlock;
+                const float* tcol = tm + i0 * nT + j;
                 float v[NV];
 #pragma unroll
-                for (int k = 0; k < NV; ++k) {
-                    // tm row i0 + k covers output rows up to i0 + k - D0; rows past NR are -inf
-                    v[k] = (colok && i0 + k < a.nRho + 2 * D0) ? tm[(i0 + k) * a.nTheta + j] : -INFINITY;
-                }
+                for (int k = 0; k < NV; ++k) v[k] = tcol[k * nT];
                 // rho max over [o, o + 2*D0] for o = 0..kRowBlock-1: suffix / core / prefix maxima
                 float suf[kRowBlock], pre[kRowBlock], core = -INFINITY;
                 suf[kRowBlock - 1] = -INFINITY;
@@ -513,20 +573,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 pre[0] = -INFINITY;
 #pragma unroll
                 for (int o = 1; o < kRowBlock; ++o) pre[o] = fmaxf(pre[o - 1], v[2 * D0 + o]);
-                const float* crow = conv + (i0 + a.p0 - a.crow0) * a.CC + (j + a.p1 - a.ccol0);
+                const float* crow = conv + (i0 + D0) * CC + j + D1;
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
                     const float m = fmaxf(fmaxf(suf[o], core), pre[o]);
                     const int i = i0 + o;
-                    const bool inside = colok && i < a.nRho;
-                    const float val = inside ? crow[o * a.CC] : 0.0f;
-                    const bool f = inside && val == m && a.rdnmask[i * a.nTheta + j];
+                    const float val = crow[o * CC];
+                    const bool f = colok && i >= i_first && val == m && a.rdnmask[i * nT + j];
                     unsigned bal = __ballot_sync(0xffffffffu, f);
                     while (bal) {
                         const int b = __ffs(bal) - 1;
                         bal &= bal - 1;
                         const float cv = __shfl_sync(0xffffffffu, val, b);
-                        list_insert(cv, i * a.nTheta + 32 * s + b, lv, lp, nB, lane);
+                        list_insert(cv, i * nT + 32 * st + b, lv, lp, nB, lane);
                     }
                 }
             }
@@ -535,78 +594,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             lv_s[warp * kMaxBands + lane] = lv;
             lp_s[warp * kMaxBands + lane] = lp;
         }
-        if (tid < kMaxBands) fin_p[tid] = -1;
-        if (tid == 0) {
-            thr_p[0] = -1;  // no threshold until warp 0 finds nB list heads
-            nsurv[0] = 0;
-        }
         __syncthreads();
 
-        // ---- 6. merge the warp lists ----
-        // (value desc, position asc) is a strict total order: positions are unique.  The
-        // threshold is the nB-th best warp-list head: a candidate it beats has nB heads ahead
-        // of it and cannot make the final list, while every member of the final list
-        // survives.  The survivors' ranks among themselves are therefore their final ranks.
-        if (warp == 0) {
-            const float hv = lane < kWarps ? lv_s[lane * kMaxBands] : 0.0f;
-            const int hp = lane < kWarps ? lp_s[lane * kMaxBands] : -1;
-            int r = 0;
-            for (int j = 0; j < kWarps; ++j) {
-                const float v = __shfl_sync(0xffffffffu, hv, j);
-                const int p = __shfl_sync(0xffffffffu, hp, j);
-                r += p >= 0 && beats(v, p, hv, hp);
-            }
-            if (hp >= 0 && r == nB - 1) {  // at most one lane: ranks of valid heads are distinct
-                thr_v[0] = hv;
-                thr_p[0] = hp;
-            }
+        // the last pattern of a unit is merged and labelled before the next unit's load
+        // overwrites the conv tile
+        if (kPack == 1 || sub == npk - 1) {
+            if (warp == 0) merge_label(q);
+            __syncthreads();
         }
-        __syncthreads();
-        const int ncand = kWarps * nB;
-        if (tid < ncand) {
-            const int cw = tid / nB, ck = tid - cw * nB;
-            const float cv = lv_s[cw * kMaxBands + ck];
-            const int cp = lp_s[cw * kMaxBands + ck];
-            const int tp = thr_p[0];
-            if (cp >= 0 && (tp < 0 || !beats(thr_v[0], tp, cv, cp)))
-                surv[atomicAdd(nsurv, 1)] = cw * kMaxBands + ck;
-        }
-        __syncthreads();
-        {
-            const int ns = nsurv[0];
-            for (int k = tid; k < ns; k += kThreads) {
-                const int ci = surv[k];
-                const float cv = lv_s[ci];
-                const int cp = lp_s[ci];
-                int rank = 0;
-                for (int j = 0; j < ns; ++j) {
-                    const int oj = surv[j];
-                    rank += beats(lv_s[oj], lp_s[oj], cv, cp);
-                }
-                if (rank < nB) {
-                    fin_v[rank] = cv;
-                    fin_p[rank] = cp;
-                }
-            }
-        }
-        __syncthreads();
-
-        // ---- 7. label: warp 0, one lane per band ----
-        if (warp == 0 && lane < nB) {
-            int pos = fin_p[lane];
-            bool has = pos >= 0;
-            int r = 0, c = 0;
-            if (has) {
-                int i = pos / a.nTheta;
-                r = i + a.p0;
-                c = (pos - i * a.nTheta) + a.p1;
-            }
-            float mn = red_f[0];
-            float mean = (float)(red_d[0] / (double)stat_count);
-            SmemConv acc{conv, a.crow0, a.ccol0, a.CC};
-            band_fit_write<float>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + q) * nB + lane);
-        }
-        __syncthreads();
         }  // sub
     }
 }
@@ -619,31 +614,32 @@ size_t smem_bytes(const FusedGeom& g, size_t store, int ngroups, size_t tm_bytes
     b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
     b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
     b += (size_t)ngroups * 8 + 2 * (kWarps + 1) * 4;
-    b += (size_t)kThreads * 4 + kMaxBands * 8;
     return b;
 }
 
 template <typename InT, typename S, int P>
-void* kernel_ptr(int k0, int k1) {
-    if (k0 == 5 && k1 == 5) return (void*)k_fused<InT, S, 5, 5, P>;
-    if (k0 == 7 && k1 == 7) return (void*)k_fused<InT, S, 7, 7, P>;
-    if (k0 == 9 && k1 == 9) return (void*)k_fused<InT, S, 9, 9, P>;
-    if (k0 == 5 && k1 == 7) return (void*)k_fused<InT, S, 5, 7, P>;
-    if (k0 == 7 && k1 == 5) return (void*)k_fused<InT, S, 7, 5, P>;
+void* kernel_ptr(int k0, int k1, int nTheta) {
+    // the common geometry (5x5 LoG, 180 theta samples) gets constant tile pitches
+    if (k0 == 5 && k1 == 5 && nTheta == 180) return (void*)k_fused<InT, S, 5, 5, P, 180>;
+    if (k0 == 5 && k1 == 5) return (void*)k_fused<InT, S, 5, 5, P, 0>;
+    if (k0 == 7 && k1 == 7) return (void*)k_fused<InT, S, 7, 7, P, 0>;
+    if (k0 == 9 && k1 == 9) return (void*)k_fused<InT, S, 9, 9, P, 0>;
+    if (k0 == 5 && k1 == 7) return (void*)k_fused<InT, S, 5, 7, P, 0>;
+    if (k0 == 7 && k1 == 5) return (void*)k_fused<InT, S, 7, 5, P, 0>;
     return nullptr;
 }
 
-void* pick_kernel(int method, int dtype, int k0, int k1, int pack) {
+void* pick_kernel(int method, int dtype, int k0, int k1, int pack, int nTheta) {
     bool h = method == EBSD_FUSED_F16;
     switch (dtype) {
         case EBSD_U8:
-            if (pack == 4 && !h) return kernel_ptr<uint8_t, float, 4>(k0, k1);
-            if (pack == 2 && !h) return kernel_ptr<uint8_t, float, 2>(k0, k1);
-            return h ? kernel_ptr<uint8_t, __half, 1>(k0, k1) : kernel_ptr<uint8_t, float, 1>(k0, k1);
+            if (pack == 4 && !h) return kernel_ptr<uint8_t, float, 4>(k0, k1, nTheta);
+            if (pack == 2 && !h) return kernel_ptr<uint8_t, float, 2>(k0, k1, nTheta);
+            return h ? kernel_ptr<uint8_t, __half, 1>(k0, k1, nTheta) : kernel_ptr<uint8_t, float, 1>(k0, k1, nTheta);
         case EBSD_U16:
-            return h ? kernel_ptr<uint16_t, __half, 1>(k0, k1) : kernel_ptr<uint16_t, float, 1>(k0, k1);
+            return h ? kernel_ptr<uint16_t, __half, 1>(k0, k1, nTheta) : kernel_ptr<uint16_t, float, 1>(k0, k1, nTheta);
         case EBSD_F32:
-            return h ? kernel_ptr<float, __half, 1>(k0, k1) : kernel_ptr<float, float, 1>(k0, k1);
+            return h ? kernel_ptr<float, __half, 1>(k0, k1, nTheta) : kernel_ptr<float, float, 1>(k0, k1, nTheta);
     }
     return nullptr;
 }
@@ -708,7 +704,8 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     const int K0 = p->k0, K1 = p->k1;
     // the fused kernel assumes the standard windows: peakPad = 2*ksz + 1 (half-window = ksz)
     bool shape_ok = p->pk0 == 2 * K0 + 1 && p->pk1 == 2 * K1 + 1 && 2 * K1 < 32 &&
-                    pick_kernel(EBSD_FUSED_F32, EBSD_U8, K0, K1, 1) != nullptr &&
+                    pick_kernel(EBSD_FUSED_F32, EBSD_U8, K0, K1, 1, p->nTheta) != nullptr &&
+                    p->nRho >= kRowBlock && p->nTheta >= 2 * K1 + 1 &&
                     p->p0 >= K0 + K0 / 2 && p->p1 >= K1 + K1 / 2;
     int pitch = p->W + 1;
     if (((int64_t)p->H * pitch + 1) * 4 >= 65535) shape_ok = false;  // byte offsets in 16 bits
@@ -977,7 +974,7 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
     if (n <= 0) return EBSD_OK;
     const int pack = fused_patterns_per_pass(p, method, dtype, n);
-    void* fn = pick_kernel(method, dtype, p->k0, p->k1, pack);
+    void* fn = pick_kernel(method, dtype, p->k0, p->k1, pack, p->nTheta);
     if (!fn) return EBSD_E_UNSUPPORTED;
     const FusedGeom& g = p->fg;
     int smem = method == EBSD_FUSED_F16 ? g.smem_f16 : g.smem_f32;
