@@ -114,6 +114,15 @@ __device__ __forceinline__ float load_pixel(const InT* p, int idx, int bg_mode, 
     return (float)p[idx];
 }
 
+// The float64 epilogue of band_fit_write<float, false> for bands [0, nbands) of `out`:
+// width from the stored log-curvature, theta/rho from the stored aveloc.
+__global__ void __launch_bounds__(256) k_band_epilogue(ebsd_bands out, int64_t nbands, LabelConsts k) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nbands; o += (int64_t)gridDim.x * blockDim.x) {
+        out.width[o] = band_width(out.width[o]);
+        band_theta_rho(out.aveloc[2 * o], out.aveloc[2 * o + 1], k, out.theta + o, out.rho + o);
+    }
+}
+
 // kPack = 2 or 4: that many uint8 patterns per pass (no background).  Pattern pixels are
 // packed as 16-bit lanes -- two per shared word, four per 8-byte element -- so one load and
 // one integer add per word gather them all; a ray sum of at most 257 uint8 values fits its
@@ -387,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 const float mn = red_f[0];
                 const float mean = (float)(red_d[0] / (double)stat_count);
                 SmemConv acc{conv, a.p0 - D0, a.p1 - D1, CC};
-                band_fit_write<float>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + qq) * nB + lane);
+                band_fit_write<float, false>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + qq) * nB + lane);
             }
         };
 
@@ -1034,7 +1043,16 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.out_offset = out_offset;
     void* args[] = {&a};
     EBSD_CUDA_TRY(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kThreads), args, (size_t)smem, st));
-    *launches += 1;
+    // the float64 part of the band fit (width, theta, rho) as a separate elementwise pass, so
+    // that the fused kernel's label warp is not held up by float64 latency
+    const int64_t nbands = n * p->nB;
+    ebsd_bands ob = *out;
+    const int64_t o0 = out_offset * p->nB;
+    ob.max += o0; ob.normmax += o0; ob.maxloc += 2 * o0; ob.avemax += o0; ob.aveloc += 2 * o0;
+    ob.width += o0; ob.theta += o0; ob.rho += o0; ob.valid += o0;
+    const int eblocks = (int)std::min<int64_t>((nbands + 255) / 256, (int64_t)sms * 8);
+    k_band_epilogue<<<eblocks, 256, 0, st>>>(ob, nbands, a.kc);
+    *launches += 2;
     return launch_status();
 }
 

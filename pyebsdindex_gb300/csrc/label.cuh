@@ -76,12 +76,34 @@ struct LabelConsts {
     const double* rho;
 };
 
+// FWHM width from the peak's log-curvature a (band_detect.py:748-753): 2 sqrt(ln 2 / -a) in
+// float64 when a < -1e-8, else 0.
+template <typename T>
+__device__ __forceinline__ T band_width(T a) {
+    return a < (T)-1.e-8 ? (T)(2.0 * sqrt(0.6931471805599453 / (double)(-a))) : (T)0;
+}
+
+// theta = pi - interp(aveloc_theta)/RADEG ; rho = -interp(aveloc_rho) in float64
+// (band_detect.py:521-522), from the record's aveloc as stored (float32 for T = float).
+template <typename T>
+__device__ __forceinline__ void band_theta_rho(T ar, T ac, const LabelConsts& k, float* theta, float* rho) {
+    double xt = (sizeof(T) == 4) ? (double)(float)ac : (double)ac;
+    double xr = (sizeof(T) == 4) ? (double)(float)ar : (double)ar;
+    const double RADEG = 180.0 / 3.141592653589793;
+    double th = __dsub_rn(3.141592653589793, __ddiv_rn(interp_arange(xt, k.theta, k.nTheta), RADEG));
+    double rh = -interp_arange(xr, k.rho, k.nRho);
+    *theta = (float)th;
+    *rho = (float)rh;
+}
+
 // Fit one band (padded-frame peak (r, c)) and write its record fields.  C(r, c) returns
-// the LoG-convolved Radon value in the padded frame as T.
-template <typename T, typename Acc>
+// the LoG-convolved Radon value in the padded frame as T.  kEpilogue = false leaves the
+// float64 epilogue to band_epilogue(): the width field then holds the log-curvature a (or
+// 0) and theta/rho are not written.
+template <typename T, bool kEpilogue = true, typename Acc>
 __device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mean,
                                const LabelConsts& k, const ebsd_bands& out, int64_t o) {
-    T vmax = (T)-2.0e6, vavemax = (T)-2.0e6, w = (T)0;
+    T vmax = (T)-2.0e6, vavemax = (T)-2.0e6, acurv = (T)0;
     T mlr = (T)0, mlc = (T)0, alr = (T)0, alc = (T)0;
     int8_t valid = 0;
     if (has) {
@@ -96,9 +118,7 @@ __device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mea
             m3 = yp < m3 ? yp : m3;
             if (m3 > (T)0) {
                 T a = r_sub(r_mul(r_sub(r_log(yp), r_log(ym)), (T)0.5), r_log(v));
-                if (a < (T)-1.e-8) {
-                    w = (T)(2.0 * sqrt(0.6931471805599453 / (double)(-a)));
-                }
+                if (a < (T)-1.e-8) acurv = a;
             }
             T nn[9];
 #pragma unroll
@@ -147,16 +167,13 @@ __device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mea
     out.avemax[o] = (float)vavemax;
     out.aveloc[2 * o] = (float)ar;
     out.aveloc[2 * o + 1] = (float)ac;
-    out.width[o] = (float)w;
     out.valid[o] = valid;
-    // theta = pi - interp(aveloc_theta)/RADEG ; rho = -interp(aveloc_rho)   (band_detect.py:521-522)
-    double xt = (sizeof(T) == 4) ? (double)(float)ac : (double)ac;
-    double xr = (sizeof(T) == 4) ? (double)(float)ar : (double)ar;
-    const double RADEG = 180.0 / 3.141592653589793;
-    double th = __dsub_rn(3.141592653589793, __ddiv_rn(interp_arange(xt, k.theta, k.nTheta), RADEG));
-    double rh = -interp_arange(xr, k.rho, k.nRho);
-    out.theta[o] = (float)th;
-    out.rho[o] = (float)rh;
+    if (kEpilogue) {
+        out.width[o] = (float)band_width(acurv);
+        band_theta_rho(ar, ac, k, out.theta + o, out.rho + o);
+    } else {
+        out.width[o] = (float)acurv;
+    }
 }
 
 }  // namespace ebsd
