@@ -128,7 +128,7 @@ int64_t ebsd_last_launch_count(ebsd_plan_t plan);
 
 /* Autotuner -- no counterpart in the reference, whose OpenCL path sizes its work by fixed
  * rules (band_detect_cl.py:252-286).  Times the fused-kernel variants that give identical
- * records for (method, dtype) -- one, two or four patterns per block pass -- on the caller's
+ * records for (method, dtype) -- one, two, four or eight patterns per block pass -- on the caller's
  * device-resident sample d_pats [n][H][W] and keeps the faster in the plan for later calls.
  * Writes the choice to *patterns_per_pass (may be NULL); 1 when only one variant applies
  * (per-stage methods, uint16/float32 input, a fitted background, FP16 storage).
@@ -136,7 +136,7 @@ int64_t ebsd_last_launch_count(ebsd_plan_t plan);
 int ebsd_plan_autotune(ebsd_plan_t plan, int method, int dtype, const void* d_pats, int64_t n,
                        void* stream, int* patterns_per_pass);
 
-/* Pins the fused kernel's patterns per block pass for later calls: 1, 2 or 4 (capped at what
+/* Pins the fused kernel's patterns per block pass for later calls: 1, 2, 4 or 8 (capped at what
  * a call allows), or 0 for the rule (the most a call allows).  For callers that tuned
  * offline; no counterpart in the reference.  Records do not depend on the choice. */
 int ebsd_plan_set_patterns_per_pass(ebsd_plan_t plan, int patterns_per_pass);

@@ -159,12 +159,12 @@ class DevicePlan:
         return int(self._lib.ebsd_last_launch_count(self.handle))
 
     def set_patterns_per_pass(self, ppp: int):
-        """Pin the fused kernel's patterns per block pass (1, 2, 4; 0 = rule)."""
+        """Pin the fused kernel's patterns per block pass (1, 2, 4, 8; 0 = rule)."""
         check(self._lib.ebsd_plan_set_patterns_per_pass(self.handle, int(ppp)), "ebsd_plan_set_patterns_per_pass")
 
     def autotune(self, pats_ptr: int, dtype: int, n: int, method, stream=0) -> int:
         """Time the record-identical kernel variants on a device-resident sample and keep the
-        faster in the plan; returns the chosen patterns per block pass (1, 2 or 4)."""
+        faster in the plan; returns the chosen patterns per block pass (1, 2, 4 or 8)."""
         ppp = C.c_int(0)
         check(self._lib.ebsd_plan_autotune(self.handle, method_id(method), int(dtype), C.c_void_p(int(pats_ptr)),
                                            int(n), C.c_void_p(int(stream)), C.byref(ppp)), "ebsd_plan_autotune")

@@ -154,7 +154,7 @@ class GPUFindBands:
         return bandData
 
     def autotune(self, sample, method=None, gpu_id=None):
-        """Time the record-identical variants of the fused kernel (one, two or four patterns per
+        """Time the record-identical variants of the fused kernel (one, two, four or eight patterns per
         block pass) on ``sample`` ([n, H, W] numpy or torch, uint8/uint16/float32) and keep
         the faster in the device plan for later ``find_bands`` calls.  No counterpart in the
         reference.  Returns the chosen patterns per pass."""

@@ -30,7 +30,7 @@ struct FusedGeom {
     int nRaysPad = 0;           // nGroups * 32
     int gpt = 0;                // groups per theta column (ceil(nRho / 32))
     int npad = 0;               // padding cells of the Radon tile
-    int quad = 0;               // the 4-patterns-per-pass tile (8-byte elements) fits
+    int quad = 0;               // the 4/8-patterns-per-pass tile (8-byte elements) fits
 };
 
 struct Workspace {
@@ -72,7 +72,7 @@ struct ebsd_plan_s {
     float* d_fray = nullptr;       // [nPx] weights: sum_px w*pixel = mean of the non-empty rays
     int64_t flut_entries = 0;
     // patterns per block pass of the fused FP32 uint8 kernel: -1 = rule (the most the plan
-    // allows: 4, else 2), else 1, 2 or 4 as chosen by ebsd_plan_autotune
+    // allows: 8, else 2), else 1, 2, 4 or 8 as chosen by ebsd_plan_autotune
     int fused_ppp = -1;
 
     // ---- workspaces ----
@@ -127,7 +127,7 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d);
 void fused_release(ebsd_plan_s* p);
 int fused_supported(const ebsd_plan_s* p, int method);
 size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);
-// 1, 2 or 4: patterns one block pass of the fused kernel would process for this call
+// 1, 2, 4 or 8: patterns one block pass of the fused kernel would process for this call
 int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t n);
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches);

@@ -123,17 +123,19 @@ __global__ void __launch_bounds__(256) k_band_epilogue(ebsd_bands out, int64_t n
     }
 }
 
-// kPack = 2 or 4: that many uint8 patterns per pass (no background).  Pattern pixels are
-// packed as 16-bit lanes -- two per shared word, four per 8-byte element -- so one load and
-// one integer add per word gather them all; a ray sum of at most 257 uint8 values fits its
-// lane, and integer sums are exact, so the means equal the float sequential sums of the
-// single-pattern pass.  The other patterns' ray means are parked in a per-CTA global scratch
+// kPack = 2, 4 or 8: that many uint8 patterns per pass (no background).  Pattern pixels are
+// packed -- as 16-bit lanes two per shared word (kPack 2) or four per 8-byte element
+// (kPack 4), or as bytes eight per 8-byte element (kPack 8, spread to 16-bit lanes by byte
+// permutes before the adds) -- so one shared load gathers a slot for all of them and one
+// integer add accumulates two; a ray sum of at most 257 uint8 values fits a 16-bit lane, and
+// integer sums are exact, so the means equal the float sequential sums of the single-pattern
+// pass.  The other patterns' ray means are parked in a per-CTA global scratch
 // (L2-resident) and reloaded once the pattern before them is finished.
 // kNT > 0: nTheta fixed at compile time, so every tile pitch is a constant (0: runtime).
 template <typename InT, typename S, int K0, int K1, int kPack, int kNT>
 __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     static_assert(kPack == 1 || (sizeof(S) == 4 && sizeof(InT) == 1), "packed modes: uint8 input, FP32 tile");
-    static_assert(kPack == 1 || kPack == 2 || kPack == 4, "1, 2 or 4 patterns per pass");
+    static_assert(kPack == 1 || kPack == 2 || kPack == 4 || kPack == 8, "1, 2, 4 or 8 patterns per pass");
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int D0 = K0;  // rho half-window of the max filter (peakPad = 2*ksz + 1)
     constexpr int D1 = K1;  // theta half-window
@@ -201,6 +203,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                     const unsigned lo = (unsigned)gp[i], hi = npk > 1 ? (unsigned)gp[a.nPx + i] : 0u;
                     ((unsigned*)pat)[y * a.pitch + x] = lo | (hi << 16);
                     v = 0.0f;
+                } else if (kPack == 8) {
+                    // eight uint8 pixels in one 8-byte element, one byte per pattern
+                    unsigned w[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) w[j] = j < npk ? (unsigned)gp[(size_t)j * a.nPx + i] : 0u;
+                    ((uint2*)pat)[y * a.pitch + x] = make_uint2(w[0] | (w[1] << 8) | (w[2] << 16) | (w[3] << 24),
+                                                                w[4] | (w[5] << 8) | (w[6] << 16) | (w[7] << 24));
+                    v = 0.0f;
                 } else if (kPack == 4) {
                     unsigned w[4];
 #pragma unroll
@@ -219,7 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             }
         }
         if (tid == 0) {
-            if (kPack == 4) ((uint2*)pat)[a.H * a.pitch] = make_uint2(0u, 0u);
+            if (kPack >= 4) ((uint2*)pat)[a.H * a.pitch] = make_uint2(0u, 0u);
             else pat[a.H * a.pitch] = 0.0f;
         }
         // FP16 storage keeps (value - m) * s: m = mean of the Radon interior (exact by
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         {
             const int g0 = wofs_s[warp], g1 = wofs_s[warp + 1];
             // each warp stream ends with kRing zero chunks, so the ring loads unconditionally
-            const uint4* ip = (kPack == 4 ? a.lut8 : a.lut) + ((size_t)wofs_s[kWarps + 1 + warp] * 32 + lane);
+            const uint4* ip = (kPack >= 4 ? a.lut8 : a.lut) + ((size_t)wofs_s[kWarps + 1 + warp] * 32 + lane);
             const unsigned char* pb = (const unsigned char*)pat;
             uint4 ring[kRing];
 #pragma unroll
@@ -281,7 +291,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             int cnt = gi < g1 ? __ldg(a.count + t) : 0;
             float rc = gi < g1 ? __ldg(a.rcount + t) : 0.0f;
             float sum = 0.0f;
-            unsigned isum = 0u, isum2 = 0u;  // packed modes: 16-bit lane sums
+            // packed modes: 16-bit lane sums, two patterns per register
+            unsigned isum = 0u, isum2 = 0u, isum3 = 0u, isum4 = 0u;
             while (gi < g1) {
 #pragma unroll
                 for (int k = 0; k < kRing; ++k) {
@@ -289,7 +300,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                         const uint4 e = ring[k];
                         ring[k] = __ldg(ip);
                         ip += 32;
-                        if (kPack == 4) {
+                        if (kPack == 8) {
+                            const unsigned o[8] = {e.x & 0xFFFF, e.x >> 16, e.y & 0xFFFF, e.y >> 16,
+                                                   e.z & 0xFFFF, e.z >> 16, e.w & 0xFFFF, e.w >> 16};
+#pragma unroll
+                            for (int k8 = 0; k8 < 8; ++k8) {
+                                // spread the byte lanes to 16-bit lanes: (b0, b1) and (b2, b3)
+                                const uint2 w = *(const uint2*)(pb + o[k8]);
+                                isum += __byte_perm(w.x, 0u, 0x4140);
+                                isum2 += __byte_perm(w.x, 0u, 0x4342);
+                                isum3 += __byte_perm(w.y, 0u, 0x4140);
+                                isum4 += __byte_perm(w.y, 0u, 0x4342);
+                            }
+                        } else if (kPack == 4) {
                             const unsigned o[8] = {e.x & 0xFFFF, e.x >> 16, e.y & 0xFFFF, e.y >> 16,
                                                    e.z & 0xFFFF, e.z >> 16, e.w & 0xFFFF, e.w >> 16};
 #pragma unroll
@@ -324,9 +347,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                                 const float fc = (float)cnt;
                                 v = cnt > 0 ? div_int_exact(isum & 0xFFFFu, fc, rc) : -1.0f;
                                 scratch[t] = cnt > 0 ? div_int_exact(isum >> 16, fc, rc) : -1.0f;
-                                if (kPack == 4) {
+                                if (kPack >= 4) {
                                     scratch[a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum2 & 0xFFFFu, fc, rc) : -1.0f;
                                     scratch[2 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum2 >> 16, fc, rc) : -1.0f;
+                                }
+                                if (kPack == 8) {
+                                    scratch[3 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum3 & 0xFFFFu, fc, rc) : -1.0f;
+                                    scratch[4 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum3 >> 16, fc, rc) : -1.0f;
+                                    scratch[5 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum4 & 0xFFFFu, fc, rc) : -1.0f;
+                                    scratch[6 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum4 >> 16, fc, rc) : -1.0f;
                                 }
                             } else {
                                 v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
@@ -339,6 +368,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                             sum = 0.0f;
                             isum = 0u;
                             isum2 = 0u;
+                            isum3 = 0u;
+                            isum4 = 0u;
                             if (gi < g1) {
                                 gs = gst_s[gi];
                                 t = (int)(gs & 0xFFFFu) * 32 + lane;
@@ -413,11 +444,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             } else {
                 // parked ray means back into the tile: warp w >= 1 takes the groups at stream
                 // positions w - 1, w - 1 + (kWarps - 1), ... (one ray per lane)
+                // four groups per step keep four L2 loads in flight per lane
                 const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
-                for (int gi = warp - 1; gi < a.nGroups; gi += kWarps - 1) {
-                    const unsigned tb = gtb_s[gi];
-                    const float v = src[(gst_s[gi] & 0xFFFFu) * 32 + lane];
-                    if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * TC] = v;
+                constexpr int kStep = kWarps - 1;
+                for (int gi = warp - 1; gi < a.nGroups; gi += 4 * kStep) {
+                    float v[4];
+                    unsigned tb[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int g = gi + u * kStep;
+                        tb[u] = g < a.nGroups ? gtb_s[g] : 0u;
+                        v[u] = g < a.nGroups ? src[(gst_s[g] & 0xFFFFu) * 32 + lane] : 0.0f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (lane < (int)(tb[u] >> 16)) tile[(tb[u] & 0xFFFFu) + lane * TC] = v[u];
                 }
                 asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");  // warps 1.. only
                 for (int k = tid - 32; k < a.npad; k += kThreads - 32) {
@@ -642,6 +683,7 @@ void* pick_kernel(int method, int dtype, int k0, int k1, int pack, int nTheta) {
     bool h = method == EBSD_FUSED_F16;
     switch (dtype) {
         case EBSD_U8:
+            if (pack == 8 && !h) return kernel_ptr<uint8_t, float, 8>(k0, k1, nTheta);
             if (pack == 4 && !h) return kernel_ptr<uint8_t, float, 4>(k0, k1, nTheta);
             if (pack == 2 && !h) return kernel_ptr<uint8_t, float, 2>(k0, k1, nTheta);
             return h ? kernel_ptr<uint8_t, __half, 1>(k0, k1, nTheta) : kernel_ptr<uint8_t, float, 1>(k0, k1, nTheta);
@@ -654,12 +696,12 @@ void* pick_kernel(int method, int dtype, int k0, int k1, int pack, int nTheta) {
 }
 
 // Packed modes apply to uint8 patterns without a background, FP32 tile, rays of <= 257
-// pixels; four per pass also needs the 8-byte-element tile and its LUT (fg.quad).  Returns
-// the largest patterns-per-pass the call may use (1, 2 or 4).
+// pixels; four or eight per pass also need the 8-byte-element tile and its LUT (fg.quad).
+// Returns the largest patterns-per-pass the call may use (1, 2 or 8).
 int max_pack(const ebsd_plan_s* p, int method, int dtype, int64_t n) {
     if (!(dtype == EBSD_U8 && method == EBSD_FUSED_F32 && p->bg_mode == 0 && p->maxCount <= 257 && n >= 2))
         return 1;
-    return p->fg.quad && p->d_flut8 ? 4 : 2;
+    return p->fg.quad && p->d_flut8 ? 8 : 2;
 }
 
 // Launch facts, set up on first use so that later launches -- also inside a CUDA-graph
@@ -968,7 +1010,7 @@ size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t) {
     if (method != EBSD_FUSED_F32 || !p->fg.ok_f32) return 0;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
-    const int rows = p->fg.quad ? 3 : 1;
+    const int rows = p->fg.quad ? 7 : 1;
     return (size_t)std::max(sms, 1) * rows * p->fg.nRaysPad * sizeof(float);
 }
 

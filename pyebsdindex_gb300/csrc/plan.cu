@@ -373,7 +373,7 @@ int ebsd_find_bands_host(ebsd_plan_t p, int method, int dtype, const void* h_pat
 }
 
 int ebsd_plan_set_patterns_per_pass(ebsd_plan_t p, int ppp) {
-    if (!p || !(ppp == 0 || ppp == 1 || ppp == 2 || ppp == 4)) return EBSD_E_ARG;
+    if (!p || !(ppp == 0 || ppp == 1 || ppp == 2 || ppp == 4 || ppp == 8)) return EBSD_E_ARG;
     std::lock_guard<std::mutex> lk(p->mtx);
     p->fused_ppp = ppp == 0 ? -1 : ppp;
     return EBSD_OK;

@@ -115,9 +115,9 @@ def test_unknown_method(cuda, pats60):
         bd.find_bands(pats60[:2], method="nope")
 
 
-@pytest.mark.parametrize("n", [2, 3, 5, 6, 7, 41])
+@pytest.mark.parametrize("n", [2, 3, 5, 6, 7, 9, 15, 41])
 def test_packed_passes_partial_units_equal_plain(cuda, n):
-    """uint8 patterns without background run four (or two) per pass in the fused kernel;
+    """uint8 patterns without background run eight (or four, two) per pass in the fused kernel;
     counts that are not a multiple leave the last pass partly empty.  Records equal the
     per-stage path's."""
     bd = make_bd()
