@@ -49,6 +49,7 @@ struct FusedArgs {
     const unsigned* padlist;   // [npad] (source tile cell << 16) | destination tile cell
     int npad;
     float* pack_scratch;       // packed modes: [gridDim.x][kPack-1][nRaysPad] parked ray means
+    unsigned one;              // 1, as a runtime value: ray-sum adds become multiply-adds (below)
     int nRays, nRaysPad, nGroups, gpt, nRho, nTheta;  // gpt: 32-ray groups per theta column
     int p0, p1, R, Tp;
     int row0, col0, TR, TC;    // Radon tile origin (padded frame) and extent
@@ -291,8 +292,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             int cnt = gi < g1 ? __ldg(a.count + t) : 0;
             float rc = gi < g1 ? __ldg(a.rcount + t) : 0.0f;
             float sum = 0.0f;
-            // packed modes: 16-bit lane sums, two patterns per register
+            // packed modes: 16-bit lane sums, two patterns per register.  The adds are written
+            // as multiply-adds by a runtime 1, which run on the FMA pipe and leave the ALU pipe
+            // (the gather's bottleneck) to the offset extraction and the byte permutes.
             unsigned isum = 0u, isum2 = 0u, isum3 = 0u, isum4 = 0u;
+            const unsigned one = a.one;
             while (gi < g1) {
 #pragma unroll
                 for (int k = 0; k < kRing; ++k) {
@@ -307,10 +311,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                             for (int k8 = 0; k8 < 8; ++k8) {
                                 // spread the byte lanes to 16-bit lanes: (b0, b1) and (b2, b3)
                                 const uint2 w = *(const uint2*)(pb + o[k8]);
-                                isum += __byte_perm(w.x, 0u, 0x4140);
-                                isum2 += __byte_perm(w.x, 0u, 0x4342);
-                                isum3 += __byte_perm(w.y, 0u, 0x4140);
-                                isum4 += __byte_perm(w.y, 0u, 0x4342);
+                                isum = __byte_perm(w.x, 0u, 0x4140) * one + isum;
+                                isum2 = __byte_perm(w.x, 0u, 0x4342) * one + isum2;
+                                isum3 = __byte_perm(w.y, 0u, 0x4140) * one + isum3;
+                                isum4 = __byte_perm(w.y, 0u, 0x4342) * one + isum4;
                             }
                         } else if (kPack == 4) {
                             const unsigned o[8] = {e.x & 0xFFFF, e.x >> 16, e.y & 0xFFFF, e.y >> 16,
@@ -318,8 +322,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 #pragma unroll
                             for (int k8 = 0; k8 < 8; ++k8) {
                                 const uint2 w = *(const uint2*)(pb + o[k8]);
-                                isum += w.x;
-                                isum2 += w.y;
+                                isum = w.x * one + isum;
+                                isum2 = w.y * one + isum2;
                             }
                         } else if (kPack == 2) {
                             isum += *(const unsigned*)(pb + (e.x & 0xFFFF));
@@ -1054,6 +1058,7 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.padlist = p->d_fpad;
     a.npad = g.npad;
     a.pack_scratch = pack > 1 ? (float*)p->ws.ptr : nullptr;
+    a.one = 1u;
     a.gpt = g.gpt;
     a.nRays = p->nRays;
     a.nRaysPad = g.nRaysPad;
