@@ -57,6 +57,12 @@ struct ebsd_plan_s {
     uint8_t* d_rdnmask = nullptr;  // [nRays]
     float* d_kernel = nullptr;     // [k0*k1]
     std::vector<float> h_kernel;   // host copy of the taps (fused-kernel parameters)
+    // separable LoG: taps[a][b] = ku[a] * kw[b] to within two float32 ulps of the largest tap
+    // (the reference's kernel, a Gaussian second derivative along rho times a Gaussian along
+    // theta, always is); the FP32 paths then convolve by rows, then by columns
+    int sep = 0;
+    std::vector<float> h_ku, h_kw;  // [k0], [k1]
+    float* d_ksep = nullptr;        // [k0 + k1]: ku then kw
     double* d_kernel64 = nullptr;  // [k0*k1]
     double* d_theta = nullptr;     // [nTheta] degrees (float32 values widened)
     double* d_rho = nullptr;       // [nRho]

@@ -8,8 +8,9 @@
 //                (stored FP32, or FP16 for EBSD_FUSED_F16)
 //   3. pad       theta mirror with rho flip + rho edge rows + zero rows below the array
 //                (band_detect.py:573-580; the FFT convolution's zero extension)
-//   4. conv      register-blocked direct LoG convolution into an FP32 conv tile, in the same
-//                multiply-add order as the per-stage kernel; min/sum for normmax on the fly
+//   4. conv      register-blocked LoG convolution into an FP32 conv tile (separable: theta
+//                taps per row, then rho taps), in the same multiply-add order as the per-stage
+//                kernel; min/sum for normmax on the fly
 //   5. peaks     separable max filter: theta max per row into the dead Radon tile, then
 //                rho max per column in registers, exact equality + rdnmask
 //                (band_detect.py:639-664); candidates go into a warp top-N list ordered
@@ -56,6 +57,8 @@ struct FusedArgs {
     int crow0, ccol0, CR, CC;  // conv tile origin and extent
     int statR1;                // end row of the statistics slice (padded frame)
     float taps[81];            // LoG taps [K0*K1] (parameter space: FMA operands, no loads)
+    float ku[9], kw[9];        // separable factors: taps[a][b] = ku[a] * kw[b] (when sep)
+    int sep;
     float ksum;                // sum of the kernel taps (FP16 centring correction)
     const float* wimg;         // [nPx] pixel weights whose dot product is the Radon mean
     const uint8_t* rdnmask;    // [nRho][nTheta]
@@ -151,16 +154,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     const int nT = kNT > 0 ? kNT : a.nTheta;
     const int CC = kNT > 0 ? kNT + 2 * D1 : a.CC;
     const int TC = kNT > 0 ? kNT + 2 * D1 + 2 * H1 : a.TC;
+    // row pitches of the conv tile, the Radon tile and the theta-max rows: odd, so that a warp
+    // walking down a column touches 32 different banks
+    const int CP = CC | 1, TP = TC | 1, MP = nT | 1;
     size_t off = 0;
     // the conv tile comes first so that the pattern tile aliased into it starts at shared
     // offset 0: the LUT then holds byte offsets usable directly as load addresses
     float* conv = (float*)(smem + off);
     float* pat = conv;  // aliased: the pattern tile is dead once the Radon is built
-    off += ((size_t)a.CR * a.CC * sizeof(float) + 15) & ~(size_t)15;
+    off += ((size_t)a.CR * (a.CC | 1) * sizeof(float) + 15) & ~(size_t)15;
     S* tile = (S*)(smem + off);
     {
         // the Radon tile region also holds the peaks' theta-max rows once the tile is dead
-        const size_t tb = (size_t)a.TR * a.TC * sizeof(S), mb = (size_t)(a.nRho + 2 * D0) * a.nTheta * sizeof(float);
+        const size_t tb = (size_t)a.TR * (a.TC | 1) * sizeof(S), mb = (size_t)(a.nRho + 2 * D0) * (a.nTheta | 1) * sizeof(float);
         off += ((tb > mb ? tb : mb) + 15) & ~(size_t)15;
     }
     float* lv_s = (float*)(smem + off);
@@ -366,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                                 if (kHalf) v = (v - cen) * scl;
                             }
                             const unsigned tb = gtb_s[gi];
-                            if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * TC] = to_store<S>(v);
+                            if (lane < (int)(tb >> 16)) tile[(tb & 0xFFFFu) + lane * TP] = to_store<S>(v);
                             ++gi;
                             pc = 0;
                             sum = 0.0f;
@@ -430,7 +436,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 }
                 const float mn = red_f[0];
                 const float mean = (float)(red_d[0] / (double)stat_count);
-                SmemConv acc{conv, a.p0 - D0, a.p1 - D1, CC};
+                SmemConv acc{conv, a.p0 - D0, a.p1 - D1, CP};
                 band_fit_write<float, false>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + qq) * nB + lane);
             }
         };
@@ -446,23 +452,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             if (warp == 0) {
                 merge_label(q - 1);
             } else {
-                // parked ray means back into the tile: warp w >= 1 takes the groups at stream
-                // positions w - 1, w - 1 + (kWarps - 1), ... (one ray per lane)
-                // four groups per step keep four L2 loads in flight per lane
+                // parked ray means back into the tile: eight threads per 32-ray group, each
+                // moving four neighbouring rays with one 16-byte load (the scratch row is mostly
+                // outside L2, so bytes in flight set the pace); two groups in flight per thread
                 const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
-                constexpr int kStep = kWarps - 1;
-                for (int gi = warp - 1; gi < a.nGroups; gi += 4 * kStep) {
-                    float v[4];
-                    unsigned tb[4];
+                constexpr int kRel = kThreads - 32;
+                const int ntask = a.nGroups * 8;
+                for (int it = tid - 32; it < ntask; it += 2 * kRel) {
+                    float4 v[2];
+                    unsigned tb[2];
+                    int j4[2];
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int g = gi + u * kStep;
-                        tb[u] = g < a.nGroups ? gtb_s[g] : 0u;
-                        v[u] = g < a.nGroups ? src[(gst_s[g] & 0xFFFFu) * 32 + lane] : 0.0f;
+                    for (int u = 0; u < 2; ++u) {
+                        const int task = it + u * kRel;
+                        const int gi = task >> 3;
+                        j4[u] = (task & 7) * 4;
+                        tb[u] = task < ntask ? gtb_s[gi] : 0u;
+                        v[u] = task < ntask ? *(const float4*)(src + (gst_s[gi] & 0xFFFFu) * 32 + j4[u])
+                                            : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     }
 #pragma unroll
-                    for (int u = 0; u < 4; ++u)
-                        if (lane < (int)(tb[u] >> 16)) tile[(tb[u] & 0xFFFFu) + lane * TC] = v[u];
+                    for (int u = 0; u < 2; ++u) {
+                        const int nval = (int)(tb[u] >> 16);
+                        S* dst = tile + (tb[u] & 0xFFFFu) + j4[u] * TP;
+                        if (j4[u] + 0 < nval) dst[0] = v[u].x;
+                        if (j4[u] + 1 < nval) dst[TP] = v[u].y;
+                        if (j4[u] + 2 < nval) dst[2 * TP] = v[u].z;
+                        if (j4[u] + 3 < nval) dst[3 * TP] = v[u].w;
+                    }
                 }
                 asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");  // warps 1.. only
                 for (int k = tid - 32; k < a.npad; k += kThreads - 32) {
@@ -501,30 +518,48 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 for (int o = 0; o < kRowBlock; ++o) acc[o] = 0.0f;
                 // tile row (cr0 + t) feeds output o through kernel row a = o + 2*H0 - t;
                 // descending t keeps each output's multiply-add order = ascending a.
-                const S* tcol = tile + cr0 * TC + cc + 2 * H1;
+                const S* tcol = tile + cr0 * TP + cc + 2 * H1;
+                if (a.sep) {
+                    // separable taps: theta convolution of each tile row (kw, ascending b),
+                    // then the rho taps (ku, ascending a) -- 10 multiply-adds per output
+                    // instead of 25, the per-stage FP32 kernel's order
+                    float hr[kRowBlock + 2 * H0];
 #pragma unroll
-                for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
-                    float v[K1];
+                    for (int t = 0; t < kRowBlock + 2 * H0; ++t) {
+                        float hv = 0.0f;
 #pragma unroll
-                    for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[t * TC - b]);
+                        for (int b = 0; b < K1; ++b) hv = fmaf(a.kw[b], to_f(tcol[t * TP - b]), hv);
+                        hr[t] = hv;
+                    }
 #pragma unroll
-                    for (int o = 0; o < kRowBlock; ++o) {
-                        const int ka = o + 2 * H0 - t;
-                        if (ka >= 0 && ka < K0) {
+                    for (int o = 0; o < kRowBlock; ++o)
 #pragma unroll
-                            for (int b = 0; b < K1; ++b) acc[o] = fmaf(a.taps[ka * K1 + b], v[b], acc[o]);
+                        for (int ka = 0; ka < K0; ++ka) acc[o] = fmaf(a.ku[ka], hr[o + 2 * H0 - ka], acc[o]);
+                } else {
+#pragma unroll
+                    for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
+                        float v[K1];
+#pragma unroll
+                        for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[t * TP - b]);
+#pragma unroll
+                        for (int o = 0; o < kRowBlock; ++o) {
+                            const int ka = o + 2 * H0 - t;
+                            if (ka >= 0 && ka < K0) {
+#pragma unroll
+                                for (int b = 0; b < K1; ++b) acc[o] = fmaf(a.taps[ka * K1 + b], v[b], acc[o]);
+                            }
                         }
                     }
                 }
                 // statistics slice: padded rows [stat_r0, stat_r1) x columns [stat_c0, stat_c1),
                 // i.e. conv rows from D0 and conv columns [D1, D1 + nTheta)
                 const bool colstat = (unsigned)(cc - D1) < (unsigned)nT;
-                float* ccol = conv + cr0 * CC + cc;
+                float* ccol = conv + cr0 * CP + cc;
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
                     if (kHalf) acc[o] = fmaf(a.ksum, cen, acc[o] * inv_scl);
                     if (cr0 + o >= cr_first) {
-                        ccol[o * CC] = acc[o];
+                        ccol[o * CP] = acc[o];
                         if (colstat && (unsigned)(cr0 + o - D0) < stat_rows) {
                             smin = fminf(smin, acc[o]);
                             ssum += acc[o];
@@ -575,10 +610,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             constexpr int kSeg = (kNT + WIN - 1) / WIN;  // segments per row when nTheta is fixed
             const int nseg = kNT > 0 ? kSeg : (nT + WIN - 1) / WIN;
             for (int task = tid; task < NR * nseg; task += kThreads) {
-                const int rr = task / nseg, sg = task - rr * nseg;
+                // neighbouring lanes take neighbouring rows (odd pitches: no bank conflicts)
+                const int sg = task / NR, rr = task - sg * NR;
                 const int j0 = sg * WIN < nT - WIN ? sg * WIN : nT - WIN;
-                const float* x = conv + rr * CC + j0;
-                float* out = tm + rr * nT + j0;
+                const float* x = conv + rr * CP + j0;
+                float* out = tm + rr * MP + j0;
                 float xv[2 * WIN - 1];
 #pragma unroll
                 for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = x[k];
@@ -613,10 +649,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 const int j = colok ? jl : nT - 1;
                 const int i_first = rb * kRowBlock;
                 const int i0 = i_first < nrho - kRowBlock ? i_first : nrho - kRowBlock;
-                const float* tcol = tm + i0 * nT + j;
+                const float* tcol = tm + i0 * MP + j;
                 float v[NV];
 #pragma unroll
-                for (int k = 0; k < NV; ++k) v[k] = tcol[k * nT];
+                for (int k = 0; k < NV; ++k) v[k] = tcol[k * MP];
                 // rho max over [o, o + 2*D0] for o = 0..kRowBlock-1: suffix / core / prefix maxima
                 float suf[kRowBlock], pre[kRowBlock], core = -INFINITY;
                 suf[kRowBlock - 1] = -INFINITY;
@@ -627,12 +663,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 pre[0] = -INFINITY;
 #pragma unroll
                 for (int o = 1; o < kRowBlock; ++o) pre[o] = fmaxf(pre[o - 1], v[2 * D0 + o]);
-                const float* crow = conv + (i0 + D0) * CC + j + D1;
+                const float* crow = conv + (i0 + D0) * CP + j + D1;
 #pragma unroll
                 for (int o = 0; o < kRowBlock; ++o) {
                     const float m = fmaxf(fmaxf(suf[o], core), pre[o]);
                     const int i = i0 + o;
-                    const float val = crow[o * CC];
+                    const float val = crow[o * CP];
                     const bool f = colok && i >= i_first && val == m && a.rdnmask[i * nT + j];
                     unsigned bal = __ballot_sync(0xffffffffu, f);
                     while (bal) {
@@ -664,8 +700,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 // host side
 // ------------------------------------------------------------------------------------------
 size_t smem_bytes(const FusedGeom& g, size_t store, int ngroups, size_t tm_bytes) {
-    size_t b = (std::max((size_t)(g.row1 - g.row0) * (g.col1 - g.col0) * store, tm_bytes) + 15) & ~(size_t)15;
-    b += ((size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0) * 4 + 15) & ~(size_t)15;
+    // odd row pitches, as the kernel lays the tiles out
+    size_t b = (std::max((size_t)(g.row1 - g.row0) * ((g.col1 - g.col0) | 1) * store, tm_bytes) + 15) & ~(size_t)15;
+    b += ((size_t)(g.crow1 - g.crow0) * ((g.ccol1 - g.ccol0) | 1) * 4 + 15) & ~(size_t)15;
     b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
     b += (size_t)ngroups * 8 + 2 * (kWarps + 1) * 4;
     return b;
@@ -778,14 +815,14 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         g.tile_pitch = pitch;
         g.threads = kThreads;
         int ngroups = p->nTheta * ((p->nRho + 31) / 32);  // 32-ray groups of the fused LUT
-        const size_t tm_bytes = (size_t)(p->nRho + 2 * D0) * p->nTheta * sizeof(float);
+        const size_t tm_bytes = (size_t)(p->nRho + 2 * D0) * (p->nTheta | 1) * sizeof(float);
         g.smem_f32 = (int)smem_bytes(g, 4, ngroups, tm_bytes);
         g.smem_f16 = (int)smem_bytes(g, 2, ngroups, tm_bytes);
-        size_t conv_cells = (size_t)(g.crow1 - g.crow0) * (g.ccol1 - g.ccol0);
+        size_t conv_cells = (size_t)(g.crow1 - g.crow0) * ((g.ccol1 - g.ccol0) | 1);
         int dev_smem = 0;
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
         g.ok = conv_cells >= (size_t)p->H * pitch + 1 && g.smem_f16 <= dev_smem && g.row0 >= 0 &&
-               (size_t)(g.row1 - g.row0) * (g.col1 - g.col0) < 65535;
+               (size_t)(g.row1 - g.row0) * ((g.col1 - g.col0) | 1) < 65535;
         g.ok_f32 = g.ok && g.smem_f32 <= dev_smem;
         // four patterns per pass: 8-byte pixel elements, byte offsets still in 16 bits
         const size_t quad_bytes = ((size_t)p->H * pitch + 1) * 8;
@@ -877,7 +914,7 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     // zero chunks so that the kernel's ring of prefetched chunks loads unconditionally
     std::vector<uint32_t> gst, gtb;
     std::vector<int32_t> wofs(2 * (kWarps + 1), 0);
-    const int TC = g.col1 - g.col0;
+    const int TP = (g.col1 - g.col0) | 1;  // Radon tile row pitch (odd, as in the kernel)
     for (int w = 0; w < kWarps; ++w) {
         std::sort(wg[w].begin(), wg[w].end());
         wofs[w + 1] = wofs[w] + (int)wg[w].size();
@@ -885,7 +922,7 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
         for (int gg : wg[w]) {
             const int j = gg / gpt, i0 = (gg % gpt) * 32;
             gst.push_back((uint32_t)gg | ((uint32_t)gch[gg] << 16));
-            const int base = (i0 + p->p0 - g.row0) * TC + (j + p->p1 - g.col0);
+            const int base = (i0 + p->p0 - g.row0) * TP + (j + p->p1 - g.col0);
             gtb.push_back((uint32_t)base | ((uint32_t)std::min(32, p->nRho - i0) << 16));
         }
     }
@@ -920,7 +957,7 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     // last interior row, rows at or below R = zero (the convolution's zero extension)
     std::vector<unsigned> padlist;
     {
-        const int TR = g.row1 - g.row0, TC = g.col1 - g.col0;
+        const int TR = g.row1 - g.row0, TC = g.col1 - g.col0, TPp = TC | 1;
         for (int tr = 0; tr < TR; ++tr)
             for (int tc = 0; tc < TC; ++tc) {
                 int r = tr + g.row0, i = r - p->p0, j = tc + g.col0 - p->p1;
@@ -931,9 +968,9 @@ int fused_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
                     int si = ic, sj = j;
                     if (j < 0) { si = p->nRho - 1 - ic; sj = p->nTheta + j; }
                     else if (j >= p->nTheta) { si = p->nRho - 1 - ic; sj = j - p->nTheta; }
-                    src = (unsigned)((si + p->p0 - g.row0) * TC + (sj + p->p1 - g.col0));
+                    src = (unsigned)((si + p->p0 - g.row0) * TPp + (sj + p->p1 - g.col0));
                 }
-                padlist.push_back((src << 16) | (unsigned)(tr * TC + tc));
+                padlist.push_back((src << 16) | (unsigned)(tr * TPp + tc));
             }
     }
     EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_fpad, padlist.size() * sizeof(unsigned)));
@@ -1079,7 +1116,18 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.CC = g.ccol1 - g.ccol0;
     a.statR1 = std::min(p->R, p->Tp - p->p0);
     for (int k = 0; k < p->k0 * p->k1 && k < 81; ++k) a.taps[k] = p->h_kernel[k];
+    a.sep = p->sep && p->k0 <= 9 && p->k1 <= 9;
+    for (int k = 0; k < 9; ++k) {
+        a.ku[k] = k < p->k0 && a.sep ? p->h_ku[k] : 0.0f;
+        a.kw[k] = k < p->k1 && a.sep ? p->h_kw[k] : 0.0f;
+    }
     a.ksum = g.ksum;
+    if (a.sep) {  // FP16 centring: the separable form's tap sum
+        double su = 0.0, sw = 0.0;
+        for (int k = 0; k < p->k0; ++k) su += p->h_ku[k];
+        for (int k = 0; k < p->k1; ++k) sw += p->h_kw[k];
+        a.ksum = (float)(su * sw);
+    }
     a.wimg = p->d_fray;
     a.rdnmask = p->d_rdnmask;
     a.bg_mode = p->bg_mode;

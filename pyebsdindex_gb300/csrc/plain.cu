@@ -93,7 +93,8 @@ __global__ void k_pad_plain(T* __restrict__ radon, int64_t n, int R, int Tp, int
 // 'same'-mode 2-D convolution over the whole padded frame, zero outside it.
 template <typename T>
 __global__ void k_conv_plain(const T* __restrict__ radon, T* __restrict__ conv,
-                             const T* __restrict__ kern, int k0, int k1, int R, int Tp) {
+                             const T* __restrict__ kern, const float* __restrict__ ksep, int sep,
+                             int k0, int k1, int R, int Tp) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int r = blockIdx.y;
     int64_t q = blockIdx.z;
@@ -101,13 +102,29 @@ __global__ void k_conv_plain(const T* __restrict__ radon, T* __restrict__ conv,
     const T* src = radon + q * (int64_t)R * Tp;
     int h0 = k0 / 2, h1 = k1 / 2;
     T acc = (T)0;
-    for (int a = 0; a < k0; ++a) {
-        int rr = r + h0 - a;
-        if (rr < 0 || rr >= R) continue;
-        for (int b = 0; b < k1; ++b) {
-            int cc = c + h1 - b;
-            if (cc < 0 || cc >= Tp) continue;
-            acc = fma(kern[a * k1 + b], src[(int64_t)rr * Tp + cc], acc);
+    if (sep) {
+        // separable taps (FP32): each kernel row's theta convolution, then the rho taps, in
+        // ascending order -- the fused kernel's arithmetic
+        for (int a = 0; a < k0; ++a) {
+            int rr = r + h0 - a;
+            if (rr < 0 || rr >= R) continue;
+            T h = (T)0;
+            for (int b = 0; b < k1; ++b) {
+                int cc = c + h1 - b;
+                if (cc < 0 || cc >= Tp) continue;
+                h = fma((T)ksep[k0 + b], src[(int64_t)rr * Tp + cc], h);
+            }
+            acc = fma((T)ksep[a], h, acc);
+        }
+    } else {
+        for (int a = 0; a < k0; ++a) {
+            int rr = r + h0 - a;
+            if (rr < 0 || rr >= R) continue;
+            for (int b = 0; b < k1; ++b) {
+                int cc = c + h1 - b;
+                if (cc < 0 || cc >= Tp) continue;
+                acc = fma(kern[a * k1 + b], src[(int64_t)rr * Tp + cc], acc);
+            }
         }
     }
     conv[q * (int64_t)R * Tp + (int64_t)r * Tp + c] = acc;
@@ -280,7 +297,10 @@ int run_chunk_t(ebsd_plan_s* p, const InT* d_pats, int64_t n, const ebsd_bands* 
     int pblocks = (int)((padcells + 255) / 256 < 152 * 32 ? (padcells + 255) / 256 : 152 * 32);
     k_pad_plain<T><<<pblocks, 256, 0, st>>>(radon, n, p->R, p->Tp, p->p0, p->p1, p->nRho, p->nTheta);
     dim3 gc((p->Tp + 127) / 128, p->R, (unsigned)n);
-    k_conv_plain<T><<<gc, 128, 0, st>>>(radon, conv, kern, p->k0, p->k1, p->R, p->Tp);
+    // FP64 keeps the full 2-D taps (the FP64 oracle); FP32 uses the separable form when the
+    // plan's kernel is separable, as the fused kernel does
+    const int sep = sizeof(T) == 4 ? p->sep : 0;
+    k_conv_plain<T><<<gc, 128, 0, st>>>(radon, conv, kern, p->d_ksep, sep, p->k0, p->k1, p->R, p->Tp);
     k_stats_plain<T><<<(unsigned)n, 256, 0, st>>>(conv, stats, p->R, p->Tp, p->p0, p->p1);
     k_dilate_theta<T><<<gc, 128, 0, st>>>(conv, tmp, p->R, p->Tp, p->pk1 / 2);
     dim3 gf((p->nTheta + 127) / 128, p->nRho, (unsigned)n);

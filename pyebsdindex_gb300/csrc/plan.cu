@@ -2,6 +2,7 @@
 #include "ebsd_internal.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -25,6 +26,7 @@ void free_plan_tables(ebsd_plan_s* p) {
     cudaFree(p->d_rdnmask);
     cudaFree(p->d_kernel);
     cudaFree(p->d_kernel64);
+    cudaFree(p->d_ksep);
     cudaFree(p->d_theta);
     cudaFree(p->d_rho);
     cudaFree(p->d_bg);
@@ -192,6 +194,27 @@ int ebsd_plan_create(const ebsd_plan_desc* d, int device, ebsd_plan_t* out) {
     if (rc == EBSD_OK) rc = upload(&p->d_rdnmask, d->rdnmask, (size_t)nRays);
     if (rc == EBSD_OK) rc = upload(&p->d_kernel, d->kernel, (size_t)p->k0 * p->k1);
     p->h_kernel.assign(d->kernel, d->kernel + (size_t)p->k0 * p->k1);
+    {
+        // rank-1 factors from the centre row and column: ku[a] = K[a][h1],
+        // kw[b] = K[h0][b] / K[h0][h1]; separable when every product is within two ulps of
+        // the largest tap from the tap it replaces
+        const int h0 = p->k0 / 2, h1 = p->k1 / 2;
+        const float kc = p->h_kernel[(size_t)h0 * p->k1 + h1];
+        float kmax = 0.0f;
+        for (float v : p->h_kernel) kmax = std::max(kmax, std::fabs(v));
+        p->h_ku.resize(p->k0);
+        p->h_kw.resize(p->k1);
+        for (int a = 0; a < p->k0; ++a) p->h_ku[a] = p->h_kernel[(size_t)a * p->k1 + h1];
+        for (int b = 0; b < p->k1; ++b) p->h_kw[b] = kc != 0.0f ? (float)((double)p->h_kernel[(size_t)h0 * p->k1 + b] / (double)kc) : 0.0f;
+        bool sep = kc != 0.0f && kmax > 0.0f;
+        for (int a = 0; sep && a < p->k0; ++a)
+            for (int b = 0; b < p->k1; ++b)
+                if (std::fabs(p->h_ku[a] * p->h_kw[b] - p->h_kernel[(size_t)a * p->k1 + b]) > kmax * 2.4e-7f) sep = false;
+        p->sep = sep ? 1 : 0;
+        std::vector<float> ks(p->h_ku);
+        ks.insert(ks.end(), p->h_kw.begin(), p->h_kw.end());
+        if (rc == EBSD_OK) rc = upload(&p->d_ksep, ks.data(), ks.size());
+    }
     if (rc == EBSD_OK) {
         std::vector<double> k64(d->kernel, d->kernel + (size_t)p->k0 * p->k1);
         rc = upload(&p->d_kernel64, k64.data(), k64.size());
