@@ -33,6 +33,8 @@ H = W = 80
 NRHO, NTHETA, NBANDS = 120, 180, 9
 BYTES_PER_PATTERN = H * W * 1 + 41 * NBANDS   # algorithmic bytes: pattern in, band fields out
 SEED = 1_000_000
+WORKLOAD = ("find_bands on 1,000,000 80x80 uint8 patterns, nTheta 180, nRho 120, nBands 9, LoG sigma 1, "
+            "rhoMaskFrac 0.1, circular mask, 10% noise-only")
 
 
 def parse():
@@ -168,8 +170,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sample / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "find_bands, 80x80 uint8, nTheta 180, nRho 120, nBands 9, host CPU sample",
-                   "patterns_per_step": sample},
+        "config": {"workload": WORKLOAD, "method": "cpu restatement (C/OpenMP)",
+                   "patterns_per_step": sample,
+                   "sample": f"each step times {sample} patterns of the 1,000,000-pattern workload's pool"},
         "cpu_baseline": dict(base, value=v),
         "e2e": {"value": v, "unit": "patterns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -350,8 +353,7 @@ def main():
             "dtype": "u8 in, f16 Radon storage, f32 accumulate" if method == "fused16" else
                      ("u8 in, f32" if method in ("plain", "fused") else "u8 in, f64"),
             "data": "synthetic",
-            "config": {"workload": "find_bands on 1,000,000 80x80 uint8 patterns, nTheta 180, nRho 120, "
-                                   "nBands 9, LoG sigma 1, rhoMaskFrac 0.1, circular mask, 10% noise-only",
+            "config": {"workload": WORKLOAD,
                        "method": method, "patterns_per_step": N, "distinct_patterns": len(pool),
                        "patterns_per_block_pass": ppp, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},

@@ -35,6 +35,10 @@ constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
 constexpr int kRowBlock = 8;
 constexpr int kRing = 2;  // LUT chunks in flight per warp (deeper rings cost registers, not latency)
+// packed modes: per CTA, per (pattern of the unit, band): the 3x3 conv block around the peak and
+// its position; then per pattern the conv minimum and mean
+constexpr int kCapBand = 10;
+constexpr int kCapFloats = 8 * kMaxBands * kCapBand + 8 * 2;
 
 struct FusedArgs {
     const void* pats;
@@ -51,6 +55,7 @@ struct FusedArgs {
     int npad;
     float* pack_scratch;       // packed modes: [gridDim.x][kPack-1][nRaysPad] parked ray means
     unsigned one;              // 1, as a runtime value: ray-sum adds become multiply-adds (below)
+    float* cap;                // packed modes: [gridDim.x][kCapFloats] captured band fits (below)
     int nRays, nRaysPad, nGroups, gpt, nRho, nTheta;  // gpt: 32-ray groups per theta column
     int p0, p1, R, Tp;
     int row0, col0, TR, TC;    // Radon tile origin (padded frame) and extent
@@ -399,33 +404,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         //      the xor butterfly agrees, goes to lane k and its list advances -- then lanes
         //      0..nB-1 fit their band (band_detect.py:691-809).  Reads the warp lists, the conv
         //      tile and the conv statistics of qq only.
-        auto merge_label = [&](int64_t qq) {
+        // k-way merge of the sorted warp lists by warp 0: lane l holds the head of warp l's list;
+        // each round the best head under (value desc, position asc) -- a strict total order --
+        // is found with two warp reductions (largest value key, then smallest position among
+        // the heads holding it), goes to lane k, and its list advances.  Returns, in lanes
+        // 0..nB-1, the position of band `lane` (-1: none).  -0 is folded into +0 first, as the
+        // value comparison of the reference's sort treats them alike.
+        auto tournament = [&]() -> int {
             int ptr = 0;
             float hv = lane < kWarps ? lv_s[lane * kMaxBands] : -INFINITY;
             int hp = lane < kWarps ? lp_s[lane * kMaxBands] : -1;
             int mypos = -1;
             for (int k = 0; k < nB; ++k) {
-                float bv = hv;
-                int bp = hp, bl = lane;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-                    const int op = __shfl_xor_sync(0xffffffffu, bp, o);
-                    const int ol = __shfl_xor_sync(0xffffffffu, bl, o);
-                    if (op >= 0 && (bp < 0 || beats(ov, op, bv, bp))) {
-                        bv = ov;
-                        bp = op;
-                        bl = ol;
-                    }
-                }
-                if (bp < 0) break;  // every list is exhausted (the same in all lanes)
-                if (lane == k) mypos = bp;
-                if (lane == bl) {
+                const unsigned u = __float_as_uint(hv + 0.0f);
+                const unsigned key = hp < 0 ? 0u : ((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+                const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+                if (kmax == 0u) break;  // every list is exhausted
+                const unsigned pmin = __reduce_min_sync(0xffffffffu, key == kmax ? (unsigned)hp : 0xffffffffu);
+                const unsigned win = __ballot_sync(0xffffffffu, key == kmax && (unsigned)hp == pmin);
+                if (lane == k) mypos = (int)pmin;
+                if (lane == __ffs(win) - 1) {
                     ++ptr;
                     hp = ptr < nB ? lp_s[lane * kMaxBands + ptr] : -1;
                     hv = ptr < nB ? lv_s[lane * kMaxBands + ptr] : -INFINITY;
                 }
             }
+            return mypos;
+        };
+        // ---- 6. merge + 7. label (warp 0), one pattern per pass: the band fit
+        //      (band_detect.py:691-809) straight from the conv tile
+        auto merge_label = [&](int64_t qq) {
+            const int mypos = tournament();
             if (lane < nB) {
                 const bool has = mypos >= 0;
                 int r = 0, c = 0;
@@ -440,6 +449,50 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 band_fit_write<float, false>(has, r, c, acc, mn, mean, a.kc, a.out, (a.out_offset + qq) * nB + lane);
             }
         };
+        // ---- 6. merge (warp 0), packed modes: the bands' 3x3 blocks, positions and the conv
+        //      statistics of pattern `sb` of the unit go to the CTA's capture scratch; the fits
+        //      run for the whole unit at once after its last pattern (label_unit)
+        float* cap = kPack > 1 ? a.cap + (size_t)blockIdx.x * kCapFloats : nullptr;
+        auto merge_capture = [&](int sb) {
+            const int mypos = tournament();
+            if (lane < nB) {
+                float* cb = cap + (sb * nB + lane) * kCapBand;
+                if (mypos >= 0) {
+                    const int i = mypos / nT, j = mypos - (mypos / nT) * nT;
+                    const float* c0 = conv + (i + D0 - 1) * CP + (j + D1 - 1);
+#pragma unroll
+                    for (int r3 = 0; r3 < 3; ++r3)
+#pragma unroll
+                        for (int c3 = 0; c3 < 3; ++c3) cb[r3 * 3 + c3] = c0[r3 * CP + c3];
+                }
+                cb[9] = __int_as_float(mypos);
+            }
+            if (lane == 0) {
+                cap[8 * kMaxBands * kCapBand + 2 * sb] = red_f[0];
+                cap[8 * kMaxBands * kCapBand + 2 * sb + 1] = (float)(red_d[0] / (double)stat_count);
+            }
+        };
+        // ---- 7. label, packed modes: every band of the unit, one thread each
+        auto label_unit = [&](int npat) {
+            for (int t = tid; t < npat * nB; t += kThreads) {
+                const int sb = t / nB, b = t - (t / nB) * nB;
+                const float* cb = cap + (sb * nB + b) * kCapBand;
+                const int pos = __float_as_int(cb[9]);
+                const bool has = pos >= 0;
+                float nn[9];
+#pragma unroll
+                for (int k9 = 0; k9 < 9; ++k9) nn[k9] = has ? cb[k9] : 0.0f;
+                int r = 0, c = 0;
+                if (has) {
+                    const int i = pos / nT;
+                    r = i + a.p0;
+                    c = (pos - i * nT) + a.p1;
+                }
+                const float mn = cap[8 * kMaxBands * kCapBand + 2 * sb];
+                const float mean = cap[8 * kMaxBands * kCapBand + 2 * sb + 1];
+                band_fit_block<float, false>(has, r, c, nn, mn, mean, a.kc, a.out, (a.out_offset + q0 + sb) * nB + b);
+            }
+        };
 
         for (int sub = 0; sub < npk; ++sub) {
         const int64_t q = q0 + sub;
@@ -450,35 +503,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         // pattern while warps 1.. reload this pattern's parked ray means and pad the tile.
         if (kPack > 1 && sub > 0) {
             if (warp == 0) {
-                merge_label(q - 1);
+                merge_capture(sub - 1);
             } else {
                 // parked ray means back into the tile: eight threads per 32-ray group, each
                 // moving four neighbouring rays with one 16-byte load (the scratch row is mostly
-                // outside L2, so bytes in flight set the pace); two groups in flight per thread
+                // outside L2, so bytes in flight set the pace); four groups in flight per thread
                 const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
                 constexpr int kRel = kThreads - 32;
                 const int ntask = a.nGroups * 8;
-                for (int it = tid - 32; it < ntask; it += 2 * kRel) {
-                    float4 v[2];
-                    unsigned tb[2];
-                    int j4[2];
+                for (int it = tid - 32; it < ntask; it += 4 * kRel) {
+                    float4 v[4];
+                    unsigned tb[4];
 #pragma unroll
-                    for (int u = 0; u < 2; ++u) {
+                    for (int u = 0; u < 4; ++u) {
                         const int task = it + u * kRel;
                         const int gi = task >> 3;
-                        j4[u] = (task & 7) * 4;
                         tb[u] = task < ntask ? gtb_s[gi] : 0u;
-                        v[u] = task < ntask ? *(const float4*)(src + (gst_s[gi] & 0xFFFFu) * 32 + j4[u])
+                        v[u] = task < ntask ? *(const float4*)(src + (gst_s[gi] & 0xFFFFu) * 32 + (task & 7) * 4)
                                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     }
 #pragma unroll
-                    for (int u = 0; u < 2; ++u) {
+                    for (int u = 0; u < 4; ++u) {
+                        const int j4 = ((it + u * kRel) & 7) * 4;
                         const int nval = (int)(tb[u] >> 16);
-                        S* dst = tile + (tb[u] & 0xFFFFu) + j4[u] * TP;
-                        if (j4[u] + 0 < nval) dst[0] = v[u].x;
-                        if (j4[u] + 1 < nval) dst[TP] = v[u].y;
-                        if (j4[u] + 2 < nval) dst[2 * TP] = v[u].z;
-                        if (j4[u] + 3 < nval) dst[3 * TP] = v[u].w;
+                        S* dst = tile + (tb[u] & 0xFFFFu) + j4 * TP;
+                        if (j4 + 0 < nval) dst[0] = v[u].x;
+                        if (j4 + 1 < nval) dst[TP] = v[u].y;
+                        if (j4 + 2 < nval) dst[2 * TP] = v[u].z;
+                        if (j4 + 3 < nval) dst[3 * TP] = v[u].w;
                     }
                 }
                 asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");  // warps 1.. only
@@ -496,6 +548,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             }
         }
         __syncthreads();
+
+        // the parked ray means of the next pattern of this unit are read back in the next pass;
+        // start moving them into L2 now (the scratch does not stay in L2 between the gather and
+        // the last patterns of a unit)
+        if (kPack > 1 && tid == 0 && sub + 1 < npk) {
+            const float* nxt = scratch + (size_t)sub * a.nRaysPad;
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nxt), "r"(a.nRaysPad * 4) : "memory");
+        }
 
         // ---- 4. LoG convolution: conv[cr][cc] = sum_a sum_b tap[a][b] tile[cr+2H0-a][cc+2H1-b],
         //      kRowBlock outputs per thread down one column.  The last row block is moved up to
@@ -686,11 +746,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         }
         __syncthreads();
 
-        // the last pattern of a unit is merged and labelled before the next unit's load
-        // overwrites the conv tile
-        if (kPack == 1 || sub == npk - 1) {
+        // the last pattern of a unit is merged before the next unit's load overwrites the conv
+        // tile; packed units are then labelled from the capture scratch (only global memory:
+        // the next unit's load runs on beside it)
+        if (kPack == 1) {
             if (warp == 0) merge_label(q);
             __syncthreads();
+        } else if (sub == npk - 1) {
+            if (warp == 0) merge_capture(sub);
+            __syncthreads();
+            label_unit(npk);
         }
         }  // sub
     }
@@ -1052,7 +1117,7 @@ size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t) {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
     const int rows = p->fg.quad ? 7 : 1;
-    return (size_t)std::max(sms, 1) * rows * p->fg.nRaysPad * sizeof(float);
+    return (size_t)std::max(sms, 1) * ((size_t)rows * p->fg.nRaysPad + kCapFloats) * sizeof(float);
 }
 
 int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t n) {
@@ -1096,6 +1161,11 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     a.npad = g.npad;
     a.pack_scratch = pack > 1 ? (float*)p->ws.ptr : nullptr;
     a.one = 1u;
+    {
+        // capture scratch after the parked-row scratch of every CTA
+        const int rows = p->fg.quad ? 7 : 1;
+        a.cap = pack > 1 ? (float*)p->ws.ptr + (size_t)sms * rows * g.nRaysPad : nullptr;
+    }
     a.gpt = g.gpt;
     a.nRays = p->nRays;
     a.nRaysPad = g.nRaysPad;

@@ -96,24 +96,24 @@ __device__ __forceinline__ void band_theta_rho(T ar, T ac, const LabelConsts& k,
     *rho = (float)rh;
 }
 
-// Fit one band (padded-frame peak (r, c)) and write its record fields.  C(r, c) returns
-// the LoG-convolved Radon value in the padded frame as T.  kEpilogue = false leaves the
-// float64 epilogue to band_epilogue(): the width field then holds the log-curvature a (or
-// 0) and theta/rho are not written.
-template <typename T, bool kEpilogue = true, typename Acc>
-__device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mean,
+// Fit one band (padded-frame peak (r, c)) from its 3x3 block nn of LoG-convolved Radon values
+// (nn[i*3 + j] = conv(r - 1 + i, c - 1 + j)) and write its record fields.  kEpilogue = false
+// leaves the float64 epilogue to a separate pass: the width field then holds the
+// log-curvature a (or 0) and theta/rho are not written.
+template <typename T, bool kEpilogue = true>
+__device__ void band_fit_block(bool has, int r, int c, const T* nn_in, T mn, T mean,
                                const LabelConsts& k, const ebsd_bands& out, int64_t o) {
     T vmax = (T)-2.0e6, vavemax = (T)-2.0e6, acurv = (T)0;
     T mlr = (T)0, mlc = (T)0, alr = (T)0, alc = (T)0;
     int8_t valid = 0;
     if (has) {
-        T v = C(r, c);
+        T v = nn_in[4];
         if (v > (T)0) {
             valid = 1;
             mlr = (T)r;
             mlc = (T)c;
             vmax = v;
-            T ym = C(r - 1, c), yp = C(r + 1, c);
+            T ym = nn_in[1], yp = nn_in[7];
             T m3 = ym < v ? ym : v;
             m3 = yp < m3 ? yp : m3;
             if (m3 > (T)0) {
@@ -122,9 +122,7 @@ __device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mea
             }
             T nn[9];
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) nn[i * 3 + j] = C(r - 1 + i, c - 1 + j);
+            for (int i = 0; i < 9; ++i) nn[i] = nn_in[i];
             // numpy float32 sum of 9 contiguous values: 8-way pairwise block, then the tail.
             T s = r_add(r_add(r_add(nn[0], nn[1]), r_add(nn[2], nn[3])),
                         r_add(r_add(nn[4], nn[5]), r_add(nn[6], nn[7])));
@@ -174,6 +172,23 @@ __device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mea
     } else {
         out.width[o] = (float)acurv;
     }
+}
+
+// The same, reading the 3x3 block through C(r, c) (the LoG-convolved Radon value in the
+// padded frame as T).
+template <typename T, bool kEpilogue = true, typename Acc>
+__device__ void band_fit_write(bool has, int r, int c, const Acc& C, T mn, T mean,
+                               const LabelConsts& k, const ebsd_bands& out, int64_t o) {
+    T nn[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) nn[i] = (T)0;
+    if (has) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) nn[i * 3 + j] = C(r - 1 + i, c - 1 + j);
+    }
+    band_fit_block<T, kEpilogue>(has, r, c, nn, mn, mean, k, out, o);
 }
 
 }  // namespace ebsd

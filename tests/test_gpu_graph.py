@@ -95,3 +95,21 @@ def test_patterns_per_pass_variants_give_identical_records(cuda, h, nRho):
             assert r[f].tobytes() == recs[0][f].tobytes(), f
     with pytest.raises(RuntimeError, match="invalid argument"):
         plan.set_patterns_per_pass(3)
+
+
+def test_non_separable_kernel_uses_2d_taps_in_both_paths(cuda):
+    """A plan whose LoG taps are not rank-1 (here: perturbed off-centre taps) convolves with
+    the 2-D taps; fused and per-stage records stay identical, and differ from the separable
+    plan's only where the kernel does."""
+    bd = make_bd(h=60, nRho=90, nBands=8)
+    pats = syn.make_patterns(40, 60, 60, seed=16, noise_frac=0.1)[0]
+    sep_fused = bd.find_bands(pats, method="fused")
+    k = np.array(bd.kernel, dtype=np.float32, copy=True)
+    kk = k.reshape(k.shape[-2:])
+    kk[0, 1] *= 1.01  # no longer a product of a rho and a theta profile
+    bd.kernel = k
+    a = bd.find_bands(pats, method="plain")
+    b = bd.find_bands(pats, method="fused")
+    for f in ("max", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
+        assert a[f].tobytes() == b[f].tobytes(), f
+    assert not np.array_equal(a["max"], sep_fused["max"])
