@@ -92,6 +92,17 @@ __device__ __forceinline__ float div_int_exact(unsigned s, float c, float r) {
     return __fmaf_rn(rem, r, q0);
 }
 
+// (hi, lo) += (bh, bl) for unevaluated float pairs: two-sum of the high parts (Knuth, TAOCP
+// vol. 2, 4.2.2), the low parts added to the error term, then renormalised.
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float bh, float bl) {
+    const float s = __fadd_rn(hi, bh);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    const float e = __fadd_rn(err, __fadd_rn(lo, bl));
+    hi = __fadd_rn(s, e);
+    lo = __fsub_rn(e, __fsub_rn(hi, s));
+}
+
 __device__ __forceinline__ bool beats(float v, int p, float w, int q) {
     return v > w || (v == w && p < q);
 }
@@ -634,25 +645,31 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 }
             }
         }
-        // block reduction of min / sum (sum in FP64 across threads)
+        // block reduction of min / sum: the per-thread float sums are combined as unevaluated
+        // float pairs (Knuth's two-sum, exact to about 2^-48), which keeps the slow float64
+        // pipe out of the 32-warp reduction; warp 0 turns the pair into a double at the end
         {
-            double dsum = (double)ssum;
+            float hi = ssum, lo = 0.0f;
             float m = smin;
             for (int o = 16; o > 0; o >>= 1) {
-                dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+                const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+                const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+                two_sum_add(hi, lo, oh, ol);
                 m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
             }
-            if (lane == 0) { red_d[warp] = dsum; red_f[warp] = m; }
+            if (lane == 0) { red_f[warp] = m; red_f[32 + warp] = hi; red_d[warp] = (double)lo; }
         }
         __syncthreads();
         if (warp == 0) {
-            double dsum = red_d[lane];
+            float hi = red_f[32 + lane], lo = (float)red_d[lane];
             float m = red_f[lane];
             for (int o = 16; o > 0; o >>= 1) {
-                dsum += __shfl_down_sync(0xffffffffu, dsum, o);
+                const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+                const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+                two_sum_add(hi, lo, oh, ol);
                 m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
             }
-            if (lane == 0) { red_d[0] = dsum; red_f[0] = m; }
+            if (lane == 0) { red_d[0] = (double)hi + (double)lo; red_f[0] = m; }
         }
         // (red_d[0] / red_f[0] are read after the next barrier)
 
