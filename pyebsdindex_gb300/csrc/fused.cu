@@ -505,6 +505,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             }
         };
 
+        // the padding cells of the Radon tile from the plan's cell list (sources are interior
+        // cells only, so the copies are independent): four list entries in flight per thread
+        auto pad_cells = [&](int first, int stride, S zero) {
+            for (int k = first; k < a.npad; k += 4 * stride) {
+                unsigned e[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) e[u] = k + u * stride < a.npad ? __ldg(a.padlist + k + u * stride) : 0xFFFFFFFFu;
+                S v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = (e[u] >> 16) == 0xFFFFu ? zero : tile[e[u] >> 16];
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (k + u * stride < a.npad) tile[e[u] & 0xFFFF] = v[u];
+            }
+        };
+
         for (int sub = 0; sub < npk; ++sub) {
         const int64_t q = q0 + sub;
         // ---- 3. pad the tile around the interior ----
@@ -545,18 +561,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                     }
                 }
                 asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");  // warps 1.. only
-                for (int k = tid - 32; k < a.npad; k += kThreads - 32) {
-                    const unsigned e = __ldg(a.padlist + k);
-                    const unsigned src2 = e >> 16;
-                    tile[e & 0xFFFF] = src2 == 0xFFFFu ? to_store<S>(0.0f) : tile[src2];
-                }
+                pad_cells(tid - 32, kThreads - 32, to_store<S>(0.0f));
             }
         } else {
-            for (int k = tid; k < a.npad; k += kThreads) {
-                const unsigned e = __ldg(a.padlist + k);
-                const unsigned src = e >> 16;
-                tile[e & 0xFFFF] = src == 0xFFFFu ? to_store<S>(kHalf ? -cen * scl : 0.0f) : tile[src];
-            }
+            pad_cells(tid, kThreads, to_store<S>(kHalf ? -cen * scl : 0.0f));
         }
         __syncthreads();
 
