@@ -174,6 +174,23 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
                float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
                float* d_out, void* stream);
 
+/* ---- band normals (Radon.radon2pole, radon_fast.py:314-397) ---------------------------- */
+#define EBSD_VENDOR_EDAX 0
+#define EBSD_VENDOR_OXFORD 1
+#define EBSD_VENDOR_EMSOFT 2
+#define EBSD_VENDOR_KIKUCHIPY 3
+#define EBSD_VENDOR_BRUKER 4
+
+/* Band (theta, rho) -> unit plane normals on the device, for [npat][nBands] bands (device
+ * arrays, e.g. the theta/rho fields ebsd_find_bands wrote): d_normals [npat][nBands][3].
+ * d_pc: DEVICE array of pattern centres in the vendor's convention, [npat][pc_stride] floats
+ * (pc_stride 3, or 4 for EMSOFT with the pixel size), or one shared row when pc_stride is 0.
+ * H, W: pattern rows, columns.  float32 arithmetic in the reference's order (sin/cos within
+ * an ulp or two of numpy's).  Asynchronous on `stream`. */
+int ebsd_radon2pole(const float* d_theta, const float* d_rho, int64_t npat, int32_t nBands,
+                    int32_t H, int32_t W, int32_t vendor, const float* d_pc, int32_t pc_stride,
+                    float* d_normals, void* stream);
+
 /* ---- differentiable path (no counterpart in the reference beyond the empty DIFF_NLPAR
  * placeholder, nlpar.py:75-77) --------------------------------------------------------- */
 

@@ -116,32 +116,7 @@ class GPUFindBands:
         if m.startswith("fused"):
             chunk = 0
         if is_torch:
-            import torch
-            t = pats
-            u16 = getattr(torch, "uint16", None)
-            if t.dtype == torch.uint8:
-                dt = _lib.EBSD_U8
-            elif u16 is not None and t.dtype == u16:
-                dt = _lib.EBSD_U16
-            else:
-                t = t.to(torch.float32)
-                dt = _lib.EBSD_F32
-            t = t.contiguous()
-            nB = int(self.nBands)
-            dev_out = {
-                "max": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
-                "normmax": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
-                "maxloc": torch.empty((nP, nB, 2), dtype=torch.float32, device=t.device),
-                "avemax": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
-                "aveloc": torch.empty((nP, nB, 2), dtype=torch.float32, device=t.device),
-                "width": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
-                "theta": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
-                "rho": torch.empty((nP, nB), dtype=torch.float32, device=t.device),
-                "valid": torch.empty((nP, nB), dtype=torch.int8, device=t.device),
-            }
-            stream = torch.cuda.current_stream(t.device).cuda_stream
-            plan.find_bands_device(t.data_ptr(), dt, nP, {k: v.data_ptr() for k, v in dev_out.items()}, m,
-                                   chunk=chunk, stream=stream)
+            dev_out = self._find_bands_dev(plan, pats, m, chunk)
             soa = {k: v.cpu().numpy() for k, v in dev_out.items()}
         else:
             arr = np.asarray(pats)
@@ -152,6 +127,47 @@ class GPUFindBands:
         if verbose > 0:
             print('Band Find Time (GPU, %s):' % m, timer() - tic0)
         return bandData
+
+    def _find_bands_dev(self, plan, t, m, chunk):
+        """Device band fields (SoA torch tensors) for CUDA patterns ``t`` [n, H, W]."""
+        import torch
+        u16 = getattr(torch, "uint16", None)
+        if t.dtype == torch.uint8:
+            dt = _lib.EBSD_U8
+        elif u16 is not None and t.dtype == u16:
+            dt = _lib.EBSD_U16
+        else:
+            t = t.to(torch.float32)
+            dt = _lib.EBSD_F32
+        t = t.contiguous()
+        nP, nB = int(t.shape[0]), int(self.nBands)
+        dev_out = {f: torch.empty((nP, nB, 2) if f in ("maxloc", "aveloc") else (nP, nB),
+                                  dtype=torch.int8 if f == "valid" else torch.float32, device=t.device)
+                   for f in _lib.BAND_FIELDS}
+        stream = torch.cuda.current_stream(t.device).cuda_stream
+        plan.find_bands_device(t.data_ptr(), dt, nP, {k: v.data_ptr() for k, v in dev_out.items()}, m,
+                               chunk=chunk, stream=stream)
+        return dev_out
+
+    def find_bands_normals(self, patterns, PC=None, vendor='EDAX', method=None, gpu_id=None):
+        """find_bands followed by Radon.radon2pole (radon_fast.py:314-397) with the band
+        normals computed on the device from the device theta/rho fields -- no host round trip
+        between detection and normals.  ``patterns``: [n, H, W] or [H, W], numpy or CUDA torch.
+        Returns (records, normals [n, nBands, 3] float32 numpy)."""
+        import torch
+        from .radon_fast import radon2pole_gpu
+        pats = patterns if type(patterns).__module__.startswith("torch") else torch.from_numpy(np.ascontiguousarray(patterns))
+        if pats.ndim == 2:
+            pats = pats[None]
+        if self.patDim is None or tuple(np.asarray(self.patDim)[-2:]) != tuple(pats.shape[-2:]):
+            self.band_detect_setup(patDim=pats.shape[-2:])
+        plan = self._device_plan(gpu_id)
+        m = self._pick_method(plan, method)
+        pats = pats.to(torch.device("cuda", plan.device))
+        dev_out = self._find_bands_dev(plan, pats, m, 0)
+        normals = radon2pole_gpu(dev_out["theta"], dev_out["rho"], self.radonPlan.imDim, PC=PC, vendor=vendor)
+        soa = {k: v.cpu().numpy() for k, v in dev_out.items()}
+        return self._records(soa, int(pats.shape[0])), normals.cpu().numpy()
 
     def autotune(self, sample, method=None, gpu_id=None):
         """Time the record-identical variants of the fused kernel (one, two, four or eight patterns per

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstddef>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 

@@ -92,6 +92,31 @@ __device__ __forceinline__ float div_int_exact(unsigned s, float c, float r) {
     return __fmaf_rn(rem, r, q0);
 }
 
+// L2 eviction-priority hints (createpolicy + cache_hint, sm_80+): the packed modes' parked
+// ray means are written once and read once a few patterns later, so they are stored
+// "evict last" and read back "evict first"; the streamed input patterns are loaded "evict
+// first" (ld.global.cs), so that the parked rows rather than the input stay in L2.
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ void st_keep(float* addr, float v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(addr), "f"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ float4 ld_once(const float* addr, uint64_t pol) {
+    float4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(addr), "l"(pol));
+    return v;
+}
+
 // (hi, lo) += (bh, bl) for unevaluated float pairs: two-sum of the high parts (Knuth, TAOCP
 // vol. 2, 4.2.2), the low parts added to the error term, then renormalised.
 __device__ __forceinline__ void two_sum_add(float& hi, float& lo, float bh, float bl) {
@@ -230,14 +255,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                     // eight uint8 pixels in one 8-byte element, one byte per pattern
                     unsigned w[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) w[j] = j < npk ? (unsigned)gp[(size_t)j * a.nPx + i] : 0u;
+                    for (int j = 0; j < 8; ++j) w[j] = j < npk ? (unsigned)__ldcs(gp + (size_t)j * a.nPx + i) : 0u;
                     ((uint2*)pat)[y * a.pitch + x] = make_uint2(w[0] | (w[1] << 8) | (w[2] << 16) | (w[3] << 24),
                                                                 w[4] | (w[5] << 8) | (w[6] << 16) | (w[7] << 24));
                     v = 0.0f;
                 } else if (kPack == 4) {
                     unsigned w[4];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) w[j] = j < npk ? (unsigned)gp[(size_t)j * a.nPx + i] : 0u;
+                    for (int j = 0; j < 4; ++j) w[j] = j < npk ? (unsigned)__ldcs(gp + (size_t)j * a.nPx + i) : 0u;
                     ((uint2*)pat)[y * a.pitch + x] = make_uint2(w[0] | (w[1] << 16), w[2] | (w[3] << 16));
                     v = 0.0f;
                 } else {
@@ -314,6 +339,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             int cnt = gi < g1 ? __ldg(a.count + t) : 0;
             float rc = gi < g1 ? __ldg(a.rcount + t) : 0.0f;
             float sum = 0.0f;
+            const uint64_t keep = kPack > 1 ? l2_evict_last_policy() : 0ull;
             // packed modes: 16-bit lane sums, two patterns per register.  The adds are written
             // as multiply-adds by a runtime 1, which run on the FMA pipe and leave the ALU pipe
             // (the gather's bottleneck) to the offset extraction and the byte permutes.
@@ -372,16 +398,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                             if (kPack > 1) {
                                 const float fc = (float)cnt;
                                 v = cnt > 0 ? div_int_exact(isum & 0xFFFFu, fc, rc) : -1.0f;
-                                scratch[t] = cnt > 0 ? div_int_exact(isum >> 16, fc, rc) : -1.0f;
+                                st_keep(scratch + t, cnt > 0 ? div_int_exact(isum >> 16, fc, rc) : -1.0f, keep);
                                 if (kPack >= 4) {
-                                    scratch[a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum2 & 0xFFFFu, fc, rc) : -1.0f;
-                                    scratch[2 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum2 >> 16, fc, rc) : -1.0f;
+                                    st_keep(scratch + a.nRaysPad + t, cnt > 0 ? div_int_exact(isum2 & 0xFFFFu, fc, rc) : -1.0f, keep);
+                                    st_keep(scratch + 2 * a.nRaysPad + t, cnt > 0 ? div_int_exact(isum2 >> 16, fc, rc) : -1.0f, keep);
                                 }
                                 if (kPack == 8) {
-                                    scratch[3 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum3 & 0xFFFFu, fc, rc) : -1.0f;
-                                    scratch[4 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum3 >> 16, fc, rc) : -1.0f;
-                                    scratch[5 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum4 & 0xFFFFu, fc, rc) : -1.0f;
-                                    scratch[6 * a.nRaysPad + t] = cnt > 0 ? div_int_exact(isum4 >> 16, fc, rc) : -1.0f;
+                                    st_keep(scratch + 3 * a.nRaysPad + t, cnt > 0 ? div_int_exact(isum3 & 0xFFFFu, fc, rc) : -1.0f, keep);
+                                    st_keep(scratch + 4 * a.nRaysPad + t, cnt > 0 ? div_int_exact(isum3 >> 16, fc, rc) : -1.0f, keep);
+                                    st_keep(scratch + 5 * a.nRaysPad + t, cnt > 0 ? div_int_exact(isum4 & 0xFFFFu, fc, rc) : -1.0f, keep);
+                                    st_keep(scratch + 6 * a.nRaysPad + t, cnt > 0 ? div_int_exact(isum4 >> 16, fc, rc) : -1.0f, keep);
                                 }
                             } else {
                                 v = cnt > 0 ? __fdiv_rn(sum, (float)cnt) : -1.0f;
@@ -536,6 +562,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 // moving four neighbouring rays with one 16-byte load (the scratch row is mostly
                 // outside L2, so bytes in flight set the pace); four groups in flight per thread
                 const float* src = scratch + (size_t)(sub - 1) * a.nRaysPad;
+                const uint64_t once = l2_evict_first_policy();
                 constexpr int kRel = kThreads - 32;
                 const int ntask = a.nGroups * 8;
                 for (int it = tid - 32; it < ntask; it += 4 * kRel) {
@@ -546,7 +573,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                         const int task = it + u * kRel;
                         const int gi = task >> 3;
                         tb[u] = task < ntask ? gtb_s[gi] : 0u;
-                        v[u] = task < ntask ? *(const float4*)(src + (gst_s[gi] & 0xFFFFu) * 32 + (task & 7) * 4)
+                        v[u] = task < ntask ? ld_once(src + (gst_s[gi] & 0xFFFFu) * 32 + (task & 7) * 4, once)
                                             : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                     }
 #pragma unroll

@@ -179,3 +179,52 @@ class Radon:
         nrm = np.linalg.norm(n, axis=1).clip(1e-12)
         n /= nrm.reshape(nPats * nBands, 1)
         return n.reshape(nPats, nBands, 3)
+
+
+VENDORS = {"EDAX": 0, "OXFORD": 1, "EMSOFT": 2, "KIKUCHIPY": 3, "BRUKER": 4}
+
+
+def radon2pole_gpu(theta, rho, imDim, PC=None, vendor='EDAX', stream=None):
+    """``Radon.radon2pole`` on the device (libebsdgpu ``ebsd_radon2pole``): band ``theta`` /
+    ``rho`` as CUDA float32 tensors [nPats, nBands] (e.g. the device fields of a find_bands
+    call) -> unit plane normals, a CUDA tensor [nPats, nBands, 3].  ``PC``: one pattern centre
+    ([3], or [4] for EMSOFT with the pixel size) or one per pattern ([nPats, 3/4]); ``imDim``:
+    (rows, columns).  No counterpart on the reference's GPU path (radon2pole runs on the host,
+    radon_fast.py:314-397)."""
+    import ctypes as C
+    import torch
+    from . import _lib
+    lib = _lib.load()
+    if not hasattr(lib, "_r2p_bound"):
+        lib.ebsd_radon2pole.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                        C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]
+        lib.ebsd_radon2pole.restype = C.c_int
+        lib._r2p_bound = True
+    ven = str.upper(vendor)
+    if ven not in VENDORS:
+        raise ValueError(f"unknown vendor {vendor!r}")
+    if PC is None:
+        PC = np.array([0.471659, 0.675044, 0.630139])
+    theta = theta.to(torch.float32).contiguous()
+    rho = rho.to(torch.float32).contiguous()
+    if theta.shape != rho.shape or theta.dim() != 2:
+        raise ValueError("theta and rho must be [nPats, nBands] tensors of the same shape")
+    n, nb = theta.shape
+    pc = torch.as_tensor(np.asarray(PC, dtype=np.float32) if not torch.is_tensor(PC) else PC,
+                         dtype=torch.float32, device=theta.device).contiguous()
+    width = 4 if ven == 'EMSOFT' else 3
+    if pc.dim() == 1:
+        if pc.numel() < width:
+            raise ValueError(f"{ven} pattern centres need {width} numbers")
+        stride = 0
+    else:
+        if pc.shape[1] < width:
+            raise ValueError(f"{ven} pattern centres need {width} numbers")
+        stride = pc.shape[1] if pc.shape[0] == n else 0
+    out = torch.empty((n, nb, 3), dtype=torch.float32, device=theta.device)
+    st = stream if stream is not None else torch.cuda.current_stream(theta.device).cuda_stream
+    _lib.check(lib.ebsd_radon2pole(C.c_void_p(theta.data_ptr()), C.c_void_p(rho.data_ptr()), int(n), int(nb),
+                                   int(imDim[0]), int(imDim[1]), VENDORS[ven], C.c_void_p(pc.data_ptr()),
+                                   int(stride), C.c_void_p(out.data_ptr()), C.c_void_p(int(st))),
+               "ebsd_radon2pole")
+    return out
