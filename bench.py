@@ -32,6 +32,12 @@ METRIC = "band-detect patterns/sec on 1 GB300: batched FP16 vs plain FP32, at <=
 H = W = 80
 NRHO, NTHETA, NBANDS = 120, 180, 9
 BYTES_PER_PATTERN = H * W * 1 + 41 * NBANDS   # algorithmic bytes: pattern in, band fields out
+# DRAM bytes (read + write) per pattern of the fused kernel at eight patterns per pass, from an
+# ncu capture of the same launch configuration on 40,000 patterns (dram__bytes_read.sum +
+# dram__bytes_write.sum = 0.648 GB + 2.273 GB); the traffic grows with the patterns, so a
+# launch's traffic is this times its patterns.  Most of it is the write-back of the parked
+# ray means (seven rows per CTA per eight patterns), not input re-reads.
+DRAM_BYTES_PER_PATTERN = (648_438_528 + 2_272_787_200) / 40_000
 SEED = 1_000_000
 WORKLOAD = ("find_bands on 1,000,000 80x80 uint8 patterns, nTheta 180, nRho 120, nBands 9, LoG sigma 1, "
             "rhoMaskFrac 0.1, circular mask, 10% noise-only")
@@ -224,7 +230,7 @@ def main():
 
     # autotune the patterns per block pass on a sample of the batch, then capture one step
     # (the whole batch is one persistent launch per 1M-pattern chunk) in a CUDA graph
-    ppp = "rule: 2 for uint8 without background"
+    ppp = "rule: 8 for uint8 without background"
     if not args.no_autotune:
         ppp = plan.autotune(pats_d.data_ptr(), _lib.EBSD_U8, min(N, 16384), method, stream=stream.cuda_stream)
     plan.reserve(method, N)
@@ -293,8 +299,10 @@ def main():
     launch_ms = float(np.mean(per_step)) / fused_launches if method.startswith("fused") else float(np.mean(per_step))
     units_per_launch = N / fused_launches if method.startswith("fused") else N
     achieved = BYTES_PER_PATTERN * units_per_launch / (launch_ms / 1000.0) / 1e9
+    traffic = DRAM_BYTES_PER_PATTERN * units_per_launch if method == "fused" and ppp in (8, "rule: 8 for uint8 without background") else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "peak_source": peak_src,
+            "traffic": traffic, "traffic_source": "ncu capture, 40,000 patterns, scaled per pattern" if traffic else None,
+            "peak_source": peak_src,
             "kernel": "k_fused (+ k_band_epilogue)" if method.startswith("fused") else "per-stage sequence (7 kernels/chunk)"}
 
     # end to end through the C ABI with pinned host buffers (H2D + D2H inside the timed region)
