@@ -7,11 +7,15 @@
 //                    pattern of the (2 sr + 1)^2 window (shifted inward at the scan edges),
 //                    weight exp(-max(d - dthresh, 0) / lam^2), centre weight 1, normalised
 //   k_nlpar_average  nlpar_cpu.py:929-934: weighted sum over the window for every pixel
+//   *_tiled          the same two for 32 neighbouring scan pixels per block, with the patterns
+//                    their windows touch staged in shared memory (used for sr <= 3)
 //
 // The float32 arithmetic keeps the reference's order: squared differences accumulate
 // sequentially over the masked-pixel list, window weights are summed and applied in window
 // order, and every add/mul is an explicitly rounded intrinsic (no contracted FMAs).
 #include "ebsd_internal.cuh"
+
+#include <algorithm>
 
 namespace ebsd {
 namespace {
@@ -135,6 +139,163 @@ __global__ void k_nlpar_average(const T* __restrict__ data, int nrows, int ncols
     out[(int64_t)pix * npx + k] = acc;
 }
 
+// ---- tiled kernels: one block per 32 neighbouring scan pixels of one scan row ------------
+// The block stages, for a chunk of pixels, the values of every pattern its windows touch
+// (2 sr + 1 rows x up to 32 + 4 sr columns of the scan) in shared memory, so that each pattern
+// is read from memory once per block instead of once per (pixel, window slot); the per-pair
+// and per-output arithmetic is the untiled kernels', in the same order.
+constexpr int kTileX = 32;  // scan pixels per block
+constexpr int kChunk = 32;  // pixel values per staged pattern per step
+constexpr int kSP = kChunk + 1;  // staged row pitch (odd: lanes on different patterns, no conflicts)
+constexpr int kTy = 16;     // threadIdx.y extent (blockDim = 32 x 16)
+
+// Distance weights of NLPAR.nlpar_nb (nlpar_cpu.py:866-927) for window slots c = ty + 16 j.
+template <int MP>
+__global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_tiled(
+        const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind,
+        int nind, float mxval, const float* __restrict__ sigma, float lam2, float dthresh, int sr,
+        float* __restrict__ wout) {
+    extern __shared__ float sm[];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileX + tx;
+    const int y = blockIdx.y, x0 = blockIdx.x * kTileX;
+    const int wn = 2 * sr + 1, winsz = wn * wn;
+    int ys, ye;
+    window(y, sr, nrows, ys, ye);
+    const int cx0 = x0 - 2 * sr > 0 ? x0 - 2 * sr : 0;
+    const int cx1 = x0 + kTileX + 2 * sr < ncols ? x0 + kTileX + 2 * sr : ncols;
+    const int ncx = cx1 - cx0, nstage = wn * ncx;
+    float* S = sm;                    // [nstage][kSP]
+    float* W = sm + nstage * kSP;     // [kTileX][winsz], then [kTileX] totals
+    float* T = W + kTileX * winsz;
+    const int x = x0 + tx;
+    const bool px_ok = x < ncols;
+    int xs, xe;
+    window(px_ok ? x : ncols - 1, sr, ncols, xs, xe);
+    const int pix = y * ncols + (px_ok ? x : ncols - 1);
+    const int cslot = (y - ys) * ncx + ((px_ok ? x : ncols - 1) - cx0);
+    float d[MP], n[MP];
+    int nbs[MP];
+#pragma unroll
+    for (int j = 0; j < MP; ++j) {
+        const int c = ty + kTy * j;
+        d[j] = 0.0f;
+        n[j] = 0.0f;
+        nbs[j] = c < winsz ? (c / wn) * ncx + (xs + c % wn - cx0) : cslot;
+    }
+    for (int q0 = 0; q0 < nind; q0 += kChunk) {
+        const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
+        const int k = tx < qn ? __ldg(ind + q0 + tx) : 0;
+        __syncthreads();  // the previous chunk has been consumed
+        for (int st = ty; st < nstage; st += kTy) {
+            const int r = st / ncx, cc = st - r * ncx;
+            const int64_t pat = (int64_t)(ys + r) * ncols + (cx0 + cc);
+            S[st * kSP + tx] = tx < qn ? __ldg(data + pat * npx + k) : 0.0f;
+        }
+        __syncthreads();
+        for (int qq = 0; qq < qn; ++qq) {
+            const float xv = S[cslot * kSP + qq];
+#pragma unroll
+            for (int j = 0; j < MP; ++j) {
+                const float yv = S[nbs[j] * kSP + qq];
+                if (yv < mxval && xv < mxval) {  // pair_ssd's order: count, difference, square
+                    n[j] = __fadd_rn(n[j], 1.0f);
+                    const float t = __fsub_rn(xv, yv);
+                    d[j] = __fadd_rn(d[j], __fmul_rn(t, t));
+                }
+            }
+        }
+    }
+    // weights (k_nlpar_weights' arithmetic), then the window-order normalisation
+#pragma unroll
+    for (int j = 0; j < MP; ++j) {
+        const int c = ty + kTy * j;
+        if (c < winsz && px_ok) {
+            const int jn = ys + c / wn, inn = xs + c % wn;
+            const int nb = inn + ncols * jn;
+            float w;
+            if (nb == pix) {
+                w = -1.0e6f;
+            } else {
+                float s0 = sigma[pix], s1 = sigma[nb];
+                s0 = __fmul_rn(s0, s0);
+                s1 = __fmul_rn(s1, s1);
+                const float ss = __fadd_rn(s0, s1);
+                const float d2 = __fsub_rn(d[j], __fmul_rn(n[j], ss));
+                const float dnorm = __fmul_rn(ss, sqrtf(__fmul_rn(2.0f, n[j])));
+                w = dnorm > 1.e-8f ? __fdiv_rn(d2, dnorm) : __fmul_rn(1e6f, n[j]);
+            }
+            w = fmaxf(__fsub_rn(w, dthresh), 0.0f);
+            w = expf(__fmul_rn(__fmul_rn(-1.0f, w), lam2));
+            W[tx * winsz + c] = w;
+        }
+    }
+    __syncthreads();
+    if (ty == 0 && px_ok) {
+        float t = 0.0f;
+        for (int c = 0; c < winsz; ++c) t = __fadd_rn(t, W[tx * winsz + c]);
+        T[tx] = t;
+    }
+    __syncthreads();
+    for (int i = tid; i < kTileX * winsz; i += kTileX * kTy) {
+        const int px = i / winsz, c = i - px * winsz;
+        if (x0 + px < ncols) wout[(int64_t)(y * ncols + x0 + px) * winsz + c] = __fdiv_rn(W[px * winsz + c], T[px]);
+    }
+}
+
+// Weighted window sum (k_nlpar_average's order) for 32 scan pixels x 32 pattern pixels per step.
+template <typename T>
+__global__ void __launch_bounds__(kTileX * kTy) k_nlpar_average_tiled(
+        const T* __restrict__ data, int nrows, int ncols, int npx, const T* __restrict__ w, int sr,
+        T* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T* sm = (T*)smraw;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileX + tx;
+    const int y = blockIdx.y, x0 = blockIdx.x * kTileX;
+    const int wn = 2 * sr + 1, winsz = wn * wn;
+    int ys, ye;
+    window(y, sr, nrows, ys, ye);
+    const int cx0 = x0 - 2 * sr > 0 ? x0 - 2 * sr : 0;
+    const int cx1 = x0 + kTileX + 2 * sr < ncols ? x0 + kTileX + 2 * sr : ncols;
+    const int ncx = cx1 - cx0, nstage = wn * ncx;
+    T* S = sm;                 // [nstage][kSP]
+    T* Wt = sm + nstage * kSP; // [kTileX][winsz]
+    const int npix_tile = ncols - x0 < kTileX ? ncols - x0 : kTileX;
+    for (int i = tid; i < npix_tile * winsz; i += kTileX * kTy)
+        Wt[i] = w[(int64_t)(y * ncols + x0) * winsz + i];
+    for (int k0 = 0; k0 < npx; k0 += kChunk) {
+        const int kn = npx - k0 < kChunk ? npx - k0 : kChunk;
+        __syncthreads();
+        for (int st = ty; st < nstage; st += kTy) {
+            const int r = st / ncx, cc = st - r * ncx;
+            const int64_t pat = (int64_t)(ys + r) * ncols + (cx0 + cc);
+            S[st * kSP + tx] = tx < kn ? data[pat * npx + k0 + tx] : (T)0;
+        }
+        __syncthreads();
+        if (tx < kn) {
+            for (int px = ty; px < npix_tile; px += kTy) {
+                int xs, xe;
+                window(x0 + px, sr, ncols, xs, xe);
+                const T* wp = Wt + px * winsz;
+                T acc = (T)0;
+                int c = 0;
+                for (int r = 0; r < wn; ++r) {
+                    const T* srow = S + (r * ncx + (xs - cx0)) * kSP + tx;
+                    for (int cc = 0; cc < wn; ++cc, ++c) acc = wadd(acc, srow[cc * kSP], wp[c]);
+                }
+                out[(int64_t)(y * ncols + x0 + px) * npx + k0 + tx] = acc;
+            }
+        }
+    }
+}
+
+size_t tiled_smem(int sr, int ncols, size_t elem, bool weights) {
+    const int wn = 2 * sr + 1;
+    const int ncx = std::min(ncols, kTileX + 4 * sr);
+    size_t b = (size_t)wn * ncx * kSP * elem + (size_t)kTileX * wn * wn * elem;
+    if (weights) b += kTileX * sizeof(float);
+    return b;
+}
+
 }  // namespace
 }  // namespace ebsd
 
@@ -165,6 +326,16 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, c
     int winsz = (2 * sr + 1) * (2 * sr + 1);
     int bs = ((winsz + 31) / 32) * 32;
     cudaStream_t st = (cudaStream_t)stream;
+    const dim3 tgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), tblock(kTileX, kTy);
+    const size_t wsm = tiled_smem(sr, ncols, sizeof(float), true), asm_ = tiled_smem(sr, ncols, sizeof(float), false);
+    if (sr <= 3 && wsm <= 48 * 1024 && asm_ <= 48 * 1024) {
+        k_nlpar_weights_tiled<4><<<tgrid, tblock, wsm, st>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval,
+                                                             d_sigma, lam2, dthresh, sr, d_work);
+        int rc = launch_status();
+        if (rc != EBSD_OK) return rc;
+        k_nlpar_average_tiled<float><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr, d_out);
+        return launch_status();
+    }
     k_nlpar_weights<<<(unsigned)(nrows * ncols), bs, winsz * sizeof(float), st>>>(
         d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma, lam2, dthresh, sr, d_work);
     int rc = launch_status();
@@ -179,6 +350,12 @@ int ebsd_nlpar_apply(const float* d_x, int32_t nrows, int32_t ncols, int32_t npx
     if (!d_x || !d_w || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10 || 2 * sr + 1 > nrows ||
         2 * sr + 1 > ncols)
         return EBSD_E_ARG;
+    const size_t asm_ = tiled_smem(sr, ncols, sizeof(float), false);
+    if (asm_ <= 48 * 1024) {
+        const dim3 tgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), tblock(kTileX, kTy);
+        k_nlpar_average_tiled<float><<<tgrid, tblock, asm_, (cudaStream_t)stream>>>(d_x, nrows, ncols, npx, d_w, sr, d_out);
+        return launch_status();
+    }
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
     k_nlpar_average<float><<<grid, 256, 0, (cudaStream_t)stream>>>(d_x, nrows, ncols, npx, d_w, sr, d_out);
     return launch_status();
