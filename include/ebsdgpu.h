@@ -191,6 +191,67 @@ int ebsd_radon2pole(const float* d_theta, const float* d_rho, int64_t npat, int3
                     int32_t H, int32_t W, int32_t vendor, const float* d_pc, int32_t pc_stride,
                     float* d_normals, void* stream);
 
+/* ---- band weights and pattern quality (_ebsd_index_single.py:751-763) ------------------
+ * For [n][nBands] band fields (device arrays, e.g. what ebsd_find_bands wrote):
+ *   adj[p][b] = (1 - |rho| * 0.5 / rhomax) * max * (theta > 2 deg ? 0.75 : 0.25)
+ *               * (theta < 178 deg ? 0.75 : 0.25) * valid        (the vote's band intensity)
+ *   pq[p] = mean_b(max * valid),  iq[p] = mean_b(normmax * valid)
+ * in float32 with the reference's operation order (means summed in numpy's pairwise order).
+ * d_pq / d_iq may be NULL.  nBands 1..128. */
+int ebsd_band_intensity(const float* d_max, const float* d_normmax, const float* d_theta,
+                        const float* d_rho, const int8_t* d_valid, int64_t n, int32_t nBands,
+                        float rhomax, float* d_adj, float* d_pq, float* d_iq, void* stream);
+
+/* ---- band indexing by triplet voting (tripletvote.BandIndexer.bandindex,
+ * tripletvote.py:492-633, with high_fidelity on) --------------------------------------- */
+typedef struct ebsd_vote_plan_s* ebsd_vote_plan_t;
+
+/* One phase library as BandIndexer.build_trip_lib (tripletvote.py:320-490) leaves it.  All
+ * pointers are HOST pointers, copied during ebsd_vote_plan_create. */
+typedef struct {
+    int32_t nfam;                /* pole families, 2..16 (BandIndexer.polefamilies rows)       */
+    int32_t ntrip;               /* triplets (angtriplets['angles'] rows), 1..8192              */
+    const double* trip_angles;   /* angtriplets['angles'] [ntrip][3], degrees, rows ascending  */
+    const int64_t* trip_family;  /* angtriplets['familyid'] [ntrip][3], each < nfam            */
+    const int64_t* lut;          /* BandIndexer.lut [3][3][3][3], entries 0..2                */
+    int32_t npoles;              /* completelib['polesCart'] rows, 1..512                     */
+    const double* poles_cart;    /* completelib['polesCart'] [npoles][3]                      */
+    const int32_t* pole_family;  /* completelib['familyid'] [npoles], each < nfam             */
+    const double* ang_table;     /* completelib['angTable'] [npoles][npoles], degrees         */
+    const int32_t* fam_count;    /* completelib['nFamily'] [nfam]                             */
+    const int64_t* fam_index;    /* completelib['famIndex'] [nfam]                            */
+    double ang_tol;              /* BandIndexer.angTol, degrees                               */
+    int32_t nband_earlyexit;     /* BandIndexer.nband_earlyexit                               */
+    int32_t simple_qweights;     /* BandIndexer.simpleqweights (0/1)                          */
+} ebsd_triplib_desc;
+
+/* bandindex outputs for n patterns (DEVICE arrays, row-major).  The last five are the
+ * vote's intermediates, written when non-NULL. */
+typedef struct {
+    double* quat;          /* [n][4] QUEST orientation (avequat)                           */
+    double* fit;           /* [n] mean band misfit, degrees                                */
+    float* cm;             /* [n] vote confidence of the matched bands (-1: < 3 matched)   */
+    int64_t* polematch;    /* [n][nBands] library pole per band (-1000: pattern unindexed) */
+    int64_t* nmatch;       /* [n] bands matched                                            */
+    int64_t* ij;           /* [n][4] (ii, jj, band1, band2) of the winning band pair       */
+    int32_t* acc_correct;  /* [n] matched bands whose voted family agrees                  */
+    double* bandfit;       /* [n][nBands] per-band misfit, degrees                         */
+    float* accw;           /* [n][nfam][nBands] weighted votes, or NULL                    */
+    float* accn;           /* [n][nfam][nBands] vote counts, or NULL                       */
+    int32_t* bandfam;      /* [n][nBands] voted family, or NULL                            */
+    float* bandrank;       /* [n][nBands] band rank, or NULL                               */
+    uint8_t* polevalid;    /* [n][nBands] band matched within angTol, or NULL              */
+} ebsd_index_out;
+
+int ebsd_vote_plan_create(const ebsd_triplib_desc* desc, int device, ebsd_vote_plan_t* out);
+int ebsd_vote_plan_destroy(ebsd_vote_plan_t plan);
+
+/* d_norms [n][nBands][3] float32 unit band normals (ebsd_radon2pole); d_intensity [n][nBands]
+ * float32 band weights (ebsd_band_intensity) or NULL for all ones.  nBands 1..32.  One warp
+ * per pattern; no allocation, no host synchronisation (CUDA-graph capturable). */
+int ebsd_band_index(ebsd_vote_plan_t plan, const float* d_norms, const float* d_intensity, int64_t n,
+                    int32_t nBands, const ebsd_index_out* out, void* stream);
+
 /* ---- differentiable path (no counterpart in the reference beyond the empty DIFF_NLPAR
  * placeholder, nlpar.py:75-77) --------------------------------------------------------- */
 

@@ -18,10 +18,15 @@ def pytest_configure(config):
 
 
 def golden_names():
-    """Band-detection golden cases (NLPAR cases and the orientation fixtures are separate)."""
+    """Band-detection golden cases (NLPAR, orientation and voting fixtures are separate)."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0]
                               for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
-                  if not n.startswith(("nlpar_", "orient_")))
+                  if not n.startswith(("nlpar_", "orient_", "vote_")))
+
+
+def vote_golden_names():
+    return sorted(os.path.splitext(os.path.basename(p))[0]
+                  for p in glob.glob(os.path.join(GOLDEN_DIR, "vote_*.npz")))
 
 
 def nlpar_golden_names():
