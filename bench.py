@@ -58,6 +58,7 @@ def parse():
     ap.add_argument("--no-variants", action="store_true", help="skip timing the other methods")
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's rule-based kernel variant")
+    ap.add_argument("--no-index", action="store_true", help="skip timing the device indexing after detection")
     return ap.parse_args()
 
 
@@ -154,6 +155,65 @@ def cpu_baseline(pool, sample, impl_kind):
         dt = time.perf_counter() - t0
         desc = f"numpy restatement of find_bands, {len(pats)} patterns, 1 process"
     return {"value": len(pats) / dt, "unit": "patterns/s", "cores": cores, "kind": "port", "sample": desc}
+
+
+VOTE_LIBRARY = os.path.join(ROOT, "tests", "golden", "vote_fcc_orient.npz")
+
+
+def time_indexing(outs, bd, N, stream, with_cpu, detect_ms):
+    """The records -> orientations chain on the device after detection (EBSDIndexer's
+    _indexbandsphase, _ebsd_index_single.py:720-800, for the FCC phase): band normals
+    (ebsd_radon2pole), band weights (ebsd_band_intensity) and triplet voting (ebsd_band_index),
+    each timed with CUDA events on the records of the whole batch, inputs resident."""
+    import torch
+    from pyebsdindex_gb300 import radon_fast, tripletvote as tv
+    d = np.load(VOTE_LIBRARY)
+    params = json.loads(str(d["params"]))
+    lib = {k[4:]: d[k] for k in d.files if k.startswith("lib_")}
+    bi = tv.BandIndexer(lib=lib, angTol=params["angTol"], nband_earlyexit=params["nband_earlyexit"],
+                        simpleqweights=params["simpleqweights"])
+    pc = [0.46, 0.70, 0.64]
+    st = stream.cuda_stream
+    vout = None
+
+    def stage(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            r = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps, r
+
+    ms_n, normals = stage(lambda: radon_fast.radon2pole_gpu(outs["theta"], outs["rho"], (H, W), PC=pc, vendor="EDAX",
+                                                            stream=st))
+    ms_i, (adj, pq, iq) = stage(lambda: tv.band_intensity_gpu(outs["max"], outs["normmax"], outs["theta"],
+                                                              outs["rho"], outs["valid"], bd.rhoMax, stream=st))
+    vout = bi.bandindex_device(normals, adj, stream=st)
+    ms_v, _ = stage(lambda: bi.bandindex_device(normals, adj, out=vout, stream=st))
+    indexed = float((vout["nmatch"] >= 3).float().mean().item())
+    res = {
+        "workload": f"records of the {N:,} detected patterns -> FCC orientations (angTol 2, QUEST), PC (0.46, 0.70, 0.64) EDAX",
+        "normals_patterns_per_s": N / (ms_n / 1000.0),
+        "intensity_patterns_per_s": N / (ms_i / 1000.0),
+        "vote_patterns_per_s": N / (ms_v / 1000.0),
+        "patterns_to_orientations_per_s": N / ((detect_ms + ms_n + ms_i + ms_v) / 1000.0),
+        "fraction_indexed": indexed,
+        "kernels": ["k_radon2pole", "k_band_intensity", "k_band_index"],
+    }
+    if with_cpu:
+        from oracle import vote_oracle as vo  # the CPU leg: the numpy restatement of bandindex
+        m = 200
+        nrm = normals[:m].cpu().numpy()
+        w = adj[:m].cpu().numpy()
+        t0 = time.perf_counter()
+        vo.bandindex(lib, params, nrm, w)
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": m / dt, "unit": "patterns/s", "cores": 1, "kind": "port",
+                               "sample": f"bandindex of the first {m} patterns' records, numpy restatement, 1 thread"}
+    return res
 
 
 def run_reference(args):
@@ -346,6 +406,11 @@ def main():
             variants[vm] = vn * 2 / (a.elapsed_time(b) / 1000.0)
         variants[method] = value / world
 
+    indexing = None
+    if not args.no_index:
+        indexing = time_indexing(outs, bd, N, stream, rank == 0 and world == 1 and not args.no_cpu,
+                                 float(np.mean(per_step)))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
@@ -366,7 +431,7 @@ def main():
                        "patterns_per_block_pass": ppp, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "variants_patterns_per_s": variants,
+            "variants_patterns_per_s": variants, "indexing": indexing,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))

@@ -38,6 +38,9 @@ struct ebsd_vote_plan_s {
     double* d_angtab = nullptr;   // [npoles][npoles]
     int32_t* d_famcnt = nullptr;  // [nfam]
     int32_t* d_famidx = nullptr;  // [nfam]
+    float* d_cand = nullptr;      // [nfam][npoles][2] band-pair cosine interval per library column
+    float* d_par = nullptr;       // [1] largest |cosine| of a band pair that is not parallel
+    float par = -1.0f;            // host copy of *d_par
 };
 
 namespace ebsd {
@@ -58,6 +61,8 @@ struct VoteArgs {
     const double* angtab;
     const int32_t* famcnt;
     const int32_t* famidx;
+    const float* cand;
+    float par;
     int nfam, ntrip, npoles, nb;
     float tol_f;
     double tol;
@@ -133,8 +138,9 @@ __device__ __forceinline__ float norm3(const float* a) {
     return __fsqrt_rn(dot3(a[0], a[1], a[2], a[0], a[1], a[2]));
 }
 
-// float32 arccos(x) * RADEG, the arccos correctly rounded
-__device__ __forceinline__ float acos_deg(float x) {
+// float32 arccos(x) * RADEG, the arccos correctly rounded (float64 arccos, rounded once); kept
+// out of line: the float64 arccos is long and the kernel is instruction-cache bound
+__device__ __noinline__ float acos_deg(float x) {
     return __fmul_rn(__double2float_rn(acos((double)x)), kRadegF);
 }
 
@@ -197,16 +203,21 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     for (int t = lane; t < 2 * nfam * nb; t += 32) accw[t] = 0.0f;
     __syncwarp();
 
-    // band-band angles, tripletvote.py:1181-1188
-    for (int t = lane; t < nb * nb; t += 32) {
-        const int i = t / nb, j = t - i * nb;
+    // band-band angles, tripletvote.py:1181-1188 (the vote reads the upper triangle only)
+    for (int t = lane; t < nb * (nb - 1) / 2; t += 32) {
+        int i = 0, r = t;
+        while (r >= nb - 1 - i) {
+            r -= nb - 1 - i;
+            ++i;
+        }
+        const int j = i + 1 + r;
         const float* a = bn + 3 * i;
         const float* b = bn + 3 * j;
         float d = fabsf(dot3(a[0], a[1], a[2], b[0], b[1], b[2]));
         d = fminf(fmaxf(d, -1.0f), 1.0f);
         float v = acos_deg(d);
         if (inten[i] < 1e-6f || inten[j] < 1e-6f) v = 10000.0f;
-        ang[t] = v;
+        ang[i * nb + j] = v;
     }
     __syncwarp();
 
@@ -317,8 +328,10 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
             int ngood = 0;
             float afit = 0.0f;
             int pm = -1, pv = 0;
-            if (acos_deg(fabsf(c12)) > tolf) {
-                const float a01 = acos_deg(c12);
+            // arccos(|c12|) > angTol and |angTable - arccos(c12)| < angTol (tripletvote.py:1517-1524) as
+            // cosine intervals precomputed with the same arccos (k_vote_thresholds)
+            if (fabsf(c12) <= A.par) {
+                const float* cint = A.cand + (size_t)f1 * npoles * 2;
                 const int row = A.famidx[f1], lo = A.famidx[f2], cnt = A.famcnt[f2];
                 float x[3];
                 cross3(v1, v2, x);
@@ -333,8 +346,7 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
                 bool any = false;
                 for (int cb = 0; cb < cnt; cb += 32) {
                     const int col = lo + cb + lane;
-                    const bool hit = cb + lane < cnt &&
-                                     fabs(__dsub_rn(A.angtab[(size_t)row * npoles + col], (double)a01)) < A.tol;
+                    const bool hit = cb + lane < cnt && c12 >= cint[2 * col] && c12 <= cint[2 * col + 1];
                     unsigned m = __ballot_sync(kFull, hit);
                     any = any || m != 0;
                     while (m) {
@@ -620,6 +632,64 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     __syncwarp();
 }
 
+// Plan-time thresholds of the TRIAD step, evaluated with the kernel's own arccos so that the
+// float comparisons replace the reference's tests exactly (acos_deg is monotone in x):
+//   par: the largest y in [0, 1] with acos_deg(y) > angTol, so that the pair test
+//        arccos(|c|) * RADEG > angTol (tripletvote.py:1517) is |c| <= par;
+//   cand[f][c] = [lo, hi]: the cosines x in [-1, 1] with |angTable[famIndex[f]][c] - acos_deg(x)|
+//        < angTol in float64 (tripletvote.py:1521-1522); empty as [+inf, -inf].
+__device__ __forceinline__ int64_t okey(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (int64_t)((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+}
+__device__ __forceinline__ float okey_float(int64_t k) {
+    const uint32_t v = (uint32_t)k;
+    return __uint_as_float((v & 0x80000000u) ? (v & 0x7fffffffu) : ~v);
+}
+
+__global__ void k_vote_thresholds(const double* __restrict__ angtab, const int32_t* __restrict__ famidx,
+                                  int nfam, int npoles, double tol, float tolf, float* __restrict__ cand,
+                                  float* __restrict__ par) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) {
+        int64_t a = okey(0.0f), b = okey(1.0f);
+        if (!(acos_deg(0.0f) > tolf)) {
+            *par = -1.0f;
+        } else {
+            while (a < b) {  // last key with the test true
+                const int64_t mid = a + (b - a + 1) / 2;
+                if (acos_deg(okey_float(mid)) > tolf) a = mid; else b = mid - 1;
+            }
+            *par = okey_float(a);
+        }
+    }
+    if (t >= nfam * npoles) return;
+    const int f = t / npoles, c = t - f * npoles;
+    const double T = angtab[(size_t)famidx[f] * npoles + c];
+    const int64_t k0 = okey(-1.0f), k1 = okey(1.0f);
+    // d(x) = T - acos_deg(x) does not decrease with x; the test is -tol < d < tol
+    int64_t a = k0, b = k1 + 1;
+    while (a < b) {  // first key with d > -tol (k1 + 1: none)
+        const int64_t mid = a + (b - a) / 2;
+        if (__dsub_rn(T, (double)acos_deg(okey_float(mid))) > -tol) b = mid; else a = mid + 1;
+    }
+    const int64_t lo = a;
+    a = k0 - 1;
+    b = k1;
+    while (a < b) {  // last key with d < tol (k0 - 1: none)
+        const int64_t mid = a + (b - a + 1) / 2;
+        if (__dsub_rn(T, (double)acos_deg(okey_float(mid))) < tol) a = mid; else b = mid - 1;
+    }
+    const int64_t hi = a;
+    if (lo > k1 || hi < k0 || lo > hi) {
+        cand[2 * t] = INFINITY;
+        cand[2 * t + 1] = -INFINITY;
+    } else {
+        cand[2 * t] = okey_float(lo);
+        cand[2 * t + 1] = okey_float(hi);
+    }
+}
+
 __global__ void __launch_bounds__(kWarps * 32) k_band_index(VoteArgs A) {
     extern __shared__ __align__(16) float vsm[];
     float* s_iv = vsm;
@@ -774,6 +844,15 @@ extern "C" int ebsd_vote_plan_create(const ebsd_triplib_desc* d, int device, ebs
     if (!rc) rc = up((void**)&p->d_angtab, d->ang_table, (size_t)np_ * np_ * 8);
     if (!rc) rc = up((void**)&p->d_famcnt, d->fam_count, (size_t)nf * 4);
     if (!rc) rc = up((void**)&p->d_famidx, fidx.data(), (size_t)nf * 4);
+    if (!rc && cudaMalloc((void**)&p->d_cand, (size_t)nf * np_ * 2 * 4) != cudaSuccess) rc = EBSD_E_NOMEM;
+    if (!rc && cudaMalloc((void**)&p->d_par, 4) != cudaSuccess) rc = EBSD_E_NOMEM;
+    if (!rc) {
+        const int total = nf * np_;
+        k_vote_thresholds<<<(total + 127) / 128, 128>>>(p->d_angtab, p->d_famidx, nf, np_, p->tol, (float)p->tol,
+                                                        p->d_cand, p->d_par);
+        rc = launch_status();
+        if (!rc && cudaMemcpy(&p->par, p->d_par, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = EBSD_E_LAUNCH;
+    }
     if (rc) {
         ebsd_vote_plan_destroy(p);
         return rc;
@@ -794,6 +873,8 @@ extern "C" int ebsd_vote_plan_destroy(ebsd_vote_plan_t p) {
     cudaFree(p->d_angtab);
     cudaFree(p->d_famcnt);
     cudaFree(p->d_famidx);
+    cudaFree(p->d_cand);
+    cudaFree(p->d_par);
     delete p;
     return EBSD_OK;
 }
@@ -826,6 +907,8 @@ extern "C" int ebsd_band_index(ebsd_vote_plan_t p, const float* d_norms, const f
     A.angtab = p->d_angtab;
     A.famcnt = p->d_famcnt;
     A.famidx = p->d_famidx;
+    A.cand = p->d_cand;
+    A.par = p->par;
     A.nfam = p->nfam;
     A.ntrip = p->ntrip;
     A.npoles = p->npoles;
