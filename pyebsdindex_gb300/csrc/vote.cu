@@ -19,7 +19,9 @@
 //     order, so that every float32 vote sum adds in the reference's order.
 #include "ebsd_internal.cuh"
 
+#include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cmath>
 #include <cstring>
 
@@ -29,7 +31,7 @@ struct ebsd_vote_plan_s {
     double tol = 0.0;
     int early = 0, simpleq = 0;
     uint8_t lut[27] = {};         // lut[:, s0, s1, s2] as 3 x 2 bits, index s0 * 9 + s1 * 3 + s2
-    float* d_iv = nullptr;        // [6][ntrip] acceptance intervals lo0, hi0, lo1, hi1, lo2, hi2
+    float* d_iv = nullptr;        // [6][ntrip] acceptance intervals lo0, hi0, lo1, hi1, lo2, hi2, rows sorted by lo0
     uint32_t* d_tfam = nullptr;   // [ntrip] f0 | f1 << 8 | f2 << 16
     double* d_tang = nullptr;     // [ntrip][3]
     float* d_pole = nullptr;      // [3][npoles] float32 poles, component-major
@@ -41,12 +43,15 @@ struct ebsd_vote_plan_s {
     float* d_cand = nullptr;      // [nfam][npoles][2] band-pair cosine interval per library column
     float* d_par = nullptr;       // [1] largest |cosine| of a band pair that is not parallel
     float par = -1.0f;            // host copy of *d_par
+    int32_t* d_orig = nullptr;    // [ntrip] library index of each interval row (rows sorted by lo0)
+    float win = 0.0f;             // widest first-angle interval (hi0 - lo0), plus a margin
 };
 
 namespace ebsd {
 namespace {
 
 constexpr int kWarps = 8;
+constexpr int kList = 96;  // matches of one band triplet held for sorting into library order
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kRadeg = 57.29577951308232;  // 180 / pi
 constexpr float kRadegF = 57.29577951308232f;
@@ -62,7 +67,8 @@ struct VoteArgs {
     const int32_t* famcnt;
     const int32_t* famidx;
     const float* cand;
-    float par;
+    const int32_t* orig;
+    float par, win;
     int nfam, ntrip, npoles, nb;
     float tol_f;
     double tol;
@@ -172,18 +178,36 @@ __host__ __device__ inline size_t align8(size_t words) { return (words + 1) & ~s
 
 // 4-byte words of one warp's region
 __host__ __device__ inline size_t warp_words(int nb, int nfam) {
-    size_t w = 3 * nb + nb + nb * nb + 2 * nfam * nb + nb + nb + 64;
+    size_t w = 3 * nb + nb + nb * nb + 2 * nfam * nb + nb + nb + 64 + kList;
     w = align8(w);
-    return w + 2 * 7 * size_t(nb);  // float64 QUEST scratch: weights, normals, poles
+    return w + 2 * (7 * size_t(nb) + 12);  // float64 QUEST scratch: weights, normals, poles, B and z
 }
 
 __host__ __device__ inline size_t block_words(int ntrip, int npoles) {
     return align8(6 * size_t(ntrip) + ntrip + 3 * size_t(npoles) + npoles);
 }
 
+// Warp-cooperative search on a monotone predicate (true for a leading run of [0, n), then
+// false): the length of the run.  32-way: each round samples 32 evenly spaced indices.
+template <class P>
+__device__ __forceinline__ int warp_count_leading(int n, int lane, P pred) {
+    int lo = 0, hi = n;  // the answer lies in [lo, hi]
+    while (hi - lo > 32) {
+        const int step = (hi - lo + 31) / 32;
+        const int idx = lo + lane * step;
+        const int c = __popc(__ballot_sync(kFull, idx < hi && pred(idx)));
+        if (c == 0) return lo;
+        const int nlo = lo + (c - 1) * step + 1;
+        hi = min(hi, lo + c * step);
+        lo = nlo;
+    }
+    const int idx = lo + lane;
+    return lo + __popc(__ballot_sync(kFull, idx < hi && pred(idx)));
+}
+
 // ---------------------------------------------------------------------------------------
 __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const float* s_iv,
-                              const uint32_t* s_tfam, const float* s_pole, const int* s_pfam,
+                              const int* s_orig, const float* s_pole, const int* s_pfam,
                               float* w) {
     const int nb = A.nb, nfam = A.nfam, ntrip = A.ntrip, npoles = A.npoles;
     const float tolf = A.tol_f;
@@ -195,7 +219,8 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     int* rarg = (int*)(accn + nfam * nb);  // [nb] band order, ascending rank
     int* bfam = rarg + nb;               // [nb]
     float* fscr = (float*)(bfam + nb);   // [64]
-    double* dscr = (double*)(w + align8(3 * nb + nb + nb * nb + 2 * nfam * nb + nb + nb + 64));
+    int* mlist = (int*)(fscr + 64);      // [kList]
+    double* dscr = (double*)(w + align8(3 * nb + nb + nb * nb + 2 * nfam * nb + nb + nb + 64 + kList));
     const unsigned lt_mask = (1u << lane) - 1u;
 
     for (int t = lane; t < 3 * nb; t += 32) bn[t] = A.norms[p * 3 * nb + t];
@@ -239,44 +264,78 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
                 const bool e1 = fabsf(__fsub_rn(a0, a1)) < tolf;
                 const bool e2 = fabsf(__fsub_rn(a1, a2)) < tolf;
                 const bool e3 = fabsf(__fsub_rn(a2, a0)) < tolf;
-                for (int base = 0; base < ntrip; base += 32) {
-                    const int q = base + lane;
-                    bool hit = false;
-                    if (q < ntrip) {
-                        hit = a0 >= s_iv[q] && a0 <= s_iv[ntrip + q] && a1 >= s_iv[2 * ntrip + q] &&
-                              a1 <= s_iv[3 * ntrip + q] && a2 >= s_iv[4 * ntrip + q] && a2 <= s_iv[5 * ntrip + q];
+                // library entries whose first-angle interval can hold a0: sorted by its lower
+                // end, so [s, e) with lo0 in [a0 - win, a0]
+                const float tgt = a0 - A.win;
+                const int e = warp_count_leading(ntrip, lane, [&](int q) { return s_iv[q] <= a0; });
+                const int s = warp_count_leading(e, lane, [&](int q) { return s_iv[q] < tgt; });
+                auto test = [&](int q) {
+                    return a0 >= s_iv[q] && a0 <= s_iv[ntrip + q] && a1 >= s_iv[2 * ntrip + q] &&
+                           a1 <= s_iv[3 * ntrip + q] && a2 >= s_iv[4 * ntrip + q] && a2 <= s_iv[5 * ntrip + q];
+                };
+                // one match, in the reference's library order (lane 0 applies them all)
+                auto apply = [&](int q) {
+                    const double* T = A.tang + 3 * (size_t)q;
+                    const float t0 = __double2float_rn(fabs(__dsub_rn(T[0], (double)a0)));
+                    const float t1 = __double2float_rn(fabs(__dsub_rn(T[1], (double)a1)));
+                    const float t2 = __double2float_rn(fabs(__dsub_rn(T[2], (double)a2)));
+                    const uint32_t fw = A.tfam[q];
+                    const int fq[3] = {int(fw & 255u), int((fw >> 8) & 255u), int((fw >> 16) & 255u)};
+                    const int f0 = fq[u0], f1 = fq[u1], f2 = fq[u2];
+                    const float w1 = __fsub_rn(tolf, __fmul_rn(0.5f, __fadd_rn(t0, t1)));
+                    const float w2 = __fsub_rn(tolf, __fmul_rn(0.5f, __fadd_rn(t0, t2)));
+                    const float w3 = __fsub_rn(tolf, __fmul_rn(0.5f, __fadd_rn(t1, t2)));
+                    auto vote = [&](int f, int b, float wt) {
+                        accw[f * nb + b] = __fadd_rn(accw[f * nb + b], wt);
+                        accn[f * nb + b] = __fadd_rn(accn[f * nb + b], 1.0f);
+                    };
+                    vote(f0, i, w1); vote(f1, j, w2); vote(f2, k, w3);
+                    if (e1) { vote(f0, j, w1); vote(f1, i, w2); vote(f2, k, w3); }
+                    if (e2) { vote(f0, i, w1); vote(f1, k, w2); vote(f2, j, w3); }
+                    if (e3) { vote(f0, k, w1); vote(f1, j, w2); vote(f2, i, w3); }
+                    if (e1 && e2 && e3) {
+                        vote(f0, k, w1); vote(f1, i, w2); vote(f2, j, w3);
+                        vote(f0, j, w1); vote(f1, k, w2); vote(f2, i, w3);
                     }
-                    unsigned m = __ballot_sync(kFull, hit);
-                    while (m) {
-                        const int src = __ffs(m) - 1;
-                        m &= m - 1;
-                        if (lane == src) {
-                            const double* T = A.tang + 3 * (size_t)q;
-                            const float t0 = __double2float_rn(fabs(__dsub_rn(T[0], (double)a0)));
-                            const float t1 = __double2float_rn(fabs(__dsub_rn(T[1], (double)a1)));
-                            const float t2 = __double2float_rn(fabs(__dsub_rn(T[2], (double)a2)));
-                            const uint32_t fw = s_tfam[q];
-                            const int fq[3] = {int(fw & 255u), int((fw >> 8) & 255u), int((fw >> 16) & 255u)};
-                            const int f0 = fq[u0], f1 = fq[u1], f2 = fq[u2];
-                            const float w1 = __fsub_rn(tolf, __fmul_rn(0.5f, __fadd_rn(t0, t1)));
-                            const float w2 = __fsub_rn(tolf, __fmul_rn(0.5f, __fadd_rn(t0, t2)));
-                            const float w3 = __fsub_rn(tolf, __fmul_rn(0.5f, __fadd_rn(t1, t2)));
-                            auto vote = [&](int f, int b, float wt) {
-                                accw[f * nb + b] = __fadd_rn(accw[f * nb + b], wt);
-                                accn[f * nb + b] = __fadd_rn(accn[f * nb + b], 1.0f);
-                            };
-                            vote(f0, i, w1); vote(f1, j, w2); vote(f2, k, w3);
-                            if (e1) { vote(f0, j, w1); vote(f1, i, w2); vote(f2, k, w3); }
-                            if (e2) { vote(f0, i, w1); vote(f1, k, w2); vote(f2, j, w3); }
-                            if (e3) { vote(f0, k, w1); vote(f1, j, w2); vote(f2, i, w3); }
-                            if (e1 && e2 && e3) {
-                                vote(f0, k, w1); vote(f1, i, w2); vote(f2, j, w3);
-                                vote(f0, j, w1); vote(f1, k, w2); vote(f2, i, w3);
+                };
+                int cnt = 0;
+                for (int base = s; base < e; base += 32) {
+                    const int q = base + lane;
+                    const bool hit = q < e && test(q);
+                    const unsigned m = __ballot_sync(kFull, hit);
+                    if (hit && cnt + __popc(m & lt_mask) < kList) mlist[cnt + __popc(m & lt_mask)] = s_orig[q];
+                    cnt += __popc(m);
+                }
+                __syncwarp();
+                if (cnt <= kList) {
+                    if (lane == 0) {
+                        for (int a = 1; a < cnt; ++a) {  // insertion sort into library order
+                            const int v = mlist[a];
+                            int b = a - 1;
+                            while (b >= 0 && mlist[b] > v) {
+                                mlist[b + 1] = mlist[b];
+                                --b;
                             }
+                            mlist[b + 1] = v;
                         }
+                        for (int a = 0; a < cnt; ++a) apply(mlist[a]);
+                    }
+                } else {
+                    // more matches than the list holds: take them one at a time, smallest
+                    // library index above the last one applied
+                    int last = -1;
+                    while (true) {
+                        int mine = INT_MAX;
+                        for (int q = s + lane; q < e; q += 32)
+                            if (test(q) && s_orig[q] > last && s_orig[q] < mine) mine = s_orig[q];
+                        const int next = __reduce_min_sync(kFull, mine);
+                        if (next == INT_MAX) break;
+                        if (lane == 0) apply(next);
+                        last = next;
                         __syncwarp();
                     }
                 }
+                __syncwarp();
             }
         }
     }
@@ -484,31 +543,40 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
                 }
             }
             __syncwarp();
-            if (lane == 0) {
-                const double ws = np_sum(wq, m);
-                for (int k = 0; k < m; ++k) wq[k] = __ddiv_rn(wq[k], ws);
-                double Bm[3][3];
-                for (int r = 0; r < 3; ++r)
-                    for (int c = 0; c < 3; ++c) {
-                        double acc = __dmul_rn(__dmul_rn(wq[0], bq[r]), pq[c]);
-                        for (int k = 1; k < m; ++k) acc = __fma_rn(__dmul_rn(wq[k], bq[3 * k + r]), pq[3 * k + c], acc);
-                        Bm[r][c] = acc;
-                    }
-                double S[3][3];
-                for (int r = 0; r < 3; ++r)
-                    for (int c = 0; c < 3; ++c) S[r][c] = __dadd_rn(Bm[r][c], Bm[c][r]);
-                double z[3] = {0.0, 0.0, 0.0};
+            double ws = 0.0;
+            if (lane == 0) ws = np_sum(wq, m);
+            ws = __shfl_sync(kFull, ws, 0);
+            if (lane < m) wq[lane] = __ddiv_rn(wq[lane], ws);
+            __syncwarp();
+            // B = (w b)^T p (lanes 0-8, one entry each) and z = sum_k w_k (b_k x p_k) (lanes
+            // 9-11, one component each), every entry in the reference's operation order
+            double* qs = dscr + 7 * nb;  // [12] B row-major, then z
+            if (lane < 9) {
+                const int r = lane / 3, c = lane - 3 * (lane / 3);
+                double acc = __dmul_rn(__dmul_rn(wq[0], bq[r]), pq[c]);
+                for (int k = 1; k < m; ++k) acc = __fma_rn(__dmul_rn(wq[k], bq[3 * k + r]), pq[3 * k + c], acc);
+                qs[lane] = acc;
+            } else if (lane < 12) {
+                const int c = lane - 9, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                double zc = 0.0;
                 for (int k = 0; k < m; ++k) {
                     const double* a = bq + 3 * k;
                     const double* b = pq + 3 * k;
-                    const double cr[3] = {__dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1])),
-                                          __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2])),
-                                          __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]))};
-                    for (int c = 0; c < 3; ++c) {
-                        const double v = __dmul_rn(wq[k], cr[c]);
-                        z[c] = k == 0 ? v : __dadd_rn(z[c], v);
-                    }
+                    const double cr = __dsub_rn(__dmul_rn(a[c1], b[c2]), __dmul_rn(a[c2], b[c1]));
+                    const double v = __dmul_rn(wq[k], cr);
+                    zc = k == 0 ? v : __dadd_rn(zc, v);
                 }
+                qs[lane] = zc;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                double Bm[3][3];
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) Bm[r][c] = qs[3 * r + c];
+                double S[3][3];
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) S[r][c] = __dadd_rn(Bm[r][c], Bm[c][r]);
+                const double z[3] = {qs[9], qs[10], qs[11]};
                 double S2[3][3];
                 for (int r = 0; r < 3; ++r)
                     for (int c = 0; c < 3; ++c)
@@ -561,24 +629,29 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
                 if (gamma < 0.0) {
                     for (int t = 0; t < 4; ++t) qout[t] = -qout[t];
                 }
-                // rotate each band normal by the quaternion (rotlib.quat_vectorL1N, p = 1) and
-                // compare with its pole
-                for (int k = 0; k < m; ++k) {
-                    const double* vv = bq + 3 * k;
-                    const double* pp = pq + 3 * k;
-                    const double w0 = qout[0], r0 = qout[1], r1 = qout[2], r2 = qout[3];
-                    double t[3] = {__dsub_rn(__dmul_rn(r1, vv[2]), __dmul_rn(r2, vv[1])),
-                                   __dsub_rn(__dmul_rn(r2, vv[0]), __dmul_rn(r0, vv[2])),
-                                   __dsub_rn(__dmul_rn(r0, vv[1]), __dmul_rn(r1, vv[0]))};
-                    for (int cc = 0; cc < 3; ++cc) t[cc] = __dadd_rn(t[cc], __dmul_rn(w0, vv[cc]));
-                    const double t2[3] = {__dsub_rn(__dmul_rn(r1, t[2]), __dmul_rn(r2, t[1])),
-                                          __dsub_rn(__dmul_rn(r2, t[0]), __dmul_rn(r0, t[2])),
-                                          __dsub_rn(__dmul_rn(r0, t[1]), __dmul_rn(r1, t[0]))};
-                    double s = 0.0;
-                    for (int cc = 0; cc < 3; ++cc)
-                        s = __dadd_rn(s, __dmul_rn(__dadd_rn(__dmul_rn(2.0, t2[cc]), vv[cc]), pp[cc]));
-                    wq[k] = s;  // weights are no longer needed: reuse for the per-band dot products
-                }
+                for (int t = 0; t < 4; ++t) qs[t] = qout[t];
+            }
+            __syncwarp();
+            // rotate each band normal by the quaternion (rotlib.quat_vectorL1N, p = 1) and take
+            // its dot product with the pole (one band per lane)
+            if (lane < m) {
+                const double* vv = bq + 3 * lane;
+                const double* pp = pq + 3 * lane;
+                const double w0 = qs[0], r0 = qs[1], r1 = qs[2], r2 = qs[3];
+                double t[3] = {__dsub_rn(__dmul_rn(r1, vv[2]), __dmul_rn(r2, vv[1])),
+                               __dsub_rn(__dmul_rn(r2, vv[0]), __dmul_rn(r0, vv[2])),
+                               __dsub_rn(__dmul_rn(r0, vv[1]), __dmul_rn(r1, vv[0]))};
+                for (int cc = 0; cc < 3; ++cc) t[cc] = __dadd_rn(t[cc], __dmul_rn(w0, vv[cc]));
+                const double t2[3] = {__dsub_rn(__dmul_rn(r1, t[2]), __dmul_rn(r2, t[1])),
+                                      __dsub_rn(__dmul_rn(r2, t[0]), __dmul_rn(r0, t[2])),
+                                      __dsub_rn(__dmul_rn(r0, t[1]), __dmul_rn(r1, t[0]))};
+                double sd = 0.0;
+                for (int cc = 0; cc < 3; ++cc)
+                    sd = __dadd_rn(sd, __dmul_rn(__dadd_rn(__dmul_rn(2.0, t2[cc]), vv[cc]), pp[cc]));
+                wq[lane] = sd;  // weights are no longer needed
+            }
+            __syncwarp();
+            if (lane == 0) {
                 mad = __ddiv_rn(np_sum(wq, m), (double)m);
             }
             __syncwarp();
@@ -690,14 +763,14 @@ __global__ void k_vote_thresholds(const double* __restrict__ angtab, const int32
     }
 }
 
-__global__ void __launch_bounds__(kWarps * 32) k_band_index(VoteArgs A) {
+__global__ void __launch_bounds__(kWarps * 32, 3) k_band_index(VoteArgs A) {
     extern __shared__ __align__(16) float vsm[];
     float* s_iv = vsm;
-    uint32_t* s_tfam = (uint32_t*)(s_iv + 6 * A.ntrip);
-    float* s_pole = (float*)(s_tfam + A.ntrip);
+    int* s_orig = (int*)(s_iv + 6 * A.ntrip);
+    float* s_pole = (float*)(s_orig + A.ntrip);
     int* s_pfam = (int*)(s_pole + 3 * A.npoles);
     for (int t = threadIdx.x; t < 6 * A.ntrip; t += blockDim.x) s_iv[t] = A.iv[t];
-    for (int t = threadIdx.x; t < A.ntrip; t += blockDim.x) s_tfam[t] = A.tfam[t];
+    for (int t = threadIdx.x; t < A.ntrip; t += blockDim.x) s_orig[t] = A.orig[t];
     for (int t = threadIdx.x; t < 3 * A.npoles; t += blockDim.x) s_pole[t] = A.pole[t];
     for (int t = threadIdx.x; t < A.npoles; t += blockDim.x) s_pfam[t] = A.pfam[t];
     __syncthreads();
@@ -705,7 +778,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_band_index(VoteArgs A) {
     float* w = vsm + block_words(A.ntrip, A.npoles) + warp * warp_words(A.nb, A.nfam);
     const int64_t stride = (int64_t)gridDim.x * kWarps;
     for (int64_t p = (int64_t)blockIdx.x * kWarps + warp; p < A.n; p += stride)
-        index_pattern(A, p, lane, s_iv, s_tfam, s_pole, s_pfam, w);
+        index_pattern(A, p, lane, s_iv, s_orig, s_pole, s_pfam, w);
 }
 
 // ---- band weights and pattern quality, _ebsd_index_single.py:751-763 ----
@@ -815,14 +888,27 @@ extern "C" int ebsd_vote_plan_create(const ebsd_triplib_desc* d, int device, ebs
                 for (int r = 0; r < 3; ++r) code |= int(d->lut[((r * 3 + s0) * 3 + s1) * 3 + s2]) << (2 * r);
                 p->lut[s0 * 9 + s1 * 3 + s2] = (uint8_t)code;
             }
-    std::vector<float> iv(6 * (size_t)nt);
+    std::vector<float> iv0(6 * (size_t)nt);
     std::vector<uint32_t> tf(nt);
     for (int q = 0; q < nt; ++q) {
         for (int c = 0; c < 3; ++c)
-            accept_interval(d->trip_angles[3 * q + c], d->ang_tol, &iv[(2 * c) * nt + q], &iv[(2 * c + 1) * nt + q]);
+            accept_interval(d->trip_angles[3 * q + c], d->ang_tol, &iv0[(2 * c) * nt + q], &iv0[(2 * c + 1) * nt + q]);
         tf[q] = uint32_t(d->trip_family[3 * q]) | uint32_t(d->trip_family[3 * q + 1]) << 8 |
                 uint32_t(d->trip_family[3 * q + 2]) << 16;
     }
+    // interval rows sorted by the lower end of the first angle's interval (library order kept
+    // in d_orig), so that a band triplet scans only the rows whose first interval can hold it
+    std::vector<int32_t> order(nt);
+    for (int q = 0; q < nt; ++q) order[q] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return iv0[a] < iv0[b]; });
+    std::vector<float> iv(6 * (size_t)nt);
+    double wmax = 0.0;
+    for (int r = 0; r < nt; ++r) {
+        const int q = order[r];
+        for (int c = 0; c < 6; ++c) iv[(size_t)c * nt + r] = iv0[(size_t)c * nt + q];
+        if (iv0[q] <= iv0[nt + q]) wmax = std::max(wmax, (double)iv0[nt + q] - (double)iv0[q]);
+    }
+    p->win = (float)(wmax + 1e-3);
     std::vector<float> pole(3 * (size_t)np_);
     for (int i = 0; i < np_; ++i)
         for (int c = 0; c < 3; ++c) pole[c * np_ + i] = (float)d->poles_cart[3 * i + c];
@@ -844,6 +930,7 @@ extern "C" int ebsd_vote_plan_create(const ebsd_triplib_desc* d, int device, ebs
     if (!rc) rc = up((void**)&p->d_angtab, d->ang_table, (size_t)np_ * np_ * 8);
     if (!rc) rc = up((void**)&p->d_famcnt, d->fam_count, (size_t)nf * 4);
     if (!rc) rc = up((void**)&p->d_famidx, fidx.data(), (size_t)nf * 4);
+    if (!rc) rc = up((void**)&p->d_orig, order.data(), (size_t)nt * 4);
     if (!rc && cudaMalloc((void**)&p->d_cand, (size_t)nf * np_ * 2 * 4) != cudaSuccess) rc = EBSD_E_NOMEM;
     if (!rc && cudaMalloc((void**)&p->d_par, 4) != cudaSuccess) rc = EBSD_E_NOMEM;
     if (!rc) {
@@ -875,6 +962,7 @@ extern "C" int ebsd_vote_plan_destroy(ebsd_vote_plan_t p) {
     cudaFree(p->d_famidx);
     cudaFree(p->d_cand);
     cudaFree(p->d_par);
+    cudaFree(p->d_orig);
     delete p;
     return EBSD_OK;
 }
@@ -909,6 +997,8 @@ extern "C" int ebsd_band_index(ebsd_vote_plan_t p, const float* d_norms, const f
     A.famidx = p->d_famidx;
     A.cand = p->d_cand;
     A.par = p->par;
+    A.orig = p->d_orig;
+    A.win = p->win;
     A.nfam = p->nfam;
     A.ntrip = p->ntrip;
     A.npoles = p->npoles;
