@@ -9,7 +9,7 @@
 // works on float32 arrays (band angles, votes, the TRIAD fit), float64 for the QUEST fit, every
 // add/multiply rounded on its own (no contraction), 3-term dot products as the fused
 // multiply-add chain BLAS uses for these shapes, sums in numpy's pairwise order.  arccos is
-// the correctly rounded float32 value (acos in float64, rounded once).
+// CUDA's float32 acosf (within two ulp, as numpy's own float32 arccos is).
 //
 // Two steps are reorganised for the GPU without changing their result:
 //   * the vote's library test |T - a| <= angTol (float64, T a library angle, a a float32 band
@@ -144,10 +144,11 @@ __device__ __forceinline__ float norm3(const float* a) {
     return __fsqrt_rn(dot3(a[0], a[1], a[2], a[0], a[1], a[2]));
 }
 
-// float32 arccos(x) * RADEG, the arccos correctly rounded (float64 arccos, rounded once); kept
-// out of line: the float64 arccos is long and the kernel is instruction-cache bound
-__device__ __noinline__ float acos_deg(float x) {
-    return __fmul_rn(__double2float_rn(acos((double)x)), kRadegF);
+// float32 arccos(x) * RADEG.  The reference's float32 arccos is numpy's (SIMD, not correctly
+// rounded: one or two ulp off for about a third of the inputs on x86); CUDA's acosf is within
+// two ulp as well, so either may sit an ulp or two from the reference's value.
+__device__ __forceinline__ float acos_deg(float x) {
+    return __fmul_rn(acosf(x), kRadegF);
 }
 
 __device__ __forceinline__ void sort3(const float* v, int& s0, int& s1, int& s2) {
