@@ -67,3 +67,49 @@ def test_plan_without_device_raises(built_lib):
     phase, _ = fake_phase()
     with pytest.raises(RuntimeError, match="CUDA device"):
         tv.BandIndexer(phase).plan()
+
+
+def test_wrapped_phases_drive_the_reference_indexer(monkeypatch):
+    """The reference's own EBSDIndexer._indexbandsphase (_ebsd_index_single.py:720-830) runs
+    with its phases wrapped; the wrapper's device call is stood in for by the oracle (no GPU
+    here), so the indexer's outputs must equal the unwrapped run's."""
+    import json
+    import warnings
+    from oracle import refshim
+    if not refshim.reference_available():
+        pytest.skip("reference source tree not available")
+    from pyebsdindex_gb300 import tripletvote as tv
+    from pyebsdindex_gb300 import synthetic as syn
+    ref = refshim.load()
+    d = np.load(os.path.join(GOLDEN_DIR, "orient_80x80.npz"))
+    params = json.loads(str(d["params"]))
+    pc = tuple(float(x) for x in d["pc"])
+
+    def make():
+        idx = ref.ebsd_index_single.EBSDIndexer(PC=pc, patDim=(80, 80), **params)
+        idx.bandDetectPlan.band_detect_setup(patDim=(80, 80), patternmask=syn.circular_mask(80, 80))
+        return idx
+
+    n = 24
+    idx = make()
+    recs = np.zeros((n, 9), dtype=idx.bandDetectPlan.dataType)
+    for f in ("max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
+        recs[f] = d["ref_" + f][:n]
+    norms = idx.bandDetectPlan.radonPlan.radon2pole(recs, PC=np.asarray(pc), vendor="EDAX")
+    with warnings.catch_warnings(), np.errstate(all="ignore"):
+        warnings.simplefilter("ignore")
+        want, _ = idx._indexbandsphase(recs, norms)
+
+    def oracle_bandindex(self, band_norms, band_intensity=None, band_widths=None, verbose=0):
+        p = {"angTol": self.angTol, "nband_earlyexit": self.nband_earlyexit, "simpleqweights": self.simpleqweights}
+        return vo.bandindex(tv.phase_library(self._phase), p, np.asarray(band_norms, np.float32),
+                            np.asarray(band_intensity, np.float32))[0]
+
+    monkeypatch.setattr(tv.BandIndexer, "bandindex", oracle_bandindex)
+    idx2 = make()
+    idx2.phaseLib = [tv.BandIndexer(ph) for ph in idx2.phaseLib]
+    with warnings.catch_warnings(), np.errstate(all="ignore"):
+        warnings.simplefilter("ignore")
+        got, _ = idx2._indexbandsphase(recs, norms)
+    for f in ("quat", "fit", "cm", "nmatch", "phase", "pq", "iq"):
+        assert np.array_equal(got[f], want[f]), f
