@@ -165,6 +165,26 @@ int ebsd_nlpar_sigma(const float* d_data, int32_t nrows, int32_t ncols, int32_t 
                      const int32_t* d_indices, int32_t nind, float datamax, int saturation_protect,
                      float* d_sigma, void* stream);
 
+/* One scan tile of NLPAR's sigma estimate for the lambda optimisation (NLPAR.calcsigma_cpu,
+ * nlpar_cpu.py:157-264, which runs sigma_numba per tile with nn = 1 as uint64: the tile's first
+ * row and column get empty windows).  Tile = rows [r0, r1) x columns [c0, c1) of the scan;
+ * datamax is the tile's own maximum (computed here).  Merges into the scan arrays: d_sigma
+ * [nrows*ncols] = min(d_sigma, tile sigma); d_d2 / d_n2 [nrows*ncols][9] (normalised distance
+ * and pixel count per window slot, nlpar_cpu.py:805-817) replaced where the tile's count is
+ * positive.  Initialise d_sigma to 1e18 and d_d2, d_n2 to 0, then call once per tile in
+ * NLPAR._calcchunks order (nlpar_cpu.py:973-1065).  d_work: (r1-r0)*(c1-c0)*19 + 1 floats. */
+int ebsd_nlpar_sigma_tile(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, int32_t r0,
+                          int32_t r1, int32_t c0, int32_t c1, const int32_t* d_indices, int32_t nind,
+                          int saturation_protect, float* d_sigma, float* d_d2, float* d_n2,
+                          float* d_work, void* stream);
+
+/* The lambda objective of NLPAR.opt_lambda_cpu (nlpar_cpu.py:107-113): mean over scan pixels
+ * (rows and columns stepped by `stride`) of |tw - 1 / (sum_q exp(-max(d2_q, dthresh) / lam^2)
+ * + 1e-12)|, in float64, into *d_out (device).  d_work: 256 doubles.  Deterministic. */
+int ebsd_nlpar_lambda_metric(const float* d_d2, int32_t nrows, int32_t ncols, int32_t stride,
+                             float dthresh, double lam, double tw, double* d_work, double* d_out,
+                             void* stream);
+
 /* NLPAR weighted neighbour average (NLPAR.nlpar_nb, nlpar_cpu.py:821-936) over a
  * (2 sr + 1)^2 search window (0 <= sr <= 10, shifted inward at the scan edges): d_out
  * [nrows*ncols][npx] float32.  d_work: caller-provided device scratch of

@@ -120,3 +120,130 @@ def nlpar(data, lam, sr, dthresh, sig, nrows, ncols, indices, saturation_protect
     for c in range(winsz):
         out = (out + (data[nbr[:, c]] * w[:, c:c + 1]).astype(np.float32)).astype(np.float32)
     return out
+
+
+# ---------------------------------------------------------------------------------------
+# lambda optimisation: NLPAR.opt_lambda_cpu (nlpar_cpu.py:94-155) with calcsigma_cpu
+# (nlpar_cpu.py:157-264) and _calcchunks (nlpar_cpu.py:973-1065)
+# ---------------------------------------------------------------------------------------
+def calcchunks(patdim, ncol, nrow, target_bytes, col_overlap=0, row_overlap=0):
+    """Scan tiling of NLPAR._calcchunks (nlpar_cpu.py:973-1065): (column chunks, row chunks),
+    each an int array [n, 2] of [start, end)."""
+    col_overlap = min(col_overlap, ncol - 1)
+    row_overlap = min(row_overlap, nrow - 1)
+    mincol = 2 if ncol >= nrow else 1
+    minrow = 2 if nrow > ncol else 1
+    nbytes = patdim[-1] * patdim[-2] * 4 * 2 * ncol * nrow
+    nchunks = int(np.ceil(nbytes / target_bytes))
+
+    def axis(n, nch, overlap):
+        step = max(n / nch, 1)
+        nch = max(int(np.ceil(max(n / step, 1))), 1)
+        step = max(int(np.round(step)), 1)
+        stepov = min(step + 2 * overlap, n)
+        out = []
+        for c in range(nch):
+            ch = [int(c * step) - int(overlap), int(c * step + stepov) - int(overlap)]
+            out.append(ch)
+            if ch[1] > n:
+                break
+        out = np.array(out, dtype=int)
+        out[0, 0] = 0
+        out[-1, 1] = n
+        if len(out) > 1:
+            out[-1, 0] = max(0, out[-2, 1] - 2 * int(overlap) - 1)
+        return out, nch
+
+    cols, ncol_chunks = axis(ncol, max(np.round(np.sqrt(nchunks * float(ncol) / nrow)), mincol), col_overlap)
+    # the row count uses the column count before the column loop's early stop (nlpar_cpu.py:994)
+    rows, _ = axis(nrow, max(np.ceil(nchunks / ncol_chunks), minrow), row_overlap)
+    return cols, rows
+
+
+def sigma_distances_chunk(data, nrows, ncols, indices, saturation_protect=True):
+    """NLPAR.sigma_numba (nlpar_cpu.py:753-818) as calcsigma_cpu calls it, with nn and the
+    row/column start-count arrays as uint64: ``j - nn`` wraps for the chunk's first row and
+    column, whose windows are then empty (sigma sqrt(1e24), no distances).  Returns sigma
+    [nrows, ncols] and the normalised distances / counts [nrows, ncols, 9] (numpy's float32
+    scalar arithmetic for the normalisation, as the reference source evaluates under numpy)."""
+    data = np.asarray(data, dtype=np.float32)
+    n0 = f32(data.shape[-1])
+    mxval = np.max(data)
+    mxval = f32(mxval + 1.0) if not saturation_protect else f32(mxval * 0.9961)
+    mind = np.full((nrows, ncols), 1e24, dtype=np.float32)
+    dout = np.zeros((nrows, ncols, 9), np.float32)
+    nout = np.zeros((nrows, ncols, 9), np.float32)
+    nbr = np.full((nrows, ncols, 9, 2), -1, np.int64)
+    jj, ii = np.mgrid[0:nrows, 0:ncols]
+    live = (jj >= 1) & (ii >= 1)
+    cstart = np.where(live, ii - 1, 0)
+    cend = np.minimum(ii + 1, ncols - 1) + 1
+    rstart = np.where(live, jj - 1, 0)
+    width = cend - cstart
+    for dj in (-1, 0, 1):
+        for di in (-1, 0, 1):
+            jn, inn = jj + dj, ii + di
+            ok = live & (jn < nrows) & (inn < ncols)
+            slot = (jn - rstart) * width + (inn - cstart)
+            sj, si = jj[ok], ii[ok]
+            sl = slot[ok]
+            nbr[sj, si, sl, 0] = jn[ok]
+            nbr[sj, si, sl, 1] = inn[ok]
+            if dj == 0 and di == 0:
+                nout[sj, si, sl] = n0
+                continue
+            d2, n2 = _pair_ssd(data, (ii + ncols * jj)[ok], (inn + ncols * jn)[ok], indices, mxval, f32(1.0e-12))
+            nout[sj, si, sl] = n2
+            dout[sj, si, sl] = d2
+            s0 = (d2 / (n2 * f32(2.0)).astype(np.float32)).astype(np.float32)
+            cand = np.where(d2 >= 1.e-3, s0, f32(1e24))
+            mind[sj, si] = np.minimum(mind[sj, si], cand)
+    sig = np.sqrt(mind).astype(np.float32)
+    s2 = sig ** 2
+    for j in range(nrows):
+        for i in range(ncols):
+            for q in range(9):
+                if nout[j, i, q] > 0:
+                    s12 = s2[j, i] + s2[nbr[j, i, q, 0], nbr[j, i, q, 1]]
+                    dout[j, i, q] -= nout[j, i, q] * s12
+                    dout[j, i, q] /= s12 * np.sqrt(2.0 * nout[j, i, q])
+    return sig, dout, nout
+
+
+def calcsigma_chunked(data, nrows, ncols, h, w, indices, saturation_protect, target_bytes):
+    """calcsigma_cpu's tile loop (nlpar_cpu.py:205-262): sigma is the minimum over tiles; a
+    tile's distances replace earlier ones where its counts are positive."""
+    cols, rows = calcchunks([w, h], ncols, nrows, target_bytes, col_overlap=1, row_overlap=1)
+    grid = np.asarray(data, np.float32).reshape(nrows, ncols, -1)
+    sigma = np.zeros((nrows, ncols), np.float32) + 1e18
+    n2 = np.zeros((nrows, ncols, 9), np.float32)
+    d2 = np.zeros((nrows, ncols, 9), np.float32)
+    for r0, r1 in rows:
+        for c0, c1 in cols:
+            chunk = grid[r0:r1, c0:c1].reshape((r1 - r0) * (c1 - c0), -1)
+            sc, dc, nc = sigma_distances_chunk(chunk, r1 - r0, c1 - c0, indices, saturation_protect)
+            sigma[r0:r1, c0:c1] = np.minimum(sigma[r0:r1, c0:c1], sc)
+            n2[r0:r1, c0:c1] = np.select([nc > 0], [nc], default=n2[r0:r1, c0:c1])
+            d2[r0:r1, c0:c1] = np.select([nc > 0], [dc], default=d2[r0:r1, c0:c1])
+    return sigma, d2, n2
+
+
+def lambda_metric(lam, d2, tw, dthresh):
+    """The objective of opt_lambda_cpu (nlpar_cpu.py:107-113)."""
+    temp = np.maximum(d2, dthresh)
+    dw = np.exp(-(temp) / lam ** 2)
+    w = np.sum(dw, axis=2) + 1e-12
+    return np.mean(np.abs(tw - 1.0 / w))
+
+
+def opt_lambda(d2, sigma_size, target_weights=(0.5, 0.34, 0.25), dthresh=0.0):
+    """Bounded Nelder-Mead per target weight from lambda = 1 (nlpar_cpu.py:139-150)."""
+    import scipy.optimize as opt
+    dthresh = np.float32(dthresh)
+    stride = 1 if sigma_size < 1e6 else 2
+    out = []
+    for tw in np.asarray(target_weights):
+        r = opt.minimize(lambda_metric, 1.0, args=(d2[0::stride, 0::stride, :], tw, dthresh), method='Nelder-Mead',
+                         bounds=[[0.001, 10.0]], options={'fatol': 0.0001})
+        out.append(r['x'])
+    return np.asarray(out).flatten()

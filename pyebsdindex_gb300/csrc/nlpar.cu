@@ -296,6 +296,139 @@ size_t tiled_smem(int sr, int ncols, size_t elem, bool weights) {
     return b;
 }
 
+
+// ---- lambda optimisation (NLPAR.opt_lambda_cpu, nlpar_cpu.py:94-155) -------------------
+// calcsigma_cpu (nlpar_cpu.py:157-264) runs sigma_numba per scan tile with nn and the tile's
+// start/count arrays as uint64, so `j - nn` wraps for the tile's first row and first column:
+// those pixels get an empty window (sigma sqrt(1e24), no distances).  Every other pixel gets
+// its clipped 3x3 window in row-major slot order (centre: count = pattern length, distance 0);
+// the distances are normalised with the tile's own sigma (nlpar_cpu.py:805-817), then merged
+// into the scan: sigma = min over tiles, a slot's distance and count replaced where the tile's
+// count is positive.
+
+__device__ __forceinline__ uint32_t fmax_key(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fmax_unkey(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// largest value of the tile's patterns (np.max(data) of the tile)
+__global__ void k_tile_max(const float* __restrict__ data, int ncols, int npx, int r0, int c0, int tr, int tc,
+                           uint32_t* __restrict__ key) {
+    const int64_t total = (int64_t)tr * tc * npx;
+    float m = -INFINITY;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t pix = t / npx;
+        const int q = (int)(t - pix * npx);
+        const int j = (int)(pix / tc), i = (int)(pix - (int64_t)j * tc);
+        m = fmaxf(m, __ldg(data + ((int64_t)(r0 + j) * ncols + (c0 + i)) * npx + q));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(key, fmax_key(m));
+}
+
+// raw distances and counts per slot, and the tile sigma; 8 lanes per pixel (the neighbours)
+__global__ void k_tile_dist(const float* __restrict__ data, int ncols, int npx, int r0, int c0, int tr, int tc,
+                            const int32_t* __restrict__ ind, int nind, int satp, const uint32_t* __restrict__ key,
+                            float* __restrict__ sig_t, float* __restrict__ d2_t, float* __restrict__ n2_t) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int pix = gt >> 3, lane8 = gt & 7;
+    const float m = fmax_unkey(*key);
+    const float mxval = satp ? __fmul_rn(m, 0.9961f) : __fadd_rn(m, 1.0f);
+    float s0 = 1e24f;
+    if (pix < tr * tc) {
+        const int j = pix / tc, i = pix - (pix / tc) * tc;
+        if (j >= 1 && i >= 1) {  // the first row and column of a tile have empty windows
+            const int cstart = i - 1, cend = min(i + 1, tc - 1) + 1, width = cend - cstart;
+            const int k = lane8 < 4 ? lane8 : lane8 + 1;
+            const int jn = j + k / 3 - 1, inn = i + k % 3 - 1;
+            if (lane8 == 0) {
+                const int cslot = width + 1;  // (j - rstart) * width + (i - cstart)
+                n2_t[(int64_t)pix * 9 + cslot] = (float)npx;
+                d2_t[(int64_t)pix * 9 + cslot] = 0.0f;
+            }
+            if (jn < tr && inn < tc) {
+                const int slot = (jn - (j - 1)) * width + (inn - cstart);
+                float d2, n2;
+                pair_ssd(data + ((int64_t)(r0 + j) * ncols + (c0 + i)) * npx,
+                         data + ((int64_t)(r0 + jn) * ncols + (c0 + inn)) * npx, ind, nind, mxval, 1.0e-12f, d2, n2);
+                n2_t[(int64_t)pix * 9 + slot] = n2;
+                d2_t[(int64_t)pix * 9 + slot] = d2;
+                if (d2 >= 1.e-3f) s0 = __fdiv_rn(d2, __fmul_rn(n2, 2.0f));
+            }
+        }
+    }
+    for (int o = 4; o > 0; o >>= 1) s0 = fminf(s0, __shfl_down_sync(0xffffffffu, s0, o, 8));
+    if (lane8 == 0 && pix < tr * tc) sig_t[pix] = __fsqrt_rn(s0);
+}
+
+// normalise with the tile sigma and merge into the scan arrays (one thread per pixel and slot)
+__global__ void k_tile_merge(int ncols, int r0, int c0, int tr, int tc, const float* __restrict__ sig_t,
+                             const float* __restrict__ d2_t, const float* __restrict__ n2_t,
+                             float* __restrict__ sigma, float* __restrict__ d2, float* __restrict__ n2) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)tr * tc * 9) return;
+    const int pix = (int)(t / 9), q = (int)(t - (int64_t)pix * 9);
+    const int j = pix / tc, i = pix - (pix / tc) * tc;
+    const int64_t g = (int64_t)(r0 + j) * ncols + (c0 + i);
+    if (q == 0) sigma[g] = fminf(sigma[g], sig_t[pix]);
+    const float n = n2_t[t];
+    if (n > 0.0f) {
+        const int cstart = i - 1, cend = min(i + 1, tc - 1) + 1, width = cend - cstart;
+        const int jj = j - 1 + q / width, ii = cstart + q % width;
+        const float sa = sig_t[pix], sb = sig_t[jj * tc + ii];
+        const float s12 = __fadd_rn(__fmul_rn(sa, sa), __fmul_rn(sb, sb));
+        float v = __fsub_rn(d2_t[t], __fmul_rn(n, s12));
+        v = __fdiv_rn(v, __fmul_rn(s12, __fsqrt_rn(__fmul_rn(2.0f, n))));
+        d2[g * 9 + q] = v;
+        n2[g * 9 + q] = n;
+    }
+}
+
+// the objective mean |tw - 1 / (sum_q exp(-max(d2, dthresh) / lam^2) + 1e-12)| over the pixels
+// (rows and columns stepped by `stride`), float64; per-block sums, then one block in order
+constexpr int kLamBlocks = 256;
+
+__global__ void k_lam_partial(const float* __restrict__ d2, int nrows, int ncols, int stride, float dthresh,
+                              double lam2, double tw, double* __restrict__ part) {
+    __shared__ double red[256];
+    const int sr = (nrows + stride - 1) / stride, sc = (ncols + stride - 1) / stride;
+    const int64_t total = (int64_t)sr * sc;
+    double acc = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int a = (int)(t / sc), b = (int)(t - (int64_t)a * sc);
+        const float* v = d2 + ((int64_t)(a * stride) * ncols + b * stride) * 9;
+        double e[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const float m = fmaxf(v[q], dthresh);  // np.maximum (no NaN in the distances)
+            e[q] = exp(__ddiv_rn((double)(-m), lam2));
+        }
+        // numpy's pairwise order for nine terms
+        double w = __dadd_rn(__dadd_rn(__dadd_rn(e[0], e[1]), __dadd_rn(e[2], e[3])),
+                             __dadd_rn(__dadd_rn(e[4], e[5]), __dadd_rn(e[6], e[7])));
+        w = __dadd_rn(__dadd_rn(w, e[8]), 1e-12);
+        acc = __dadd_rn(acc, fabs(__dsub_rn(tw, __ddiv_rn(1.0, w))));
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] = __dadd_rn(red[threadIdx.x], red[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_lam_final(const double* __restrict__ part, int nparts, double count, double* __restrict__ out) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double s = 0.0;
+        for (int b = 0; b < nparts; ++b) s = __dadd_rn(s, part[b]);
+        *out = __ddiv_rn(s, count);
+    }
+}
+
 }  // namespace
 }  // namespace ebsd
 
@@ -311,6 +444,49 @@ int ebsd_nlpar_sigma(const float* d_data, int32_t nrows, int32_t ncols, int32_t 
     int64_t threads = (int64_t)nrows * ncols * 8;
     k_nlpar_sigma<<<(unsigned)((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
         d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma);
+    return launch_status();
+}
+
+int ebsd_nlpar_sigma_tile(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, int32_t r0, int32_t r1,
+                          int32_t c0, int32_t c1, const int32_t* d_indices, int32_t nind, int saturation_protect,
+                          float* d_sigma, float* d_d2, float* d_n2, float* d_work, void* stream) {
+    if (!d_data || !d_indices || !d_sigma || !d_d2 || !d_n2 || !d_work || nrows <= 0 || ncols <= 0 || npx <= 0 ||
+        nind < 0 || nind > npx)
+        return EBSD_E_ARG;
+    if (r0 < 0 || c0 < 0 || r1 > nrows || c1 > ncols || r1 <= r0 || c1 <= c0) return EBSD_E_ARG;
+    const int tr = r1 - r0, tc = c1 - c0;
+    const int64_t tp = (int64_t)tr * tc;
+    cudaStream_t st = (cudaStream_t)stream;
+    float* sig_t = d_work;
+    float* d2_t = sig_t + tp;
+    float* n2_t = d2_t + tp * 9;
+    uint32_t* key = (uint32_t*)(n2_t + tp * 9);
+    EBSD_CUDA_TRY(cudaMemsetAsync(d2_t, 0, (size_t)tp * 18 * sizeof(float) + sizeof(uint32_t), st));
+    const int64_t elems = tp * npx;
+    const int mb = (int)std::min<int64_t>((elems + 255) / 256, 152 * 8);
+    k_tile_max<<<mb, 256, 0, st>>>(d_data, ncols, npx, r0, c0, tr, tc, key);
+    int rc = launch_status();
+    if (rc != EBSD_OK) return rc;
+    const int64_t th = tp * 8;
+    k_tile_dist<<<(unsigned)((th + 255) / 256), 256, 0, st>>>(d_data, ncols, npx, r0, c0, tr, tc, d_indices, nind,
+                                                             saturation_protect, key, sig_t, d2_t, n2_t);
+    rc = launch_status();
+    if (rc != EBSD_OK) return rc;
+    const int64_t tm = tp * 9;
+    k_tile_merge<<<(unsigned)((tm + 255) / 256), 256, 0, st>>>(ncols, r0, c0, tr, tc, sig_t, d2_t, n2_t, d_sigma,
+                                                              d_d2, d_n2);
+    return launch_status();
+}
+
+int ebsd_nlpar_lambda_metric(const float* d_d2, int32_t nrows, int32_t ncols, int32_t stride, float dthresh,
+                             double lam, double tw, double* d_work, double* d_out, void* stream) {
+    if (!d_d2 || !d_work || !d_out || nrows <= 0 || ncols <= 0 || stride < 1) return EBSD_E_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t sr = (nrows + stride - 1) / stride, sc = (ncols + stride - 1) / stride;
+    k_lam_partial<<<kLamBlocks, 256, 0, st>>>(d_d2, nrows, ncols, stride, dthresh, lam * lam, tw, d_work);
+    int rc = launch_status();
+    if (rc != EBSD_OK) return rc;
+    k_lam_final<<<1, 32, 0, st>>>(d_work, kLamBlocks, (double)(sr * sc), d_out);
     return launch_status();
 }
 

@@ -21,7 +21,48 @@ import numpy as np
 
 from . import _lib
 
-__all__ = ["NLPAR"]
+__all__ = ["NLPAR", "scan_tiles"]
+
+
+def host_memory_bytes():
+    """Total host memory (what psutil.virtual_memory().total reports on Linux)."""
+    import os
+    try:
+        return int(os.sysconf("SC_PAGE_SIZE")) * int(os.sysconf("SC_PHYS_PAGES"))
+    except (ValueError, OSError, AttributeError):
+        return 64 << 30
+
+
+def scan_tiles(patdim, ncol, nrow, target_bytes, col_overlap=0, row_overlap=0):
+    """The reference's scan tiling (NLPAR._calcchunks, nlpar_cpu.py:973-1065): column and row
+    ranges [start, end) as int arrays [n, 2].  At least two column tiles when ncol >= nrow
+    (two row tiles otherwise), about target_bytes of float32 input+output per tile, tiles
+    overlapping by the given rows / columns on each side."""
+    col_overlap = min(col_overlap, ncol - 1)
+    row_overlap = min(row_overlap, nrow - 1)
+    nchunks = int(np.ceil(patdim[-1] * patdim[-2] * 8 * ncol * nrow / target_bytes))
+
+    def ranges(n, count, overlap):
+        step = max(n / count, 1)
+        count = max(int(np.ceil(max(n / step, 1))), 1)
+        step = max(int(np.round(step)), 1)
+        span = min(step + 2 * overlap, n)
+        out = []
+        for c in range(count):
+            out.append([int(c * step) - int(overlap), int(c * step + span) - int(overlap)])
+            if out[-1][1] > n:
+                break
+        out = np.array(out, dtype=int)
+        out[0, 0], out[-1, 1] = 0, n
+        if len(out) > 1:
+            out[-1, 0] = max(0, out[-2, 1] - 2 * int(overlap) - 1)
+        return out, count
+
+    cols, ncount = ranges(ncol, max(np.round(np.sqrt(nchunks * float(ncol) / nrow)), 2 if ncol >= nrow else 1),
+                          col_overlap)
+    # the row count divides by the column count before the column list stops early
+    rows, _ = ranges(nrow, max(np.ceil(nchunks / ncount), 2 if nrow > ncol else 1), row_overlap)
+    return cols, rows
 
 
 def _bind():
@@ -34,6 +75,13 @@ def _bind():
                                    C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
         lib.ebsd_nlpar.restype = C.c_int
+        lib.ebsd_nlpar_sigma_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                              C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int, C.c_void_p,
+                                              C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ebsd_nlpar_sigma_tile.restype = C.c_int
+        lib.ebsd_nlpar_lambda_metric.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_double,
+                                                 C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ebsd_nlpar_lambda_metric.restype = C.c_int
         lib._nlpar_bound = True
     return lib
 
@@ -102,6 +150,82 @@ class NLPAR:
                                         float(t.max().item()), int(bool(sp)), sig.data_ptr(), stream),
                    "ebsd_nlpar_sigma")
         return sig if is_torch else sig.cpu().numpy()
+
+    def _sigma_tiles(self, data, nrows, ncols, saturation_protect, target_bytes):
+        import torch
+        lib = _bind()
+        sp = self.saturation_protect if saturation_protect is None else saturation_protect
+        t, ind, nrows, ncols, shape, is_torch, dev = self._prepare(data, nrows, ncols)
+        h, w = shape[-2], shape[-1]
+        if target_bytes is None:
+            target_bytes = min(32e9, host_memory_bytes() // 4)
+        cols, rows = scan_tiles([w, h], ncols, nrows, target_bytes, col_overlap=1, row_overlap=1)
+        sig = torch.full((nrows, ncols), 1e18, dtype=torch.float32, device=dev)
+        d2 = torch.zeros((nrows, ncols, 9), dtype=torch.float32, device=dev)
+        n2 = torch.zeros((nrows, ncols, 9), dtype=torch.float32, device=dev)
+        tmax = max((r1 - r0) * (c1 - c0) for r0, r1 in rows for c0, c1 in cols)
+        work = torch.empty(tmax * 19 + 1, dtype=torch.float32, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        for r0, r1 in rows:
+            for c0, c1 in cols:
+                _lib.check(lib.ebsd_nlpar_sigma_tile(t.data_ptr(), nrows, ncols, t.shape[1], int(r0), int(r1), int(c0),
+                                                     int(c1), ind.data_ptr(), ind.numel(), int(bool(sp)),
+                                                     sig.data_ptr(), d2.data_ptr(), n2.data_ptr(), work.data_ptr(),
+                                                     stream), "ebsd_nlpar_sigma_tile")
+        return sig, d2, n2, is_torch
+
+    def calcsigma_tiles_array(self, data, nrows=None, ncols=None, saturation_protect=None, target_bytes=None):
+        """sigma, normalised neighbour distances d2 and counts n2 ([nrows, ncols, 9]) as
+        NLPAR.calcsigma_cpu computes them for the lambda optimisation (nlpar_cpu.py:157-264):
+        sigma_numba per scan tile (tiles from ``scan_tiles``, one row / column of overlap) with
+        the reference's uint64 window arithmetic -- each tile's first row and column get empty
+        windows -- merged tile by tile.  Device tensors for torch input, else numpy."""
+        sig, d2, n2, is_torch = self._sigma_tiles(data, nrows, ncols, saturation_protect, target_bytes)
+        if is_torch:
+            return sig, d2, n2
+        return sig.cpu().numpy(), d2.cpu().numpy(), n2.cpu().numpy()
+
+    def opt_lambda_array(self, data, nrows=None, ncols=None, target_weights=(0.5, 0.34, 0.25), autoupdate=True,
+                         dthresh=None, saturation_protect=None, target_bytes=None, verbose=0):
+        """NLPAR.opt_lambda_cpu (nlpar_cpu.py:94-155) on the device: sigma and the normalised
+        neighbour distances per scan tile (``calcsigma_tiles_array``), then, for each target
+        weight, scipy's bounded Nelder-Mead from lambda = 1 (the reference's call and options)
+        on the objective mean |tw - 1 / sum_q exp(-max(d2_q, dthresh) / lam^2)|, evaluated on
+        the device (every second row and column for scans of 1e6 pixels or more).  Sets
+        ``self.lam`` to the median when ``autoupdate``; returns the lambda values."""
+        import torch
+        import scipy.optimize as opt
+        lib = _bind()
+        if dthresh is not None:
+            self.dthresh = dthresh
+        dth = np.float32(self.dthresh if np.isscalar(self.dthresh) else self.dthresh[0])
+        sig, d2, _, _ = self._sigma_tiles(data, nrows, ncols, saturation_protect, target_bytes)
+        nr, nc = int(sig.shape[0]), int(sig.shape[1])
+        stride = 1 if nr * nc < 1e6 else 2
+        dev = d2.device
+        work = torch.empty(256, dtype=torch.float64, device=dev)
+        res = torch.empty(1, dtype=torch.float64, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+
+        def objective(lam, tw):
+            _lib.check(lib.ebsd_nlpar_lambda_metric(d2.data_ptr(), nr, nc, stride, float(dth),
+                                                    float(np.asarray(lam).ravel()[0]), float(tw), work.data_ptr(),
+                                                    res.data_ptr(), stream), "ebsd_nlpar_lambda_metric")
+            return float(res.item())
+
+        vals = []
+        for tw in np.asarray(target_weights):
+            r = opt.minimize(objective, 1.0, args=(tw,), method='Nelder-Mead', bounds=[[0.001, 10.0]],
+                             options={'fatol': 0.0001})
+            vals.append(r['x'])
+        vals = np.asarray(vals).flatten()
+        if verbose >= 2:
+            print("Range of lambda values: ", vals, "Optimal Choice: ", np.median(vals))
+        if autoupdate:
+            self.lam = np.median(vals)
+        if self.sigma is None:
+            self.sigma = sig.cpu().numpy()
+        return vals
 
     def calcnlpar_array(self, data, nrows=None, ncols=None, lam=None, searchradius=None, dthresh=None,
                         saturation_protect=None, sigma=None, reset_sigma=False):
