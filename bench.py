@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="launch directly instead of replaying a CUDA graph")
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's rule-based kernel variant")
     ap.add_argument("--no-index", action="store_true", help="skip timing the device indexing after detection")
+    ap.add_argument("--no-file", action="store_true", help="skip timing detection streamed from a UP1 file")
+    ap.add_argument("--file-patterns", type=int, default=262_144, help="patterns in the UP1 file timed")
     return ap.parse_args()
 
 
@@ -158,6 +160,47 @@ def cpu_baseline(pool, sample, impl_kind):
 
 
 VOTE_LIBRARY = os.path.join(ROOT, "tests", "golden", "vote_fcc_orient.npz")
+
+
+def time_file(bd, plan, method, pool, n):
+    """find_bands streamed from an EDAX UP1 file (ebsd_find_bands_file: parallel reads into
+    pinned buffers overlapping the copies and the detection), records to host memory.  The
+    file is written just before, so it is read from the page cache."""
+    import shutil
+    import tempfile
+    from pyebsdindex_gb300.ebsd_pattern import write_up
+    n = max(512, (n // 512) * 512)  # a 512-column scan
+    d = tempfile.mkdtemp(prefix="ebsdbench_")
+    try:
+        need = n * H * W + 4096
+        if shutil.disk_usage(d).free < 3 * need:
+            return {"skipped": f"{need / 1e9:.1f} GB file does not fit the temporary directory"}
+        reps = (n + len(pool) - 1) // len(pool)
+        pats = np.tile(pool, (reps, 1, 1))[:n]
+        path = os.path.join(d, "bench.up1")
+        write_up(path, pats, nCols=512, nRows=n // 512)
+        del pats
+        import torch
+        from pyebsdindex_gb300 import _lib
+        from pyebsdindex_gb300.ebsd_pattern import _bind as bind_up
+        lib = bind_up()
+        hout = {k: torch.empty(((n, NBANDS, 2) if k in ("maxloc", "aveloc") else (n, NBANDS)),
+                               dtype=torch.int8 if k == "valid" else torch.float32, pin_memory=True)
+                for k in _lib.BAND_FIELDS}
+        hb = _lib.Bands(**{k: _lib.C.c_void_p(v.data_ptr()) for k, v in hout.items()})
+
+        def run(count):
+            _lib.check(lib.ebsd_find_bands_file(plan.handle, _lib.method_id(method), path.encode(), 0, 0, count,
+                                                _lib.C.byref(hb), 0), "ebsd_find_bands_file")
+        run(min(n, 65536))  # pinned chunk buffers, page cache
+        t0 = time.perf_counter()
+        run(n)
+        dt = time.perf_counter() - t0
+        return {"value": n / dt, "unit": "patterns/s", "patterns": n, "file_bytes": need - 4096 + 42,
+                "source": "ebsd_find_bands_file: UP1 file in the page cache, 65,536-pattern chunks, band fields "
+                          "to pinned host arrays"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
 
 
 def time_indexing(outs, bd, N, stream, with_cpu, detect_ms):
@@ -406,6 +449,10 @@ def main():
             variants[vm] = vn * 2 / (a.elapsed_time(b) / 1000.0)
         variants[method] = value / world
 
+    file_e2e = None
+    if rank == 0 and not args.no_file:
+        file_e2e = time_file(bd, plan, method, pool, args.file_patterns)
+
     indexing = None
     if not args.no_index:
         indexing = time_indexing(outs, bd, N, stream, rank == 0 and world == 1 and not args.no_cpu,
@@ -431,7 +478,7 @@ def main():
                        "patterns_per_block_pass": ppp, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "variants_patterns_per_s": variants, "indexing": indexing,
+            "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))

@@ -37,6 +37,7 @@ extern "C" {
 #define EBSD_E_DEVICE (-6)     /* no usable CUDA device / wrong device                    */
 #define EBSD_E_TIMEOUT (-7)    /* a bounded device-side wait gave up                      */
 #define EBSD_E_SCRATCH (-8)    /* request needs more scratch than the static array holds   */
+#define EBSD_E_IO (-9)         /* a pattern file could not be opened, read or parsed       */
 
 /* ---- pattern element types (BandDetect.find_bands accepts uint8, uint16, float32) ---- */
 #define EBSD_U8 0
@@ -210,6 +211,38 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
 int ebsd_radon2pole(const float* d_theta, const float* d_rho, int64_t npat, int32_t nBands,
                     int32_t H, int32_t W, int32_t vendor, const float* d_pc, int32_t pc_stride,
                     float* d_normals, void* stream);
+
+/* ---- EDAX UP1 / UP2 pattern files (ebsd_pattern.UPFile, ebsd_pattern.py:435-570) ------- */
+/* Header fields as UPFile.read_header (ebsd_pattern.py:449-513) sets them. */
+typedef struct {
+    int32_t version;         /* format version: 1, or >= 3                                  */
+    int32_t W, H;            /* patternW, patternH                                           */
+    int32_t bytes_per_px;    /* 1 (.up1, uint8) or 2 (.up2, uint16)                          */
+    int64_t file_pos;        /* byte offset of the first pattern (filePos)                   */
+    int64_t n_patterns;      /* nPatterns (version 1: from the file size)                    */
+    int64_t n_cols, n_rows;  /* nCols, nRows (version 1: nPatterns x 1)                      */
+    int32_t extra_patterns;  /* extraPatterns (version >= 3)                                 */
+    int32_t hexflag;         /* hexflag (version >= 3)                                       */
+    double x_step, y_step;   /* xStep, yStep (version >= 3, else 0)                          */
+    int64_t file_bytes;      /* file size                                                    */
+} ebsd_up_info;
+
+/* Parses the header of `path` (.up1 / .up2, else bitdepth 8 or 16 decides the pixel type). */
+int ebsd_up_read_header(const char* path, int bitdepth, ebsd_up_info* info);
+
+/* Reads patterns [pat_start, pat_start + n) into h_dst (n * H * W pixels of the file's type)
+ * with `threads` parallel positional reads (0: a default); pinned destinations make the later
+ * host-to-device copies asynchronous.  UPFile.pat_reader (ebsd_pattern.py:515-537). */
+int ebsd_up_read(const char* path, const ebsd_up_info* info, int64_t pat_start, int64_t n,
+                 void* h_dst, int threads);
+
+/* find_bands on patterns [pat_start, pat_start + n) of a UP1 / UP2 file, records to host
+ * arrays: a reader thread fills three pinned chunk buffers from the file while two CUDA
+ * streams copy, detect and copy back, so file reads, copies and compute overlap.  The file's
+ * pattern size must be the plan's; the pixel type is the file's (uint8 / uint16).  `chunk`
+ * <= 0 picks the plan's default.  Synchronous. */
+int ebsd_find_bands_file(ebsd_plan_t plan, int method, const char* path, int bitdepth,
+                         int64_t pat_start, int64_t n, const ebsd_bands* h_out, int64_t chunk);
 
 /* ---- band weights and pattern quality (_ebsd_index_single.py:751-763) ------------------
  * For [n][nBands] band fields (device arrays, e.g. what ebsd_find_bands wrote):

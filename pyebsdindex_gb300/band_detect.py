@@ -149,6 +149,32 @@ class GPUFindBands:
                                chunk=chunk, stream=stream)
         return dev_out
 
+    def find_bands_file(self, path, patStart=0, nPat=-1, method=None, chunk=0, gpu_id=None):
+        """find_bands on patterns [patStart, patStart + nPat) of an EDAX UP1 / UP2 file (nPat
+        -1: to the end; clamped to the file as UPFile.read_data does, ebsd_pattern.py:253-262),
+        streamed by ebsd_find_bands_file: a reader thread fills pinned chunk buffers while two
+        CUDA streams copy and detect, so the file read overlaps the GPU work.  The plan is set
+        up for the file's pattern size if it is not already.  Returns the record array."""
+        import ctypes as C
+        from .ebsd_pattern import get_pattern_file_obj, _bind as _bind_up
+        f = get_pattern_file_obj(path)
+        dim = (int(f.patternH), int(f.patternW))
+        if self.patDim is None or tuple(np.asarray(self.patDim)[-2:]) != dim:
+            self.band_detect_setup(patDim=dim)
+        start = int(patStart)
+        n = int(f.nPatterns) - start if int(nPat) == -1 else max(int(nPat), 1)
+        n = min(n, int(f.nPatterns) - start)
+        if start < 0 or n < 0:
+            raise ValueError("patStart outside the file")
+        plan = self._device_plan(gpu_id)
+        m = self._pick_method(plan, method)
+        out = _lib.alloc_host_bands(n, int(self.nBands))
+        b = _lib.bands_struct(out)
+        lib = _bind_up()
+        _lib.check(lib.ebsd_find_bands_file(plan.handle, _lib.method_id(m), str(f.filepath).encode(), 0, start, n,
+                                            C.byref(b), int(chunk)), "ebsd_find_bands_file")
+        return self._records(out, n)
+
     def find_bands_normals(self, patterns, PC=None, vendor='EDAX', method=None, gpu_id=None):
         """find_bands followed by Radon.radon2pole (radon_fast.py:314-397) with the band
         normals computed on the device from the device theta/rho fields -- no host round trip

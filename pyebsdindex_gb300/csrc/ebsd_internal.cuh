@@ -96,6 +96,14 @@ struct ebsd_plan_s {
     void* h_out_dev[2] = {nullptr, nullptr};
     size_t h_in_bytes = 0, h_out_bytes = 0;
 
+    // host pipelines (ebsd_find_bands_host for pageable input, ebsd_find_bands_file): pinned
+    // chunk buffers the filler thread fills
+    void* h_pin[3] = {nullptr, nullptr, nullptr};
+    size_t h_pin_bytes = 0;
+    // pinned staging of records for pageable output arrays (two chunk slots)
+    void* h_outpin[2] = {nullptr, nullptr};
+    size_t h_outpin_bytes = 0;
+
     int64_t last_launches = 0;
 };
 
@@ -119,6 +127,11 @@ inline int launch_status() {
 inline size_t elem_size(int dtype) {
     return dtype == EBSD_U8 ? 1 : (dtype == EBSD_U16 ? 2 : 4);
 }
+
+// UP pattern files: patfile.cu ----------------------------------------------------------
+int up_parse_header(const char* path, int bitdepth, ebsd_up_info* info);
+int up_read_range(int fd, const ebsd_up_info* info, int64_t start, int64_t n, void* dst, int threads);
+int default_read_threads();
 
 // Per-stage (plain) path: plain.cu ------------------------------------------------------
 size_t plain_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);

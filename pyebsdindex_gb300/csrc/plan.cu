@@ -1,6 +1,12 @@
 // C-ABI entry points: plan lifetime, method dispatch, chunking and the host-buffer pipeline.
 #include "ebsd_internal.cuh"
 
+#include <condition_variable>
+#include <fcntl.h>
+#include <thread>
+#include <unistd.h>
+#include <utility>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -46,6 +52,16 @@ void free_plan_tables(ebsd_plan_s* p) {
         p->h_in_dev[i] = nullptr;
         p->h_out_dev[i] = nullptr;
     }
+    for (int i = 0; i < 3; ++i) {
+        if (p->h_pin[i]) cudaFreeHost(p->h_pin[i]);
+        p->h_pin[i] = nullptr;
+    }
+    p->h_pin_bytes = 0;
+    for (int i = 0; i < 2; ++i) {
+        if (p->h_outpin[i]) cudaFreeHost(p->h_outpin[i]);
+        p->h_outpin[i] = nullptr;
+    }
+    p->h_outpin_bytes = 0;
 }
 
 bool is_plain(int method) { return method == EBSD_PLAIN_F32 || method == EBSD_PLAIN_F64; }
@@ -104,6 +120,245 @@ int run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t
     return fused_run_chunk(p, method, dtype, d_pats, n, out, out_off, st, launches);
 }
 
+
+bool all_outputs(const ebsd_bands* b) {
+    return b->max && b->normmax && b->maxloc && b->avemax && b->aveloc && b->width && b->theta && b->rho && b->valid;
+}
+
+// Page-locked (pinned or registered) host memory: copies from or to it run asynchronously.
+bool is_pinned(const void* ptr) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+void parallel_copy(void* dst, const void* src, size_t bytes, int threads) {
+    threads = (int)std::max<size_t>(1, std::min<size_t>((size_t)threads, bytes >> 22));  // >= 4 MiB each
+    if (threads == 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const size_t part = ((bytes / threads) + 4095) & ~size_t(4095);
+    for (int t = 0; t < threads; ++t) {
+        const size_t a = std::min(bytes, t * part), b = std::min(bytes, a + part);
+        pool.emplace_back([=] { std::memcpy((char*)dst + a, (const char*)src + a, b - a); });
+    }
+    for (auto& th : pool) th.join();
+}
+
+// Where a host pipeline's patterns come from: a host array, or patterns of a UP file.
+struct ChunkSource {
+    const char* mem = nullptr;
+    bool mem_pinned = false;
+    int fd = -1;
+    const ebsd_up_info* info = nullptr;
+    int64_t file_start = 0;
+    size_t pat_bytes = 0;
+};
+
+// The device layout of one chunk's band fields (nb = patterns x bands).
+ebsd_bands chunk_fields(char* base, size_t nb) {
+    ebsd_bands d;
+    d.max = (float*)base;
+    d.normmax = d.max + nb;
+    d.maxloc = d.normmax + nb;
+    d.avemax = d.maxloc + 2 * nb;
+    d.aveloc = d.avemax + nb;
+    d.width = d.aveloc + 2 * nb;
+    d.theta = d.width + nb;
+    d.rho = d.theta + nb;
+    d.valid = (int8_t*)(d.rho + nb);
+    return d;
+}
+
+// Host-buffer pipeline shared by ebsd_find_bands_host and ebsd_find_bands_file.  Two CUDA
+// streams alternate chunks: chunk k + 1's upload overlaps chunk k's detection (the shared
+// workspace orders the detections through events).  Pageable or file input goes through three
+// pinned slots that a filler thread fills ahead (parallel positional reads, or a parallel
+// memcpy); pinned input is uploaded directly.  Records go straight to pinned output arrays, or
+// through two pinned staging buffers copied out while the next chunk computes.
+int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src, int64_t n, const ebsd_bands* h_out,
+                  int64_t chunk) {
+    if (chunk <= 0) chunk = is_plain(method) ? default_chunk(p, method) : 65536;
+    if (is_plain(method)) chunk = std::min<int64_t>(chunk, 65535);
+    chunk = std::min(chunk, n);
+    int rc = reserve(p, method, chunk);
+    if (rc != EBSD_OK) return rc;
+    const int nB = p->nB;
+    const size_t in_bytes = (size_t)chunk * src.pat_bytes;
+    const size_t out_bytes = (size_t)chunk * nB * (10 * sizeof(float) + 1) + 256;
+    for (int i = 0; i < 2; ++i) {
+        if (!p->hstream[i]) EBSD_CUDA_TRY(cudaStreamCreateWithFlags(&p->hstream[i], cudaStreamNonBlocking));
+        if (!p->hevent[i]) EBSD_CUDA_TRY(cudaEventCreateWithFlags(&p->hevent[i], cudaEventDisableTiming));
+    }
+    auto regrow = [](void** bufs, int count, size_t* have, size_t want, bool host) -> int {
+        if (want <= *have) return EBSD_OK;
+        for (int i = 0; i < count; ++i) {
+            if (bufs[i]) host ? cudaFreeHost(bufs[i]) : cudaFree(bufs[i]);
+            bufs[i] = nullptr;
+        }
+        *have = 0;
+        for (int i = 0; i < count; ++i) {
+            const cudaError_t e = host ? cudaHostAlloc(&bufs[i], want, cudaHostAllocDefault) : cudaMalloc(&bufs[i], want);
+            if (e != cudaSuccess) return e == cudaErrorMemoryAllocation ? EBSD_E_NOMEM : EBSD_E_LAUNCH;
+        }
+        *have = want;
+        return EBSD_OK;
+    };
+    const bool ring = !(src.mem && src.mem_pinned);
+    const bool direct_out = is_pinned(h_out->max) && is_pinned(h_out->normmax) && is_pinned(h_out->maxloc) &&
+                            is_pinned(h_out->avemax) && is_pinned(h_out->aveloc) && is_pinned(h_out->width) &&
+                            is_pinned(h_out->theta) && is_pinned(h_out->rho) && is_pinned(h_out->valid);
+    if ((rc = regrow(p->h_in_dev, 2, &p->h_in_bytes, in_bytes, false)) != EBSD_OK) return rc;
+    if ((rc = regrow(p->h_out_dev, 2, &p->h_out_bytes, out_bytes, false)) != EBSD_OK) return rc;
+    if (ring && (rc = regrow(p->h_pin, 3, &p->h_pin_bytes, in_bytes, true)) != EBSD_OK) return rc;
+    if (!direct_out && (rc = regrow(p->h_outpin, 2, &p->h_outpin_bytes, out_bytes, true)) != EBSD_OK) return rc;
+    const int64_t nchunks = (n + chunk - 1) / chunk;
+    const int threads = default_read_threads();
+
+    // filler thread: chunk k into pinned slot k % 3 once the slot is free
+    std::mutex m;
+    std::condition_variable cv;
+    int64_t ready[3] = {-1, -1, -1};
+    bool free_slot[3] = {true, true, true};
+    int fill_err = EBSD_OK;
+    bool stop = false;
+    std::thread filler;
+    if (ring) {
+        filler = std::thread([&] {
+            for (int64_t k = 0; k < nchunks; ++k) {
+                const int sl = (int)(k % 3);
+                {
+                    std::unique_lock<std::mutex> g(m);
+                    cv.wait(g, [&] { return free_slot[sl] || stop; });
+                    if (stop) return;
+                    free_slot[sl] = false;
+                }
+                const int64_t s0 = k * chunk, cnt = std::min(chunk, n - s0);
+                int r = EBSD_OK;
+                if (src.fd >= 0)
+                    r = up_read_range(src.fd, src.info, src.file_start + s0, cnt, p->h_pin[sl], threads);
+                else
+                    parallel_copy(p->h_pin[sl], src.mem + (size_t)s0 * src.pat_bytes, (size_t)cnt * src.pat_bytes,
+                                  threads);
+                {
+                    std::lock_guard<std::mutex> g(m);
+                    if (r != EBSD_OK) fill_err = r;
+                    ready[sl] = k;
+                }
+                cv.notify_all();
+                if (r != EBSD_OK) return;
+            }
+        });
+    }
+
+    cudaEvent_t copied[3], done_compute[2], out_done[2];
+    for (int i = 0; i < 3; ++i) cudaEventCreateWithFlags(&copied[i], cudaEventDisableTiming);
+    for (int i = 0; i < 2; ++i) cudaEventCreateWithFlags(&done_compute[i], cudaEventDisableTiming);
+    for (int i = 0; i < 2; ++i) cudaEventCreateWithFlags(&out_done[i], cudaEventDisableTiming);
+    int64_t staged_s[2] = {-1, -1}, staged_n[2] = {0, 0};
+    auto flush = [&](int ds) {  // staged records of slot ds -> the caller's arrays
+        if (staged_s[ds] < 0) return;
+        cudaEventSynchronize(out_done[ds]);
+        const size_t nb = (size_t)staged_n[ds] * nB;
+        const ebsd_bands st = chunk_fields((char*)p->h_outpin[ds], nb);
+        const ebsd_bands ho = offset_bands(*h_out, staged_s[ds], nB);
+        std::memcpy(ho.max, st.max, nb * 4);
+        std::memcpy(ho.normmax, st.normmax, nb * 4);
+        std::memcpy(ho.maxloc, st.maxloc, nb * 8);
+        std::memcpy(ho.avemax, st.avemax, nb * 4);
+        std::memcpy(ho.aveloc, st.aveloc, nb * 8);
+        std::memcpy(ho.width, st.width, nb * 4);
+        std::memcpy(ho.theta, st.theta, nb * 4);
+        std::memcpy(ho.rho, st.rho, nb * 4);
+        std::memcpy(ho.valid, st.valid, nb);
+        staged_s[ds] = -1;
+    };
+    for (int64_t k = 0; k < nchunks && rc == EBSD_OK; ++k) {
+        const int sl = (int)(k % 3), ds = (int)(k % 2);
+        const int64_t s0 = k * chunk, cnt = std::min(chunk, n - s0);
+        cudaStream_t st = p->hstream[ds];
+        const void* host_in = src.mem + (size_t)s0 * src.pat_bytes;
+        if (ring) {
+            std::unique_lock<std::mutex> g(m);
+            cv.wait(g, [&] { return ready[sl] == k || fill_err != EBSD_OK; });
+            if (fill_err != EBSD_OK) {
+                rc = fill_err;
+                break;
+            }
+            host_in = p->h_pin[sl];
+        }
+        if (cudaMemcpyAsync(p->h_in_dev[ds], host_in, (size_t)cnt * src.pat_bytes, cudaMemcpyHostToDevice, st) !=
+                cudaSuccess ||
+            cudaEventRecord(copied[sl], st) != cudaSuccess ||
+            (k > 0 && cudaStreamWaitEvent(st, done_compute[ds ^ 1], 0) != cudaSuccess)) {
+            rc = EBSD_E_LAUNCH;
+            break;
+        }
+        const size_t nb = (size_t)cnt * nB;
+        const ebsd_bands dev = chunk_fields((char*)p->h_out_dev[ds], nb);
+        rc = run_chunk(p, method, dtype, p->h_in_dev[ds], cnt, &dev, 0, st, &p->last_launches);
+        if (rc != EBSD_OK) break;
+        cudaEventRecord(done_compute[ds], st);
+        ebsd_bands dst;
+        if (direct_out) {
+            dst = offset_bands(*h_out, s0, nB);
+        } else {
+            flush(ds);  // chunk k - 2's records leave the staging buffer first
+            dst = chunk_fields((char*)p->h_outpin[ds], nb);
+        }
+        const std::pair<void*, const void*> parts[9] = {
+            {dst.max, dev.max}, {dst.normmax, dev.normmax}, {dst.maxloc, dev.maxloc}, {dst.avemax, dev.avemax},
+            {dst.aveloc, dev.aveloc}, {dst.width, dev.width}, {dst.theta, dev.theta}, {dst.rho, dev.rho},
+            {dst.valid, dev.valid}};
+        const size_t sizes[9] = {nb * 4, nb * 4, nb * 8, nb * 4, nb * 8, nb * 4, nb * 4, nb * 4, nb};
+        for (int f = 0; f < 9 && rc == EBSD_OK; ++f)
+            if (cudaMemcpyAsync(parts[f].first, parts[f].second, sizes[f], cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                rc = EBSD_E_LAUNCH;
+        if (!direct_out) {
+            cudaEventRecord(out_done[ds], st);
+            staged_s[ds] = s0;
+            staged_n[ds] = cnt;
+        }
+        if (k >= 1) {
+            if (ring) {  // chunk k - 1's upload was issued an iteration ago; its slot takes chunk k + 2
+                const int ps = (int)((k - 1) % 3);
+                cudaEventSynchronize(copied[ps]);
+                {
+                    std::lock_guard<std::mutex> g(m);
+                    free_slot[ps] = true;
+                }
+                cv.notify_all();
+            }
+            if (!direct_out) flush(ds ^ 1);  // chunk k - 1, while chunk k computes
+        }
+    }
+    if (ring) {
+        {
+            std::lock_guard<std::mutex> g(m);
+            stop = true;
+        }
+        cv.notify_all();
+        filler.join();
+    }
+    const cudaError_t e0 = cudaStreamSynchronize(p->hstream[0]);
+    const cudaError_t e1 = cudaStreamSynchronize(p->hstream[1]);
+    if (rc == EBSD_OK && !direct_out) {
+        flush(0);
+        flush(1);
+    }
+    for (int i = 0; i < 3; ++i) cudaEventDestroy(copied[i]);
+    for (int i = 0; i < 2; ++i) cudaEventDestroy(done_compute[i]);
+    for (int i = 0; i < 2; ++i) cudaEventDestroy(out_done[i]);
+    if (rc != EBSD_OK) return rc;
+    if (e0 != cudaSuccess || e1 != cudaSuccess) return EBSD_E_LAUNCH;
+    return EBSD_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -121,6 +376,7 @@ const char* ebsd_strerror(int code) {
         case EBSD_E_DEVICE: return "no usable CUDA device";
         case EBSD_E_TIMEOUT: return "a bounded device-side wait timed out";
         case EBSD_E_SCRATCH: return "request needs more scratch than the library's 64 MiB static device array holds";
+        case EBSD_E_IO: return "pattern file could not be opened, read or parsed";
         default: return "unknown error";
     }
 }
@@ -304,95 +560,44 @@ int ebsd_find_bands_host(ebsd_plan_t p, int method, int dtype, const void* h_pat
     if (!p || !h_out || n < 0) return EBSD_E_ARG;
     if (n > 0 && !h_pats) return EBSD_E_ARG;
     if (dtype != EBSD_U8 && dtype != EBSD_U16 && dtype != EBSD_F32) return EBSD_E_DTYPE;
-    if (!h_out->max || !h_out->normmax || !h_out->maxloc || !h_out->avemax || !h_out->aveloc ||
-        !h_out->width || !h_out->theta || !h_out->rho || !h_out->valid)
-        return EBSD_E_ARG;
+    if (!all_outputs(h_out)) return EBSD_E_ARG;
     int rc = check_method(p, method);
     if (rc != EBSD_OK) return rc;
     std::lock_guard<std::mutex> lk(p->mtx);
     if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
     p->last_launches = 0;
     if (n == 0) return EBSD_OK;
-    if (chunk <= 0) chunk = is_plain(method) ? default_chunk(p, method) : 65536;
-    if (is_plain(method)) chunk = std::min<int64_t>(chunk, 65535);
-    chunk = std::min(chunk, n);
-    rc = reserve(p, method, chunk);
-    if (rc != EBSD_OK) return rc;
+    ChunkSource src;
+    src.mem = (const char*)h_pats;
+    src.mem_pinned = is_pinned(h_pats);
+    src.pat_bytes = (size_t)p->nPx * elem_size(dtype);
+    return host_pipeline(p, method, dtype, src, n, h_out, chunk);
+}
 
-    const int nB = p->nB;
-    size_t es = elem_size(dtype);
-    size_t in_bytes = (size_t)chunk * p->nPx * es;
-    // nine fields per band: eight float fields of which maxloc/aveloc are pairs (10 floats)
-    // plus the int8 'valid' = 41 bytes per band
-    size_t out_bytes = (size_t)chunk * nB * (10 * sizeof(float) + 1) + 256;
-    for (int i = 0; i < 2; ++i) {
-        if (!p->hstream[i]) EBSD_CUDA_TRY(cudaStreamCreateWithFlags(&p->hstream[i], cudaStreamNonBlocking));
-        if (!p->hevent[i]) EBSD_CUDA_TRY(cudaEventCreateWithFlags(&p->hevent[i], cudaEventDisableTiming));
-    }
-    if (in_bytes > p->h_in_bytes) {
-        for (int i = 0; i < 2; ++i) {
-            cudaFree(p->h_in_dev[i]);
-            p->h_in_dev[i] = nullptr;
-        }
-        p->h_in_bytes = 0;
-        for (int i = 0; i < 2; ++i) EBSD_CUDA_TRY(cudaMalloc(&p->h_in_dev[i], in_bytes));
-        p->h_in_bytes = in_bytes;
-    }
-    if (out_bytes > p->h_out_bytes) {
-        for (int i = 0; i < 2; ++i) {
-            cudaFree(p->h_out_dev[i]);
-            p->h_out_dev[i] = nullptr;
-        }
-        p->h_out_bytes = 0;
-        for (int i = 0; i < 2; ++i) EBSD_CUDA_TRY(cudaMalloc(&p->h_out_dev[i], out_bytes));
-        p->h_out_bytes = out_bytes;
-    }
-    // the workspace is shared by both streams: chunk k+1's compute waits for chunk k's
-    // compute (event), while its H2D copy overlaps chunk k's compute and D2H copy.
-    cudaEvent_t done_compute[2];
-    for (int i = 0; i < 2; ++i) EBSD_CUDA_TRY(cudaEventCreateWithFlags(&done_compute[i], cudaEventDisableTiming));
-    int slot = 0;
-    int64_t prev = -1;
-    for (int64_t s = 0; s < n; s += chunk, slot ^= 1) {
-        int64_t m = std::min(chunk, n - s);
-        cudaStream_t st = p->hstream[slot];
-        EBSD_CUDA_TRY(cudaMemcpyAsync(p->h_in_dev[slot], (const char*)h_pats + (size_t)s * p->nPx * es,
-                                      (size_t)m * p->nPx * es, cudaMemcpyHostToDevice, st));
-        if (prev >= 0) EBSD_CUDA_TRY(cudaStreamWaitEvent(st, done_compute[slot ^ 1], 0));
-        char* ob = (char*)p->h_out_dev[slot];
-        size_t nb = (size_t)m * nB;
-        ebsd_bands dev;
-        dev.max = (float*)ob;
-        dev.normmax = dev.max + nb;
-        dev.maxloc = dev.normmax + nb;
-        dev.avemax = dev.maxloc + 2 * nb;
-        dev.aveloc = dev.avemax + nb;
-        dev.width = dev.aveloc + 2 * nb;
-        dev.theta = dev.width + nb;
-        dev.rho = dev.theta + nb;
-        dev.valid = (int8_t*)(dev.rho + nb);
-        rc = run_chunk(p, method, dtype, p->h_in_dev[slot], m, &dev, 0, st, &p->last_launches);
-        if (rc != EBSD_OK) break;
-        EBSD_CUDA_TRY(cudaEventRecord(done_compute[slot], st));
-        ebsd_bands ho = offset_bands(*h_out, s, nB);
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.max, dev.max, nb * 4, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.normmax, dev.normmax, nb * 4, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.maxloc, dev.maxloc, nb * 8, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.avemax, dev.avemax, nb * 4, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.aveloc, dev.aveloc, nb * 8, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.width, dev.width, nb * 4, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.theta, dev.theta, nb * 4, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.rho, dev.rho, nb * 4, cudaMemcpyDeviceToHost, st));
-        EBSD_CUDA_TRY(cudaMemcpyAsync(ho.valid, dev.valid, nb, cudaMemcpyDeviceToHost, st));
-        // the next use of this slot's buffers (two chunks later) is ordered on this stream
-        prev = s;
-    }
-    cudaError_t e0 = cudaStreamSynchronize(p->hstream[0]);
-    cudaError_t e1 = cudaStreamSynchronize(p->hstream[1]);
-    for (int i = 0; i < 2; ++i) cudaEventDestroy(done_compute[i]);
+int ebsd_find_bands_file(ebsd_plan_t p, int method, const char* path, int bitdepth, int64_t pat_start, int64_t n,
+                         const ebsd_bands* h_out, int64_t chunk) {
+    if (!p || !path || !h_out || n < 0 || pat_start < 0) return EBSD_E_ARG;
+    if (!all_outputs(h_out)) return EBSD_E_ARG;
+    ebsd_up_info info;
+    int rc = up_parse_header(path, bitdepth, &info);
     if (rc != EBSD_OK) return rc;
-    if (e0 != cudaSuccess || e1 != cudaSuccess) return EBSD_E_LAUNCH;
-    return EBSD_OK;
+    if (info.H != p->H || info.W != p->W || pat_start + n > info.n_patterns) return EBSD_E_ARG;
+    const int dtype = info.bytes_per_px == 1 ? EBSD_U8 : EBSD_U16;
+    rc = check_method(p, method);
+    if (rc != EBSD_OK) return rc;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
+    p->last_launches = 0;
+    if (n == 0) return EBSD_OK;
+    ChunkSource src;
+    src.fd = open(path, O_RDONLY);
+    if (src.fd < 0) return EBSD_E_IO;
+    src.info = &info;
+    src.file_start = pat_start;
+    src.pat_bytes = (size_t)p->nPx * info.bytes_per_px;
+    rc = host_pipeline(p, method, dtype, src, n, h_out, chunk);
+    close(src.fd);
+    return rc;
 }
 
 int ebsd_plan_set_patterns_per_pass(ebsd_plan_t p, int ppp) {

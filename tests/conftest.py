@@ -21,7 +21,7 @@ def golden_names():
     """Band-detection golden cases (NLPAR, orientation and voting fixtures are separate)."""
     return sorted(n for n in (os.path.splitext(os.path.basename(p))[0]
                               for p in glob.glob(os.path.join(GOLDEN_DIR, "*.npz")))
-                  if not n.startswith(("nlpar_", "orient_", "vote_")))
+                  if not n.startswith(("nlpar", "orient_", "vote_")))
 
 
 def vote_golden_names():
@@ -31,7 +31,7 @@ def vote_golden_names():
 
 def nlpar_golden_names():
     return sorted(os.path.splitext(os.path.basename(p))[0]
-                  for p in glob.glob(os.path.join(GOLDEN_DIR, "nlpar_*.npz")))
+                  for p in glob.glob(os.path.join(GOLDEN_DIR, "nlpar_*.npz")))  # not nlparlam_*
 
 
 def load_golden(name):

@@ -1,0 +1,60 @@
+"""BandDetect.find_bands_file (ebsd_find_bands_file: a reader thread fills pinned chunk buffers
+from a UP1 / UP2 file while two streams copy and detect) must give the records find_bands
+gives for the same patterns in memory, bit for bit, whatever the chunking."""
+import os
+
+import numpy as np
+import pytest
+
+import pyebsdindex_gb300 as pg
+from pyebsdindex_gb300 import synthetic as syn
+from pyebsdindex_gb300.ebsd_pattern import write_up
+
+pytestmark = pytest.mark.gpu
+FIELDS = ("max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid")
+
+
+def plan(h=80, nRho=120):
+    bd = pg.BandDetect(nTheta=180, nRho=nRho, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=9)
+    bd.band_detect_setup(patDim=(h, h), patternmask=syn.circular_mask(h, h))
+    return bd
+
+
+@pytest.mark.parametrize("method,chunk", [("fused", 0), ("fused", 700), ("plain", 500)])
+def test_file_stream_equals_in_memory(cuda, tmp_path, method, chunk):
+    pats = syn.make_patterns(2900, 80, 80, seed=51, noise_frac=0.1)[0]
+    path = os.path.join(tmp_path, "scan.up1")
+    write_up(path, pats, nCols=58, nRows=50)
+    bd = plan()
+    want = bd.find_bands(pats, method=method)
+    got = bd.find_bands_file(path, method=method, chunk=chunk)
+    for f in FIELDS:
+        assert got[f].tobytes() == want[f].tobytes(), f
+    part = bd.find_bands_file(path, patStart=1234, nPat=777, method=method, chunk=chunk)
+    for f in FIELDS:
+        assert part[f].tobytes() == want[f][1234:2011].tobytes(), f
+    tail = bd.find_bands_file(path, patStart=2890, nPat=100, method=method)  # clamped to the file
+    assert tail.shape[0] == 10
+
+
+def test_uint16_file(cuda, tmp_path):
+    pats = (syn.make_patterns(600, 60, 60, seed=52, noise_frac=0.1)[0].astype(np.uint16) * 16)
+    path = os.path.join(tmp_path, "scan.up2")
+    write_up(path, pats, version=1)
+    bd = plan(60, 90)
+    want = bd.find_bands(pats)
+    got = bd.find_bands_file(path, chunk=256)
+    for f in FIELDS:
+        assert got[f].tobytes() == want[f].tobytes(), f
+
+
+def test_file_sets_up_the_plan_for_its_size(cuda, tmp_path):
+    pats = syn.make_patterns(50, 60, 60, seed=53, noise_frac=0.1)[0]
+    path = os.path.join(tmp_path, "s.up1")
+    write_up(path, pats)
+    bd = pg.BandDetect(nTheta=180, nRho=90, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=8)
+    got = bd.find_bands_file(path)
+    assert got.shape == (50, 8)
+    assert np.array_equal(got["max"], bd.find_bands(pats)["max"])
+    with pytest.raises(RuntimeError, match="pattern file"):
+        bd.find_bands_file(os.path.join(tmp_path, "missing.up1"))
