@@ -244,6 +244,19 @@ int ebsd_up_read(const char* path, const ebsd_up_info* info, int64_t pat_start, 
 int ebsd_find_bands_file(ebsd_plan_t plan, int method, const char* path, int bitdepth,
                          int64_t pat_start, int64_t n, const ebsd_bands* h_out, int64_t chunk);
 
+/* ebsd_find_bands_host / ebsd_find_bands_file with the bands written as records: h_records
+ * [n][nBands] records of `itemsize` bytes (the reference's BandDetect.dataType,
+ * band_detect.py:110-115), the nine band fields (max, normmax, maxloc[2], avemax, aveloc[2],
+ * width, theta, rho as float32, valid as int8, in ebsd_bands order) at field_offsets[9] bytes;
+ * every other byte is zero.  Records are packed on the host, in parallel, while the next
+ * chunk runs on the GPU. */
+int ebsd_find_bands_host_records(ebsd_plan_t plan, int method, int dtype, const void* h_pats,
+                                 int64_t n, void* h_records, int32_t itemsize,
+                                 const int32_t* field_offsets, int64_t chunk);
+int ebsd_find_bands_file_records(ebsd_plan_t plan, int method, const char* path, int bitdepth,
+                                 int64_t pat_start, int64_t n, void* h_records, int32_t itemsize,
+                                 const int32_t* field_offsets, int64_t chunk);
+
 /* ---- band weights and pattern quality (_ebsd_index_single.py:751-763) ------------------
  * For [n][nBands] band fields (device arrays, e.g. what ebsd_find_bands wrote):
  *   adj[p][b] = (1 - |rho| * 0.5 / rhomax) * max * (theta > 2 deg ? 0.75 : 0.25)

@@ -79,6 +79,12 @@ def load():
         lib.ebsd_find_bands.restype = C.c_int
         lib.ebsd_find_bands_host.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, C.POINTER(Bands), C.c_int64]
         lib.ebsd_find_bands_host.restype = C.c_int
+        lib.ebsd_find_bands_host_records.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, P, C.c_int32,
+                                                     C.POINTER(C.c_int32), C.c_int64]
+        lib.ebsd_find_bands_host_records.restype = C.c_int
+        lib.ebsd_find_bands_file_records.argtypes = [P, C.c_int, C.c_char_p, C.c_int, C.c_int64, C.c_int64, P,
+                                                     C.c_int32, C.POINTER(C.c_int32), C.c_int64]
+        lib.ebsd_find_bands_file_records.restype = C.c_int
         lib.ebsd_last_launch_count.argtypes = [P]
         lib.ebsd_last_launch_count.restype = C.c_int64
         lib.ebsd_plan_autotune.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, P, C.POINTER(C.c_int)]
@@ -183,6 +189,31 @@ class DevicePlan:
                                              n, C.byref(b), int(chunk)), "ebsd_find_bands_host")
         return out
 
+    def find_bands_host_records(self, pats: np.ndarray, method, rec_dtype, chunk=0):
+        """Host patterns [n,H,W] -> (n, nBands) record array of ``rec_dtype`` (the reference's
+        BandDetect.dataType): the records are packed by the library while the GPU runs."""
+        dt = DTYPES.get(pats.dtype)
+        if dt is None:
+            raise TypeError(f"unsupported pattern dtype {pats.dtype}")
+        pats = np.ascontiguousarray(pats)
+        n = pats.shape[0]
+        rec = np.empty((n, self.nBands), dtype=rec_dtype)
+        offs = record_offsets(rec_dtype)
+        check(self._lib.ebsd_find_bands_host_records(self.handle, method_id(method), dt, C.c_void_p(pats.ctypes.data),
+                                                     n, C.c_void_p(rec.ctypes.data), rec_dtype.itemsize, offs,
+                                                     int(chunk)), "ebsd_find_bands_host_records")
+        return rec
+
+    def find_bands_file_records(self, path: str, pat_start: int, n: int, method, rec_dtype, chunk=0):
+        """Patterns [pat_start, pat_start + n) of a UP1 / UP2 file -> record array."""
+        rec = np.empty((n, self.nBands), dtype=rec_dtype)
+        offs = record_offsets(rec_dtype)
+        check(self._lib.ebsd_find_bands_file_records(self.handle, method_id(method), str(path).encode(), 0,
+                                                     int(pat_start), int(n), C.c_void_p(rec.ctypes.data),
+                                                     rec_dtype.itemsize, offs, int(chunk)),
+              "ebsd_find_bands_file_records")
+        return rec
+
     def find_bands_device(self, pats_ptr: int, dtype: int, n: int, out_ptrs: dict, method, chunk=0, stream=0):
         """Device patterns -> device SoA outputs (raw pointers), asynchronous on `stream`."""
         b = Bands(**{k: C.c_void_p(int(out_ptrs[k])) for k in BAND_FIELDS})
@@ -200,6 +231,20 @@ class DevicePlan:
             self.close()
         except Exception:
             pass
+
+
+def record_offsets(rec_dtype):
+    """Byte offsets of the nine band fields in a record dtype, in BAND_FIELDS order (checked
+    to be float32, pairs of float32 for maxloc / aveloc, int8 for valid)."""
+    want = {"maxloc": (np.float32, (2,)), "aveloc": (np.float32, (2,)), "valid": (np.int8, ())}
+    offs = (C.c_int32 * 9)()
+    for i, f in enumerate(BAND_FIELDS):
+        ft, off = rec_dtype.fields[f][:2]
+        base, shape = want.get(f, (np.float32, ()))
+        if ft.base != np.dtype(base) or ft.shape != shape:
+            raise TypeError(f"record field {f!r} has type {ft}, expected {np.dtype(base)}{shape}")
+        offs[i] = off
+    return offs
 
 
 def alloc_host_bands(n, nB):

@@ -115,6 +115,7 @@ class GPUFindBands:
         chunk = int(chunksize) if (chunksize is not None and chunksize > 0) else 0
         if m.startswith("fused"):
             chunk = 0
+        soa = None
         if is_torch:
             dev_out = self._find_bands_dev(plan, pats, m, chunk)
             soa = {k: v.cpu().numpy() for k, v in dev_out.items()}
@@ -122,8 +123,9 @@ class GPUFindBands:
             arr = np.asarray(pats)
             if arr.dtype not in (np.uint8, np.uint16, np.float32):
                 arr = arr.astype(np.float32)
-            soa = plan.find_bands_host(arr, m, chunk=chunk)
-        bandData = self._records(soa, nP)
+            bandData = plan.find_bands_host_records(arr, m, self.dataType, chunk=chunk)
+        if soa is not None:
+            bandData = self._records(soa, nP)
         if verbose > 0:
             print('Band Find Time (GPU, %s):' % m, timer() - tic0)
         return bandData
@@ -155,8 +157,7 @@ class GPUFindBands:
         streamed by ebsd_find_bands_file: a reader thread fills pinned chunk buffers while two
         CUDA streams copy and detect, so the file read overlaps the GPU work.  The plan is set
         up for the file's pattern size if it is not already.  Returns the record array."""
-        import ctypes as C
-        from .ebsd_pattern import get_pattern_file_obj, _bind as _bind_up
+        from .ebsd_pattern import get_pattern_file_obj
         f = get_pattern_file_obj(path)
         dim = (int(f.patternH), int(f.patternW))
         if self.patDim is None or tuple(np.asarray(self.patDim)[-2:]) != dim:
@@ -168,12 +169,7 @@ class GPUFindBands:
             raise ValueError("patStart outside the file")
         plan = self._device_plan(gpu_id)
         m = self._pick_method(plan, method)
-        out = _lib.alloc_host_bands(n, int(self.nBands))
-        b = _lib.bands_struct(out)
-        lib = _bind_up()
-        _lib.check(lib.ebsd_find_bands_file(plan.handle, _lib.method_id(m), str(f.filepath).encode(), 0, start, n,
-                                            C.byref(b), int(chunk)), "ebsd_find_bands_file")
-        return self._records(out, n)
+        return plan.find_bands_file_records(str(f.filepath), start, n, m, self.dataType, chunk=chunk)
 
     def find_bands_normals(self, patterns, PC=None, vendor='EDAX', method=None, gpu_id=None):
         """find_bands followed by Radon.radon2pole (radon_fast.py:314-397) with the band

@@ -160,6 +160,51 @@ struct ChunkSource {
     size_t pat_bytes = 0;
 };
 
+// Record output: an array of fixed-size records (one per band) with the nine band fields at
+// byte offsets (the reference's BandDetect.dataType, band_detect.py:110-115); every other
+// byte of a record is zero, as np.zeros leaves it.
+struct RecordSink {
+    char* base = nullptr;
+    int32_t itemsize = 0;
+    int32_t off[9] = {};
+};
+
+// Staged SoA fields of `nb` bands -> records [first, first + nb), in parallel.
+void pack_records(const RecordSink& rs, int64_t first, const ebsd_bands& st, size_t nb, int threads) {
+    auto work = [&](size_t a, size_t b) {
+        for (size_t i = a; i < b; ++i) {
+            char* r = rs.base + (size_t)(first + (int64_t)i) * rs.itemsize;
+            std::memset(r, 0, rs.itemsize);
+            std::memcpy(r + rs.off[0], st.max + i, 4);
+            std::memcpy(r + rs.off[1], st.normmax + i, 4);
+            std::memcpy(r + rs.off[2], st.maxloc + 2 * i, 8);
+            std::memcpy(r + rs.off[3], st.avemax + i, 4);
+            std::memcpy(r + rs.off[4], st.aveloc + 2 * i, 8);
+            std::memcpy(r + rs.off[5], st.width + i, 4);
+            std::memcpy(r + rs.off[6], st.theta + i, 4);
+            std::memcpy(r + rs.off[7], st.rho + i, 4);
+            std::memcpy(r + rs.off[8], st.valid + i, 1);
+        }
+    };
+    threads = (int)std::max<size_t>(1, std::min<size_t>((size_t)threads, nb / 4096));
+    if (threads == 1) {
+        work(0, nb);
+        return;
+    }
+    std::vector<std::thread> pool;
+    const size_t part = (nb + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(work, std::min(nb, t * part), std::min(nb, (t + 1) * part));
+    for (auto& th : pool) th.join();
+}
+
+bool valid_sink(const RecordSink& rs) {
+    const int sizes[9] = {4, 4, 8, 4, 8, 4, 4, 4, 1};
+    if (!rs.base || rs.itemsize <= 0) return false;
+    for (int f = 0; f < 9; ++f)
+        if (rs.off[f] < 0 || rs.off[f] + sizes[f] > rs.itemsize) return false;
+    return true;
+}
+
 // The device layout of one chunk's band fields (nb = patterns x bands).
 ebsd_bands chunk_fields(char* base, size_t nb) {
     ebsd_bands d;
@@ -182,7 +227,7 @@ ebsd_bands chunk_fields(char* base, size_t nb) {
 // memcpy); pinned input is uploaded directly.  Records go straight to pinned output arrays, or
 // through two pinned staging buffers copied out while the next chunk computes.
 int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src, int64_t n, const ebsd_bands* h_out,
-                  int64_t chunk) {
+                  int64_t chunk, const RecordSink* sink = nullptr) {
     if (chunk <= 0) chunk = is_plain(method) ? default_chunk(p, method) : 65536;
     if (is_plain(method)) chunk = std::min<int64_t>(chunk, 65535);
     chunk = std::min(chunk, n);
@@ -210,9 +255,10 @@ int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src,
         return EBSD_OK;
     };
     const bool ring = !(src.mem && src.mem_pinned);
-    const bool direct_out = is_pinned(h_out->max) && is_pinned(h_out->normmax) && is_pinned(h_out->maxloc) &&
-                            is_pinned(h_out->avemax) && is_pinned(h_out->aveloc) && is_pinned(h_out->width) &&
-                            is_pinned(h_out->theta) && is_pinned(h_out->rho) && is_pinned(h_out->valid);
+    const bool direct_out = !sink && is_pinned(h_out->max) && is_pinned(h_out->normmax) &&
+                            is_pinned(h_out->maxloc) && is_pinned(h_out->avemax) && is_pinned(h_out->aveloc) &&
+                            is_pinned(h_out->width) && is_pinned(h_out->theta) && is_pinned(h_out->rho) &&
+                            is_pinned(h_out->valid);
     if ((rc = regrow(p->h_in_dev, 2, &p->h_in_bytes, in_bytes, false)) != EBSD_OK) return rc;
     if ((rc = regrow(p->h_out_dev, 2, &p->h_out_bytes, out_bytes, false)) != EBSD_OK) return rc;
     if (ring && (rc = regrow(p->h_pin, 3, &p->h_pin_bytes, in_bytes, true)) != EBSD_OK) return rc;
@@ -266,6 +312,11 @@ int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src,
         cudaEventSynchronize(out_done[ds]);
         const size_t nb = (size_t)staged_n[ds] * nB;
         const ebsd_bands st = chunk_fields((char*)p->h_outpin[ds], nb);
+        if (sink) {
+            pack_records(*sink, staged_s[ds] * nB, st, nb, threads);
+            staged_s[ds] = -1;
+            return;
+        }
         const ebsd_bands ho = offset_bands(*h_out, staged_s[ds], nB);
         std::memcpy(ho.max, st.max, nb * 4);
         std::memcpy(ho.normmax, st.normmax, nb * 4);
@@ -596,6 +647,63 @@ int ebsd_find_bands_file(ebsd_plan_t p, int method, const char* path, int bitdep
     src.file_start = pat_start;
     src.pat_bytes = (size_t)p->nPx * info.bytes_per_px;
     rc = host_pipeline(p, method, dtype, src, n, h_out, chunk);
+    close(src.fd);
+    return rc;
+}
+
+int ebsd_find_bands_host_records(ebsd_plan_t p, int method, int dtype, const void* h_pats, int64_t n,
+                                 void* h_records, int32_t itemsize, const int32_t* field_offsets, int64_t chunk) {
+    if (!p || n < 0 || !field_offsets) return EBSD_E_ARG;
+    if (n > 0 && (!h_pats || !h_records)) return EBSD_E_ARG;
+    if (dtype != EBSD_U8 && dtype != EBSD_U16 && dtype != EBSD_F32) return EBSD_E_DTYPE;
+    RecordSink rs;
+    rs.base = (char*)h_records;
+    rs.itemsize = itemsize;
+    for (int f = 0; f < 9; ++f) rs.off[f] = field_offsets[f];
+    if (n > 0 && !valid_sink(rs)) return EBSD_E_ARG;
+    int rc = check_method(p, method);
+    if (rc != EBSD_OK) return rc;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
+    p->last_launches = 0;
+    if (n == 0) return EBSD_OK;
+    ChunkSource src;
+    src.mem = (const char*)h_pats;
+    src.mem_pinned = is_pinned(h_pats);
+    src.pat_bytes = (size_t)p->nPx * elem_size(dtype);
+    const ebsd_bands none{};
+    return host_pipeline(p, method, dtype, src, n, &none, chunk, &rs);
+}
+
+int ebsd_find_bands_file_records(ebsd_plan_t p, int method, const char* path, int bitdepth, int64_t pat_start,
+                                 int64_t n, void* h_records, int32_t itemsize, const int32_t* field_offsets,
+                                 int64_t chunk) {
+    if (!p || !path || n < 0 || pat_start < 0 || !field_offsets) return EBSD_E_ARG;
+    if (n > 0 && !h_records) return EBSD_E_ARG;
+    RecordSink rs;
+    rs.base = (char*)h_records;
+    rs.itemsize = itemsize;
+    for (int f = 0; f < 9; ++f) rs.off[f] = field_offsets[f];
+    if (n > 0 && !valid_sink(rs)) return EBSD_E_ARG;
+    ebsd_up_info info;
+    int rc = up_parse_header(path, bitdepth, &info);
+    if (rc != EBSD_OK) return rc;
+    if (info.H != p->H || info.W != p->W || pat_start + n > info.n_patterns) return EBSD_E_ARG;
+    const int dtype = info.bytes_per_px == 1 ? EBSD_U8 : EBSD_U16;
+    rc = check_method(p, method);
+    if (rc != EBSD_OK) return rc;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
+    p->last_launches = 0;
+    if (n == 0) return EBSD_OK;
+    ChunkSource src;
+    src.fd = open(path, O_RDONLY);
+    if (src.fd < 0) return EBSD_E_IO;
+    src.info = &info;
+    src.file_start = pat_start;
+    src.pat_bytes = (size_t)p->nPx * info.bytes_per_px;
+    const ebsd_bands none{};
+    rc = host_pipeline(p, method, dtype, src, n, &none, chunk, &rs);
     close(src.fd);
     return rc;
 }
