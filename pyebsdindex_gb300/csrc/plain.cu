@@ -59,6 +59,58 @@ __global__ void k_radon_plain(const InT* __restrict__ pats, const uint16_t* __re
     radon[q * (int64_t)R * Tp + (int64_t)(i + p0) * Tp + (j + p1)] = val;
 }
 
+// The same ray means with the patterns staged in shared memory (P patterns per block, the
+// threads striding over the rays; each LUT entry read once serves the P patterns): the
+// gathers hit shared memory instead of scattered global loads.  Used without a background
+// and when the patterns fit; every per-ray sum keeps the sequential LUT order, so the values
+// equal k_radon_plain's.
+template <typename InT, typename T, int P>
+__global__ void __launch_bounds__(1024) k_radon_smem(const InT* __restrict__ pats, const uint16_t* __restrict__ lut16,
+                                                    const int32_t* __restrict__ lut32,
+                                                    const int32_t* __restrict__ count, int64_t n, int nRays,
+                                                    int nTheta, int nPx, T* __restrict__ radon, int R, int Tp, int p0,
+                                                    int p1) {
+    extern __shared__ __align__(16) unsigned char rsm[];
+    InT* px = (InT*)rsm;
+    const int64_t q0 = (int64_t)blockIdx.x * P;
+    const int np = (int)(n - q0 < P ? n - q0 : P);
+    for (int t = threadIdx.x; t < np * nPx; t += blockDim.x) px[t] = pats[q0 * nPx + t];
+    __syncthreads();
+    for (int r = threadIdx.x; r < nRays; r += blockDim.x) {
+        const int cnt = count[r];
+        T sum[P];
+#pragma unroll
+        for (int i = 0; i < P; ++i) sum[i] = (T)0;
+        for (int k = 0; k < cnt; ++k) {
+            const int idx = lut16 ? (int)lut16[(size_t)k * nRays + r] : lut32[(size_t)k * nRays + r];
+#pragma unroll
+            for (int i = 0; i < P; ++i) sum[i] = r_add(sum[i], (T)px[i * nPx + idx]);
+        }
+        const int ri = r / nTheta, rj = r - (r / nTheta) * nTheta;
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            if (i < np) {
+                const T val = cnt >= 1 ? r_div(sum[i], (T)cnt) : (T)-1;
+                radon[(q0 + i) * (int64_t)R * Tp + (int64_t)(ri + p0) * Tp + (rj + p1)] = val;
+            }
+        }
+    }
+}
+
+template <typename InT, typename T, int P>
+int launch_radon_smem(const ebsd_plan_s* p, const InT* d_pats, int64_t n, T* radon, cudaStream_t st) {
+    const size_t bytes = (size_t)P * p->nPx * sizeof(InT);
+    static int raised[64] = {};
+    if (bytes > 48 * 1024 && raised[p->device] < (int)bytes) {
+        EBSD_CUDA_TRY(cudaFuncSetAttribute(k_radon_smem<InT, T, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)bytes));
+        raised[p->device] = (int)bytes;
+    }
+    k_radon_smem<InT, T, P><<<(unsigned)((n + P - 1) / P), 1024, bytes, st>>>(
+        d_pats, p->d_lut16, p->d_lut32, p->d_count, n, p->nRays, p->nTheta, p->nPx, radon, p->R, p->Tp, p->p0, p->p1);
+    return launch_status();
+}
+
 // Fills every padding cell from the interior: theta padding is the theta-wrapped column
 // flipped in rho, rho padding repeats the first/last interior row (after theta padding).
 template <typename T>
@@ -289,10 +341,19 @@ int run_chunk_t(ebsd_plan_s* p, const InT* d_pats, int64_t n, const ebsd_bands* 
     uint8_t* flags = (uint8_t*)(stats + 2 * n);
     const T* kern = sizeof(T) == 4 ? (const T*)p->d_kernel : (const T*)p->d_kernel64;
 
-    dim3 gr((p->nRays + 127) / 128, (unsigned)n);
-    k_radon_plain<InT, T><<<gr, 128, 0, st>>>(d_pats, p->d_lut16, p->d_lut32, p->d_count, p->nRays,
-                                              p->nTheta, p->nPx, p->bg_mode, p->d_bg, p->d_bgf, radon,
-                                              p->R, p->Tp, p->p0, p->p1);
+    const size_t px_smem = (size_t)p->nPx * sizeof(InT);
+    constexpr size_t kRadonSmem = 200 * 1024;
+    if (p->bg_mode == 0 && px_smem <= kRadonSmem) {
+        const int rrc = (4 * px_smem <= kRadonSmem && n >= 4)   ? launch_radon_smem<InT, T, 4>(p, d_pats, n, radon, st)
+                        : (2 * px_smem <= kRadonSmem && n >= 2) ? launch_radon_smem<InT, T, 2>(p, d_pats, n, radon, st)
+                                                                : launch_radon_smem<InT, T, 1>(p, d_pats, n, radon, st);
+        if (rrc != EBSD_OK) return rrc;
+    } else {
+        dim3 gr((p->nRays + 127) / 128, (unsigned)n);
+        k_radon_plain<InT, T><<<gr, 128, 0, st>>>(d_pats, p->d_lut16, p->d_lut32, p->d_count, p->nRays,
+                                                  p->nTheta, p->nPx, p->bg_mode, p->d_bg, p->d_bgf, radon,
+                                                  p->R, p->Tp, p->p0, p->p1);
+    }
     int64_t padcells = (int64_t)cells * n;
     int pblocks = (int)((padcells + 255) / 256 < 152 * 32 ? (padcells + 255) / 256 : 152 * 32);
     k_pad_plain<T><<<pblocks, 256, 0, st>>>(radon, n, p->R, p->Tp, p->p0, p->p1, p->nRho, p->nTheta);
