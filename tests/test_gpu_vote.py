@@ -239,3 +239,24 @@ def test_bad_arguments(cuda):
         tv.BandIndexer(lib=bad).plan()
     with pytest.raises(NotImplementedError):
         tv.BandIndexer(lib=lib, high_fidelity=False).plan()
+
+
+def test_many_matches_per_triplet_take_the_ordered_fallback(cuda):
+    """A library whose triplet rows repeat 40 times gives band triplets more matches than the
+    kernel's 96-entry list: those take the one-at-a-time path, still in library order.  The
+    oracle runs the same duplicated library."""
+    lib, params, ins, _ = load("vote_fcc_syn")
+    dup = dict(lib)
+    dup["trip_angles"] = np.tile(lib["trip_angles"], (40, 1))
+    dup["trip_familyid"] = np.tile(lib["trip_familyid"], (40, 1))
+    n = 40
+    got = run(indexer(dup, params), ins["norms"][:n], ins["inten"][:n])
+    want, mid = vo.bandindex(dup, params, ins["norms"][:n], ins["inten"][:n])
+    assert (mid["accn"].max(axis=(1, 2)) > 96).any()  # some band triplet overflowed the list
+    same = np.ones(n, bool)
+    for k, v in zip(("quat", "fit", "cm", "polematch", "nmatch", "ij", "acc_correct", "bandfit"), want):
+        if k in INTS:
+            same &= rows_equal(got[k], v)
+    same &= rows_equal(got["accn"], mid["accn"])
+    assert same.mean() >= 0.9
+    np.testing.assert_allclose(got["accw"][same], mid["accw"][same], rtol=1e-5, atol=1e-4)
