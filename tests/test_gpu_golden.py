@@ -1,6 +1,6 @@
 """GPU find_bands against the reference's golden vectors (all pattern types and plan shapes).
 
-Tolerances (the spec bar): integer peak locations identical for >= 99.9% of bands,
+Tolerances (the accuracy bar of the batched metric): integer peak locations identical for >= 99.9% of bands,
 sub-pixel (aveloc) within 1e-3 Radon pixels; the other float fields within the stated
 relative tolerances.  The device convolves directly while the reference uses an FFT
 convolution, so values differ at the float32 rounding level.
