@@ -44,6 +44,8 @@ struct ebsd_vote_plan_s {
     float* d_par = nullptr;       // [1] largest |cosine| of a band pair that is not parallel
     float par = -1.0f;            // host copy of *d_par
     int32_t* d_orig = nullptr;    // [ntrip] library index of each interval row (rows sorted by lo0)
+    void* d_quest = nullptr;      // QUEST hand-over scratch, quest_cap patterns
+    int64_t quest_cap = 0;
     float win = 0.0f;             // widest first-angle interval (hi0 - lo0), plus a margin
 };
 
@@ -55,6 +57,15 @@ constexpr int kList = 96;  // matches of one band triplet held for sorting into 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr double kRadeg = 57.29577951308232;  // 180 / pi
 constexpr float kRadegF = 57.29577951308232f;
+
+// What the warp hands to the scalar QUEST solve for one pattern: S = B + B^T (upper triangle
+// S00 S01 S02 S11 S12 S22), z, and the bands in the fit (bit j: band j; m of them; m < 3: no fit).
+struct QuestInput {
+    double S[6];
+    double z[3];
+    uint32_t mask;
+    int32_t m;
+};
 
 struct VoteArgs {
     const float* iv;
@@ -78,6 +89,7 @@ struct VoteArgs {
     const float* inten;
     int64_t n;
     ebsd_index_out out;
+    QuestInput* quest;  // [n] scratch, device
 };
 
 __device__ __forceinline__ float addf(float a, float b) { return __fadd_rn(a, b); }
@@ -518,10 +530,8 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     }
     __syncwarp();
 
-    // ---- QUEST fit, tripletvote.py:903-1020 ----
-    double qout[4] = {1.0, 0.0, 0.0, 0.0};
-    double mad = -1.0;
-    double bdot = -1.0;
+    // ---- QUEST fit, tripletvote.py:903-1020: the weighted B matrix and z vector here (lanes),
+    // the scalar solve and the fits in k_quest / k_quest_fit (one thread per pattern) ----
     {
         if (lane < nb) wq[lane] = (double)wsel;
         __syncwarp();
@@ -533,6 +543,7 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
         const bool g2 = lane < nb && wn > 1.0e-7;
         const unsigned g2m = __ballot_sync(kFull, g2);
         const int m = __popc(g2m);
+        QuestInput* qi = A.quest + p;
         if (m >= 3) {
             const int slot = __popc(g2m & lt_mask);
             if (g2) {
@@ -570,95 +581,20 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
                 qs[lane] = zc;
             }
             __syncwarp();
-            if (lane == 0) {
-                double Bm[3][3];
-                for (int r = 0; r < 3; ++r)
-                    for (int c = 0; c < 3; ++c) Bm[r][c] = qs[3 * r + c];
-                double S[3][3];
-                for (int r = 0; r < 3; ++r)
-                    for (int c = 0; c < 3; ++c) S[r][c] = __dadd_rn(Bm[r][c], Bm[c][r]);
-                const double z[3] = {qs[9], qs[10], qs[11]};
-                double S2[3][3];
-                for (int r = 0; r < 3; ++r)
-                    for (int c = 0; c < 3; ++c)
-                        S2[r][c] = __fma_rn(S[r][2], S[2][c], __fma_rn(S[r][1], S[1][c], __dmul_rn(S[r][0], S[0][c])));
-                const double det =
-                    __dadd_rn(__dsub_rn(__dmul_rn(S[0][0], __dsub_rn(__dmul_rn(S[1][1], S[2][2]), __dmul_rn(S[1][2], S[2][1]))),
-                                        __dmul_rn(S[0][1], __dsub_rn(__dmul_rn(S[1][0], S[2][2]), __dmul_rn(S[1][2], S[2][0])))),
-                              __dmul_rn(S[0][2], __dsub_rn(__dmul_rn(S[1][0], S[2][1]), __dmul_rn(S[1][1], S[2][0]))));
-                const double kk = __dadd_rn(__dadd_rn(__dsub_rn(__dmul_rn(S[1][1], S[2][2]), __dmul_rn(S[1][2], S[2][1])),
-                                                      __dsub_rn(__dmul_rn(S[0][0], S[2][2]), __dmul_rn(S[0][2], S[2][0]))),
-                                            __dsub_rn(__dmul_rn(S[0][0], S[1][1]), __dmul_rn(S[1][0], S[0][1])));
-                const double sig = __dmul_rn(0.5, __dadd_rn(__dadd_rn(S[0][0], S[1][1]), S[2][2]));
-                const double sig2 = __dmul_rn(sig, sig);
-                double u[3], v[3];
-                for (int c = 0; c < 3; ++c) {
-                    u[c] = __fma_rn(z[2], S2[2][c], __fma_rn(z[1], S2[1][c], __dmul_rn(z[0], S2[0][c])));
-                    v[c] = __fma_rn(z[2], S[2][c], __fma_rn(z[1], S[1][c], __dmul_rn(z[0], S[0][c])));
-                }
-                const double d = __fma_rn(u[2], z[2], __fma_rn(u[1], z[1], __dmul_rn(u[0], z[0])));
-                const double c = __dadd_rn(det, __fma_rn(v[2], z[2], __fma_rn(v[1], z[1], __dmul_rn(v[0], z[0]))));
-                const double b = __dadd_rn(sig2, __fma_rn(z[2], z[2], __fma_rn(z[1], z[1], __dmul_rn(z[0], z[0]))));
-                const double a = __dsub_rn(sig2, kk);
-                const double apb = __dadd_rn(a, b);
-                const double cst = __dsub_rn(__dadd_rn(__dmul_rn(a, b), __dmul_rn(c, sig)), d);
-                double lam = 1.0, dlam = 1e6;
-                for (int it = 0; dlam > 1.0e-12 && it < 10; ++it) {
-                    const double lam0 = lam;
-                    const double l2 = __dmul_rn(lam, lam);
-                    const double num = __dadd_rn(__dsub_rn(__dsub_rn(__dmul_rn(l2, l2), __dmul_rn(apb, l2)), __dmul_rn(c, lam)), cst);
-                    const double den = __dsub_rn(__dsub_rn(__dmul_rn(4.0, __dmul_rn(l2, lam)), __dmul_rn(__dmul_rn(2.0, apb), lam)), c);
-                    lam = __dsub_rn(lam, __ddiv_rn(num, den));
-                    dlam = fabs(__dsub_rn(lam0, lam));
-                }
-                const double beta = __dsub_rn(lam, sig);
-                const double alpha = __dadd_rn(__dsub_rn(__dmul_rn(lam, lam), sig2), kk);
-                const double gamma = __dsub_rn(__dmul_rn(__dadd_rn(lam, sig), alpha), det);
-                double X[3];
-                for (int r = 0; r < 3; ++r) {
-                    double M[3];
-                    for (int cc = 0; cc < 3; ++cc)
-                        M[cc] = __dadd_rn(__dadd_rn(r == cc ? alpha : 0.0, __dmul_rn(beta, S[r][cc])), S2[r][cc]);
-                    X[r] = __fma_rn(M[2], z[2], __fma_rn(M[1], z[1], __dmul_rn(M[0], z[0])));
-                }
-                const double qn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(gamma, gamma), __dmul_rn(X[0], X[0])),
-                                                                 __dmul_rn(X[1], X[1])), __dmul_rn(X[2], X[2])));
-                qout[0] = __ddiv_rn(gamma, qn);
-                qout[1] = __ddiv_rn(X[0], qn);
-                qout[2] = __ddiv_rn(X[1], qn);
-                qout[3] = __ddiv_rn(X[2], qn);
-                if (gamma < 0.0) {
-                    for (int t = 0; t < 4; ++t) qout[t] = -qout[t];
-                }
-                for (int t = 0; t < 4; ++t) qs[t] = qout[t];
+            // S = B + B^T (symmetric: S[r][c] and S[c][r] are the same sum), then z
+            if (lane < 6) {
+                const int r = lane < 3 ? 0 : (lane < 5 ? 1 : 2);
+                const int c = lane < 3 ? lane : (lane < 5 ? lane - 2 : 2);
+                qi->S[lane] = __dadd_rn(qs[3 * r + c], qs[3 * c + r]);
+            } else if (lane < 9) {
+                qi->z[lane - 6] = qs[9 + lane - 6];
+            } else if (lane == 9) {
+                qi->mask = g2m;
+                qi->m = m;
             }
-            __syncwarp();
-            // rotate each band normal by the quaternion (rotlib.quat_vectorL1N, p = 1) and take
-            // its dot product with the pole (one band per lane)
-            if (lane < m) {
-                const double* vv = bq + 3 * lane;
-                const double* pp = pq + 3 * lane;
-                const double w0 = qs[0], r0 = qs[1], r1 = qs[2], r2 = qs[3];
-                double t[3] = {__dsub_rn(__dmul_rn(r1, vv[2]), __dmul_rn(r2, vv[1])),
-                               __dsub_rn(__dmul_rn(r2, vv[0]), __dmul_rn(r0, vv[2])),
-                               __dsub_rn(__dmul_rn(r0, vv[1]), __dmul_rn(r1, vv[0]))};
-                for (int cc = 0; cc < 3; ++cc) t[cc] = __dadd_rn(t[cc], __dmul_rn(w0, vv[cc]));
-                const double t2[3] = {__dsub_rn(__dmul_rn(r1, t[2]), __dmul_rn(r2, t[1])),
-                                      __dsub_rn(__dmul_rn(r2, t[0]), __dmul_rn(r0, t[2])),
-                                      __dsub_rn(__dmul_rn(r0, t[1]), __dmul_rn(r1, t[0]))};
-                double sd = 0.0;
-                for (int cc = 0; cc < 3; ++cc)
-                    sd = __dadd_rn(sd, __dmul_rn(__dadd_rn(__dmul_rn(2.0, t2[cc]), vv[cc]), pp[cc]));
-                wq[lane] = sd;  // weights are no longer needed
-            }
-            __syncwarp();
-            if (lane == 0) {
-                mad = __ddiv_rn(np_sum(wq, m), (double)m);
-            }
-            __syncwarp();
-            if (g2) bdot = wq[slot];
-            for (int t = 0; t < 4; ++t) qout[t] = __shfl_sync(kFull, qout[t], 0);
-            mad = __shfl_sync(kFull, mad, 0);
+        } else if (lane == 0) {
+            qi->mask = 0;
+            qi->m = 0;
         }
     }
 
@@ -684,8 +620,6 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     if (lane < nb) {
         const int64_t e = p * nb + lane;
         o.polematch[e] = best_pm;
-        const double bc = bdot < -1.0 ? -1.0 : (bdot > 1.0 ? 1.0 : bdot);
-        o.bandfit[e] = __dmul_rn(acos(bc), kRadeg);
         if (o.bandfam) o.bandfam[e] = fam;
         if (o.bandrank) o.bandrank[e] = rank;
         if (o.polevalid) o.polevalid[e] = (uint8_t)best_pv;
@@ -695,9 +629,6 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     if (o.accn)
         for (int t = lane; t < nfam * nb; t += 32) o.accn[p * nfam * nb + t] = accn[t];
     if (lane == 0) {
-        for (int t = 0; t < 4; ++t) o.quat[4 * p + t] = qout[t];
-        const double mc = mad < -1.0 ? -1.0 : (mad > 1.0 ? 1.0 : mad);
-        o.fit[p] = __dmul_rn(acos(mc), kRadeg);
         o.cm[p] = cm2;
         o.nmatch[p] = best_n;
         for (int t = 0; t < 4; ++t) o.ij[4 * p + t] = bij[t];
@@ -761,6 +692,114 @@ __global__ void k_vote_thresholds(const double* __restrict__ angtab, const int32
     } else {
         cand[2 * t] = okey_float(lo);
         cand[2 * t + 1] = okey_float(hi);
+    }
+}
+
+
+// ---- the scalar QUEST solve (tripletvote.py:955-993), one thread per pattern so that every
+// float64 instruction carries a full warp of patterns ----
+__global__ void k_quest(const QuestInput* __restrict__ qin, int64_t n, double* __restrict__ quat) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const QuestInput& qi = qin[p];
+        double qout[4] = {1.0, 0.0, 0.0, 0.0};
+        if (qi.m >= 3) {
+            const double S[3][3] = {{qi.S[0], qi.S[1], qi.S[2]}, {qi.S[1], qi.S[3], qi.S[4]}, {qi.S[2], qi.S[4], qi.S[5]}};
+            const double z[3] = {qi.z[0], qi.z[1], qi.z[2]};
+            double S2[3][3];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c)
+                    S2[r][c] = __fma_rn(S[r][2], S[2][c], __fma_rn(S[r][1], S[1][c], __dmul_rn(S[r][0], S[0][c])));
+            const double det =
+                __dadd_rn(__dsub_rn(__dmul_rn(S[0][0], __dsub_rn(__dmul_rn(S[1][1], S[2][2]), __dmul_rn(S[1][2], S[2][1]))),
+                                    __dmul_rn(S[0][1], __dsub_rn(__dmul_rn(S[1][0], S[2][2]), __dmul_rn(S[1][2], S[2][0])))),
+                          __dmul_rn(S[0][2], __dsub_rn(__dmul_rn(S[1][0], S[2][1]), __dmul_rn(S[1][1], S[2][0]))));
+            const double kk = __dadd_rn(__dadd_rn(__dsub_rn(__dmul_rn(S[1][1], S[2][2]), __dmul_rn(S[1][2], S[2][1])),
+                                                  __dsub_rn(__dmul_rn(S[0][0], S[2][2]), __dmul_rn(S[0][2], S[2][0]))),
+                                        __dsub_rn(__dmul_rn(S[0][0], S[1][1]), __dmul_rn(S[1][0], S[0][1])));
+            const double sig = __dmul_rn(0.5, __dadd_rn(__dadd_rn(S[0][0], S[1][1]), S[2][2]));
+            const double sig2 = __dmul_rn(sig, sig);
+            double u[3], v[3];
+            for (int c = 0; c < 3; ++c) {
+                u[c] = __fma_rn(z[2], S2[2][c], __fma_rn(z[1], S2[1][c], __dmul_rn(z[0], S2[0][c])));
+                v[c] = __fma_rn(z[2], S[2][c], __fma_rn(z[1], S[1][c], __dmul_rn(z[0], S[0][c])));
+            }
+            const double d = __fma_rn(u[2], z[2], __fma_rn(u[1], z[1], __dmul_rn(u[0], z[0])));
+            const double c = __dadd_rn(det, __fma_rn(v[2], z[2], __fma_rn(v[1], z[1], __dmul_rn(v[0], z[0]))));
+            const double b = __dadd_rn(sig2, __fma_rn(z[2], z[2], __fma_rn(z[1], z[1], __dmul_rn(z[0], z[0]))));
+            const double a = __dsub_rn(sig2, kk);
+            const double apb = __dadd_rn(a, b);
+            const double cst = __dsub_rn(__dadd_rn(__dmul_rn(a, b), __dmul_rn(c, sig)), d);
+            double lam = 1.0, dlam = 1e6;
+            for (int it = 0; dlam > 1.0e-12 && it < 10; ++it) {
+                const double lam0 = lam;
+                const double l2 = __dmul_rn(lam, lam);
+                const double num = __dadd_rn(__dsub_rn(__dsub_rn(__dmul_rn(l2, l2), __dmul_rn(apb, l2)), __dmul_rn(c, lam)), cst);
+                const double den = __dsub_rn(__dsub_rn(__dmul_rn(4.0, __dmul_rn(l2, lam)), __dmul_rn(__dmul_rn(2.0, apb), lam)), c);
+                lam = __dsub_rn(lam, __ddiv_rn(num, den));
+                dlam = fabs(__dsub_rn(lam0, lam));
+            }
+            const double beta = __dsub_rn(lam, sig);
+            const double alpha = __dadd_rn(__dsub_rn(__dmul_rn(lam, lam), sig2), kk);
+            const double gamma = __dsub_rn(__dmul_rn(__dadd_rn(lam, sig), alpha), det);
+            double X[3];
+            for (int r = 0; r < 3; ++r) {
+                double M[3];
+                for (int cc = 0; cc < 3; ++cc)
+                    M[cc] = __dadd_rn(__dadd_rn(r == cc ? alpha : 0.0, __dmul_rn(beta, S[r][cc])), S2[r][cc]);
+                X[r] = __fma_rn(M[2], z[2], __fma_rn(M[1], z[1], __dmul_rn(M[0], z[0])));
+            }
+            const double qn = __dsqrt_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(gamma, gamma), __dmul_rn(X[0], X[0])),
+                                                             __dmul_rn(X[1], X[1])), __dmul_rn(X[2], X[2])));
+            qout[0] = __ddiv_rn(gamma, qn);
+            qout[1] = __ddiv_rn(X[0], qn);
+            qout[2] = __ddiv_rn(X[1], qn);
+            qout[3] = __ddiv_rn(X[2], qn);
+            if (gamma < 0.0)
+                for (int t = 0; t < 4; ++t) qout[t] = -qout[t];
+        }
+        for (int t = 0; t < 4; ++t) quat[4 * p + t] = qout[t];
+    }
+}
+
+// ---- per-band and mean fit (tripletvote.py:994-1018, rotlib.quat_vectorL1N with p = 1, and
+// the arccos of bandindex, :601-604), one thread per pattern ----
+__global__ void k_quest_fit(const QuestInput* __restrict__ qin, const float* __restrict__ norms,
+                            const int64_t* __restrict__ polematch, const double* __restrict__ pole64,
+                            const double* __restrict__ quat, int64_t n, int nb, double* __restrict__ fit,
+                            double* __restrict__ bandfit) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const QuestInput& qi = qin[p];
+        const int m = qi.m >= 3 ? qi.m : 0;
+        const double w0 = quat[4 * p], r0 = quat[4 * p + 1], r1 = quat[4 * p + 2], r2 = quat[4 * p + 3];
+        double dots[32];
+        int k = 0;
+        for (int j = 0; j < nb; ++j) {
+            double bd = -1.0;
+            if (m > 0 && ((qi.mask >> j) & 1u)) {
+                const float* f = norms + (p * nb + j) * 3;
+                const double vv[3] = {(double)f[0], (double)f[1], (double)f[2]};
+                const int64_t pm = polematch[p * nb + j];
+                const double* pp = pole64 + 3 * (pm > 0 ? pm : 0);
+                double t[3] = {__dsub_rn(__dmul_rn(r1, vv[2]), __dmul_rn(r2, vv[1])),
+                               __dsub_rn(__dmul_rn(r2, vv[0]), __dmul_rn(r0, vv[2])),
+                               __dsub_rn(__dmul_rn(r0, vv[1]), __dmul_rn(r1, vv[0]))};
+                for (int cc = 0; cc < 3; ++cc) t[cc] = __dadd_rn(t[cc], __dmul_rn(w0, vv[cc]));
+                const double t2[3] = {__dsub_rn(__dmul_rn(r1, t[2]), __dmul_rn(r2, t[1])),
+                                      __dsub_rn(__dmul_rn(r2, t[0]), __dmul_rn(r0, t[2])),
+                                      __dsub_rn(__dmul_rn(r0, t[1]), __dmul_rn(r1, t[0]))};
+                double sd = 0.0;
+                for (int cc = 0; cc < 3; ++cc)
+                    sd = __dadd_rn(sd, __dmul_rn(__dadd_rn(__dmul_rn(2.0, t2[cc]), vv[cc]), pp[cc]));
+                bd = sd;
+                dots[k++] = sd;
+            }
+            const double bc = bd < -1.0 ? -1.0 : (bd > 1.0 ? 1.0 : bd);
+            bandfit[p * nb + j] = __dmul_rn(acos(bc), kRadeg);
+        }
+        double mad = -1.0;
+        if (m > 0) mad = __ddiv_rn(np_sum(dots, m), (double)m);
+        const double mc = mad < -1.0 ? -1.0 : (mad > 1.0 ? 1.0 : mad);
+        fit[p] = __dmul_rn(acos(mc), kRadeg);
     }
 }
 
@@ -964,6 +1003,7 @@ extern "C" int ebsd_vote_plan_destroy(ebsd_vote_plan_t p) {
     cudaFree(p->d_cand);
     cudaFree(p->d_par);
     cudaFree(p->d_orig);
+    cudaFree(p->d_quest);
     delete p;
     return EBSD_OK;
 }
@@ -1010,19 +1050,57 @@ extern "C" int ebsd_band_index(ebsd_vote_plan_t p, const float* d_norms, const f
     A.simpleq = p->simpleq;
     std::memcpy(A.lut, p->lut, 27);
     A.lut[27] = 0;
-    A.norms = d_norms;
-    A.inten = d_intensity;
-    A.n = n;
-    A.out = *out;
+    // patterns go in pieces of at most kQuestChunk; the hand-over scratch is allocated on the
+    // first call (make it outside a CUDA-graph capture) and reused
+    constexpr int64_t kQuestChunk = 1 << 20;
+    const int64_t cap = std::min<int64_t>(n, kQuestChunk);
+    if (cap > p->quest_cap) {
+        cudaFree(p->d_quest);
+        p->d_quest = nullptr;
+        p->quest_cap = 0;
+        EBSD_CUDA_TRY(cudaMalloc(&p->d_quest, (size_t)cap * sizeof(QuestInput)));
+        p->quest_cap = cap;
+    }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_band_index, kWarps * 32, smem);
     if (per_sm < 1) per_sm = 1;
-    const int64_t need = (n + kWarps - 1) / kWarps;
-    const int blocks = (int)std::min<int64_t>(need, (int64_t)sms * per_sm);
-    k_band_index<<<blocks, kWarps * 32, smem, (cudaStream_t)stream>>>(A);
-    return launch_status();
+    const int nf = p->nfam;
+    for (int64_t off = 0; off < n; off += kQuestChunk) {
+        const int64_t cnt = std::min<int64_t>(kQuestChunk, n - off);
+        A.norms = d_norms + off * nBands * 3;
+        A.inten = d_intensity ? d_intensity + off * nBands : nullptr;
+        A.n = cnt;
+        ebsd_index_out o = *out;
+        o.quat += 4 * off;
+        o.fit += off;
+        o.cm += off;
+        o.polematch += off * nBands;
+        o.nmatch += off;
+        o.ij += 4 * off;
+        o.acc_correct += off;
+        o.bandfit += off * nBands;
+        if (o.accw) o.accw += off * nf * nBands;
+        if (o.accn) o.accn += off * nf * nBands;
+        if (o.bandfam) o.bandfam += off * nBands;
+        if (o.bandrank) o.bandrank += off * nBands;
+        if (o.polevalid) o.polevalid += off * nBands;
+        A.out = o;
+        A.quest = (QuestInput*)p->d_quest;
+        const int64_t need = (cnt + kWarps - 1) / kWarps;
+        const int blocks = (int)std::min<int64_t>(need, (int64_t)sms * per_sm);
+        k_band_index<<<blocks, kWarps * 32, smem, (cudaStream_t)stream>>>(A);
+        int rc = launch_status();
+        if (rc != EBSD_OK) return rc;
+        const int qb = (int)std::min<int64_t>((cnt + 127) / 128, (int64_t)sms * 16);
+        k_quest<<<qb, 128, 0, (cudaStream_t)stream>>>(A.quest, cnt, o.quat);
+        if ((rc = launch_status()) != EBSD_OK) return rc;
+        k_quest_fit<<<qb, 128, 0, (cudaStream_t)stream>>>(A.quest, A.norms, o.polematch, p->d_pole64, o.quat, cnt,
+                                                         nBands, o.fit, o.bandfit);
+        if ((rc = launch_status()) != EBSD_OK) return rc;
+    }
+    return EBSD_OK;
 }
 
 extern "C" int ebsd_band_intensity(const float* d_max, const float* d_normmax, const float* d_theta,
