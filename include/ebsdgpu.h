@@ -314,7 +314,11 @@ int ebsd_vote_plan_destroy(ebsd_vote_plan_t plan);
 
 /* d_norms [n][nBands][3] float32 unit band normals (ebsd_radon2pole); d_intensity [n][nBands]
  * float32 band weights (ebsd_band_intensity) or NULL for all ones.  nBands 1..32.  One warp
- * per pattern; no allocation, no host synchronisation (CUDA-graph capturable). */
+ * per pattern for the vote and the band assignment, then one thread per pattern for the QUEST
+ * solve and the fits, through a plan-owned hand-over buffer of up to 2^20 patterns: the first
+ * call allocates it (make that call outside a CUDA-graph capture); later calls allocate
+ * nothing and do not synchronise with the host.  One plan per stream: calls on one plan from
+ * different streams at the same time share that buffer. */
 int ebsd_band_index(ebsd_vote_plan_t plan, const float* d_norms, const float* d_intensity, int64_t n,
                     int32_t nBands, const ebsd_index_out* out, void* stream);
 
