@@ -426,8 +426,20 @@ def main():
         for _ in range(e2e_steps):
             e2e_step()
         dt = time.perf_counter() - t0
+        in_place = plan.host_input_in_place()
+        # the same with the input staged by copy engines instead of read in place
+        plan.set_host_input(0)
+        e2e_step()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        dt_copy = time.perf_counter() - t0
+        plan.set_host_input(-1)
         e2e = {"value": N * e2e_steps / dt * world, "unit": "patterns/s", "h2d_bytes_per_step": N * H * W,
-               "d2h_bytes_per_step": N * nB * 41}
+               "d2h_bytes_per_step": N * nB * 41,
+               "input_path": ("pinned patterns read in place by the kernels over NVLink-C2C (every byte crosses "
+                              "the link each step)") if in_place else "pinned patterns staged by copy engines",
+               "copy_engine_value": N * e2e_steps / dt_copy * world}
         del host, hout
 
     # the other methods on the same device-resident input, for the batched-vs-plain comparison

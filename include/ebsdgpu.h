@@ -123,6 +123,16 @@ int ebsd_find_bands(ebsd_plan_t plan, int method, int dtype, const void* d_pats,
 int ebsd_find_bands_host(ebsd_plan_t plan, int method, int dtype, const void* h_pats,
                          int64_t n, const ebsd_bands* h_out, int64_t chunk);
 
+/* How ebsd_find_bands_host[_records] moves PINNED host input to the GPU.  -1 (default):
+ * the kernels read it in place over the CPU-GPU link when the device uses the host's page
+ * tables (GB300's NVLink-C2C), else copy engines stage it chunk by chunk; 0: always stage
+ * with copies; 1: always read in place.  Either way every input byte crosses the link once
+ * per call.  Pageable input is always staged through pinned buffers. */
+int ebsd_plan_set_host_input(ebsd_plan_t plan, int mode);
+
+/* 1 when pinned host input is read in place under the plan's current mode, 0 when copied. */
+int ebsd_plan_host_input_in_place(ebsd_plan_t plan);
+
 /* Number of kernel launches the last ebsd_find_bands / ebsd_find_bands_host call on this
  * plan issued (for launch accounting by benchmarks). */
 int64_t ebsd_last_launch_count(ebsd_plan_t plan);

@@ -89,6 +89,10 @@ def load():
         lib.ebsd_last_launch_count.restype = C.c_int64
         lib.ebsd_plan_autotune.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, P, C.POINTER(C.c_int)]
         lib.ebsd_plan_autotune.restype = C.c_int
+        lib.ebsd_plan_set_host_input.argtypes = [P, C.c_int]
+        lib.ebsd_plan_set_host_input.restype = C.c_int
+        lib.ebsd_plan_host_input_in_place.argtypes = [P]
+        lib.ebsd_plan_host_input_in_place.restype = C.c_int
         lib.ebsd_plan_set_patterns_per_pass.argtypes = [P, C.c_int]
         lib.ebsd_plan_set_patterns_per_pass.restype = C.c_int
         lib.ebsd_strerror.argtypes = [C.c_int]
@@ -167,6 +171,16 @@ class DevicePlan:
     def set_patterns_per_pass(self, ppp: int):
         """Pin the fused kernel's patterns per block pass (1, 2, 4, 8; 0 = rule)."""
         check(self._lib.ebsd_plan_set_patterns_per_pass(self.handle, int(ppp)), "ebsd_plan_set_patterns_per_pass")
+
+    def set_host_input(self, mode: int):
+        """Pinned host input: -1 read in place on coherent CPU-GPU links (default), 0 copy, 1 in place."""
+        check(self._lib.ebsd_plan_set_host_input(self.handle, int(mode)), "ebsd_plan_set_host_input")
+
+    def host_input_in_place(self) -> bool:
+        r = self._lib.ebsd_plan_host_input_in_place(self.handle)
+        if r < 0:
+            check(r, "ebsd_plan_host_input_in_place")
+        return r == 1
 
     def autotune(self, pats_ptr: int, dtype: int, n: int, method, stream=0) -> int:
         """Time the record-identical kernel variants on a device-resident sample and keep the

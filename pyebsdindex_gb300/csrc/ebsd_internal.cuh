@@ -100,6 +100,9 @@ struct ebsd_plan_s {
     // chunk buffers the filler thread fills
     void* h_pin[3] = {nullptr, nullptr, nullptr};
     size_t h_pin_bytes = 0;
+    // pinned host input: -1 read in place when the GPU reaches host memory through the host
+    // page tables (NVLink-C2C), else copy; 0 always copy; 1 always read in place
+    int host_input_mode = -1;
     // pinned staging of records for pageable output arrays (two chunk slots)
     void* h_outpin[2] = {nullptr, nullptr};
     size_t h_outpin_bytes = 0;

@@ -255,11 +255,23 @@ int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src,
         return EBSD_OK;
     };
     const bool ring = !(src.mem && src.mem_pinned);
+    // pinned input read in place by the kernels over the CPU-GPU link (no staging copy) when
+    // the device uses the host page tables (GB300's NVLink-C2C) or the caller asked for it
+    const char* in_place = nullptr;
+    if (!ring && p->host_input_mode != 0) {
+        int coherent = 0;
+        cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, p->device);
+        cudaPointerAttributes pa;
+        if ((p->host_input_mode == 1 || coherent) && cudaPointerGetAttributes(&pa, src.mem) == cudaSuccess &&
+            pa.devicePointer)
+            in_place = (const char*)pa.devicePointer;
+        cudaGetLastError();
+    }
     const bool direct_out = !sink && is_pinned(h_out->max) && is_pinned(h_out->normmax) &&
                             is_pinned(h_out->maxloc) && is_pinned(h_out->avemax) && is_pinned(h_out->aveloc) &&
                             is_pinned(h_out->width) && is_pinned(h_out->theta) && is_pinned(h_out->rho) &&
                             is_pinned(h_out->valid);
-    if ((rc = regrow(p->h_in_dev, 2, &p->h_in_bytes, in_bytes, false)) != EBSD_OK) return rc;
+    if (!in_place && (rc = regrow(p->h_in_dev, 2, &p->h_in_bytes, in_bytes, false)) != EBSD_OK) return rc;
     if ((rc = regrow(p->h_out_dev, 2, &p->h_out_bytes, out_bytes, false)) != EBSD_OK) return rc;
     if (ring && (rc = regrow(p->h_pin, 3, &p->h_pin_bytes, in_bytes, true)) != EBSD_OK) return rc;
     if (!direct_out && (rc = regrow(p->h_outpin, 2, &p->h_outpin_bytes, out_bytes, true)) != EBSD_OK) return rc;
@@ -343,16 +355,22 @@ int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src,
             }
             host_in = p->h_pin[sl];
         }
-        if (cudaMemcpyAsync(p->h_in_dev[ds], host_in, (size_t)cnt * src.pat_bytes, cudaMemcpyHostToDevice, st) !=
-                cudaSuccess ||
-            cudaEventRecord(copied[sl], st) != cudaSuccess ||
-            (k > 0 && cudaStreamWaitEvent(st, done_compute[ds ^ 1], 0) != cudaSuccess)) {
+        const void* kin = p->h_in_dev[ds];
+        if (in_place) {
+            kin = in_place + (size_t)s0 * src.pat_bytes;
+        } else if (cudaMemcpyAsync(p->h_in_dev[ds], host_in, (size_t)cnt * src.pat_bytes, cudaMemcpyHostToDevice,
+                                   st) != cudaSuccess ||
+                   cudaEventRecord(copied[sl], st) != cudaSuccess) {
+            rc = EBSD_E_LAUNCH;
+            break;
+        }
+        if (k > 0 && cudaStreamWaitEvent(st, done_compute[ds ^ 1], 0) != cudaSuccess) {
             rc = EBSD_E_LAUNCH;
             break;
         }
         const size_t nb = (size_t)cnt * nB;
         const ebsd_bands dev = chunk_fields((char*)p->h_out_dev[ds], nb);
-        rc = run_chunk(p, method, dtype, p->h_in_dev[ds], cnt, &dev, 0, st, &p->last_launches);
+        rc = run_chunk(p, method, dtype, kin, cnt, &dev, 0, st, &p->last_launches);
         if (rc != EBSD_OK) break;
         cudaEventRecord(done_compute[ds], st);
         ebsd_bands dst;
@@ -706,6 +724,22 @@ int ebsd_find_bands_file_records(ebsd_plan_t p, int method, const char* path, in
     rc = host_pipeline(p, method, dtype, src, n, &none, chunk, &rs);
     close(src.fd);
     return rc;
+}
+
+int ebsd_plan_set_host_input(ebsd_plan_t p, int mode) {
+    if (!p || mode < -1 || mode > 1) return EBSD_E_ARG;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    p->host_input_mode = mode;
+    return EBSD_OK;
+}
+
+int ebsd_plan_host_input_in_place(ebsd_plan_t p) {
+    if (!p) return EBSD_E_ARG;
+    if (p->host_input_mode != -1) return p->host_input_mode;
+    int coherent = 0;
+    if (cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, p->device) != cudaSuccess)
+        return EBSD_E_DEVICE;
+    return coherent ? 1 : 0;
 }
 
 int ebsd_plan_set_patterns_per_pass(ebsd_plan_t p, int ppp) {

@@ -58,3 +58,24 @@ def test_file_sets_up_the_plan_for_its_size(cuda, tmp_path):
     assert np.array_equal(got["max"], bd.find_bands(pats)["max"])
     with pytest.raises(RuntimeError, match="pattern file"):
         bd.find_bands_file(os.path.join(tmp_path, "missing.up1"))
+
+
+@pytest.mark.parametrize("method", ["fused", "plain"])
+def test_pinned_input_in_place_or_copied(cuda, method):
+    """Pinned host input read in place by the kernels (the default on a coherent CPU-GPU link)
+    or staged by copies gives the same records as device input."""
+    import torch
+    from pyebsdindex_gb300 import _lib
+    pats = syn.make_patterns(1500, 80, 80, seed=54, noise_frac=0.1)[0]
+    bd = plan()
+    want = bd.find_bands(torch.from_numpy(pats).cuda(), method=method)
+    pinned = torch.from_numpy(pats).pin_memory().numpy()
+    dp = bd._device_plan()
+    for mode in (-1, 0, 1):
+        dp.set_host_input(mode)
+        got = dp.find_bands_host_records(pinned, method, bd.dataType, chunk=400)
+        for f in FIELDS:
+            assert got[f].tobytes() == want[f].tobytes(), (mode, f)
+    dp.set_host_input(-1)
+    with pytest.raises(RuntimeError, match="invalid argument"):
+        dp.set_host_input(2)
