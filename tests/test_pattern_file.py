@@ -19,7 +19,8 @@ def ref():
 
 def make_file(tmp_path, name, n, h, w, dtype, version, ncols=None, nrows=None, step=(1.5, 2.25)):
     from pyebsdindex_gb300.ebsd_pattern import write_up
-    rng = np.random.default_rng(hash(name) & 0xffff)
+    import zlib
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
     hi = 256 if dtype == np.uint8 else 4096
     pats = rng.integers(0, hi, size=(n, h, w)).astype(dtype)
     path = os.path.join(tmp_path, name)
@@ -37,7 +38,6 @@ def test_reader_matches_reference(tmp_path, ref, built_lib, case):
     name, n, h, w, dt, ver, nc, nr = case
     path, pats = make_file(tmp_path, name, n, h, w, dt, ver, nc, nr)
     mine = ep.get_pattern_file_obj(path)
-    theirs = ref_file = None
     import importlib
     rp = importlib.import_module("pyebsdindex.ebsd_pattern")
     theirs = rp.get_pattern_file_obj(path)

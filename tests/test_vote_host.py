@@ -113,3 +113,16 @@ def test_wrapped_phases_drive_the_reference_indexer(monkeypatch):
         got, _ = idx2._indexbandsphase(recs, norms)
     for f in ("quat", "fit", "cm", "nmatch", "phase", "pq", "iq"):
         assert np.array_equal(got[f], want[f]), f
+
+
+def test_record_offsets_check_the_field_types():
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300 import _lib
+    dt = pg.record_dtype()
+    offs = _lib.record_offsets(dt)
+    assert [offs[i] for i in range(9)] == [dt.fields[f][1] for f in _lib.BAND_FIELDS]
+    bad = np.dtype([("max", np.float64), ("normmax", np.float32), ("maxloc", np.float32, (2,)),
+                    ("avemax", np.float32), ("aveloc", np.float32, (2,)), ("width", np.float32),
+                    ("theta", np.float32), ("rho", np.float32), ("valid", np.int8)])
+    with pytest.raises(TypeError, match="max"):
+        _lib.record_offsets(bad)
