@@ -247,15 +247,17 @@ def time_indexing(outs, bd, N, stream, with_cpu, detect_ms):
         "kernels": ["k_radon2pole", "k_band_intensity", "k_band_index"],
     }
     if with_cpu:
-        from oracle import vote_oracle as vo  # the CPU leg: the numpy restatement of bandindex
-        m = 200
+        from oracle import votecport  # the CPU leg: the C/OpenMP restatement of bandindex
+        m = min(N, 65536)
         nrm = normals[:m].cpu().numpy()
         w = adj[:m].cpu().numpy()
+        votecport.bandindex(lib, params, nrm[:1024], w[:1024])  # threads up
         t0 = time.perf_counter()
-        vo.bandindex(lib, params, nrm, w)
+        votecport.bandindex(lib, params, nrm, w)
         dt = time.perf_counter() - t0
-        res["cpu_baseline"] = {"value": m / dt, "unit": "patterns/s", "cores": 1, "kind": "port",
-                               "sample": f"bandindex of the first {m} patterns' records, numpy restatement, 1 thread"}
+        res["cpu_baseline"] = {"value": m / dt, "unit": "patterns/s", "cores": votecport.threads(), "kind": "port",
+                               "sample": f"bandindex of the first {m} patterns' records, C/OpenMP restatement, "
+                                         f"all host threads"}
     return res
 
 
