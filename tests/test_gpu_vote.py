@@ -260,3 +260,34 @@ def test_many_matches_per_triplet_take_the_ordered_fallback(cuda):
     same &= rows_equal(got["accn"], mid["accn"])
     assert same.mean() >= 0.9
     np.testing.assert_allclose(got["accw"][same], mid["accw"][same], rtol=1e-5, atol=1e-4)
+
+
+def test_many_bands_against_the_c_port(cuda):
+    """24 bands per pattern (the kernel's per-warp tables grow with nBands): seeded FCC normals
+    under random rotations with 0.3 deg of noise, against the C/OpenMP restatement of bandindex
+    (oracle/c/votecpu.c, libm arccos): nMatch equal on every pattern, pole match and band pair
+    on at least 98 %, quaternions within 1e-7 there."""
+    from oracle import votecport
+    lib, params, _, _ = load("vote_fcc_syn")
+    rng = np.random.default_rng(77)
+    poles = np.asarray(lib["polesCart"])
+    n, nb = 120, 24
+    norms = np.zeros((n, nb, 3), np.float32)
+    for p in range(n):
+        q = rng.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        pick = rng.choice(poles.shape[0], size=nb, replace=False)
+        v = (R @ poles[pick].T).T + rng.normal(scale=np.deg2rad(0.3), size=(nb, 3))
+        norms[p] = v / np.linalg.norm(v, axis=1, keepdims=True)
+    inten = np.sort(rng.uniform(0.3, 1.0, (n, nb)).astype(np.float32), axis=1)[:, ::-1].copy()
+    got = run(indexer(lib, params), norms, inten)
+    want = dict(zip(("quat", "fit", "cm", "polematch", "nmatch", "ij", "acc_correct", "bandfit"),
+                    votecport.bandindex(lib, params, norms, inten)))
+    assert np.array_equal(got["nmatch"], want["nmatch"])
+    same = rows_equal(got["polematch"], want["polematch"]) & rows_equal(got["ij"], want["ij"])
+    assert same.mean() >= 0.98, same.mean()
+    np.testing.assert_allclose(got["quat"][same], want["quat"][same], atol=1e-7)
