@@ -10,6 +10,7 @@
 // row-major, uint8 for .up1, uint16 for .up2.
 #include "ebsd_internal.cuh"
 
+#include <cctype>
 #include <cerrno>
 #include <cmath>
 #include <cstring>
