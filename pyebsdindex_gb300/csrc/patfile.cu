@@ -63,7 +63,7 @@ int up_parse_header(const char* path, int bitdepth, ebsd_up_info* info) {
     else return EBSD_E_ARG;
     const int fd = open(path, O_RDONLY);
     if (fd < 0) return EBSD_E_IO;
-    struct stat st;
+    struct stat st {};
     unsigned char h[42];
     std::memset(h, 0, sizeof(h));
     int rc = EBSD_OK;
