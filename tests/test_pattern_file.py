@@ -83,3 +83,39 @@ def test_unreadable_files_raise(tmp_path, built_lib):
         ep.get_pattern_file_obj(bad)
     with pytest.raises(RuntimeError, match="pattern file"):
         ep.get_pattern_file_obj(os.path.join(tmp_path, "missing.up1"))
+
+
+@pytest.mark.parametrize("version", [1, 3])
+def test_writer_header_matches_reference_writer(tmp_path, ref, built_lib, version):
+    """write_up lays out the header as the reference's UPFile.write_header (ebsd_pattern.py:573-620)."""
+    import importlib
+    from pyebsdindex_gb300.ebsd_pattern import write_up
+    rp = importlib.import_module("pyebsdindex_gb300.ebsd_pattern")
+    pats = np.arange(6 * 8 * 10, dtype=np.uint8).reshape(6, 8, 10)
+    mine = os.path.join(tmp_path, "m.up1")
+    write_up(mine, pats, nCols=3, nRows=2, version=version, xStep=0.5, yStep=0.25)
+    refmod = importlib.import_module("pyebsdindex.ebsd_pattern")
+    theirs = os.path.join(tmp_path, "t.up1")
+    f = refmod.UPFile(theirs)
+    f.version, f.patternW, f.patternH = version, 10, 8
+    f.nCols, f.nRows, f.xStep, f.yStep = 3, 2, 0.5, 0.25
+    f.extraPatterns, f.hexflag = 0, 0
+    f.write_header(writeBlank=False)
+    head = 16 if version == 1 else 42
+    assert open(mine, "rb").read()[:head] == open(theirs, "rb").read()[:head]
+    assert rp.get_pattern_file_obj(mine).read_data(patStartCount=[0, -1], returnArrayOnly=True)[0].tobytes() \
+        == pats.tobytes()
+
+
+def test_other_extension_with_bitdepth(tmp_path, built_lib):
+    import shutil
+    from pyebsdindex_gb300 import ebsd_pattern as ep
+    path, pats = make_file(tmp_path, "f.up2", 12, 9, 11, np.uint16, 3, 4, 3)
+    other = os.path.join(tmp_path, "scan.dat")
+    shutil.copyfile(path, other)
+    f = ep.UPFile(other)
+    f.read_header(bitdepth=16)
+    got, _ = f.read_data(patStartCount=[0, -1], returnArrayOnly=True)
+    assert got.dtype == np.uint16 and got.tobytes() == pats.tobytes()
+    with pytest.raises(RuntimeError, match="invalid argument"):
+        ep.UPFile(other).read_header()
