@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-index", action="store_true", help="skip timing the device indexing after detection")
     ap.add_argument("--no-file", action="store_true", help="skip timing detection streamed from a UP1 file")
     ap.add_argument("--file-patterns", type=int, default=262_144, help="patterns in the UP1 file timed")
+    ap.add_argument("--lambda-scan", action="store_true",
+                    help="also time NLPAR's lambda optimisation on a 400x500 scan of 80x80 patterns")
     return ap.parse_args()
 
 
@@ -160,6 +162,29 @@ def cpu_baseline(pool, sample, impl_kind):
 
 
 VOTE_LIBRARY = os.path.join(ROOT, "tests", "golden", "vote_fcc_orient.npz")
+
+
+def time_lambda(dev):
+    """NLPAR.opt_lambda_array (the reference's opt_lambda_cpu, nlpar_cpu.py:94-155) on a 400x500
+    scan of 80x80 patterns held on the device as float32: per-tile sigma and neighbour
+    distances, then three bounded Nelder-Mead searches on the device objective.  The scan is
+    a seeded 50x50 Voronoi scan tiled 8x10."""
+    import torch
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300 import synthetic as syn
+    small, _ = syn.voronoi_scan(50, 50, ngrains=40, h=H, w=W, seed=11)
+    grid = np.tile(small.reshape(50, 50, H, W), (8, 10, 1, 1)).reshape(400 * 500, H, W)
+    d = torch.from_numpy(grid).to(dev).to(torch.float32)
+    nl = pg.NLPAR(lam=0.7, searchradius=3)
+    nl.opt_lambda_array(d[:2500], 50, 50)  # warm-up (kernels, pools)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lam = nl.opt_lambda_array(d, 400, 500)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return {"seconds": dt, "patterns_per_s": 400 * 500 / dt, "lambda": [float(x) for x in lam],
+            "workload": "opt_lambda on a 400x500 scan of 80x80 patterns (device float32), target weights "
+                        "0.5 / 0.34 / 0.25"}
 
 
 def time_file(bd, plan, method, pool, n):
@@ -467,6 +492,10 @@ def main():
     if rank == 0 and not args.no_file:
         file_e2e = time_file(bd, plan, method, pool, args.file_patterns)
 
+    nlpar_lambda = None
+    if rank == 0 and args.lambda_scan:
+        nlpar_lambda = time_lambda(dev)
+
     indexing = None
     if not args.no_index:
         indexing = time_indexing(outs, bd, N, stream, rank == 0 and world == 1 and not args.no_cpu,
@@ -493,6 +522,7 @@ def main():
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
+            "nlpar_lambda": nlpar_lambda,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))
