@@ -58,11 +58,12 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr double kRadeg = 57.29577951308232;  // 180 / pi
 constexpr float kRadegF = 57.29577951308232f;
 
-// What the warp hands to the scalar QUEST solve for one pattern: S = B + B^T (upper triangle
-// S00 S01 S02 S11 S12 S22), z, and the bands in the fit (bit j: band j; m of them; m < 3: no fit).
+// What the warp hands to the QUEST solve for one pattern: the bands chosen for the weights
+// (bit j: band j) and the number of matched bands; k_quest adds the bands in the fit (mask, m;
+// m < 3: no fit) for k_quest_fit.
 struct QuestInput {
-    double S[6];
-    double z[3];
+    uint32_t sel;
+    int32_t ngood;
     uint32_t mask;
     int32_t m;
 };
@@ -191,9 +192,7 @@ __host__ __device__ inline size_t align8(size_t words) { return (words + 1) & ~s
 
 // 4-byte words of one warp's region
 __host__ __device__ inline size_t warp_words(int nb, int nfam) {
-    size_t w = 3 * nb + nb + nb * nb + 2 * nfam * nb + nb + nb + 64 + kList;
-    w = align8(w);
-    return w + 2 * (7 * size_t(nb) + 12);  // float64 QUEST scratch: weights, normals, poles, B and z
+    return align8(3 * size_t(nb) + nb + nb * nb + 2 * size_t(nfam) * nb + nb + nb + 64 + kList);
 }
 
 __host__ __device__ inline size_t block_words(int ntrip, int npoles) {
@@ -233,7 +232,6 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
     int* bfam = rarg + nb;               // [nb]
     float* fscr = (float*)(bfam + nb);   // [64]
     int* mlist = (int*)(fscr + 64);      // [kList]
-    double* dscr = (double*)(w + align8(3 * nb + nb + nb * nb + 2 * nfam * nb + nb + nb + 64 + kList));
     const unsigned lt_mask = (1u << lane) - 1u;
 
     for (int t = lane; t < 3 * nb; t += 32) bn[t] = A.norms[p * 3 * nb + t];
@@ -495,14 +493,12 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
         }
     }
 
-    // ---- QUEST weights, tripletvote.py:856-901 ----
+    // ---- QUEST weights, tripletvote.py:856-901: the band selection here (its scores need the
+    // votes); the float64 weights, B and z and the solve in k_quest, one thread per pattern ----
     const bool good = lane < nb && best_pv != 0;
     const unsigned goodm = __ballot_sync(kFull, good);
     const int ngood = __popc(goodm);
-    double* wq = dscr;             // [nb]
-    double* bq = dscr + nb;        // [nb][3]
-    double* pq = dscr + 4 * nb;    // [nb][3]
-    float wsel = 0.0f;
+    unsigned selm = 0;
     if (ngood >= 3) {
         float sc = -1.0f;
         if (!A.simpleq) {
@@ -520,82 +516,12 @@ __device__ void index_pattern(const VoteArgs& A, int64_t p, int lane, const floa
             pos += (s < sc) || (s == sc && c < lane);
         }
         const int nfit = ngood < 6 ? ngood : 6;
-        const double wd = (lane < nb && (nb - 1 - pos) < nfit) ? (double)inten[lane] : 0.0;
-        if (lane < nb) wq[lane] = wd;
-        __syncwarp();
-        double tot = 0.0;
-        if (lane == 0) tot = np_sum(wq, nb);
-        tot = __shfl_sync(kFull, tot, 0);
-        wsel = __double2float_rn(__ddiv_rn(wd, tot));  // stored as float32, tripletvote.py:899
+        selm = __ballot_sync(kFull, lane < nb && (nb - 1 - pos) < nfit);
     }
-    __syncwarp();
-
-    // ---- QUEST fit, tripletvote.py:903-1020: the weighted B matrix and z vector here (lanes),
-    // the scalar solve and the fits in k_quest / k_quest_fit (one thread per pattern) ----
-    {
-        if (lane < nb) wq[lane] = (double)wsel;
-        __syncwarp();
-        double tot = 0.0;
-        if (lane == 0) tot = np_maximum(np_sum(wq, nb), 1e-12);
-        tot = __shfl_sync(kFull, tot, 0);
-        __syncwarp();
-        const double wn = __ddiv_rn((double)wsel, tot);
-        const bool g2 = lane < nb && wn > 1.0e-7;
-        const unsigned g2m = __ballot_sync(kFull, g2);
-        const int m = __popc(g2m);
+    if (lane == 0) {
         QuestInput* qi = A.quest + p;
-        if (m >= 3) {
-            const int slot = __popc(g2m & lt_mask);
-            if (g2) {
-                wq[slot] = wn;
-                const double* pc = A.pole64 + 3 * (size_t)(best_pm > 0 ? best_pm : 0);
-                for (int c = 0; c < 3; ++c) {
-                    bq[3 * slot + c] = (double)bn[3 * lane + c];
-                    pq[3 * slot + c] = pc[c];
-                }
-            }
-            __syncwarp();
-            double ws = 0.0;
-            if (lane == 0) ws = np_sum(wq, m);
-            ws = __shfl_sync(kFull, ws, 0);
-            if (lane < m) wq[lane] = __ddiv_rn(wq[lane], ws);
-            __syncwarp();
-            // B = (w b)^T p (lanes 0-8, one entry each) and z = sum_k w_k (b_k x p_k) (lanes
-            // 9-11, one component each), every entry in the reference's operation order
-            double* qs = dscr + 7 * nb;  // [12] B row-major, then z
-            if (lane < 9) {
-                const int r = lane / 3, c = lane - 3 * (lane / 3);
-                double acc = __dmul_rn(__dmul_rn(wq[0], bq[r]), pq[c]);
-                for (int k = 1; k < m; ++k) acc = __fma_rn(__dmul_rn(wq[k], bq[3 * k + r]), pq[3 * k + c], acc);
-                qs[lane] = acc;
-            } else if (lane < 12) {
-                const int c = lane - 9, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-                double zc = 0.0;
-                for (int k = 0; k < m; ++k) {
-                    const double* a = bq + 3 * k;
-                    const double* b = pq + 3 * k;
-                    const double cr = __dsub_rn(__dmul_rn(a[c1], b[c2]), __dmul_rn(a[c2], b[c1]));
-                    const double v = __dmul_rn(wq[k], cr);
-                    zc = k == 0 ? v : __dadd_rn(zc, v);
-                }
-                qs[lane] = zc;
-            }
-            __syncwarp();
-            // S = B + B^T (symmetric: S[r][c] and S[c][r] are the same sum), then z
-            if (lane < 6) {
-                const int r = lane < 3 ? 0 : (lane < 5 ? 1 : 2);
-                const int c = lane < 3 ? lane : (lane < 5 ? lane - 2 : 2);
-                qi->S[lane] = __dadd_rn(qs[3 * r + c], qs[3 * c + r]);
-            } else if (lane < 9) {
-                qi->z[lane - 6] = qs[9 + lane - 6];
-            } else if (lane == 9) {
-                qi->mask = g2m;
-                qi->m = m;
-            }
-        } else if (lane == 0) {
-            qi->mask = 0;
-            qi->m = 0;
-        }
+        qi->sel = selm;
+        qi->ngood = ngood;
     }
 
     // ---- vote confidence of the matched bands, tripletvote.py:2057-2075 ----
@@ -698,13 +624,70 @@ __global__ void k_vote_thresholds(const double* __restrict__ angtab, const int32
 
 // ---- the scalar QUEST solve (tripletvote.py:955-993), one thread per pattern so that every
 // float64 instruction carries a full warp of patterns ----
-__global__ void k_quest(const QuestInput* __restrict__ qin, int64_t n, double* __restrict__ quat) {
+__global__ void k_quest(QuestInput* __restrict__ qin, int64_t n, int nb, const float* __restrict__ norms,
+                        const float* __restrict__ inten, const int64_t* __restrict__ polematch,
+                        const double* __restrict__ pole64, double* __restrict__ quat) {
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const QuestInput& qi = qin[p];
+        QuestInput& qi = qin[p];
         double qout[4] = {1.0, 0.0, 0.0, 0.0};
-        if (qi.m >= 3) {
-            const double S[3][3] = {{qi.S[0], qi.S[1], qi.S[2]}, {qi.S[1], qi.S[3], qi.S[4]}, {qi.S[2], qi.S[4], qi.S[5]}};
-            const double z[3] = {qi.z[0], qi.z[1], qi.z[2]};
+        // band weights (tripletvote.py:885-899): the chosen bands' intensities normalised to
+        // sum one, stored as float32
+        float wsel[32];
+        double wq[32];
+        for (int j = 0; j < nb; ++j) {
+            const float it = inten ? inten[p * nb + j] : 1.0f;
+            wq[j] = (qi.ngood >= 3 && ((qi.sel >> j) & 1u)) ? (double)it : 0.0;
+        }
+        double tot = np_sum(wq, nb);
+        for (int j = 0; j < nb; ++j) wsel[j] = qi.ngood >= 3 ? __double2float_rn(__ddiv_rn(wq[j], tot)) : 0.0f;
+        // the fit's weights (tripletvote.py:912-914, 940-947)
+        for (int j = 0; j < nb; ++j) wq[j] = (double)wsel[j];
+        tot = np_maximum(np_sum(wq, nb), 1e-12);
+        double wn[32];
+        int idx[32];
+        int m = 0;
+        uint32_t mask = 0;
+        for (int j = 0; j < nb; ++j) {
+            const double w = __ddiv_rn((double)wsel[j], tot);
+            if (w > 1.0e-7) {
+                wn[m] = w;
+                idx[m] = j;
+                mask |= 1u << j;
+                ++m;
+            }
+        }
+        qi.mask = m >= 3 ? mask : 0u;
+        qi.m = m >= 3 ? m : 0;
+        if (m >= 3) {
+            const double ws = np_sum(wn, m);
+            for (int k = 0; k < m; ++k) wn[k] = __ddiv_rn(wn[k], ws);
+            auto bcomp = [&](int k, int c) { return (double)norms[(p * nb + idx[k]) * 3 + c]; };
+            auto pcomp = [&](int k, int c) {
+                const int64_t pm = polematch[p * nb + idx[k]];
+                return pole64[3 * (pm > 0 ? pm : 0) + c];
+            };
+            // B = (w b)^T p and z = sum_k w_k (b_k x p_k), in the reference's operation order
+            double Bm[3][3];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) {
+                    double acc = __dmul_rn(__dmul_rn(wn[0], bcomp(0, r)), pcomp(0, c));
+                    for (int k = 1; k < m; ++k) acc = __fma_rn(__dmul_rn(wn[k], bcomp(k, r)), pcomp(k, c), acc);
+                    Bm[r][c] = acc;
+                }
+            double z[3];
+            for (int c = 0; c < 3; ++c) {
+                const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                double zc = 0.0;
+                for (int k = 0; k < m; ++k) {
+                    const double cr = __dsub_rn(__dmul_rn(bcomp(k, c1), pcomp(k, c2)), __dmul_rn(bcomp(k, c2), pcomp(k, c1)));
+                    const double v = __dmul_rn(wn[k], cr);
+                    zc = k == 0 ? v : __dadd_rn(zc, v);
+                }
+                z[c] = zc;
+            }
+            double S[3][3];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c) S[r][c] = __dadd_rn(Bm[r][c], Bm[c][r]);
             double S2[3][3];
             for (int r = 0; r < 3; ++r)
                 for (int c = 0; c < 3; ++c)
@@ -1094,7 +1077,8 @@ extern "C" int ebsd_band_index(ebsd_vote_plan_t p, const float* d_norms, const f
         int rc = launch_status();
         if (rc != EBSD_OK) return rc;
         const int qb = (int)std::min<int64_t>((cnt + 127) / 128, (int64_t)sms * 16);
-        k_quest<<<qb, 128, 0, (cudaStream_t)stream>>>(A.quest, cnt, o.quat);
+        k_quest<<<qb, 128, 0, (cudaStream_t)stream>>>(A.quest, cnt, nBands, A.norms, A.inten, o.polematch,
+                                                     p->d_pole64, o.quat);
         if ((rc = launch_status()) != EBSD_OK) return rc;
         k_quest_fit<<<qb, 128, 0, (cudaStream_t)stream>>>(A.quest, A.norms, o.polematch, p->d_pole64, o.quat, cnt,
                                                          nBands, o.fit, o.bandfit);
