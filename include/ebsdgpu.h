@@ -38,6 +38,7 @@ extern "C" {
 #define EBSD_E_TIMEOUT (-7)    /* a bounded device-side wait gave up                      */
 #define EBSD_E_SCRATCH (-8)    /* request needs more scratch than the static array holds   */
 #define EBSD_E_IO (-9)         /* a pattern file could not be opened, read or parsed       */
+#define EBSD_E_FORMAT (-10)    /* a pattern file in a form not read (compressed, version 0) */
 
 /* ---- pattern element types (BandDetect.find_bands accepts uint8, uint16, float32) ---- */
 #define EBSD_U8 0
@@ -246,7 +247,54 @@ int ebsd_up_read_header(const char* path, int bitdepth, ebsd_up_info* info);
 int ebsd_up_read(const char* path, const ebsd_up_info* info, int64_t pat_start, int64_t n,
                  void* h_dst, int threads);
 
-/* find_bands on patterns [pat_start, pat_start + n) of a UP1 / UP2 file, records to host
+/* ---- Oxford .ebsp and ThermoFisher .pat pattern files (ebsd_pattern.EBSPFile, :709-1088;
+ * ebsd_pattern.TFPatFile, :1090-1395) ---------------------------------------------------- */
+#define EBSD_PF_EBSP 2
+#define EBSD_PF_TFPAT 3
+
+/* Header fields as EBSPFile.read_header (ebsd_pattern.py:724-918) / TFPatFile.read_header
+ * (:1113-1167) find them.  Both formats keep one record per pattern: `record_head` bytes, the
+ * pixels, then (EBSP) an optional x, y footer.  EBSP records sit where a table of uint64
+ * positions (filePos; 0: pattern not stored, read as zeros) says; TFPAT records follow one
+ * another from `first_record`, each an (x, y) pixel location pair of uint32 and the pixels. */
+typedef struct {
+    int32_t format;          /* EBSD_PF_EBSP or EBSD_PF_TFPAT                                */
+    int32_t version;         /* EBSP: minus the leading int64 (1-5); TFPAT: the leading uint32 */
+    int32_t W, H;            /* patternW, patternH                                           */
+    int32_t bytes_per_px;    /* EBSP 1, 2 or 4 (from the first record); TFPAT 2 (uint16)     */
+    int32_t record_head;     /* bytes in front of the pixels: EBSP 16 (24 from version 5), TFPAT 8 */
+    int64_t n_patterns;      /* nPatterns                                                    */
+    int64_t first_record;    /* EBSP: byte of the position table; TFPAT: byte of the first record (filePos) */
+    int64_t record_bytes;    /* TFPAT: bytes per record; EBSP: 0 (positions from the table)  */
+    int64_t file_bytes;      /* file size                                                    */
+    int32_t has_xy;          /* EBSP: records carry x, y (float64) after the pixels           */
+    int32_t xy_flag_bytes;   /* EBSP: 1 (a flag byte in front of x and of y) or 0 (version 1) */
+    int32_t is_scan;         /* TFPAT: the header's scan flag (< 0: n_cols x n_rows patterns) */
+    int32_t bitdepth;        /* TFPAT: the header's bit depth                                 */
+    int32_t has_background;  /* TFPAT: a background pattern (uint16) at byte 25               */
+    int32_t reserved;
+    int64_t n_cols, n_rows;  /* TFPAT: the header's scan columns and rows                    */
+} ebsd_pf_info;
+
+/* Parses the header of an .ebsp or .pat file (by extension).  EBSD_E_IO for a file that cannot
+ * be read or parsed, EBSD_E_FORMAT for compressed EBSP files and version 0 of either format,
+ * which the reference does not read either. */
+int ebsd_pf_read_header(const char* path, ebsd_pf_info* info);
+
+/* EBSP: the n_patterns record positions (filePos) into h_pos. */
+int ebsd_pf_read_positions(const char* path, const ebsd_pf_info* info, uint64_t* h_pos);
+
+/* Reads patterns [pat_start, pat_start + n) into h_dst (n * H * W pixels of the file's type;
+ * may be NULL to read h_aux only) and, when h_aux is not NULL, per pattern: EBSP x, y as two
+ * float64 (zeros without a footer), TFPAT the record's two uint32 pixel locations.  h_pos:
+ * the positions ebsd_pf_read_positions returned (EBSP; ignored for TFPAT).  Runs of records at
+ * a constant spacing are read in large positional reads, by `threads` threads (0: a default).
+ * EBSPFile.pat_reader (ebsd_pattern.py:920-958), TFPatFile.pat_reader (:1190-1225). */
+int ebsd_pf_read(const char* path, const ebsd_pf_info* info, const uint64_t* h_pos,
+                 int64_t pat_start, int64_t n, void* h_dst, void* h_aux, int threads);
+
+/* find_bands on patterns [pat_start, pat_start + n) of a UP1 / UP2, EBSP or TFPAT file (by
+ * extension; any other extension is read as UP with `bitdepth` 8 or 16), records to host
  * arrays: a reader thread fills three pinned chunk buffers from the file while two CUDA
  * streams copy, detect and copy back, so file reads, copies and compute overlap.  The file's
  * pattern size must be the plan's; the pixel type is the file's (uint8 / uint16).  `chunk`

@@ -170,3 +170,40 @@ def find_bands(bd, pats, **kw):
     with warnings.catch_warnings(), np.errstate(all="ignore"):
         warnings.simplefilter("ignore")
         return bd.find_bands(pats, **kw)
+
+
+class _ScalarSlotArray(np.ndarray):
+    """An ndarray that accepts a one-element array where one element goes, as numpy < 2.x did
+    (numpy 2.5 raises "setting an array element with a sequence")."""
+
+    def __setitem__(self, key, value):
+        if isinstance(value, np.ndarray) and value.size == 1 and np.ndim(np.asarray(self)[key]) == 0:
+            value = value.reshape(())[()]
+        super().__setitem__(key, value)
+
+
+class _LegacyNumpy(types.ModuleType):
+    """numpy as seen by a reference module whose arrays take one-element arrays into scalar
+    slots: ``zeros`` returns _ScalarSlotArray views, everything else is numpy's own."""
+
+    def __init__(self):
+        super().__init__("numpy")
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def zeros(*a, **k):
+        return np.zeros(*a, **k).view(_ScalarSlotArray)
+
+
+def pattern_module():
+    """The reference's ebsd_pattern module (ebsd_pattern.py) with the numpy shim above:
+    EBSPFile.read_header stores the one-element arrays np.fromfile returns into scalar slots
+    (ebsd_pattern.py:884-887), which numpy 2.5 refuses."""
+    import importlib
+    load()
+    mod = importlib.import_module("pyebsdindex.ebsd_pattern")
+    if not isinstance(mod.np, _LegacyNumpy):
+        mod.np = _LegacyNumpy()
+    return mod

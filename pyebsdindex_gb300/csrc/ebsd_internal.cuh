@@ -135,6 +135,12 @@ inline size_t elem_size(int dtype) {
 int up_parse_header(const char* path, int bitdepth, ebsd_up_info* info);
 int up_read_range(int fd, const ebsd_up_info* info, int64_t start, int64_t n, void* dst, int threads);
 int default_read_threads();
+// Oxford EBSP / ThermoFisher TFPAT files: patfile.cu
+bool pf_path(const char* path);  // .ebsp or .pat
+int pf_parse_header(const char* path, ebsd_pf_info* info);
+int pf_read_positions(int fd, const ebsd_pf_info* info, uint64_t* pos);
+int pf_read_range(int fd, const ebsd_pf_info* info, const uint64_t* pos, int64_t start, int64_t n, void* dst,
+                  void* aux, int threads);
 
 // Per-stage (plain) path: plain.cu ------------------------------------------------------
 size_t plain_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);

@@ -150,12 +150,15 @@ void parallel_copy(void* dst, const void* src, size_t bytes, int threads) {
     for (auto& th : pool) th.join();
 }
 
-// Where a host pipeline's patterns come from: a host array, or patterns of a UP file.
+// Where a host pipeline's patterns come from: a host array, or patterns of a UP file, or of
+// an EBSP / TFPAT file (pf, with EBSP's record positions).
 struct ChunkSource {
     const char* mem = nullptr;
     bool mem_pinned = false;
     int fd = -1;
     const ebsd_up_info* info = nullptr;
+    const ebsd_pf_info* pf = nullptr;
+    const uint64_t* pos = nullptr;
     int64_t file_start = 0;
     size_t pat_bytes = 0;
 };
@@ -298,7 +301,10 @@ int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src,
                 }
                 const int64_t s0 = k * chunk, cnt = std::min(chunk, n - s0);
                 int r = EBSD_OK;
-                if (src.fd >= 0)
+                if (src.fd >= 0 && src.pf)
+                    r = pf_read_range(src.fd, src.pf, src.pos, src.file_start + s0, cnt, p->h_pin[sl], nullptr,
+                                      threads);
+                else if (src.fd >= 0)
                     r = up_read_range(src.fd, src.info, src.file_start + s0, cnt, p->h_pin[sl], threads);
                 else
                     parallel_copy(p->h_pin[sl], src.mem + (size_t)s0 * src.pat_bytes, (size_t)cnt * src.pat_bytes,
@@ -428,6 +434,56 @@ int host_pipeline(ebsd_plan_s* p, int method, int dtype, const ChunkSource& src,
     return EBSD_OK;
 }
 
+// A pattern file opened for a host pipeline: its header (UP, or EBSP / TFPAT by extension),
+// EBSP's record positions, the descriptor; closed when it goes out of scope.
+struct PatternFile {
+    ebsd_up_info up{};
+    ebsd_pf_info pf{};
+    std::vector<uint64_t> pos;
+    const char* path = nullptr;
+    ChunkSource src;
+    int dtype = EBSD_U8;
+
+    int open_file(const ebsd_plan_s* p, const char* file, int bitdepth, int64_t start, int64_t n) {
+        path = file;
+        int64_t npat = 0;
+        int bpp = 0, W = 0, H = 0;
+        if (pf_path(file)) {
+            int rc = pf_parse_header(file, &pf);
+            if (rc != EBSD_OK) return rc;
+            npat = pf.n_patterns, bpp = pf.bytes_per_px, W = pf.W, H = pf.H;
+            src.pf = &pf;
+        } else {
+            int rc = up_parse_header(file, bitdepth, &up);
+            if (rc != EBSD_OK) return rc;
+            npat = up.n_patterns, bpp = up.bytes_per_px, W = up.W, H = up.H;
+            src.info = &up;
+        }
+        if (H != p->H || W != p->W || start + n > npat) return EBSD_E_ARG;
+        if (bpp != 1 && bpp != 2) return EBSD_E_DTYPE;
+        dtype = bpp == 1 ? EBSD_U8 : EBSD_U16;
+        src.file_start = start;
+        src.pat_bytes = (size_t)p->nPx * bpp;
+        return EBSD_OK;
+    }
+
+    int open_data() {
+        src.fd = open(path, O_RDONLY);
+        if (src.fd < 0) return EBSD_E_IO;
+        if (src.pf && pf.format == EBSD_PF_EBSP) {
+            pos.resize((size_t)pf.n_patterns);
+            int rc = pf_read_positions(src.fd, &pf, pos.data());
+            if (rc != EBSD_OK) return rc;
+            src.pos = pos.data();
+        }
+        return EBSD_OK;
+    }
+
+    ~PatternFile() {
+        if (src.fd >= 0) close(src.fd);
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -446,6 +502,7 @@ const char* ebsd_strerror(int code) {
         case EBSD_E_TIMEOUT: return "a bounded device-side wait timed out";
         case EBSD_E_SCRATCH: return "request needs more scratch than the library's 64 MiB static device array holds";
         case EBSD_E_IO: return "pattern file could not be opened, read or parsed";
+        case EBSD_E_FORMAT: return "pattern file format or version not read (compressed or version 0)";
         default: return "unknown error";
     }
 }
@@ -647,26 +704,17 @@ int ebsd_find_bands_file(ebsd_plan_t p, int method, const char* path, int bitdep
                          const ebsd_bands* h_out, int64_t chunk) {
     if (!p || !path || !h_out || n < 0 || pat_start < 0) return EBSD_E_ARG;
     if (!all_outputs(h_out)) return EBSD_E_ARG;
-    ebsd_up_info info;
-    int rc = up_parse_header(path, bitdepth, &info);
+    PatternFile pf;
+    int rc = pf.open_file(p, path, bitdepth, pat_start, n);
     if (rc != EBSD_OK) return rc;
-    if (info.H != p->H || info.W != p->W || pat_start + n > info.n_patterns) return EBSD_E_ARG;
-    const int dtype = info.bytes_per_px == 1 ? EBSD_U8 : EBSD_U16;
     rc = check_method(p, method);
     if (rc != EBSD_OK) return rc;
     std::lock_guard<std::mutex> lk(p->mtx);
     if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
     p->last_launches = 0;
     if (n == 0) return EBSD_OK;
-    ChunkSource src;
-    src.fd = open(path, O_RDONLY);
-    if (src.fd < 0) return EBSD_E_IO;
-    src.info = &info;
-    src.file_start = pat_start;
-    src.pat_bytes = (size_t)p->nPx * info.bytes_per_px;
-    rc = host_pipeline(p, method, dtype, src, n, h_out, chunk);
-    close(src.fd);
-    return rc;
+    if ((rc = pf.open_data()) != EBSD_OK) return rc;
+    return host_pipeline(p, method, pf.dtype, pf.src, n, h_out, chunk);
 }
 
 int ebsd_find_bands_host_records(ebsd_plan_t p, int method, int dtype, const void* h_pats, int64_t n,
@@ -703,27 +751,18 @@ int ebsd_find_bands_file_records(ebsd_plan_t p, int method, const char* path, in
     rs.itemsize = itemsize;
     for (int f = 0; f < 9; ++f) rs.off[f] = field_offsets[f];
     if (n > 0 && !valid_sink(rs)) return EBSD_E_ARG;
-    ebsd_up_info info;
-    int rc = up_parse_header(path, bitdepth, &info);
+    PatternFile pf;
+    int rc = pf.open_file(p, path, bitdepth, pat_start, n);
     if (rc != EBSD_OK) return rc;
-    if (info.H != p->H || info.W != p->W || pat_start + n > info.n_patterns) return EBSD_E_ARG;
-    const int dtype = info.bytes_per_px == 1 ? EBSD_U8 : EBSD_U16;
     rc = check_method(p, method);
     if (rc != EBSD_OK) return rc;
     std::lock_guard<std::mutex> lk(p->mtx);
     if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
     p->last_launches = 0;
     if (n == 0) return EBSD_OK;
-    ChunkSource src;
-    src.fd = open(path, O_RDONLY);
-    if (src.fd < 0) return EBSD_E_IO;
-    src.info = &info;
-    src.file_start = pat_start;
-    src.pat_bytes = (size_t)p->nPx * info.bytes_per_px;
+    if ((rc = pf.open_data()) != EBSD_OK) return rc;
     const ebsd_bands none{};
-    rc = host_pipeline(p, method, dtype, src, n, &none, chunk, &rs);
-    close(src.fd);
-    return rc;
+    return host_pipeline(p, method, pf.dtype, pf.src, n, &none, chunk, &rs);
 }
 
 int ebsd_plan_set_host_input(ebsd_plan_t p, int mode) {

@@ -1,6 +1,7 @@
 """BandDetect.find_bands_file (ebsd_find_bands_file: a reader thread fills pinned chunk buffers
-from a UP1 / UP2 file while two streams copy and detect) must give the records find_bands
-gives for the same patterns in memory, bit for bit, whatever the chunking."""
+from a UP1 / UP2, Oxford .ebsp or ThermoFisher .pat file while two streams copy and detect)
+must give the records find_bands gives for the same patterns in memory, bit for bit, whatever
+the chunking."""
 import os
 
 import numpy as np
@@ -8,7 +9,7 @@ import pytest
 
 import pyebsdindex_gb300 as pg
 from pyebsdindex_gb300 import synthetic as syn
-from pyebsdindex_gb300.ebsd_pattern import write_up
+from pyebsdindex_gb300.ebsd_pattern import write_ebsp, write_tfpat, write_up
 
 pytestmark = pytest.mark.gpu
 FIELDS = ("max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid")
@@ -35,6 +36,36 @@ def test_file_stream_equals_in_memory(cuda, tmp_path, method, chunk):
         assert part[f].tobytes() == want[f][1234:2011].tobytes(), f
     tail = bd.find_bands_file(path, patStart=2890, nPat=100, method=method)  # clamped to the file
     assert tail.shape[0] == 10
+
+
+@pytest.mark.parametrize("kind", ["ebsp-u8", "ebsp-u16-v5", "tfpat"])
+def test_record_files_stream_equal_in_memory(cuda, tmp_path, kind):
+    """EBSP and TFPAT records (a header and footer around each pattern) gathered into the
+    pinned chunks; an EBSP pattern that is not stored is detected as a zero pattern."""
+    pats = syn.make_patterns(1300, 80, 80, seed=55, noise_frac=0.1)[0]
+    if kind == "ebsp-u8":
+        path = os.path.join(tmp_path, "scan.ebsp")
+        write_ebsp(path, pats, nCols=50, nRows=26, version=4)
+        with open(path, "r+b") as f:  # pattern 700 not stored
+            f.seek(9 + 8 * 700)
+            f.write(np.uint64(0).tobytes())
+        pats[700] = 0
+    elif kind == "ebsp-u16-v5":
+        pats = pats.astype(np.uint16) * 16
+        path = os.path.join(tmp_path, "scan.ebsp")
+        write_ebsp(path, pats, nCols=50, nRows=26, version=5)
+    else:
+        pats = pats.astype(np.uint16) * 16
+        path = os.path.join(tmp_path, "scan.pat")
+        write_tfpat(path, pats, nCols=50, nRows=26, bitdepth=12, background=np.zeros((80, 80)))
+    bd = plan()
+    want = bd.find_bands(pats)
+    got = bd.find_bands_file(path, chunk=300)
+    for f in FIELDS:
+        assert got[f].tobytes() == want[f].tobytes(), (kind, f)
+    part = bd.find_bands_file(path, patStart=650, nPat=400, chunk=128)
+    for f in FIELDS:
+        assert part[f].tobytes() == want[f][650:1050].tobytes(), (kind, f)
 
 
 def test_uint16_file(cuda, tmp_path):
