@@ -116,6 +116,49 @@ class EBSDPatterns:
         self.xyLocations = None
 
 
+def pat_flt2int(patterns, typeout=None, method='clip', scalevalue=0.98, maxScale=None):
+    """Patterns to an unsigned integer type (ebsd_pattern.py:118-182): 'clip' to the type's
+    range (capped at maxScale), 'fullscale' (min to 0, the max -- or maxScale -- to
+    scalevalue * the type's maximum, rounded) or 'scale' (negative minimum lifted to 0, then as
+    'fullscale').  A floating typeout returns the patterns cast."""
+    pats = patterns.patterns if isinstance(patterns, EBSDPatterns) else patterns
+    if pats.ndim == 2:
+        pats = pats.reshape(1, pats.shape[0], pats.shape[1])
+    shp = pats.shape
+    maxp, minp = pats.max(), pats.min()
+    if typeout is None:
+        typeout = np.uint8
+        if maxp > 258:
+            typeout = np.uint16
+    if isinstance(typeout(0), np.floating):
+        return pats.astype(typeout)
+    minval, maxval = 0, 255
+    if isinstance(typeout(0), np.uint16):
+        typeout, minval, maxval = np.uint16, 0, 65535
+    patsout = np.zeros(shp, dtype=typeout)
+    if method == 'clip':
+        if maxScale is not None:
+            maxval = min(maxScale, maxval)
+        patsout[:, :, :] = pats.clip(minval, maxval).astype(dtype=typeout)
+    elif method == 'fullscale':
+        temp = pats.astype(np.float32) - minp
+        if maxScale is None:
+            maxScale = temp.max()
+        temp *= scalevalue * maxval / maxScale
+        temp = np.around(temp.clip(0, maxval))
+        patsout[:, :, :] = temp.astype(typeout)
+    elif method == 'scale':
+        temp = pats.astype(np.float32)
+        if minp < minval:
+            temp += minval - minp
+        if maxScale is None:
+            maxScale = temp.max()
+        temp *= scalevalue * maxval / maxScale
+        temp = np.around(temp)
+        patsout[:, :, :] = temp.astype(typeout)
+    return patsout
+
+
 class EBSDPatternFile:
     """What every pattern-file reader shares (ebsd_pattern.py:208-433): the path, the scan
     attributes, ``read_data`` over a format's ``pat_reader``."""
@@ -214,6 +257,85 @@ class EBSDPatternFile:
         out.patterns, out.xyLocations = patterns, xyloc
         return out
 
+    def write_data(self, newpatterns=None, patStartCount=[0, -1], writeHead=False, flt2int='clip', scalevalue=0.98,
+                   maxScale=None):
+        """Write patterns into the file (ebsd_pattern.py:335-400): a run [start, count] (count -1:
+        all given patterns) or a slab [[col, row], [ncol, nrow]], converted to the file's pixel
+        type by ``pat_flt2int``.  The file must exist (``copy_file``, or write_up / write_ebsp /
+        write_tfpat for a new one)."""
+        if not os.path.isfile(self.filepath):
+            raise FileNotFoundError(f"{self.filepath}: create the file first (copy_file or write_up / write_ebsp / "
+                                    "write_tfpat)")
+        if isinstance(newpatterns, EBSDPatterns):
+            pats = newpatterns.patterns
+        else:
+            pats = np.asarray(newpatterns)
+            if pats.ndim == 2:
+                pats = pats.reshape(1, pats.shape[0], pats.shape[1])
+        npats = pats.shape[0]
+        mx = pats.max() if maxScale is None else maxScale
+        pse = np.asarray(patStartCount)
+        if pse.ndim == 1:
+            patStart = np.int64(pse[0])
+            nPatToWrite = np.int64(pse[-1])
+            if nPatToWrite == -1:
+                nPatToWrite = npats
+            if nPatToWrite == 0:
+                nPatToWrite = 1
+            if (patStart + nPatToWrite) > self.nPatterns:
+                nPatToWrite = self.nPatterns - patStart
+            pat2write = pat_flt2int(pats, typeout=self.filedatatype, method=flt2int, scalevalue=scalevalue,
+                                    maxScale=None)
+            self.pat_writer(pat2write, int(patStart), int(nPatToWrite), self.filedatatype)
+        else:
+            colstart, ncolwrite = np.int64(pse[0, 0]), np.int64(pse[1, 0])
+            rowstart, nrowwrite = np.int64(pse[0, 1]), np.int64(pse[1, 1])
+            if ncolwrite < 0:
+                ncolwrite = np.int64(self.nCols - colstart)
+            if nrowwrite < 0:
+                nrowwrite = np.int64(self.nRows - rowstart)
+            if (colstart + ncolwrite) > self.nCols:
+                ncolwrite = np.int64(self.nCols - colstart)
+            if (rowstart + nrowwrite) > self.nRows:
+                nrowwrite = np.int64(self.nRows - rowstart)
+            for i in range(int(nrowwrite)):
+                pstart = np.int64(np.int64(np.int64(rowstart + i) * self.nCols) + colstart)
+                self.write_data(newpatterns=pats[int(i * ncolwrite):int((i + 1) * ncolwrite)],
+                                patStartCount=[pstart, ncolwrite], writeHead=False, flt2int=flt2int,
+                                scalevalue=0.98, maxScale=mx)
+
+    def pat_writer(self, pat2write, patStart, nPatToWrite, typewrite):
+        raise NotImplementedError
+
+    def copy_file(self, newpath, **kwargs):
+        """A copy of the file at ``newpath`` (default: the path + '.copy'), ebsd_pattern.py:402-410."""
+        import shutil
+        src = Path(self.filepath).expanduser().resolve()
+        dst = Path(str(np.atleast_1d(newpath)[0])).expanduser().resolve() if newpath is not None \
+            else Path(str(src) + '.copy')
+        shutil.copyfile(src, dst)
+
+    def _copy_header_only(self, newpath, head_bytes):
+        """Header bytes copied, the rest of the file's length zero-filled (UPFile / TFPatFile
+        copy_file with empty_data)."""
+        src = Path(self.filepath).expanduser().resolve()
+        dst = Path(str(np.atleast_1d(newpath)[0])).expanduser().resolve() if newpath is not None \
+            else Path(str(src) + '.copy')
+        with open(src, 'rb') as f:
+            head = f.read(int(head_bytes))
+            size = f.seek(0, 2)
+        with open(dst, 'wb') as f:
+            f.write(head)
+            f.seek(size - 1, 0)
+            f.write(b"\0")
+        return dst
+
+    def read_datamaxmin(self):  # files without stored data limits
+        pass
+
+    def write_datamaxmin(self):
+        pass
+
 
 class UPFile(EBSDPatternFile):
     """EDAX UP1 / UP2 reader with the reference ``UPFile`` interface."""
@@ -273,6 +395,22 @@ class UPFile(EBSDPatternFile):
         xyloc[:, 0] *= self.xStep
         xyloc[:, 1] *= self.yStep
         return out, xyloc
+
+
+    def pat_writer(self, pat2write, patStart, nPatToWrite, typewrite):
+        """Patterns [patStart, patStart + nPatToWrite) in place (ebsd_pattern.py:622-635)."""
+        per = int(self.patternW) * int(self.patternH) * np.dtype(typewrite).itemsize
+        with open(self.filepath, 'r+b') as f:
+            f.seek(per * int(patStart) + int(self.filePos))
+            np.ascontiguousarray(pat2write[0:nPatToWrite], dtype=typewrite).tofile(f)
+
+    def copy_file(self, newpath, **kwargs):
+        """UPFile.copy_file (ebsd_pattern.py:680-706): with empty_data the header and a
+        zero-filled body of the same length."""
+        if kwargs.get('empty_data', False):
+            self._copy_header_only(newpath, self.filePos)
+            return
+        EBSDPatternFile.copy_file(self, newpath)
 
 
 class EBSPFile(EBSDPatternFile):
@@ -348,6 +486,30 @@ class EBSPFile(EBSDPatternFile):
                                         C.c_void_p(out.ctypes.data), C.c_void_p(xyloc.ctypes.data), 0),
                    "ebsd_pf_read")
         return out, xyloc
+
+
+    def pat_writer(self, pat2write, patStart, nPatToWrite, typewrite):
+        """Records of patterns [patStart, patStart + nPatToWrite) in place: the record header,
+        the pixels and, with positions, the footer of x, y relative to the scan centre
+        (EBSPFile.pat_writer, ebsd_pattern.py:1055-1088; version-5 files get their 6-word
+        header back).  Patterns that are not stored are skipped."""
+        h, w = int(self.patternH), int(self.patternW)
+        nbytes = h * w * np.dtype(self.filedatatype).itemsize
+        rh = np.zeros(6 if int(self.version) >= 5 else 4, dtype=np.uint32)
+        rh[-3:] = (h, w, nbytes)
+        flag = b'\x01' if int(self.version) >= 2 else b''
+        with open(self.filepath, 'r+b') as f:
+            for i in range(int(patStart), int(patStart) + int(nPatToWrite)):
+                if int(self.filePos[i]) <= 0:
+                    continue
+                f.seek(int(self.filePos[i]))
+                f.write(rh.tobytes())
+                f.write(np.ascontiguousarray(pat2write[i - int(patStart)], dtype=typewrite).tobytes())
+                if self.hasxypos:
+                    row, col = divmod(i, int(self.nCols))
+                    x = (np.float64(col) - float(self.nCols * 0.5)) * self.xStep
+                    y = (np.float64(row) - float(self.nRows * 0.5)) * self.yStep
+                    f.write(flag + np.float64(x).tobytes() + flag + np.float64(y).tobytes())
 
 
 class TFPatFile(EBSDPatternFile):
@@ -438,6 +600,39 @@ class TFPatFile(EBSDPatternFile):
         xyloc[:, 0] *= self.xStep
         xyloc[:, 1] *= self.yStep
         return out, xyloc
+
+
+    def pat_writer(self, pat2write, patStart, nPatToWrite, typewrite=None, bitdepth=None):
+        """Records of patterns [patStart, patStart + nPatToWrite) in place: (column, row) and
+        the pixels clipped to 2**bitdepth - 1 (TFPatFile.pat_writer, ebsd_pattern.py:1266-1300)."""
+        bitdepth = int(self.bitdepth if bitdepth is None else bitdepth)
+        h, w = int(self.patternH), int(self.patternW)
+        n = int(nPatToWrite)
+        recs = np.empty(n, dtype=np.dtype([('loc', np.uint32, (2,)), ('pat', np.uint16, (h, w))]))
+        idx = np.arange(int(patStart), int(patStart) + n)
+        recs['loc'][:, 0] = idx % int(self.nCols)
+        recs['loc'][:, 1] = idx // int(self.nCols)
+        recs['pat'] = pat_flt2int(np.asarray(pat2write[0:n]), typeout=np.uint16, method='clip',
+                                  maxScale=(1 << bitdepth) - 1)
+        with open(self.filepath, 'r+b') as f:
+            f.seek(int(self.filePos) + int(patStart) * (h * w * 2 + 8))
+            recs.tofile(f)
+        return 0
+
+    def copy_file(self, newpath, **kwargs):
+        """TFPatFile.copy_file (ebsd_pattern.py:1327-1360): with empty_data the header (and
+        background) and a zero-filled body; the .ebsd file of the same name is copied along."""
+        import shutil
+        src = Path(self.filepath).expanduser().resolve()
+        if kwargs.get('empty_data', False):
+            dst = self._copy_header_only(newpath, self.filePos)
+        else:
+            dst = Path(str(np.atleast_1d(newpath)[0])).expanduser().resolve() if newpath is not None \
+                else Path(str(src) + '.copy')
+            shutil.copyfile(src, dst)
+        side = src.with_suffix('.ebsd')
+        if side.exists():
+            shutil.copyfile(side, Path(dst).with_suffix('.ebsd'))
 
 
 def write_up(path, patterns, nCols=None, nRows=None, version=3, xStep=1.0, yStep=1.0, hexflag=0):

@@ -1,12 +1,21 @@
-"""NLPAR (non-local pattern averaging) on the GPU, with array input and output.
+"""NLPAR (non-local pattern averaging) on the GPU, on arrays and on pattern files.
 
 The reference's ``NLPAR`` (nlpar_cpu.py:47-1072, OpenCL nlpar_cl.py) reads and writes pattern
-files; here the same computation runs on arrays held in host or device memory so that it can
-sit directly in front of band detection without a file round trip:
+files.  Here the computation runs on arrays held in host or device memory, so that it can sit
+directly in front of band detection without a file round trip:
 
     nl = NLPAR(lam=0.7, searchradius=3)
     smooth = nl.calcnlpar_array(patterns, nrows, ncols)       # same shape, float32
     bands = band_detect_plan.find_bands(smooth)
+
+and the reference's file interface -- ``setfile``, ``calcsigma``, ``opt_lambda``,
+``calcnlpar``, ``auto_nlpar`` -- runs the same kernels on UP1 / UP2, .ebsp and .pat files
+(pyebsdindex_gb300.ebsd_pattern), with the reference's scan tiling, halos, sigma merging
+and output file:
+
+    nl = NLPAR("scan.up1", searchradius=3)
+    nl.opt_lambda()                   # sets nl.lam
+    out = nl.calcnlpar()              # writes scan_NLPAR_l{lam:.2f}sr3.up1, returns its path
 
 ``calcsigma_array`` restates ``NLPAR.sigma_numba`` (nlpar_cpu.py:753-796) and
 ``calcnlpar_array`` restates ``NLPAR.nlpar_nb`` (nlpar_cpu.py:821-936) as ``calcnlpar_cpu``
@@ -99,7 +108,11 @@ class NLPAR:
         self.saturation_protect = saturation_protect
         self.stem_scale = stem_scale
         self.automask = automask
-        self.filepath = filename
+        self.filepath = None
+        self.hdfdatapath = None
+        self.filepathout = None
+        self.hdfdatapathout = None
+        self.setfile(filename)
         self.mask = None
         self.sigma = None
         self.sigmann = 1
@@ -263,3 +276,278 @@ class NLPAR:
                    "ebsd_nlpar")
         out = out.reshape(shape)
         return out if is_torch else out.cpu().numpy()
+
+    # -- the reference's file interface (nlpar_cpu.py:81-92, :94-281, :283-540, :542-677) ------
+    def setfile(self, filepath=None):
+        """The input pattern file (nlpar_cpu.py:542-552)."""
+        self.filepath = None
+        self.hdfdatapath = None
+        pathtemp = np.atleast_1d(filepath)
+        if pathtemp[0] is not None:
+            from pathlib import Path
+            self.filepath = Path(str(pathtemp[0]))
+            self.hdfdatapath = pathtemp[1] if pathtemp.size > 1 else None
+
+    def getinfileobj(self):
+        """The input file's reader; its scan shape becomes nrows / ncols unless they are set, in
+        which case they override the file's (nlpar_cpu.py:633-656)."""
+        from . import ebsd_pattern
+        if self.filepath is None:
+            return None
+        f = ebsd_pattern.get_pattern_file_obj(self.filepath)
+        if f.nRows is not None:
+            if self.nrows is None:
+                self.nrows = f.nRows
+            else:
+                f.nRows = self.nrows
+        if f.nCols is not None:
+            if self.ncols is None:
+                self.ncols = f.nCols
+            else:
+                f.nCols = self.ncols
+        return f
+
+    def setoutfile(self, patternfile, filepath=None):
+        """The output file (nlpar_cpu.py:554-631): ``filepath`` when given (not the input
+        file), else the input's name with ``_NLPAR_l{lam:.2f}sr{sr}`` before the extension; the
+        input's header copied there with an empty body (EBSP files are copied whole)."""
+        from pathlib import Path
+        self.filepathout = None
+        self.hdfdatapathout = None
+        fpath = np.atleast_1d(filepath)[0]
+        if fpath is not None:
+            self.filepathout = Path(str(fpath)).expanduser().resolve()
+            if self.filepathout.exists() and self.filepathout.samefile(patternfile.filepath):
+                raise ValueError('Error: File input and output are exactly the same.')
+            patternfile.copy_file([self.filepathout, None], empty_data=True)
+            return
+        if patternfile is not None:
+            p = Path(patternfile.filepath)
+            appnd = "_NLPAR_l{:1.2f}".format(self.lam) + "sr{:d}".format(self.searchradius)
+            newfilepath = str(p.parent / Path(p.stem + appnd + p.suffix))
+            patternfile.copy_file(newfilepath, empty_data=True)
+            self.filepathout = newfilepath
+
+    def getoutfileobj(self):
+        """The output file's reader with the scan shape in use (nlpar_cpu.py:658-677)."""
+        from . import ebsd_pattern
+        if self.filepathout is None:
+            return None
+        f = ebsd_pattern.get_pattern_file_obj(self.filepathout)
+        if self.nrows is not None:
+            f.nRows = self.nrows
+        else:
+            self.nrows = f.nRows
+        if self.ncols is not None:
+            f.nCols = self.ncols
+        else:
+            self.ncols = f.nCols
+        return f
+
+    @staticmethod
+    def _first(v):
+        return v if np.isscalar(v) else np.asarray(v).ravel()[0]
+
+    def _file_scan(self, stem_scale):
+        """The whole scan of the input file as float32 [nrows * ncols, H, W] (square-rooted
+        above the file's minimum with stem_scale, as calcsigma_cpu does)."""
+        f = self.getinfileobj()
+        if f is None:
+            raise ValueError("no input file: NLPAR(filename) or setfile(path) first")
+        nrows, ncols = int(self.nrows), int(self.ncols)
+        data, _ = f.read_data(patStartCount=[[0, 0], [ncols, nrows]], convertToFloat=True, returnArrayOnly=True)
+        if stem_scale:
+            data = np.sqrt(data.astype(np.float32) - np.float32(data.min())).astype(np.float32)
+        return f, data, nrows, ncols
+
+    @staticmethod
+    def _target_bytes(chunksize):
+        return float(chunksize) if chunksize > 0 else min(32e9, host_memory_bytes() // 4)
+
+    def calcsigma(self, chunksize=0, nn=1, saturation_protect=None, automask=None, stem_scale=None, verbose=2,
+                  **kwargs):
+        """NLPAR.calcsigma_cpu (nlpar_cpu.py:186-281) on the input file: sigma [nrows, ncols]
+        and the normalised neighbour distances d2 and counts n2 [nrows, ncols, 9], per scan tile
+        of about ``chunksize`` bytes (0: the reference's default), merged as the reference
+        merges them.  The scan is read once and held on the device."""
+        if int(nn) != 1:
+            raise NotImplementedError("only nn = 1 (the reference's default) is built")
+        self.sigmann = 1
+        if saturation_protect is not None:
+            self.saturation_protect = saturation_protect
+        if automask is not None:
+            self.automask = automask
+        if stem_scale is not None:
+            self.stem_scale = stem_scale
+        _, data, nrows, ncols = self._file_scan(bool(self._first(self.stem_scale)))
+        return self.calcsigma_tiles_array(data, nrows, ncols, saturation_protect=bool(self._first(self.saturation_protect)),
+                                          target_bytes=self._target_bytes(chunksize))
+
+    def opt_lambda(self, target_weights=(0.5, 0.34, 0.25), autoupdate=True, dthresh=None, verbose=2, chunksize=0,
+                   saturation_protect=None, automask=None, stem_scale=None, **kwargs):
+        """NLPAR.opt_lambda_cpu (nlpar_cpu.py:94-184) on the input file: the lambda values for
+        the target weights (``opt_lambda_array`` on the file's scan), their median in ``lam``
+        when ``autoupdate``."""
+        if saturation_protect is not None:
+            self.saturation_protect = saturation_protect
+        if automask is not None:
+            self.automask = automask
+        if stem_scale is not None:
+            self.stem_scale = stem_scale
+        _, data, nrows, ncols = self._file_scan(bool(self._first(self.stem_scale)))
+        vals = self.opt_lambda_array(data, nrows, ncols, target_weights=target_weights, autoupdate=autoupdate,
+                                     dthresh=dthresh, saturation_protect=bool(self._first(self.saturation_protect)),
+                                     target_bytes=self._target_bytes(chunksize), verbose=0)
+        if verbose >= 1:
+            print("Range of lambda values: ", vals)
+            print("Optimal Choice: ", np.median(vals))
+        return vals
+
+    def _tile_sigma(self, data, nrows, ncols, saturation_protect):
+        """sigma_numba with nn = 1 over one tile (nlpar_cpu.py:486-490)."""
+        return np.asarray(self.calcsigma_array(data, nrows, ncols, saturation_protect=saturation_protect))
+
+    def _tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma):
+        """nlpar_nb over one tile with the tile's merged sigma (nlpar_cpu.py:496-509); the
+        object's own parameters and sigma are left as they were."""
+        keep = (self.lam, self.searchradius, self.dthresh, self.sigma)
+        try:
+            return np.asarray(self.calcnlpar_array(data, nrows, ncols, lam=lam, searchradius=sr, dthresh=dthresh,
+                                                   saturation_protect=saturation_protect, sigma=sigma))
+        finally:
+            self.lam, self.searchradius, self.dthresh, self.sigma = keep
+
+    def calcnlpar(self, chunksize=0, searchradius=None, lam=None, dthresh=None, saturation_protect=None,
+                  automask=None, stem_scale=None, filename=None, fileout=None, reset_sigma=False, backsub=False,
+                  rescale=False, verbose=2, diff_offset=None, **kwargs):
+        """NLPAR.calcnlpar_cpu (nlpar_cpu.py:283-540) on the input file, written to the output
+        file (``setoutfile``); returns the output path.  The scan goes in tiles of about
+        ``chunksize`` bytes (0: the reference's default) with ``searchradius`` rows and columns
+        of halo, in the reference's order: per tile, its sigma merged into ``self.sigma`` by
+        minimum (unless a sigma is already set, e.g. by ``opt_lambda``), the average over the
+        tile, the tile's interior clipped to the output file's pixel type and written."""
+        if searchradius is not None:
+            self.searchradius = searchradius
+        sr = int(self._first(self.searchradius))
+        if lam is not None:
+            self.lam = lam
+        lam = np.float32(self._first(self.lam))
+        if dthresh is not None:
+            self.dthresh = dthresh
+        dthresh = np.float32(self._first(self.dthresh))
+        if diff_offset is not None:
+            self.diff_offset = diff_offset
+        if float(self._first(self.diff_offset)) != 0.0:
+            raise NotImplementedError("diff_offset other than 0 is not built")
+        if saturation_protect is not None:
+            self.saturation_protect = saturation_protect
+        sp = bool(self._first(self.saturation_protect))
+        if automask is not None:
+            self.automask = automask
+        if stem_scale is not None:
+            self.stem_scale = stem_scale
+        stem = bool(self._first(self.stem_scale))
+        if backsub:
+            raise NotImplementedError("backsub (the fitted Gaussian background) is not built")
+        if filename is not None:
+            self.setfile(filepath=filename)
+        patternfile = self.getinfileobj()
+        if patternfile is None:
+            raise ValueError("no input file: NLPAR(filename), setfile(path) or filename=")
+        self.setoutfile(patternfile, filepath=fileout)
+        patternfileout = self.getoutfileobj()
+        nrows, ncols = np.int64(self.nrows), np.int64(self.ncols)
+        if patternfileout.nCols is None:
+            patternfileout.nCols = ncols
+        if patternfileout.nRows is None:
+            patternfileout.nRows = nrows
+        pwidth, pheight = int(patternfile.patternW), int(patternfile.patternH)
+        cols, rows = scan_tiles([pwidth, pheight], int(ncols), int(nrows), self._target_bytes(chunksize),
+                                col_overlap=sr, row_overlap=sr)
+        if self.automask is True and self.mask is None:
+            self.mask = self.makeautomask(pheight, pwidth)
+        if self.mask is None:
+            self.mask = np.ones((pheight, pwidth), dtype=np.uint8)
+        calcsigma = False
+        if self.sigma is None or reset_sigma:
+            calcsigma = True
+            self.sigma = np.zeros((nrows, ncols), dtype=np.float32) + 1e24
+        if np.asarray(self.sigma).size == 1:
+            self.sigma = np.zeros((nrows, ncols), dtype=np.float32) + np.asarray(self.sigma).ravel()[0]
+            calcsigma = False
+        shp = np.asarray(self.sigma).shape
+        if shp[0] != nrows and shp[1] != ncols:
+            self.sigma = np.zeros((nrows, ncols), dtype=np.float32) + 1e24
+            calcsigma = True
+        self.sigma = np.asarray(self.sigma, dtype=np.float32)
+        sigma = self.sigma
+        mxval = None
+        if rescale:
+            if np.issubdtype(patternfileout.filedatatype, np.integer):
+                mxval = np.iinfo(patternfileout.filedatatype).max
+            else:
+                rescale = False
+        datamin = None
+        if stem:
+            full, _ = patternfile.read_data(patStartCount=[[0, 0], [int(ncols), int(nrows)]], convertToFloat=True,
+                                            returnArrayOnly=True)
+            datamin = np.float32(full.min())
+            del full
+        if verbose >= 1:
+            print("lambda:", self.lam, "search radius:", self.searchradius, "dthresh:", self.dthresh)
+        nrc, ncc = len(rows), len(cols)
+        ndone = 0
+        for rowchunk in range(nrc):
+            rstart, rend = int(rows[rowchunk, 0]), int(rows[rowchunk, 1])
+            nrowchunk = rend - rstart
+            rstartcalc = sr if rowchunk > 0 else 0
+            rendcalc = nrowchunk - sr if rowchunk < nrc - 1 else nrowchunk
+            nrowcalc = rendcalc - rstartcalc
+            for colchunk in range(ncc):
+                cstart, cend = int(cols[colchunk, 0]), int(cols[colchunk, 1])
+                ncolchunk = cend - cstart
+                cstartcalc = sr if colchunk > 0 else 0
+                cendcalc = ncolchunk - sr if colchunk < ncc - 1 else ncolchunk
+                ncolcalc = cendcalc - cstartcalc
+                data, _ = patternfile.read_data(patStartCount=[[cstart, rstart], [ncolchunk, nrowchunk]],
+                                                convertToFloat=True, returnArrayOnly=True)
+                if stem:
+                    data = np.sqrt(data.astype(np.float32) - datamin).astype(np.float32)
+                if calcsigma:
+                    sigchunk = self._tile_sigma(data, nrowchunk, ncolchunk, sp)
+                    sigchunk = np.minimum(sigma[rstart:rend, cstart:cend], sigchunk)
+                    sigma[rstart:rend, cstart:cend] = sigchunk
+                else:
+                    sigchunk = sigma[rstart:rend, cstart:cend]
+                out = self._tile_nlpar(data, nrowchunk, ncolchunk, lam, sr, dthresh, sp,
+                                       np.ascontiguousarray(sigchunk))
+                out = out.reshape(nrowchunk, ncolchunk, -1)[rstartcalc:rstartcalc + nrowcalc,
+                                                            cstartcalc:cstartcalc + ncolcalc, :]
+                if stem:
+                    out = out ** 2 + datamin
+                out = out.reshape(nrowcalc * ncolcalc, pheight, pwidth)
+                if rescale:
+                    for i in range(out.shape[0]):
+                        temp = out[i]
+                        temp -= temp.min()
+                        temp *= np.float32(mxval) / temp.max()
+                        out[i] = temp
+                patternfileout.write_data(newpatterns=out,
+                                          patStartCount=[[np.int64(cstart + cstartcalc), np.int64(rstart + rstartcalc)],
+                                                         [ncolcalc, nrowcalc]], flt2int='clip', scalevalue=1.0)
+                ndone += 1
+                if verbose >= 2:
+                    print("tiles complete: ", ndone, "/", nrc * ncc, sep='', end='\r')
+        if verbose >= 2:
+            print('', end='')
+        return str(patternfileout.filepath)
+
+    def auto_nlpar(self, filename=None, fileout=None, lindex=1, **kwargs):
+        """opt_lambda, then calcnlpar with the lambda of target weight ``lindex`` unless ``lam``
+        is given (nlpar_cpu.py:81-92)."""
+        if filename is not None:
+            self.setfile(filename)
+        lam = self.opt_lambda(autoupdate=True, **kwargs)
+        if 'lam' not in kwargs:
+            kwargs['lam'] = lam[int(lindex)]
+        return self.calcnlpar(fileout=fileout, **kwargs)
