@@ -151,12 +151,35 @@ std::string lower_ext(const char* path) {
     return ext;
 }
 
+// The uint64 entries from an EBSP file's table start, read forward in blocks of 512 KB so that
+// a corrupt first position cannot make the header parse hold the whole file.
+struct TableCursor {
+    static constexpr int64_t kBlock = 1 << 16;
+    int fd;
+    int64_t table;  // byte of entry 0
+    int64_t avail;  // entries the file holds from there
+    std::vector<uint64_t> buf;
+    int64_t base = -1;
+
+    bool get(int64_t k, uint64_t* v) {
+        if (k < 0 || k >= avail) return false;
+        if (base < 0 || k < base || k >= base + (int64_t)buf.size()) {
+            const int64_t n = std::min<int64_t>(kBlock, avail - k);
+            buf.resize((size_t)n);
+            if (!read_exact(fd, buf.data(), (size_t)n * 8, table + 8 * k)) return false;
+            base = k;
+        }
+        *v = buf[(size_t)(k - base)];
+        return true;
+    }
+};
+
 // EBSPFile.read_header, ebsd_pattern.py:724-858: the version, the record-position table (its
 // length: version <= 4, the entries in front of the lowest stored position; version 5, the
 // first entry that equals height + (width << 32)), the first record's header, the footer flag.
 int ebsp_header(int fd, ebsd_pf_info* I) {
     const int64_t fsz = I->file_bytes;
-    unsigned char b[24];
+    unsigned char b[8];
     if (!read_exact(fd, b, 8, 0)) return EBSD_E_IO;
     const uint64_t raw = le_get<uint64_t>(b);
     const int64_t v = (int64_t)(0 - raw);  // the file stores minus the version
@@ -167,45 +190,44 @@ int ebsp_header(int fd, ebsd_pf_info* I) {
     const int64_t table = v >= 4 ? 9 : 8;
     I->record_head = 4 * pph;
     I->first_record = table;
+    TableCursor tab{fd, table, std::max<int64_t>(0, (fsz - table) / 8)};
     // the first stored position (leading entries may be 0)
     uint64_t loc0 = 0;
-    for (int64_t k = 0; loc0 == 0; ++k) {
-        if (table + 8 * (k + 1) > fsz) return EBSD_E_IO;
-        if (!read_exact(fd, b, 8, table + 8 * k)) return EBSD_E_IO;
-        loc0 = le_get<uint64_t>(b);
-    }
-    // the entries from the table start up to loc0 / 8 of them (as far as the file goes)
+    for (int64_t k = 0; loc0 == 0; ++k)
+        if (!tab.get(k, &loc0)) return EBSD_E_IO;
+    // the reference holds the entries from the table start up to loc0 / 8 of them
     const double want = (double)(int64_t)loc0 / 8.0 + 0.001;
-    int64_t nread = want > 0 ? (int64_t)want : 0;
-    nread = std::min<int64_t>(nread, (fsz - table) / 8);
-    std::vector<uint64_t> tab((size_t)std::max<int64_t>(nread, 1));
-    if (nread > 0 && !read_exact(fd, tab.data(), (size_t)nread * 8, table)) return EBSD_E_IO;
+    const int64_t nread = std::min<int64_t>(want > 0 ? (int64_t)want : 0, tab.avail);
+    tab.avail = nread;
+    uint64_t first = 0;
+    if (!tab.get(0, &first)) return EBSD_E_IO;
     int64_t npat = 0;
     if (v <= 4) {
         int64_t loc1 = (int64_t)((double)((int64_t)loc0 - table) / 8.0 + 0.001);
         int64_t counter = 0;
         while (loc1 != counter) {
-            if (counter >= nread || counter < 0) return EBSD_E_IO;
-            const uint64_t e = tab[(size_t)counter];
+            uint64_t e;
+            if (!tab.get(counter, &e)) return EBSD_E_IO;  // the reference indexes past its array
             if (e != 0 && e >= (uint64_t)table) loc1 = std::min(loc1, (int64_t)((double)(e - (uint64_t)table) / 8.0));
             ++counter;
         }
         npat = counter;
     } else {
         uint32_t w[6];
-        if (nread < 1 || !read_exact(fd, w, sizeof(w), (int64_t)tab[0])) return EBSD_E_IO;
+        if (!read_exact(fd, w, sizeof(w), (int64_t)first)) return EBSD_E_IO;
         if (w[0] == 1) return EBSD_E_FORMAT;  // compressed patterns
         const uint64_t magic = (uint64_t)w[3] + ((uint64_t)w[4] << 32);
         npat = -1;
-        for (int64_t k = 0; k < nread && npat < 0; ++k)
-            if (tab[(size_t)k] == magic) npat = k;
+        uint64_t e;
+        for (int64_t k = 0; npat < 0 && tab.get(k, &e); ++k)
+            if (e == magic) npat = k;
         if (npat < 0) return EBSD_E_IO;
     }
     if (npat <= 0) return EBSD_E_IO;
     I->n_patterns = npat;
     // the first record's header: compressed flag, height, width, pixel bytes
     uint32_t w[6];
-    if (!read_exact(fd, w, 4 * (size_t)pph, (int64_t)tab[0])) return EBSD_E_IO;
+    if (!read_exact(fd, w, 4 * (size_t)pph, (int64_t)first)) return EBSD_E_IO;
     if (w[0] == 1) return EBSD_E_FORMAT;
     I->W = (int32_t)w[pph - 2];
     I->H = (int32_t)w[pph - 3];
@@ -222,9 +244,11 @@ int ebsp_header(int fd, ebsd_pf_info* I) {
         I->has_xy = 1;
         I->xy_flag_bytes = 0;
     } else {
-        uint64_t lo = 0;
-        for (int64_t k = 0; k < npat; ++k)
-            if (tab[(size_t)k] > 0 && (lo == 0 || tab[(size_t)k] < lo)) lo = tab[(size_t)k];
+        uint64_t lo = 0, e;
+        for (int64_t k = 0; k < npat; ++k) {
+            if (!tab.get(k, &e)) return EBSD_E_IO;
+            if (e > 0 && (lo == 0 || e < lo)) lo = e;
+        }
         if (lo == 0) return EBSD_E_IO;
         unsigned char flag = 0;
         if (read_exact(fd, &flag, 1, (int64_t)lo + 4 * pph + nbytes) && flag > 0) {

@@ -227,3 +227,23 @@ def test_unsupported_and_broken_files_raise(tmp_path, built_lib):
         ep.get_pattern_file_obj(os.path.join(tmp_path, "x.tiff"))
     with pytest.raises(NotImplementedError):
         ep.get_pattern_file_obj(os.path.join(tmp_path, "x.h5oina"))
+
+
+def test_ebsp_table_across_read_blocks(tmp_path, rp, built_lib):
+    """More records than one 64 Ki-entry block of the position table, a pattern not stored
+    beyond the first block: the header parse streams the table and agrees with the reference."""
+    from pyebsdindex_gb300 import ebsd_pattern as ep
+    n = 70_000
+    pats = patterns("blocks", n, 4, 4, np.uint8, 256)
+    path = os.path.join(tmp_path, "many.ebsp")
+    ep.write_ebsp(path, pats, nCols=350, nRows=200, xStep=1.0, yStep=1.0, version=3)
+    with open(path, "r+b") as f:
+        f.seek(8 + 8 * 66_000)
+        f.write(np.uint64(0).tobytes())
+    mine = ep.get_pattern_file_obj(path)
+    theirs = rp.get_pattern_file_obj(path)
+    same_attrs(mine, theirs, EBSP_ATTRS)
+    a, axy = mine.read_data(patStartCount=[65_990, 20], returnArrayOnly=True)
+    b, bxy = theirs.read_data(patStartCount=[65_990, 20], returnArrayOnly=True)
+    assert a.tobytes() == b.tobytes() and axy.tobytes() == bxy.tobytes()
+    assert not a[10].any()
