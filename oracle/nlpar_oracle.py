@@ -11,10 +11,16 @@ TEST INFRASTRUCTURE ONLY (imported by tests/ and the golden generator as the che
                       inward at the scan edges), weights exp(-max(d - dthresh, 0) / lam^2),
                       centre weight 1, and the weighted average over all pattern pixels
 
-Arithmetic follows the reference's float32 operation order: the squared differences are
+Arithmetic follows the reference's operation order and types: the squared differences are
 accumulated sequentially over the masked pixel list, the weights are summed and applied in
-window order.  The loops are vectorised over scan pixels, so each accumulation is a numpy
-float32 array operation that performs the same scalar roundings.
+window order.  ``sigma_numba`` keeps its sums in float32; in ``nlpar_nb`` the square
+``np.float32(d0 - d1) ** np.int32(2)`` is float64 (float32 ** int32 promotes), so the
+pair's sum, the subtraction of n (sigma0^2 + sigma1^2) and the division by the norm run in
+float64 and the distance is rounded to float32 once, when the weight is stored
+(nlpar_cpu.py:902-916).  For integer patterns whose pair sums stay below 2^24 the float32 and
+float64 sums agree; for other data (stem_scale's square roots, large uint16 counts) they do
+not.  The loops are vectorised over scan pixels, so each accumulation is a numpy array
+operation that performs the same scalar roundings.
 """
 from __future__ import annotations
 
@@ -46,6 +52,23 @@ def _pair_ssd(data, idx0, idx1, indices, mxval, n_init):
         ok = (b < mxval) & (a < mxval)
         t = (a - b).astype(np.float32)
         d2 = np.where(ok, (d2 + t * t).astype(np.float32), d2)
+        n2 = np.where(ok, (n2 + f32(1.0)).astype(np.float32), n2)
+    return d2, n2
+
+
+def _pair_ssd64(data, idx0, idx1, indices, mxval):
+    """nlpar_nb's pair sum (nlpar_cpu.py:902-909): float64 squares of the float32 differences,
+    summed in float64 in masked-pixel order; the count in float32."""
+    d2 = np.zeros(idx0.shape, dtype=np.float64)
+    n2 = np.zeros(idx0.shape, dtype=np.float32)
+    a_all = data[idx0]
+    b_all = data[idx1]
+    for q in indices:
+        a = a_all[..., q]
+        b = b_all[..., q]
+        ok = (b < mxval) & (a < mxval)
+        t = (a - b).astype(np.float32).astype(np.float64)
+        d2 = np.where(ok, d2 + t * t, d2)
         n2 = np.where(ok, (n2 + f32(1.0)).astype(np.float32), n2)
     return d2, n2
 
@@ -103,11 +126,11 @@ def nlpar(data, lam, sr, dthresh, sig, nrows, ncols, indices, saturation_protect
     idx0 = np.repeat(np.arange(npx)[:, None], winsz, axis=1)
     centre = nbr == idx0
     s2 = (sig.astype(np.float32) ** 2).astype(np.float32).ravel()
-    d2, n2 = _pair_ssd(data, idx0, nbr, indices, mxval, f32(0.0))
+    d2, n2 = _pair_ssd64(data, idx0, nbr, indices, mxval)
     ssum = (s2[idx0] + s2[nbr]).astype(np.float32)
-    d2 = (d2 - (n2 * ssum).astype(np.float32)).astype(np.float32)
+    d2 = d2 - (n2 * ssum).astype(np.float32).astype(np.float64)
     dnorm = (ssum * np.sqrt((f32(2.0) * n2).astype(np.float32))).astype(np.float32)
-    d2 = np.where(dnorm > f32(1.e-8), (d2 / np.where(dnorm > 0, dnorm, 1)).astype(np.float32),
+    d2 = np.where(dnorm > f32(1.e-8), (d2 / np.where(dnorm > 0, dnorm, 1).astype(np.float64)).astype(np.float32),
                   (f32(1e6) * n2).astype(np.float32))
     w = np.where(centre, f32(-1.0e6), d2).astype(np.float32)
     w = np.maximum((w - dthresh).astype(np.float32), f32(0.0))

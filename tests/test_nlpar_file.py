@@ -208,3 +208,20 @@ def test_opt_lambda_and_calcsigma_files_match_reference(tmp_path, ref, oracle_sc
         warnings.simplefilter("ignore")
         rn.calcnlpar_cpu(fileout=theirs, verbose=0)
     assert open(mine, "rb").read() == open(theirs, "rb").read()
+
+
+@pytest.mark.parametrize("opts", [dict(stem_scale=True), dict(rescale=True), dict(dthresh=0.3, saturation_protect=False)])
+def test_calcnlpar_options_match_reference(tmp_path, ref, oracle_tiles, built_lib, opts):
+    """stem_scale (square root above the file's minimum, squared back), rescale (each output
+    pattern stretched to the file type's range) and a distance threshold without saturation
+    protection, as calcnlpar_cpu applies them."""
+    from pyebsdindex_gb300.nlpar import NLPAR
+    pats = scan(7, 9, 16, 19)
+    src = write("up1", str(tmp_path), pats, 7, 9)
+    mine, theirs = os.path.join(tmp_path, "m.up1"), os.path.join(tmp_path, "t.up1")
+    NLPAR(src, lam=0.8, searchradius=2).calcnlpar(fileout=mine, chunksize=40_000, verbose=0, **opts)
+    rn = ref.nlpar_cpu.NLPAR(src, lam=0.8, searchradius=2)
+    with warnings.catch_warnings(), np.errstate(all="ignore"):
+        warnings.simplefilter("ignore")
+        rn.calcnlpar_cpu(fileout=theirs, chunksize=40_000, verbose=0, **opts)
+    assert open(mine, "rb").read() == open(theirs, "rb").read()
