@@ -417,6 +417,39 @@ class NLPAR:
         finally:
             self.lam, self.searchradius, self.dthresh, self.sigma = keep
 
+    def backsub(self, data):
+        """NLPAR.backsub (nlpar_cpu.py:679-734): a 2-D Gaussian on a plane fitted by least squares
+        (scipy's curve_fit) to the mean of the patterns [n, H, W] over the mask, its mean removed,
+        subtracted from every pattern in place; the plain mean pattern when the fit does not
+        converge.  Host preprocessing of a tile, as in the reference."""
+        import scipy.optimize as opt
+
+        def surface(x, y, a, x0, y0, sx, sy, c, d, e):
+            return a * np.exp(- ((x - x0) ** 2) / (2.0 * sx ** 2) - ((y - y0) ** 2) / (2.0 * sy ** 2)) + c + d * x + e * y
+
+        def model(M, *p):
+            return surface(M[0], M[1], *p)
+
+        back = np.mean(data, axis=0)
+        ny, nx = data.shape[-2], data.shape[-1]
+        x = np.broadcast_to(np.arange(nx, dtype=float).reshape(1, nx), (ny, nx)).ravel()
+        y = np.broadcast_to(np.arange(ny, dtype=float), (nx, ny)).T.ravel()
+        if self.mask is None:
+            self.mask = self.makeautomask(ny, nx) if self.automask is True else np.ones((ny, nx), np.uint8)
+        wh = np.nonzero(np.asarray(self.mask).ravel())[0]
+        z = back.ravel()[wh]
+        peak = np.unravel_index(back.argmax(), back.shape)
+        p0 = [(z.max() - z.min()), peak[1], peak[0], nx / 2.355, ny / 2.355, z.min(), 0, 0]
+        try:
+            popt, _ = opt.curve_fit(model, np.vstack((x[wh], y[wh])), z, p0)
+            fit = surface(x, y, *popt).reshape(ny, nx)
+        except RuntimeError:
+            print('Warning: no convergence on back subtract ... using mean of the patterns.')
+            fit = back
+        fit -= np.mean(fit)
+        data -= fit
+        return data
+
     def calcnlpar(self, chunksize=0, searchradius=None, lam=None, dthresh=None, saturation_protect=None,
                   automask=None, stem_scale=None, filename=None, fileout=None, reset_sigma=False, backsub=False,
                   rescale=False, verbose=2, diff_offset=None, **kwargs):
@@ -447,8 +480,6 @@ class NLPAR:
         if stem_scale is not None:
             self.stem_scale = stem_scale
         stem = bool(self._first(self.stem_scale))
-        if backsub:
-            raise NotImplementedError("backsub (the fitted Gaussian background) is not built")
         if filename is not None:
             self.setfile(filepath=filename)
         patternfile = self.getinfileobj()
@@ -513,6 +544,8 @@ class NLPAR:
                                                 convertToFloat=True, returnArrayOnly=True)
                 if stem:
                     data = np.sqrt(data.astype(np.float32) - datamin).astype(np.float32)
+                if backsub:
+                    data = self.backsub(data)
                 if calcsigma:
                     sigchunk = self._tile_sigma(data, nrowchunk, ncolchunk, sp)
                     sigchunk = np.minimum(sigma[rstart:rend, cstart:cend], sigchunk)

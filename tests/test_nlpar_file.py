@@ -225,3 +225,27 @@ def test_calcnlpar_options_match_reference(tmp_path, ref, oracle_tiles, built_li
         warnings.simplefilter("ignore")
         rn.calcnlpar_cpu(fileout=theirs, chunksize=40_000, verbose=0, **opts)
     assert open(mine, "rb").read() == open(theirs, "rb").read()
+
+
+def test_backsub_matches_reference(tmp_path, ref, oracle_tiles, built_lib):
+    """The fitted background (a Gaussian on a plane over the tile's mean pattern) as the
+    reference's NLPAR.backsub computes it, alone and inside calcnlpar."""
+    from pyebsdindex_gb300.nlpar import NLPAR
+    pats = scan(7, 9, 20, 23)
+    data = pats.astype(np.float32)
+    mine = NLPAR(searchradius=1)
+    mine.mask = mine.makeautomask(20, 20)
+    theirs = ref.nlpar_cpu.NLPAR(searchradius=1)
+    theirs.mask = theirs.makeautomask(20, 20)
+    with warnings.catch_warnings(), np.errstate(all="ignore"):
+        warnings.simplefilter("ignore")
+        want = theirs.backsub(data.copy())
+    assert mine.backsub(data.copy()).tobytes() == want.tobytes()
+    src = write("up1", str(tmp_path), pats, 7, 9)
+    a, b = os.path.join(tmp_path, "a.up1"), os.path.join(tmp_path, "b.up1")
+    NLPAR(src, lam=0.8, searchradius=1).calcnlpar(fileout=a, backsub=True, chunksize=50_000, verbose=0)
+    rn = ref.nlpar_cpu.NLPAR(src, lam=0.8, searchradius=1)
+    with warnings.catch_warnings(), np.errstate(all="ignore"):
+        warnings.simplefilter("ignore")
+        rn.calcnlpar_cpu(fileout=b, backsub=True, chunksize=50_000, verbose=0)
+    assert open(a, "rb").read() == open(b, "rb").read()
