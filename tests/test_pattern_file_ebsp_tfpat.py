@@ -247,3 +247,34 @@ def test_ebsp_table_across_read_blocks(tmp_path, rp, built_lib):
     b, bxy = theirs.read_data(patStartCount=[65_990, 20], returnArrayOnly=True)
     assert a.tobytes() == b.tobytes() and axy.tobytes() == bxy.tobytes()
     assert not a[10].any()
+
+
+def test_ebsp_records_out_of_order(tmp_path, rp, built_lib):
+    """Records stored in another order than the table (here reversed, with spacing gaps): every
+    run breaks at each record and the reads still gather the right pixels and footers."""
+    from pyebsdindex_gb300 import ebsd_pattern as ep
+    n, h, w = 40, 6, 7
+    pats = patterns("rev", n, h, w, np.uint8, 256)
+    path = os.path.join(tmp_path, "rev.ebsp")
+    table_end = 8 + 8 * n
+    rec = 16 + h * w + 18
+    pos = np.empty(n, np.uint64)
+    with open(path, "wb") as f:
+        f.write(np.uint64((1 << 64) - 2).tobytes())
+        f.write(b"\0" * (8 * n))
+        at = table_end
+        for i in reversed(range(n)):
+            pos[i] = at
+            r, c = divmod(i, 8)
+            f.write(np.array([0, h, w, h * w], np.uint32).tobytes() + pats[i].tobytes())
+            f.write(b"\x01" + np.float64((c - 4.0) * 0.5).tobytes() + b"\x01" + np.float64((r - 2.5) * 0.5).tobytes())
+            f.write(b"\xee" * (i % 3))  # uneven gaps between records
+            at += rec + (i % 3)
+        f.seek(8)
+        f.write(pos.tobytes())
+    mine = ep.get_pattern_file_obj(path)
+    theirs = rp.get_pattern_file_obj(path)
+    same_attrs(mine, theirs, EBSP_ATTRS)
+    same_reads(mine, theirs, n)
+    got, _ = mine.read_data(patStartCount=[0, -1], returnArrayOnly=True)
+    assert got.tobytes() == pats.tobytes()
