@@ -219,7 +219,7 @@ class DevicePlan:
         return rec
 
     def find_bands_file_records(self, path: str, pat_start: int, n: int, method, rec_dtype, chunk=0):
-        """Patterns [pat_start, pat_start + n) of a UP1 / UP2 file -> record array."""
+        """Patterns [pat_start, pat_start + n) of a UP1 / UP2, .ebsp or .pat file -> record array."""
         rec = np.empty((n, self.nBands), dtype=rec_dtype)
         offs = record_offsets(rec_dtype)
         check(self._lib.ebsd_find_bands_file_records(self.handle, method_id(method), str(path).encode(), 0,

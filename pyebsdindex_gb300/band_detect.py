@@ -164,10 +164,11 @@ class GPUFindBands:
         return dev_out
 
     def find_bands_file(self, path, patStart=0, nPat=-1, method=None, chunk=0, gpu_id=None):
-        """find_bands on patterns [patStart, patStart + nPat) of an EDAX UP1 / UP2 file (nPat
-        -1: to the end; clamped to the file as UPFile.read_data does, ebsd_pattern.py:253-262),
-        streamed by ebsd_find_bands_file: a reader thread fills pinned chunk buffers while two
-        CUDA streams copy and detect, so the file read overlaps the GPU work.  The plan is set
+        """find_bands on patterns [patStart, patStart + nPat) of an EDAX UP1 / UP2, Oxford .ebsp
+        or ThermoFisher .pat file (nPat -1: to the end; clamped to the file as read_data does,
+        ebsd_pattern.py:253-262), streamed by ebsd_find_bands_file: a reader thread fills pinned
+        chunk buffers while two CUDA streams copy and detect, so the file read overlaps the GPU
+        work.  The plan is set
         up for the file's pattern size if it is not already.  Returns the record array."""
         from .ebsd_pattern import get_pattern_file_obj
         f = get_pattern_file_obj(path)
