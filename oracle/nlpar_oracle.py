@@ -17,9 +17,10 @@ window order.  ``sigma_numba`` keeps its sums in float32; in ``nlpar_nb`` the sq
 ``np.float32(d0 - d1) ** np.int32(2)`` is float64 (float32 ** int32 promotes), so the
 pair's sum, the subtraction of n (sigma0^2 + sigma1^2) and the division by the norm run in
 float64 and the distance is rounded to float32 once, when the weight is stored
-(nlpar_cpu.py:902-916).  For integer patterns whose pair sums stay below 2^24 the float32 and
-float64 sums agree; for other data (stem_scale's square roots, large uint16 counts) they do
-not.  The loops are vectorised over scan pixels, so each accumulation is a numpy array
+(nlpar_cpu.py:902-916).  That is the reference as it runs under numpy's promotion rules (the
+import shim); numba types float32 ** int as float32, so the compiled reference, like the device
+kernel, sums in float32.  For integer patterns whose pair sums stay below 2^24 the two agree;
+for other data (stem_scale's square roots, large uint16 counts) they do not.  The loops are vectorised over scan pixels, so each accumulation is a numpy array
 operation that performs the same scalar roundings.
 """
 from __future__ import annotations
