@@ -492,24 +492,53 @@ class EBSPFile(EBSDPatternFile):
         """Records of patterns [patStart, patStart + nPatToWrite) in place: the record header,
         the pixels and, with positions, the footer of x, y relative to the scan centre
         (EBSPFile.pat_writer, ebsd_pattern.py:1055-1088; version-5 files get their 6-word
-        header back).  Patterns that are not stored are skipped."""
+        header back).  Patterns that are not stored are skipped.  Records that follow one
+        another in the file are packed into one array and written with one call."""
         h, w = int(self.patternH), int(self.patternW)
+        pdt = np.dtype(typewrite)
         nbytes = h * w * np.dtype(self.filedatatype).itemsize
-        rh = np.zeros(6 if int(self.version) >= 5 else 4, dtype=np.uint32)
-        rh[-3:] = (h, w, nbytes)
-        flag = b'\x01' if int(self.version) >= 2 else b''
+        words = 6 if int(self.version) >= 5 else 4
+        flag = 1 if int(self.version) >= 2 else 0
+        names, formats, offsets = ['head', 'pix'], [(np.uint32, (words,)), (pdt, (h * w,))], [0, 4 * words]
+        size = 4 * words + h * w * pdt.itemsize
+        if self.hasxypos:
+            if flag:
+                names += ['fx', 'x', 'fy', 'y']
+                formats += [np.uint8, np.float64, np.uint8, np.float64]
+                offsets += [size, size + 1, size + 9, size + 10]
+                size += 18
+            else:
+                names += ['x', 'y']
+                formats += [np.float64, np.float64]
+                offsets += [size, size + 8]
+                size += 16
+        rec = np.dtype({'names': names, 'formats': formats, 'offsets': offsets, 'itemsize': size})
+        p0, n = int(patStart), int(nPatToWrite)
+        pos = np.asarray(self.filePos[p0:p0 + n], dtype=np.int64)
+        idx = np.arange(p0, p0 + n)
+        pats = np.asarray(pat2write[0:n]).reshape(n, h * w)
         with open(self.filepath, 'r+b') as f:
-            for i in range(int(patStart), int(patStart) + int(nPatToWrite)):
-                if int(self.filePos[i]) <= 0:
+            k = 0
+            while k < n:
+                if pos[k] <= 0:
+                    k += 1
                     continue
-                f.seek(int(self.filePos[i]))
-                f.write(rh.tobytes())
-                f.write(np.ascontiguousarray(pat2write[i - int(patStart)], dtype=typewrite).tobytes())
+                e = k + 1
+                while e < n and pos[e] == pos[e - 1] + size:
+                    e += 1
+                out = np.zeros(e - k, dtype=rec)
+                out['head'][:, -3:] = (h, w, nbytes)
+                out['pix'] = pats[k:e]
                 if self.hasxypos:
-                    row, col = divmod(i, int(self.nCols))
-                    x = (np.float64(col) - float(self.nCols * 0.5)) * self.xStep
-                    y = (np.float64(row) - float(self.nRows * 0.5)) * self.yStep
-                    f.write(flag + np.float64(x).tobytes() + flag + np.float64(y).tobytes())
+                    row, col = np.divmod(idx[k:e], int(self.nCols))
+                    out['x'] = (col.astype(np.float64) - float(self.nCols * 0.5)) * self.xStep
+                    out['y'] = (row.astype(np.float64) - float(self.nRows * 0.5)) * self.yStep
+                    if flag:
+                        out['fx'] = 1
+                        out['fy'] = 1
+                f.seek(int(pos[k]))
+                out.tofile(f)
+                k = e
 
 
 class TFPatFile(EBSDPatternFile):
