@@ -278,3 +278,40 @@ def test_ebsp_records_out_of_order(tmp_path, rp, built_lib):
     same_reads(mine, theirs, n)
     got, _ = mine.read_data(patStartCount=[0, -1], returnArrayOnly=True)
     assert got.tobytes() == pats.tobytes()
+
+
+def test_edge_cases(tmp_path, rp, built_lib):
+    """A UP file holding no patterns, a one-pattern EBSP file (the reference's step guess
+    indexes past its arrays there; here the y step is 0), a TFPAT file whose size is not a
+    whole number of records (its count from the file size, rounded down), truncated headers."""
+    from pyebsdindex_gb300 import ebsd_pattern as ep
+    empty = os.path.join(tmp_path, "e.up1")
+    ep.write_up(empty, np.zeros((0, 8, 8), np.uint8), nCols=0, nRows=0)
+    mine, theirs = ep.get_pattern_file_obj(empty), rp.get_pattern_file_obj(empty)
+    assert int(mine.nPatterns) == int(theirs.nPatterns) == 0
+    a, _ = mine.read_data(patStartCount=[0, -1], returnArrayOnly=True)
+    b, _ = theirs.read_data(patStartCount=[0, -1], returnArrayOnly=True)
+    assert a.shape == b.shape == (0, 8, 8)
+
+    one = os.path.join(tmp_path, "one.ebsp")
+    ep.write_ebsp(one, patterns("one", 1, 5, 6, np.uint8, 256), version=2)
+    f = ep.get_pattern_file_obj(one)
+    assert int(f.nPatterns) == 1 and int(f.nCols) == 1 and int(f.nRows) == 1 and float(f.yStep) == 0.0
+    with pytest.raises(IndexError):
+        rp.get_pattern_file_obj(one)
+
+    pats = patterns("frac", 9, 6, 5, np.uint16, 4096)
+    odd = os.path.join(tmp_path, "odd.pat")
+    ep.write_tfpat(odd, pats, nCols=3, nRows=3, isscan=False)
+    with open(odd, "ab") as fh:
+        fh.write(b"\x00" * 17)  # a partial record at the end
+    mine, theirs = ep.get_pattern_file_obj(odd), rp.get_pattern_file_obj(odd)
+    same_attrs(mine, theirs, TFPAT_ATTRS)
+    assert int(mine.nPatterns) == 9
+
+    for name, head in (("t.up1", b"\x03\x00\x00\x00\x10"), ("t.ebsp", b"\xfe\xff\xff\xff"), ("t.pat", b"\x01\x00\x00\x00\x02")):
+        p = os.path.join(tmp_path, name)
+        with open(p, "wb") as fh:
+            fh.write(head)
+        with pytest.raises(RuntimeError, match="pattern file"):
+            ep.get_pattern_file_obj(p)
