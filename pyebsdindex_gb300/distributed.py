@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["shard_bounds", "find_bands_sharded", "gather_records", "max_time"]
+__all__ = ["shard_bounds", "find_bands_sharded", "find_bands_file_sharded", "gather_records", "max_time"]
 
 
 def shard_bounds(n, rank, world):
@@ -28,6 +28,18 @@ def find_bands_sharded(bd, patterns, rank, world, **kwargs):
     Returns (start, records)."""
     s, e = shard_bounds(len(patterns), rank, world)
     return s, bd.find_bands(patterns[s:e], **kwargs)
+
+
+def find_bands_file_sharded(bd, path, rank, world, **kwargs):
+    """This rank's records from a pattern file (UP1 / UP2, .ebsp, .pat): its contiguous share
+    of the file's patterns, streamed by ``bd.find_bands_file`` -- each rank reads only its own
+    byte ranges.  Returns (start, records)."""
+    from .ebsd_pattern import get_pattern_file_obj
+    n = int(get_pattern_file_obj(path).nPatterns)
+    s, e = shard_bounds(n, rank, world)
+    if e == s:
+        return s, np.zeros((0, bd.nBands), dtype=bd.dataType)
+    return s, bd.find_bands_file(path, patStart=s, nPat=e - s, **kwargs)
 
 
 def gather_records(start, records, group=None):

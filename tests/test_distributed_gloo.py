@@ -1,6 +1,6 @@
-"""The multi-process path on CPU: two gloo ranks shard a batch, each runs a stand-in band
-detector on its slice (no GPU here), rank 0 gathers the records in order, and the timing
-reduction takes the maximum over ranks."""
+"""The multi-process path on CPU: two gloo ranks shard a batch (or a pattern file), each runs
+a stand-in band detector on its slice (no GPU here), rank 0 gathers the records in order,
+and the timing reduction takes the maximum over ranks."""
 import os
 import socket
 
@@ -34,6 +34,11 @@ class _StubDetect:
         out["max"] = pats.reshape(len(pats), -1).sum(1, dtype=np.float64)[:, None]
         return out
 
+    def find_bands_file(self, path, patStart=0, nPat=-1, **kw):
+        from pyebsdindex_gb300.ebsd_pattern import get_pattern_file_obj
+        pats, _ = get_pattern_file_obj(path).read_data(patStartCount=[patStart, nPat], returnArrayOnly=True)
+        return self.find_bands(pats.astype(np.float32))
+
 
 def _worker(rank, world, port, q):
     import torch.distributed as dist
@@ -49,6 +54,42 @@ def _worker(rank, world, port, q):
         q.put((allrec["max"][:, 0].tolist(), t))
     dist.barrier()
     dist.destroy_process_group()
+
+
+def _file_worker(rank, world, port, path, q):
+    import torch.distributed as dist
+    from pyebsdindex_gb300.distributed import find_bands_file_sharded, gather_records
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    start, rec = find_bands_file_sharded(_StubDetect(), path, rank, world)
+    allrec = gather_records(start, rec)
+    if rank == 0:
+        q.put(allrec["max"][:, 0].tolist())
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_shard_a_pattern_file(tmp_path, built_lib):
+    """Each rank reads only its share of an .ebsp file; rank 0 gathers the records in order."""
+    import multiprocessing as mp
+    from pyebsdindex_gb300.ebsd_pattern import write_ebsp
+    pats = (np.arange(13 * 6 * 6) % 251).astype(np.uint8).reshape(13, 6, 6)
+    path = os.path.join(tmp_path, "s.ebsp")
+    write_ebsp(path, pats, nCols=13, nRows=1)
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_file_worker, args=(r, 2, port, path, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    maxes = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert maxes == pats.reshape(13, -1).sum(1, dtype=np.float64).tolist()
 
 
 def test_two_gloo_ranks_shard_and_gather():
