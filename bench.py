@@ -60,7 +60,11 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the plan's rule-based kernel variant")
     ap.add_argument("--no-index", action="store_true", help="skip timing the device indexing after detection")
     ap.add_argument("--no-file", action="store_true", help="skip timing detection streamed from a UP1 file")
-    ap.add_argument("--file-patterns", type=int, default=262_144, help="patterns in the UP1 file timed")
+    ap.add_argument("--file-patterns", type=int, default=262_144, help="patterns in the file timed")
+    ap.add_argument("--file-format", default="up1", choices=["up1", "ebsp", "pat"],
+                    help="format of the file timed (EDAX UP1, Oxford .ebsp, ThermoFisher .pat)")
+    ap.add_argument("--nlpar-file", action="store_true",
+                    help="also time NLPAR's file interface (opt_lambda, calcnlpar) on a 400x500 UP1 scan")
     ap.add_argument("--lambda-scan", action="store_true",
                     help="also time NLPAR's lambda optimisation on a 400x500 scan of 80x80 patterns")
     return ap.parse_args()
@@ -187,23 +191,66 @@ def time_lambda(dev):
                         "0.5 / 0.34 / 0.25"}
 
 
-def time_file(bd, plan, method, pool, n):
-    """find_bands streamed from an EDAX UP1 file (ebsd_find_bands_file: parallel reads into
-    pinned buffers overlapping the copies and the detection), records to host memory.  The
-    file is written just before, so it is read from the page cache."""
+def time_nlpar_file():
+    """NLPAR's file interface on a 400x500 scan of 80x80 uint8 patterns in a UP1 file (a seeded
+    50x50 Voronoi scan tiled 8x10, written just before): opt_lambda (sigma and distances per
+    tile, three Nelder-Mead searches), then calcnlpar (per tile: read, sigma, the average on
+    the device, the interior clipped and written to the output file), wall-clock each."""
     import shutil
     import tempfile
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300 import synthetic as syn
     from pyebsdindex_gb300.ebsd_pattern import write_up
+    d = tempfile.mkdtemp(prefix="ebsdbench_")
+    try:
+        if shutil.disk_usage(d).free < 3 * 400 * 500 * H * W:
+            return {"skipped": "the scan does not fit the temporary directory"}
+        small, _ = syn.voronoi_scan(50, 50, ngrains=40, h=H, w=W, seed=11)
+        grid = np.tile(small.reshape(50, 50, H, W), (8, 10, 1, 1)).reshape(400 * 500, H, W)
+        src = os.path.join(d, "scan.up1")
+        write_up(src, grid, nCols=500, nRows=400)
+        del grid
+        warm = os.path.join(d, "warm.up1")
+        write_up(warm, small, nCols=50, nRows=50)
+        pg.NLPAR(warm, searchradius=3).auto_nlpar(fileout=os.path.join(d, "warm_out.up1"), verbose=0)
+        nl = pg.NLPAR(src, searchradius=3)
+        t0 = time.perf_counter()
+        lam = nl.opt_lambda(verbose=0)
+        t1 = time.perf_counter()
+        nl.calcnlpar(fileout=os.path.join(d, "out.up1"), verbose=0)
+        t2 = time.perf_counter()
+        return {"opt_lambda_s": t1 - t0, "calcnlpar_s": t2 - t1, "calcnlpar_patterns_per_s": 400 * 500 / (t2 - t1),
+                "lambda": [float(x) for x in lam],
+                "workload": "NLPAR file interface, 400x500 scan of 80x80 uint8 patterns, UP1 in the page cache, "
+                            "search radius 3"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def time_file(bd, plan, method, pool, n, fmt="up1"):
+    """find_bands streamed from a pattern file -- EDAX UP1 (default), Oxford .ebsp (uint8
+    records with x, y footers) or ThermoFisher .pat (uint16 records) -- by
+    ebsd_find_bands_file: parallel reads into pinned buffers overlapping the copies and the
+    detection, records to host memory.  The file is written just before, so it is read from
+    the page cache."""
+    import shutil
+    import tempfile
+    from pyebsdindex_gb300.ebsd_pattern import write_ebsp, write_tfpat, write_up
     n = max(512, (n // 512) * 512)  # a 512-column scan
     d = tempfile.mkdtemp(prefix="ebsdbench_")
     try:
-        need = n * H * W + 4096
+        need = n * H * W * (2 if fmt == "pat" else 1) + n * 64 + 4096
         if shutil.disk_usage(d).free < 3 * need:
             return {"skipped": f"{need / 1e9:.1f} GB file does not fit the temporary directory"}
         reps = (n + len(pool) - 1) // len(pool)
         pats = np.tile(pool, (reps, 1, 1))[:n]
-        path = os.path.join(d, "bench.up1")
-        write_up(path, pats, nCols=512, nRows=n // 512)
+        path = os.path.join(d, "bench." + fmt)
+        if fmt == "ebsp":
+            write_ebsp(path, pats, nCols=512, nRows=n // 512)
+        elif fmt == "pat":
+            write_tfpat(path, pats.astype(np.uint16), nCols=512, nRows=n // 512, bitdepth=8)
+        else:
+            write_up(path, pats, nCols=512, nRows=n // 512)
         del pats
         import torch
         from pyebsdindex_gb300 import _lib
@@ -221,9 +268,10 @@ def time_file(bd, plan, method, pool, n):
         t0 = time.perf_counter()
         run(n)
         dt = time.perf_counter() - t0
-        return {"value": n / dt, "unit": "patterns/s", "patterns": n, "file_bytes": need - 4096 + 42,
-                "source": "ebsd_find_bands_file: UP1 file in the page cache, 65,536-pattern chunks, band fields "
-                          "to pinned host arrays"}
+        kind = {"up1": "UP1", "ebsp": "EBSP", "pat": "TFPAT"}[fmt]
+        return {"value": n / dt, "unit": "patterns/s", "patterns": n, "file_bytes": os.path.getsize(path),
+                "source": f"ebsd_find_bands_file: {kind} file in the page cache, 65,536-pattern chunks, band "
+                          "fields to pinned host arrays"}
     finally:
         shutil.rmtree(d, ignore_errors=True)
 
@@ -490,11 +538,14 @@ def main():
 
     file_e2e = None
     if rank == 0 and not args.no_file:
-        file_e2e = time_file(bd, plan, method, pool, args.file_patterns)
+        file_e2e = time_file(bd, plan, method, pool, args.file_patterns, args.file_format)
 
     nlpar_lambda = None
     if rank == 0 and args.lambda_scan:
         nlpar_lambda = time_lambda(dev)
+    nlpar_file = None
+    if rank == 0 and args.nlpar_file:
+        nlpar_file = time_nlpar_file()
 
     indexing = None
     if not args.no_index:
@@ -522,7 +573,7 @@ def main():
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
-            "nlpar_lambda": nlpar_lambda,
+            "nlpar_lambda": nlpar_lambda, "nlpar_file": nlpar_file,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))
