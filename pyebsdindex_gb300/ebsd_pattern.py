@@ -734,12 +734,29 @@ def write_ebsp(path, patterns, nCols=None, nRows=None, xStep=1.0, yStep=1.0, ver
     table_end = head + 8 * n + (8 if version >= 5 else 0)
     rec = 4 * words + nbytes + footer
     pos = np.arange(n, dtype=np.uint64) * np.uint64(rec) + np.uint64(table_end)
-    rh = np.zeros(words, dtype=np.uint32)
-    rh[-3:] = (h, w, nbytes)
-    col = np.arange(n) % nCols
-    row = np.arange(n) // nCols
-    x = (col.astype(np.float64) - float(nCols * 0.5)) * xStep
-    y = (row.astype(np.float64) - float(nRows * 0.5)) * yStep
+    base = 4 * words + nbytes
+    names, formats, offsets = ['head', 'pix'], [(np.uint32, (words,)), (pats.dtype, (h * w,))], [0, 4 * words]
+    if not hasxypos:
+        names, formats, offsets = names + ['flag'], formats + [np.uint8], offsets + [base]
+    elif version >= 2:
+        names += ['fx', 'x', 'fy', 'y']
+        formats += [np.uint8, np.float64, np.uint8, np.float64]
+        offsets += [base, base + 1, base + 9, base + 10]
+    else:
+        names += ['x', 'y']
+        formats += [np.float64, np.float64]
+        offsets += [base, base + 8]
+    recs = np.zeros(n, dtype=np.dtype({'names': names, 'formats': formats, 'offsets': offsets, 'itemsize': rec}))
+    recs['head'][:, -3:] = (h, w, nbytes)
+    recs['pix'] = pats.reshape(n, h * w)
+    if hasxypos:
+        col = np.arange(n) % nCols
+        row = np.arange(n) // nCols
+        recs['x'] = (col.astype(np.float64) - float(nCols * 0.5)) * xStep
+        recs['y'] = (row.astype(np.float64) - float(nRows * 0.5)) * yStep
+        if version >= 2:
+            recs['fx'] = 1
+            recs['fy'] = 1
     with open(os.path.expanduser(str(path)), 'wb') as f:
         f.write(np.uint64((1 << 64) - version).tobytes())
         if version >= 4:
@@ -747,14 +764,7 @@ def write_ebsp(path, patterns, nCols=None, nRows=None, xStep=1.0, yStep=1.0, ver
         f.write(pos.tobytes())
         if version >= 5:
             f.write(np.uint64(h + (w << 32)).tobytes())
-        for i in range(n):
-            f.write(rh.tobytes())
-            f.write(pats[i].tobytes())
-            if hasxypos:
-                flag = b'\x01' if version >= 2 else b''
-                f.write(flag + np.float64(x[i]).tobytes() + flag + np.float64(y[i]).tobytes())
-            else:
-                f.write(b'\x00')
+        recs.tofile(f)
 
 
 def write_tfpat(path, patterns, nCols=None, nRows=None, bitdepth=16, background=None, version=1, isscan=True):
