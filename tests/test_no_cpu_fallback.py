@@ -35,6 +35,17 @@ def test_nlpar_entry_points_raise(built_lib):
             call()
 
 
+def test_nlpar_file_interface_raises(built_lib, tmp_path):
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300.ebsd_pattern import write_ebsp
+    path = os.path.join(tmp_path, "s.ebsp")
+    write_ebsp(path, np.random.default_rng(1).integers(0, 255, (12, 16, 16)).astype(np.uint8), nCols=4, nRows=3)
+    for call in (lambda: pg.NLPAR(path, searchradius=1).calcnlpar(fileout=os.path.join(tmp_path, "o.ebsp"), verbose=0),
+                 lambda: pg.NLPAR(path).opt_lambda(verbose=0), lambda: pg.NLPAR(path).calcsigma(verbose=0)):
+        with pytest.raises((RuntimeError, AssertionError)):
+            call()
+
+
 def test_vote_entry_points_raise(built_lib):
     from oracle import vote_oracle as vo
     from pyebsdindex_gb300 import tripletvote as tv
