@@ -73,3 +73,24 @@ def test_lambda_and_sigma_on_a_file(cuda, tmp_path):
     assert sig_f.tobytes() == sig_a.tobytes() and d2_f.tobytes() == d2_a.tobytes() and n2_f.tobytes() == n2_a.tobytes()
     out = NLPAR(src, searchradius=1).auto_nlpar(fileout=os.path.join(tmp_path, "auto.up1"), verbose=0)
     assert read_all(out).shape == (14 * 16, 32, 32)
+
+
+NLPARFILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nlparfile")
+
+
+@pytest.mark.parametrize("name", ["onetile_9x11_16", "tiles_10x12_16"])
+def test_calcnlpar_against_reference_run(cuda, tmp_path, name):
+    """The device path on the committed reference runs of calcnlpar_cpu (tests/golden/nlparfile/):
+    merged sigma bit-identical, output patterns within one count of the reference's file."""
+    import json
+    import shutil
+    p = json.load(open(os.path.join(NLPARFILE, name + ".json")))
+    src = os.path.join(tmp_path, "in.up1")
+    shutil.copyfile(os.path.join(NLPARFILE, name + "_in.up1"), src)
+    nl = NLPAR(src, lam=p["lam"], searchradius=p["searchradius"])
+    out = nl.calcnlpar(chunksize=p["chunksize"], fileout=os.path.join(tmp_path, "out.up1"), verbose=0)
+    assert nl.sigma.tobytes() == np.load(os.path.join(NLPARFILE, name + "_sigma.npy")).tobytes()
+    a = read_all(out).astype(np.int16)
+    b = read_all(os.path.join(NLPARFILE, name + "_out.up1")).astype(np.int16)
+    assert np.abs(a - b).max() <= 1
+    assert (a == b).mean() > 0.995

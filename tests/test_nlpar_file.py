@@ -249,3 +249,24 @@ def test_backsub_matches_reference(tmp_path, ref, oracle_tiles, built_lib):
         warnings.simplefilter("ignore")
         rn.calcnlpar_cpu(fileout=b, backsub=True, chunksize=50_000, verbose=0)
     assert open(a, "rb").read() == open(b, "rb").read()
+
+
+NLPARFILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nlparfile")
+
+
+@pytest.mark.parametrize("name", ["onetile_9x11_16", "tiles_10x12_16"])
+def test_calcnlpar_matches_committed_reference_run(tmp_path, oracle_tiles, built_lib, name):
+    """The host logic on the committed reference runs (tests/golden/nlparfile/, made by
+    tests/golden/make_nlpar_file_golden.py): output file and merged sigma identical, with no
+    reference tree needed."""
+    import json
+    import shutil
+    from pyebsdindex_gb300.nlpar import NLPAR
+    p = json.load(open(os.path.join(NLPARFILE, name + ".json")))
+    src = os.path.join(tmp_path, "in.up1")
+    shutil.copyfile(os.path.join(NLPARFILE, name + "_in.up1"), src)
+    out = os.path.join(tmp_path, "out.up1")
+    nl = NLPAR(src, lam=p["lam"], searchradius=p["searchradius"])
+    nl.calcnlpar(chunksize=p["chunksize"], fileout=out, verbose=0)
+    assert open(out, "rb").read() == open(os.path.join(NLPARFILE, name + "_out.up1"), "rb").read()
+    assert nl.sigma.tobytes() == np.load(os.path.join(NLPARFILE, name + "_sigma.npy")).tobytes()
