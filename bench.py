@@ -3,9 +3,15 @@
 Workload (the batched configuration): 1,000,000 synthetic 80x80 uint8 EBSD patterns, Radon
 nTheta=180 x nRho=120, LoG sigma 1.0 px, rhoMaskFrac 0.1, nBands=9, circular detector mask;
 10% of the patterns carry no bands (background + Poisson noise only).  A step is one
-find_bands pass over the whole batch.  The patterns are a pool of seeded distinct patterns
-(pattern i uses seed BASE+i) tiled to the batch size; the 6.4 GB input is larger than L2, so
-no L2 flush is needed between steps.
+find_bands pass over the whole batch.  The patterns are a pool of 65,536 seeded distinct
+patterns (pattern i uses seed BASE+i; generated by a process pool before the GPU is touched)
+tiled to the batch size; the 6.4 GB input is larger than L2, so no L2 flush is needed
+between steps.
+
+The line carries the accuracy of the timed method's records: against the FP64 per-stage
+method (plain64, the FP64 GPU oracle) on 32,768 patterns of the timed batch, and -- in the
+CPU-baseline leg -- against the oracle's FFT restatement of the reference's find_bands on
+2,048 of them.
 
   python bench.py [--gpus N --steps K --warmup W] [--method fused16|fused|plain|plain64]
   python bench.py --impl reference     # the CPU restatement of the reference on the host cores
@@ -38,6 +44,11 @@ BYTES_PER_PATTERN = H * W * 1 + 41 * NBANDS   # algorithmic bytes: pattern in, b
 # launch's traffic is this times its patterns.  Most of it is the write-back of the parked
 # ray means (seven rows per CTA per eight patterns), not input re-reads.
 DRAM_BYTES_PER_PATTERN = (648_438_528 + 2_272_787_200) / 40_000
+# warp instructions per pattern of the same kernel (ncu smsp__inst_executed.sum, same capture):
+# the issue roofline of an issue-bound kernel is 4 warp-instructions per SM per clock
+WARP_INST_PER_PATTERN = 6.55e9 / 40_000
+ACCURACY_PATTERNS = 32_768      # timed-batch patterns graded against plain64 (FP64 GPU oracle)
+ORACLE_PATTERNS = 2_048         # of those, graded against the oracle's FFT path (CPU leg)
 SEED = 1_000_000
 WORKLOAD = ("find_bands on 1,000,000 80x80 uint8 patterns, nTheta 180, nRho 120, nBands 9, LoG sigma 1, "
             "rhoMaskFrac 0.1, circular mask, 10% noise-only")
@@ -51,7 +62,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default=None)
     ap.add_argument("--patterns", type=int, default=1_000_000)
-    ap.add_argument("--pool", type=int, default=2048)
+    ap.add_argument("--pool", type=int, default=65_536)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=0, help="patterns in the timed CPU sample")
@@ -85,12 +96,42 @@ def make_plan():
     return bd
 
 
-def make_pool(n):
+def _pool_part(args):
+    start, count = args
     from pyebsdindex_gb300 import synthetic as syn
-    out = []
-    for s in range(0, n, 256):
-        out.append(syn.make_patterns(min(256, n - s), H, W, seed=SEED, start=s, noise_frac=0.1)[0])
-    return np.concatenate(out)
+    return syn.make_patterns(count, H, W, seed=SEED, start=start, noise_frac=0.1)[0]
+
+
+def host_executor():
+    """A spawn process pool over the host cores (pattern generation, the oracle leg)."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    return ProcessPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1)), mp_context=mp.get_context("spawn"))
+
+
+def make_pool(n, ex=None):
+    """Patterns 0..n-1 of the seeded pool (pattern i from seed SEED + i), in parallel parts."""
+    parts = [(s, min(1024, n - s)) for s in range(0, n, 1024)]
+    if ex is None or len(parts) == 1:
+        return np.concatenate([_pool_part(a) for a in parts])
+    return np.concatenate(list(ex.map(_pool_part, parts)))
+
+
+def _oracle_part(pats):
+    from oracle import band_oracle as bo
+    from pyebsdindex_gb300 import synthetic as syn
+    plan = bo.Plan((H, W), NTHETA, NRHO, 1.0, 1.0, 0.1, NBANDS, mask=syn.circular_mask(H, W))
+    return bo.find_bands(plan, pats, conv="fft")
+
+
+def oracle_accuracy(ex, pats, dev_fields):
+    """CPU-baseline leg: the oracle's FFT restatement of the reference find_bands on ``pats``
+    (the first patterns of the timed batch) -> agreement of the device records with it."""
+    from pyebsdindex_gb300.accuracy import compare_records
+    chunks = [pats[s:s + 256] for s in range(0, len(pats), 256)]
+    ref = np.concatenate(list(ex.map(_oracle_part, chunks)))
+    got = {k: v[:len(pats)].cpu().numpy() for k, v in dev_fields.items()}
+    return compare_records(got, ref)
 
 
 class ClockSampler:
@@ -339,7 +380,8 @@ def run_reference(args):
     if rank != 0:
         return
     sample = args.cpu_sample or 4096
-    pool = make_pool(min(args.pool, sample))
+    with host_executor() as ex:
+        pool = make_pool(min(args.pool, sample), ex)
     pool = np.concatenate([pool] * ((sample + len(pool) - 1) // len(pool)))[:sample]
     vals = []
     base = None
@@ -368,6 +410,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    # the pattern pool is generated by spawned host processes before the GPU is touched
+    ex = host_executor()
+    pool = make_pool(args.pool, ex)
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -377,6 +422,7 @@ def main():
     dev = torch.device("cuda", local)
 
     bd = make_plan()
+    bd.gpu_id = local
     plan = bd._device_plan(local)
     method = args.method
     if method is None:
@@ -386,7 +432,6 @@ def main():
     from pyebsdindex_gb300 import _lib
 
     N = args.patterns
-    pool = make_pool(args.pool)
     pool_d = torch.from_numpy(pool).to(dev)
     reps = (N + len(pool) - 1) // len(pool)
     pats_d = pool_d.repeat(reps, 1, 1)[:N].contiguous()
@@ -482,49 +527,90 @@ def main():
             "traffic": traffic, "traffic_source": "ncu capture, 40,000 patterns, scaled per pattern" if traffic else None,
             "peak_source": peak_src,
             "kernel": "k_fused (+ k_band_epilogue)" if method.startswith("fused") else "per-stage sequence (7 kernels/chunk)"}
+    if method == "fused" and clocks.get("sm_mhz"):
+        # the roofline that binds this kernel: instruction issue, 4 warp-instructions per SM
+        # per clock at the sampled SM clock; warp-instructions per pattern from ncu
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        issue_peak = 4.0 * sms * clocks["sm_mhz"] * 1e6
+        issue_achieved = WARP_INST_PER_PATTERN * units_per_launch / (launch_ms / 1000.0)
+        roof.update({"issue_achieved": issue_achieved, "issue_peak": issue_peak, "issue_unit": "warp-inst/s",
+                     "issue_frac": issue_achieved / issue_peak,
+                     "issue_source": "smsp__inst_executed.sum per pattern from ncu (40,000 patterns); peak = 4 x SMs x "
+                                     "median sampled SM clock"})
 
-    # end to end through the C ABI with pinned host buffers (H2D + D2H inside the timed region)
+    # accuracy of the timed records: against the FP64 per-stage method (plain64, the FP64 GPU
+    # oracle) on the first patterns of the timed batch, whose records the last step wrote
+    acc = None
+    if method != "plain64":
+        from pyebsdindex_gb300.accuracy import compare_records
+        na = min(N, ACCURACY_PATTERNS)
+        ref64 = {k: torch.empty((na,) + tuple(v.shape[1:]), dtype=v.dtype, device=dev) for k, v in outs.items()}
+        plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, na, {k: v.data_ptr() for k, v in ref64.items()},
+                               "plain64", stream=stream.cuda_stream)
+        torch.cuda.synchronize()
+        acc = {"vs_plain64": dict(compare_records({k: v[:na] for k, v in outs.items()}, ref64), patterns=na),
+               "bar": "integer peaks identical on >= 99.9% of bands, aveloc within 1e-3 Radon px"}
+        del ref64
+
+    # end to end through the drop-in call: BandDetect.find_bands(numpy uint8 [N, 80, 80]) ->
+    # the reference's (N, nBands) record array (band_detect.py:411, dtype :110-115); every
+    # step moves the patterns from host memory to the GPU and the records back
     e2e = None
     if not args.no_e2e:
+        host_np = np.ascontiguousarray(np.tile(pool, (reps, 1, 1))[:N])
+        e2e_steps = max(1, min(args.steps, 3))
+        bd.find_bands(host_np[:65536], method=method)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            rec = bd.find_bands(host_np, method=method)
+        dt = time.perf_counter() - t0
+        assert rec.shape == (N, nB) and rec.dtype == bd.dataType
+        del rec
+        # the C ABI with pinned host buffers, band fields as arrays (no record packing)
         host = torch.empty((N, H, W), dtype=torch.uint8, pin_memory=True)
-        host.copy_(pats_d.cpu())
+        host.copy_(torch.from_numpy(host_np))
         hout = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in outs.items()}
         hb = _lib.Bands(**{k: _lib.C.c_void_p(v.data_ptr()) for k, v in hout.items()})
         lib = _lib.load()
 
-        def e2e_step():
+        def soa_step():
             _lib.check(lib.ebsd_find_bands_host(plan.handle, _lib.method_id(method), _lib.EBSD_U8,
                                                 _lib.C.c_void_p(host.data_ptr()), N, _lib.C.byref(hb), 0))
-        e2e_step()
+        soa_step()
         t0 = time.perf_counter()
-        e2e_steps = max(1, min(args.steps, 3))
         for _ in range(e2e_steps):
-            e2e_step()
-        dt = time.perf_counter() - t0
+            soa_step()
+        dt_soa = time.perf_counter() - t0
         in_place = plan.host_input_in_place()
         # the same with the input staged by copy engines instead of read in place
         plan.set_host_input(0)
-        e2e_step()
+        soa_step()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            e2e_step()
+            soa_step()
         dt_copy = time.perf_counter() - t0
         plan.set_host_input(-1)
         e2e = {"value": N * e2e_steps / dt * world, "unit": "patterns/s", "h2d_bytes_per_step": N * H * W,
                "d2h_bytes_per_step": N * nB * 41,
-               "input_path": ("pinned patterns read in place by the kernels over NVLink-C2C (every byte crosses "
-                              "the link each step)") if in_place else "pinned patterns staged by copy engines",
-               "copy_engine_value": N * e2e_steps / dt_copy * world}
-        del host, hout
+               "call": "BandDetect.find_bands(numpy uint8 [N, 80, 80]) -> reference record array (209 B per band)",
+               "c_abi_value": N * e2e_steps / dt_soa * world,
+               "c_abi_call": "ebsd_find_bands_host, pinned patterns and pinned band-field arrays",
+               "c_abi_input_path": ("pinned patterns read in place by the kernels over NVLink-C2C (every byte crosses "
+                                    "the link each step)") if in_place else "pinned patterns staged by copy engines",
+               "c_abi_copy_engine_value": N * e2e_steps / dt_copy * world}
+        del host, hout, host_np
 
     # the other methods on the same device-resident input, for the batched-vs-plain comparison
     variants = {}
     if not args.no_variants:
+        # separate outputs: `outs` keeps the timed method's records for the indexing below
+        vouts = {k: torch.empty_like(v) for k, v in outs.items()}
+        vptrs = {k: v.data_ptr() for k, v in vouts.items()}
         for vm, vn in (("plain", min(N, 131072)), ("fused", N), ("fused16", N)):
             if vm == method or (vm.startswith("fused") and not plan.supported(vm)):
                 continue
             def vstep():
-                plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, vn, ptrs, vm, stream=stream.cuda_stream)
+                plan.find_bands_device(pats_d.data_ptr(), _lib.EBSD_U8, vn, vptrs, vm, stream=stream.cuda_stream)
             vstep()
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -535,6 +621,7 @@ def main():
             torch.cuda.synchronize()
             variants[vm] = vn * 2 / (a.elapsed_time(b) / 1000.0)
         variants[method] = value / world
+        del vouts
 
     file_e2e = None
     if rank == 0 and not args.no_file:
@@ -558,6 +645,17 @@ def main():
             cpu = cpu_baseline(pool, args.cpu_sample or min(len(pool), 2048), "port")
         except Exception as e:  # reported, never silently replaced
             cpu = {"value": None, "error": str(e)}
+        if acc is not None:
+            # the oracle's FFT restatement of the reference find_bands on the first patterns of
+            # the timed batch, run by the host process pool; the records graded are the timed
+            # step's (plain64 above overwrote nothing of `outs`)
+            try:
+                no = min(N, ORACLE_PATTERNS)
+                acc["vs_oracle_fft"] = dict(oracle_accuracy(ex, pool[:no] if no <= len(pool) else
+                                                            pats_d[:no].cpu().numpy(), outs), patterns=no)
+            except Exception as e:
+                acc["vs_oracle_fft"] = {"error": str(e)}
+    ex.shutdown()
 
     if rank == 0:
         line = {
@@ -571,7 +669,7 @@ def main():
                        "method": method, "patterns_per_step": N, "distinct_patterns": len(pool),
                        "patterns_per_block_pass": ppp, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "accuracy": acc,
             "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
             "nlpar_lambda": nlpar_lambda, "nlpar_file": nlpar_file,
             "gpu_launches": launches_per_step * args.steps,

@@ -164,7 +164,8 @@ int ebsd_plan_set_patterns_per_pass(ebsd_plan_t plan, int patterns_per_pass);
  * 2*pad_theta) + nRho*nTheta + 8)) patterns per call (183 at 80x80, nRho 120, nTheta 180);
  * larger n returns EBSD_E_SCRATCH.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress, device current) and caches it: make that first call before
- * any stream capture.  All calls share the array; calls that overlap on the GPU race. */
+ * any stream capture.  All calls share the array; calls that overlap on the GPU race.  The
+ * caller's current device is the same after the call as before it. */
 int ebsd_find_bands_static(ebsd_plan_t plan, int dtype, const void* d_pats, int64_t n,
                            const ebsd_bands* d_out, void* stream);
 

@@ -22,13 +22,14 @@ import warnings
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("PYEBSDINDEX_REFERENCE", "/root/reference")
+# the reference source tree is named by the environment only; without it the callers skip
+REFERENCE_ROOT = os.environ.get("PYEBSDINDEX_REFERENCE", "")
 
 _loaded = None
 
 
 def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REFERENCE_ROOT, "pyebsdindex", "band_detect.py"))
+    return bool(REFERENCE_ROOT) and os.path.isfile(os.path.join(REFERENCE_ROOT, "pyebsdindex", "band_detect.py"))
 
 
 def _make_numba_stub() -> types.ModuleType:

@@ -45,10 +45,12 @@ def getopenclparam(**kwargs):
 
 def _digest(*arrays):
     """Key of the plan inputs for the device-plan cache.  Arrays up to 1 MiB are hashed in
-    full; larger ones (the Radon LUT, 13.8 MB at 80x80) by identity -- buffer address, shape,
-    strides, dtype -- and 4,096 evenly spaced elements, so that the per-call cost stays far
-    below a chunk's GPU time (EBSDIndexer calls find_bands per chunk of ~528 patterns).  A new
-    LUT array gives a new key; editing a large array in place is not detected."""
+    full; larger ones (the Radon LUT, 13.8 MB at 80x80) by 4,096 evenly spaced elements, so
+    that the per-call cost stays far below a chunk's GPU time (EBSDIndexer calls find_bands per
+    chunk of ~528 patterns).  Large arrays are also matched by object identity: the cache
+    holds a reference to them (``_large_inputs``), so a new array can never take a cached
+    array's address.  Editing a large array in place is detected only where the sample
+    changes."""
     h = hashlib.sha1()
     for a in arrays:
         if a is None:
@@ -59,12 +61,16 @@ def _digest(*arrays):
         if a.nbytes <= (1 << 20):
             h.update(np.ascontiguousarray(a).tobytes())
         else:
-            h.update(str((a.__array_interface__["data"][0], a.strides)).encode())
             flat = a.reshape(-1)
             step = max(1, flat.size // 4096)
             h.update(np.ascontiguousarray(flat[::step]).tobytes())
             h.update(np.ascontiguousarray(flat[-1:]).tobytes())
     return h.hexdigest()
+
+
+def _large_inputs(*arrays):
+    """The plan inputs above 1 MiB, as objects (compared by identity)."""
+    return tuple(a for a in arrays if a is not None and np.asarray(a).nbytes > (1 << 20))
 
 
 class GPUFindBands:
@@ -77,11 +83,14 @@ class GPUFindBands:
         dev = self.gpu_id if gpu_id is None else int(gpu_id)
         rp = self.radonPlan
         bg = self.backgroundsub
+        inputs = (rp.indexPlan, self.kernel, self.rdnmask, rp.theta, rp.rho, bg)
         key = (dev, tuple(np.asarray(self.patDim).tolist()), int(rp.nTheta), int(rp.nRho), int(self.nBands),
                tuple(np.asarray(self.padding).tolist()), tuple(np.asarray(self.peakPad).tolist()),
-               _digest(rp.indexPlan, self.kernel, self.rdnmask, rp.theta, rp.rho, bg))
+               _digest(*inputs))
+        large = _large_inputs(*inputs)
         cache = getattr(self, "_gpu_plan_cache", None)
-        if cache is not None and cache[0] == key:
+        if (cache is not None and cache[0] == key and len(cache[2]) == len(large)
+                and all(x is y for x, y in zip(cache[2], large))):
             return cache[1]
         bgarr = None
         if bg is not None:
@@ -94,7 +103,7 @@ class GPUFindBands:
             kernel=np.asarray(self.kernel, dtype=np.float32).reshape(np.asarray(self.kernel).shape[-2:]),
             lut=rp.indexPlan, rdnmask=np.asarray(self.rdnmask).astype(np.uint8), theta=rp.theta,
             rho=rp.rho, background=bgarr, device=dev)
-        self._gpu_plan_cache = (key, plan)
+        self._gpu_plan_cache = (key, plan, large)
         return plan
 
     def _pick_method(self, plan, method):

@@ -20,6 +20,8 @@
 //   * The device address of the array is looked up with cudaGetSymbolAddress the first time
 //     the entry point runs on a device (with that device current) and cached; make that
 //     first call on each device before any stream capture.
+//   * The caller's current device is left as it was: the call switches to the plan's device
+//     for its own work and switches back on every return.
 //   * All calls share the one array per device and the kernels overwrite every scratch cell
 //     they read before reading it, so nothing needs clearing between calls; two calls whose
 //     work overlaps on the GPU (different streams, or different host threads) race on the
@@ -52,6 +54,19 @@ int scratch_address(int device, void** out) {
     return EBSD_OK;
 }
 
+// Keeps the caller's current device: switches to the plan's device for the call's lifetime.
+struct DeviceGuard {
+    int saved = -1;
+    bool ok = false;
+    explicit DeviceGuard(int device) {
+        if (cudaGetDevice(&saved) != cudaSuccess) return;
+        ok = saved == device || cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
+
 }  // namespace
 
 extern "C" int ebsd_find_bands_static(ebsd_plan_t p, int dtype, const void* d_pats, int64_t n,
@@ -65,7 +80,8 @@ extern "C" int ebsd_find_bands_static(ebsd_plan_t p, int dtype, const void* d_pa
     if (n == 0) return EBSD_OK;
     if (n > 65535 || ebsd::plain_workspace_bytes(p, EBSD_PLAIN_F32, n) > kStaticScratchBytes)
         return EBSD_E_SCRATCH;
-    if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
+    DeviceGuard guard(p->device);
+    if (!guard.ok) return EBSD_E_DEVICE;
     void* scratch = nullptr;
     int rc = scratch_address(p->device, &scratch);
     if (rc != EBSD_OK) return rc;

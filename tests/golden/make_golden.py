@@ -2,7 +2,6 @@
 
 Run from the repository root on a machine that has the reference source tree:
 
-    python tests/golden/make_golden.py            # reference at /root/reference
     PYEBSDINDEX_REFERENCE=/path/to/PyEBSDIndex python tests/golden/make_golden.py
 
 The reference's CPU ``BandDetect.find_bands`` (band_detect.py:411-526) is imported through

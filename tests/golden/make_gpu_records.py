@@ -4,10 +4,9 @@ Run from the repository root on a machine with a CUDA GPU and the built library:
 
     python tests/golden/make_gpu_records.py [out.npz]     # default tests/golden/orient_80x80_gpu.npz
 
-Reads ``tests/golden/orient_80x80.npz`` (made by ``make_orientation_golden.py``), installs the
-reference's lookup table from ``tests/golden/c1_80_u8.npz`` (same geometry; the host's
-float32 sin/cos cannot perturb it) and stores, per method, every band-record field the
-indexer reads.  ``tests/test_orientation_agreement.py`` indexes these with the reference's
+Reads ``tests/golden/orient_80x80.npz`` (made by ``make_orientation_golden.py``), detects its
+patterns with the plan this host builds (the product's own Radon table) and stores, per
+method, every band-record field the indexer reads.  ``tests/test_orientation_agreement.py`` indexes these with the reference's
 triplet voting.
 """
 from __future__ import annotations
@@ -34,7 +33,6 @@ def main():
     p = json.loads(str(fx["params"]))
     bd = pg.BandDetect(**p)
     bd.band_detect_setup(patDim=(80, 80), patternmask=syn.circular_mask(80, 80))
-    bd.radonPlan.indexPlan = np.load(os.path.join(HERE, "c1_80_u8.npz"))["lut"].astype(np.int64)
     rec = {}
     for m in METHODS:
         r = bd.find_bands(fx["patterns"], method=m)
