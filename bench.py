@@ -46,7 +46,7 @@ BYTES_PER_PATTERN = H * W * 1 + 41 * NBANDS   # algorithmic bytes: pattern in, b
 DRAM_BYTES_PER_PATTERN = (648_438_528 + 2_272_787_200) / 40_000
 # warp instructions per pattern of the same kernel (ncu smsp__inst_executed.sum, same capture):
 # the issue roofline of an issue-bound kernel is 4 warp-instructions per SM per clock
-WARP_INST_PER_PATTERN = 6.55e9 / 40_000
+WARP_INST_PER_PATTERN = 6.546e9 / 40_000
 ACCURACY_PATTERNS = 32_768      # timed-batch patterns graded against plain64 (FP64 GPU oracle)
 ORACLE_PATTERNS = 2_048         # of those, graded against the oracle's FFT path (CPU leg)
 SEED = 1_000_000

@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libebsdgpu.so")
 
-SOURCES = ["plan.cu", "plain.cu", "fused.cu", "noalloc.cu", "nlpar.cu", "diff.cu", "poles.cu", "vote.cu", "patfile.cu"]
+SOURCES = ["plan.cu", "plain.cu", "fused.cu", "slab.cu", "noalloc.cu", "nlpar.cu", "diff.cu", "poles.cu", "vote.cu", "patfile.cu"]
 HEADERS = ["ebsd_internal.cuh", "label.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v"]

@@ -34,6 +34,18 @@ struct FusedGeom {
     int quad = 0;               // the 4/8-patterns-per-pass tile (8-byte elements) fits
 };
 
+// Theta-slab fused geometry (slab.cu): plans whose padded Radon image does not fit on chip
+// next to its LoG image run the fused path in theta slabs of up to Ts output columns.
+struct SlabGeom {
+    int ok = 0;                 // the slab kernel takes this plan (uint8 / uint16 input)
+    int ok_f32 = 0;             // ... and float32 input (a float32 pattern tile fits)
+    int nslab = 0, Ts = 0;      // slabs; widest slab's output columns
+    int maxg = 0;               // most 32-ray groups of one slab
+    int TR = 0, TBP = 0, CCP = 0, MP = 0, rho0 = 0, rpad_end = 0, CR = 0, statR = 0;
+    int pitch = 0;              // pattern tile row pitch (elements)
+    int smem[3] = {0, 0, 0};    // dynamic shared memory bytes per dtype (uint8, uint16, float32)
+};
+
 struct Workspace {
     void* ptr = nullptr;
     size_t bytes = 0;
@@ -81,6 +93,12 @@ struct ebsd_plan_s {
     // patterns per block pass of the fused FP32 uint8 kernel: -1 = rule (the most the plan
     // allows: 8, else 2), else 1, 2, 4 or 8 as chosen by ebsd_plan_autotune
     int fused_ppp = -1;
+
+    // theta-slab fused tables (see slab.cu)
+    ebsd::SlabGeom sg;
+    uint16_t* d_slut = nullptr;    // per-slab, per-warp LUT streams (pattern element offsets)
+    int32_t* d_stab = nullptr;     // [gst][gtb][slab_g][slab_j][wofs][count]
+    int32_t s_gst = 0, s_gtb = 0, s_slabg = 0, s_slabj = 0, s_wofs = 0, s_count = 0;  // offsets into d_stab
 
     // ---- workspaces ----
     std::mutex mtx;
@@ -160,5 +178,13 @@ size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t chunk);
 int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t n);
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches);
+
+// Theta-slab fused path: slab.cu -----------------------------------------------------------
+int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d);
+void slab_release(ebsd_plan_s* p);
+// the slab kernel serves this (method, dtype): FP32 method, plan too large for the single tile
+bool slab_serves(const ebsd_plan_s* p, int method, int dtype);
+int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
+                   int64_t out_offset, cudaStream_t st, int64_t* launches);
 
 }  // namespace ebsd

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
     // offset 0: the LUT then holds byte offsets usable directly as load addresses
     float* conv = (float*)(smem + off);
     float* pat = conv;  // aliased: the pattern tile is dead once the Radon is built
-    off += ((size_t)a.CR * (a.CC | 1) * sizeof(float) + 15) & ~(size_t)15;
+    off += ((size_t)(a.CR + 2 * H0) * (a.CC | 1) * sizeof(float) + 15) & ~(size_t)15;  // two-pass conv
     S* tile = (S*)(smem + off);
     {
         // the Radon tile region also holds the peaks' theta-max rows once the tile is dead
@@ -603,19 +603,103 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
             asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nxt), "r"(a.nRaysPad * 4) : "memory");
         }
 
-        // ---- 4. LoG convolution: conv[cr][cc] = sum_a sum_b tap[a][b] tile[cr+2H0-a][cc+2H1-b],
-        //      kRowBlock outputs per thread down one column.  The last row block is moved up to
-        //      end at CR, so no load leaves the tile; rows it shares with the block above are
-        //      neither stored again nor counted twice.
+        // ---- 4. LoG convolution: conv[cr][cc] = sum_a sum_b tap[a][b] tile[cr+2H0-a][cc+2H1-b]
+        //      with the statistics slice's min and sum on the fly (padded rows [stat_r0,
+        //      stat_r1) x columns [stat_c0, stat_c1), i.e. conv rows from D0 and conv columns
+        //      [D1, D1 + nTheta)).
         float smin = INFINITY, ssum = 0.0f;
-        {
+        const unsigned stat_rows = (unsigned)(stat_r1 - stat_r0);
+        if (a.sep) {
+            // Separable taps (the reference's LoG is a Gaussian second derivative along rho
+            // times a Gaussian along theta), in two passes through the conv region, which holds
+            // TR rows: (a) theta taps along every Radon tile row, h[r][cc] = sum_b kw[b]
+            // tile[r][cc + 2H1 - b] (ascending b), 16 outputs per thread from a sliding row of
+            // 16 + K1 - 1 loads, lanes on neighbouring rows; (b) rho taps down each column,
+            // conv[cr][cc] = sum_a ku[a] h[cr + 2H0 - a][cc] (ascending a), in place: each
+            // thread walks a strip of rows of one column with a register window of K0 h rows
+            // and writes each output over its own h row as soon as it is computed (later
+            // outputs of the strip read only later rows).  The strip above reads this strip's
+            // first 2H0 h rows, so those outputs are held in registers and written after a
+            // barrier.  The multiply-add order is the per-stage FP32 kernel's.
+            constexpr int kSegA = 16;
+            const int TR = a.CR + 2 * H0;
+            {
+                const int nseg = (CC + kSegA - 1) / kSegA;
+                for (int task = tid; task < TR * nseg; task += kThreads) {
+                    const int sg = task / TR, r = task - sg * TR;
+                    const int c0 = sg * kSegA < CC - kSegA ? sg * kSegA : CC - kSegA;
+                    const S* trow = tile + r * TP + c0;
+                    float x[kSegA + K1 - 1];
+#pragma unroll
+                    for (int k = 0; k < kSegA + K1 - 1; ++k) x[k] = to_f(trow[k]);
+                    float* hrow = conv + r * CP + c0;
+#pragma unroll
+                    for (int j = 0; j < kSegA; ++j) {
+                        float hv = 0.0f;
+#pragma unroll
+                        for (int b = 0; b < K1; ++b) hv = fmaf(a.kw[b], x[j + 2 * H1 - b], hv);
+                        hrow[j] = hv;
+                    }
+                }
+            }
+            __syncthreads();
+            {
+                const int CR = a.CR;
+                // strips per column: as many as fit one task per thread (at least 8 rows each)
+                const int nstrip = CC >= kThreads ? 1 : (kThreads / CC < (CR + 7) / 8 ? kThreads / CC : (CR + 7) / 8);
+                const int L = (CR + nstrip - 1) / nstrip;
+                const int ntask = nstrip * CC;
+                // more than one round only with one strip per column (no strip boundaries)
+                const int rounds = (ntask + kThreads - 1) / kThreads;
+                for (int rd = 0; rd < rounds; ++rd) {
+                    const int task = rd * kThreads + tid;
+                    const int st = task < ntask ? task / CC : 0, cc = task < ntask ? task - st * CC : 0;
+                    const int o0 = st * L, o1 = task < ntask ? (o0 + L < CR ? o0 + L : CR) : 0;
+                    float* hcol = conv + cc;
+                    const bool colstat = (unsigned)(cc - D1) < (unsigned)nT;
+                    float w[K0], held[K0 - 1];
+#pragma unroll
+                    for (int k = 0; k < K0 - 1; ++k) {
+                        w[k] = o0 < o1 ? hcol[(o0 + k) * CP] : 0.0f;
+                        held[k] = 0.0f;
+                    }
+                    // window slot of h row (o0 + m): m mod K0; K0 outputs per step keep every
+                    // slot index a constant
+                    for (int o = o0; o < o1; o += K0) {
+#pragma unroll
+                        for (int j = 0; j < K0; ++j) {
+                            const int oj = o + j;
+                            if (oj < o1) {
+                                w[(j + K0 - 1) % K0] = hcol[(oj + K0 - 1) * CP];
+                                float acc = 0.0f;
+#pragma unroll
+                                for (int ka = 0; ka < K0; ++ka) acc = fmaf(a.ku[ka], w[(j + K0 - 1 - ka) % K0], acc);
+                                if (kHalf) acc = fmaf(a.ksum, cen, acc * inv_scl);
+                                if (j < K0 - 1 && o == o0) held[j < K0 - 1 ? j : 0] = acc;
+                                else hcol[oj * CP] = acc;
+                                if (colstat && (unsigned)(oj - D0) < stat_rows) {
+                                    smin = fminf(smin, acc);
+                                    ssum += acc;
+                                }
+                            }
+                        }
+                    }
+                    __syncthreads();
+#pragma unroll
+                    for (int k = 0; k < K0 - 1; ++k)
+                        if (o0 + k < o1) hcol[(o0 + k) * CP] = held[k];
+                }
+            }
+        } else {
+            // 2-D taps: kRowBlock outputs per thread down one column.  The last row block is
+            // moved up to end at CR, so no load leaves the tile; rows it shares with the block
+            // above are neither stored again nor counted twice.
             const int CR = a.CR;
             const int nrb = (CR + kRowBlock - 1) / kRowBlock;
             const int ntask = nrb * CC;
             // task = rb * CC + cc, advanced by kThreads without a division per task
             int cc = tid % CC, rb = tid / CC;
             const int dcc = kThreads % CC, drb = kThreads / CC;
-            const unsigned stat_rows = (unsigned)(stat_r1 - stat_r0);
             for (int task = tid; task < ntask; task += kThreads) {
                 const int cr_first = rb * kRowBlock;
                 const int cr0 = cr_first < CR - kRowBlock ? cr_first : CR - kRowBlock;
@@ -625,40 +709,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 // tile row (cr0 + t) feeds output o through kernel row a = o + 2*H0 - t;
                 // descending t keeps each output's multiply-add order = ascending a.
                 const S* tcol = tile + cr0 * TP + cc + 2 * H1;
-                if (a.sep) {
-                    // separable taps: theta convolution of each tile row (kw, ascending b),
-                    // then the rho taps (ku, ascending a) -- 10 multiply-adds per output
-                    // instead of 25, the per-stage FP32 kernel's order
-                    float hr[kRowBlock + 2 * H0];
 #pragma unroll
-                    for (int t = 0; t < kRowBlock + 2 * H0; ++t) {
-                        float hv = 0.0f;
+                for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
+                    float v[K1];
 #pragma unroll
-                        for (int b = 0; b < K1; ++b) hv = fmaf(a.kw[b], to_f(tcol[t * TP - b]), hv);
-                        hr[t] = hv;
-                    }
+                    for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[t * TP - b]);
 #pragma unroll
-                    for (int o = 0; o < kRowBlock; ++o)
+                    for (int o = 0; o < kRowBlock; ++o) {
+                        const int ka = o + 2 * H0 - t;
+                        if (ka >= 0 && ka < K0) {
 #pragma unroll
-                        for (int ka = 0; ka < K0; ++ka) acc[o] = fmaf(a.ku[ka], hr[o + 2 * H0 - ka], acc[o]);
-                } else {
-#pragma unroll
-                    for (int t = kRowBlock + 2 * H0 - 1; t >= 0; --t) {
-                        float v[K1];
-#pragma unroll
-                        for (int b = 0; b < K1; ++b) v[b] = to_f(tcol[t * TP - b]);
-#pragma unroll
-                        for (int o = 0; o < kRowBlock; ++o) {
-                            const int ka = o + 2 * H0 - t;
-                            if (ka >= 0 && ka < K0) {
-#pragma unroll
-                                for (int b = 0; b < K1; ++b) acc[o] = fmaf(a.taps[ka * K1 + b], v[b], acc[o]);
-                            }
+                            for (int b = 0; b < K1; ++b) acc[o] = fmaf(a.taps[ka * K1 + b], v[b], acc[o]);
                         }
                     }
                 }
-                // statistics slice: padded rows [stat_r0, stat_r1) x columns [stat_c0, stat_c1),
-                // i.e. conv rows from D0 and conv columns [D1, D1 + nTheta)
                 const bool colstat = (unsigned)(cc - D1) < (unsigned)nT;
                 float* ccol = conv + cr0 * CP + cc;
 #pragma unroll
@@ -819,7 +883,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 size_t smem_bytes(const FusedGeom& g, size_t store, int ngroups, size_t tm_bytes) {
     // odd row pitches, as the kernel lays the tiles out
     size_t b = (std::max((size_t)(g.row1 - g.row0) * ((g.col1 - g.col0) | 1) * store, tm_bytes) + 15) & ~(size_t)15;
-    b += ((size_t)(g.crow1 - g.crow0) * ((g.ccol1 - g.ccol0) | 1) * 4 + 15) & ~(size_t)15;
+    b += ((size_t)(g.row1 - g.row0) * ((g.ccol1 - g.ccol0) | 1) * 4 + 15) & ~(size_t)15;
     b += (size_t)kWarps * kMaxBands * 8 + 32 * 8 + 80 * 4;
     b += (size_t)ngroups * 8 + 2 * (kWarps + 1) * 4;
     return b;
@@ -857,7 +921,8 @@ void* pick_kernel(int method, int dtype, int k0, int k1, int pack, int nTheta) {
 // pixels; four or eight per pass also need the 8-byte-element tile and its LUT (fg.quad).
 // Returns the largest patterns-per-pass the call may use (1, 2 or 8).
 int max_pack(const ebsd_plan_s* p, int method, int dtype, int64_t n) {
-    if (!(dtype == EBSD_U8 && method == EBSD_FUSED_F32 && p->bg_mode == 0 && p->maxCount <= 257 && n >= 2))
+    if (!(dtype == EBSD_U8 && method == EBSD_FUSED_F32 && p->fg.ok_f32 && p->bg_mode == 0 && p->maxCount <= 257 &&
+          n >= 2))
         return 1;
     return p->fg.quad && p->d_flut8 ? 8 : 2;
 }
@@ -1158,9 +1223,22 @@ void fused_release(ebsd_plan_s* p) {
 }
 
 int fused_supported(const ebsd_plan_s* p, int method) {
+    // plans too large for the single tile run the FP32 method in theta slabs (slab.cu)
+    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32 && p->sg.ok) return 1;
     if (!p->fg.ok) return 0;
     if (method == EBSD_FUSED_F32) return p->fg.ok_f32;
     return method == EBSD_FUSED_F16;
+}
+
+void band_epilogue_launch(const ebsd_bands& out, int64_t out_offset, int64_t n, int nB, const LabelConsts& kc,
+                          int sms, cudaStream_t st) {
+    const int64_t nbands = n * nB;
+    ebsd_bands ob = out;
+    const int64_t o0 = out_offset * nB;
+    ob.max += o0; ob.normmax += o0; ob.maxloc += 2 * o0; ob.avemax += o0; ob.aveloc += 2 * o0;
+    ob.width += o0; ob.theta += o0; ob.rho += o0; ob.valid += o0;
+    const int eblocks = (int)std::min<int64_t>((nbands + 255) / 256, (int64_t)sms * 8);
+    if (eblocks > 0) k_band_epilogue<<<eblocks, 256, 0, st>>>(ob, nbands, kc);
 }
 
 // packed-mode scratch: (patterns per pass - 1) rows of parked ray means per resident CTA
@@ -1182,6 +1260,10 @@ int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
     if (n <= 0) return EBSD_OK;
+    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) {
+        if (!slab_serves(p, method, dtype)) return EBSD_E_UNSUPPORTED;
+        return slab_run_chunk(p, dtype, d_pats, n, out, out_offset, st, launches);
+    }
     const int pack = fused_patterns_per_pass(p, method, dtype, n);
     void* fn = pick_kernel(method, dtype, p->k0, p->k1, pack, p->nTheta);
     if (!fn) return EBSD_E_UNSUPPORTED;
@@ -1262,15 +1344,10 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     EBSD_CUDA_TRY(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kThreads), args, (size_t)smem, st));
     // the float64 part of the band fit (width, theta, rho) as a separate elementwise pass, so
     // that the fused kernel's label warp is not held up by float64 latency
-    const int64_t nbands = n * p->nB;
-    ebsd_bands ob = *out;
-    const int64_t o0 = out_offset * p->nB;
-    ob.max += o0; ob.normmax += o0; ob.maxloc += 2 * o0; ob.avemax += o0; ob.aveloc += 2 * o0;
-    ob.width += o0; ob.theta += o0; ob.rho += o0; ob.valid += o0;
-    const int eblocks = (int)std::min<int64_t>((nbands + 255) / 256, (int64_t)sms * 8);
-    k_band_epilogue<<<eblocks, 256, 0, st>>>(ob, nbands, a.kc);
+    band_epilogue_launch(*out, out_offset, n, p->nB, a.kc, sms, st);
     *launches += 2;
     return launch_status();
 }
 
 }  // namespace ebsd
+

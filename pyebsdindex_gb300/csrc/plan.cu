@@ -38,6 +38,7 @@ void free_plan_tables(ebsd_plan_s* p) {
     cudaFree(p->d_bg);
     cudaFree(p->d_bgf);
     fused_release(p);
+    slab_release(p);
     cudaFree(p->ws.ptr);
     p->ws = Workspace{};
     cudaFree(p->stats.ptr);
@@ -615,6 +616,7 @@ int ebsd_plan_create(const ebsd_plan_desc* d, int device, ebsd_plan_t* out) {
         }
     }
     if (rc == EBSD_OK) rc = fused_prepare(p, d);
+    if (rc == EBSD_OK) rc = slab_prepare(p, d);
     if (rc != EBSD_OK) {
         free_plan_tables(p);
         delete p;

@@ -1,0 +1,811 @@
+// Fused band detection in theta slabs, for plans whose padded Radon image does not fit in
+// shared memory next to its LoG image (120x120 and 240x240 patterns with nRho = 1.5 * size).
+//
+// One persistent CTA per SM, one pattern at a time.  The pattern stays in shared memory
+// (uint8 / uint16 / float32 elements as stored) while the theta range is processed in slabs
+// of Ts output columns.  For each slab:
+//   1. radon   the rays of the slab's Ts columns plus D1 + H1 columns on either side (the max
+//              filter's and the LoG's theta reach), one ray per lane as in the single-tile
+//              kernel: per-warp streams of 32-ray groups (32 neighbouring rho at one theta),
+//              8 pattern-element offsets per lane per 16-byte LUT load, sums in the LUT's
+//              column (or row) order -- exact integers for uint8/uint16 patterns -- and the
+//              mean as a correctly rounded quotient (rdn_loops, radon_fast.py:281-310).
+//              Columns beyond theta 0 / 180 deg are the theta-wrapped rays written rho-flipped,
+//              as band_detect.py:573-575 pads the Radon image.
+//   2. pad     rho padding rows: the first / last interior row, zero from row R on
+//              (band_detect.py:578-580 and the FFT convolution's zero extension).
+//   3. conv    two-pass separable LoG (theta taps along rows, rho taps down columns in place)
+//              with the multiply-add order of the per-stage kernels; the statistics slice's
+//              min and sum accumulate over the slabs' own columns.
+//   4. peaks   theta max of the conv rows, rho max, exact equality with the conv value and
+//              the Radon mask (band_detect.py:639-664); warp top-N lists ordered by (value
+//              desc, position asc) with positions i * nTheta + j of the whole image.
+//   5. merge   warp 0 takes the slab's best nB peaks (k-way tournament over the warp lists)
+//              with their 3x3 conv blocks and merges them into the pattern's running top-N,
+//              while the other warps start the next slab.  Under one strict total order the
+//              top-N of the union equals the top-N of the slabs' top-N lists, so the bands equal
+//              those of the single-tile kernel.
+// After the last slab: the min / mean reduction and the band fits (band_detect.py:691-809)
+// from the captured blocks; width, theta and rho in float64 by the shared epilogue pass.
+#include "ebsd_internal.cuh"
+#include "label.cuh"
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+
+namespace ebsd {
+
+void band_epilogue_launch(const ebsd_bands& out, int64_t out_offset, int64_t n, int nB, const LabelConsts& kc,
+                          int sms, cudaStream_t st);
+
+namespace {
+
+constexpr int kThreads = 1024;
+constexpr int kWarps = kThreads / 32;
+constexpr int kRowBlock = 8;
+constexpr int kRing = 2;
+constexpr int kBlk = 12;  // running top-N entry: value, position, 9 conv values, pad
+
+struct SlabArgs {
+    const void* pats;
+    int64_t n;
+    int H, W, pitch;           // pattern tile: H rows of pitch W + 1 elements, then one zero element
+    const uint4* lut;          // per-slab, per-warp streams of 8 element offsets per lane per chunk
+    const uint32_t* gst;       // [all slabs' groups] source group id | chunks << 16
+    const uint32_t* gtb;       // same order: tile offset of lane 0 | rays << 16 | rho-flipped << 22
+    const int32_t* slab_g;     // [nslab + 1] first group of each slab
+    const int32_t* slab_j;     // [nslab + 1] first output theta column of each slab
+    const int32_t* wofs;       // [nslab][2 * (kWarps + 1)] per-warp first group (slab-relative), first chunk
+    const int32_t* count;      // [nTheta * gpt * 32] in-mask pixels of each ray (source group * 32 + lane)
+    int nslab, maxg;
+    int nRho, nTheta, nB;
+    int p0, p1;
+    int TR, TBP, CCP, MP;      // Radon tile rows, Radon / conv / theta-max pitches
+    int rho0;                  // tile row of interior row 0 (p0 - row0)
+    int rpad_end;              // tile rows from here on are zero (padded row R)
+    int CR;                    // conv rows
+    int statR;                 // statistics rows (conv rows [D0, D0 + statR))
+    float ku[9], kw[9];
+    const uint8_t* rdnmask;
+    LabelConsts kc;
+    ebsd_bands out;
+    int64_t out_offset;
+};
+
+__device__ __forceinline__ bool beats(float v, int p, float w, int q) {
+    return v > w || (v == w && p < q);
+}
+
+__device__ __forceinline__ void list_insert(float v, int pos, float& lv, int& lp, int nB, int lane) {
+    unsigned ahead = __ballot_sync(0xffffffffu, lane < nB && lp >= 0 && beats(lv, lp, v, pos));
+    int ins = __popc(ahead);
+    if (ins < nB) {
+        float uv = __shfl_up_sync(0xffffffffu, lv, 1);
+        int up = __shfl_up_sync(0xffffffffu, lp, 1);
+        if (lane > ins && lane < nB) { lv = uv; lp = up; }
+        if (lane == ins) { lv = v; lp = pos; }
+    }
+}
+
+template <typename InT, int K0, int K1>
+__global__ void __launch_bounds__(kThreads, 1) k_slab(SlabArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int D0 = K0, D1 = K1;          // max-filter half windows (peakPad = 2*ksz + 1)
+    constexpr int H1 = K1 / 2;               // LoG half width along theta
+    constexpr int WIN = 2 * D1 + 1;
+    constexpr int NV = kRowBlock + 2 * D0;
+    constexpr bool kInt = sizeof(InT) < 4;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nB = a.nB, TBP = a.TBP, CCP = a.CCP, MP = a.MP;
+
+    size_t off = 0;
+    InT* pat = (InT*)(smem + off);
+    off += ((size_t)(a.H * a.pitch + 1) * sizeof(InT) + 15) & ~(size_t)15;
+    float* tile = (float*)(smem + off);  // Radon slab; later the theta-max rows
+    off += ((size_t)a.TR * TBP * sizeof(float) + 15) & ~(size_t)15;
+    float* conv = (float*)(smem + off);  // TR rows: the two-pass convolution's theta pass
+    off += ((size_t)a.TR * CCP * sizeof(float) + 15) & ~(size_t)15;
+    float* lv_s = (float*)(smem + off);
+    off += kWarps * kMaxBands * sizeof(float);
+    int* lp_s = (int*)(smem + off);
+    off += kWarps * kMaxBands * sizeof(int);
+    float* run = (float*)(smem + off);   // running top-N: [kMaxBands][kBlk], ping-pong
+    off += 2 * kMaxBands * kBlk * sizeof(float);
+    float* red_f = (float*)(smem + off);
+    off += 80 * sizeof(float);
+    double* red_d = (double*)(smem + off);
+    off += 32 * sizeof(double);
+    int* wofs_s = (int*)(smem + off);
+    off += 2 * (kWarps + 1) * sizeof(int);
+    unsigned* gst_s = (unsigned*)(smem + off);
+    off += (size_t)a.maxg * sizeof(unsigned);
+    unsigned* gtb_s = (unsigned*)(smem + off);
+
+    const int stat_rows = a.statR;
+    for (int64_t q = blockIdx.x; q < a.n; q += gridDim.x) {
+        // ---- the pattern into shared memory; one zero element after it (the LUT's pad slot)
+        {
+            const InT* gp = (const InT*)a.pats + q * (int64_t)a.H * a.W;
+            for (int y = warp; y < a.H; y += kWarps)
+                for (int x = lane; x < a.W; x += 32) pat[y * a.pitch + x] = gp[y * a.W + x];
+            if (tid == 0) pat[a.H * a.pitch] = (InT)0;
+        }
+        float smin = INFINITY, ssum = 0.0f;
+        int cur = 0;  // running list buffer
+        if (tid < kMaxBands) {
+            run[tid * kBlk + 1] = __int_as_float(-1);
+            run[kMaxBands * kBlk + tid * kBlk + 1] = __int_as_float(-1);
+        }
+
+        // slab merge (warp 0): the slab's nB best peaks from the warp lists, their 3x3 conv
+        // blocks from the conv region, merged into the running list by rank
+        auto slab_merge = [&](int j0) {
+            int ptr = 0;
+            float hv = lane < kWarps ? lv_s[lane * kMaxBands] : -INFINITY;
+            int hp = lane < kWarps ? lp_s[lane * kMaxBands] : -1;
+            int mypos = -1;
+            float myval = 0.0f;
+            for (int k = 0; k < nB; ++k) {
+                const unsigned u = __float_as_uint(hv + 0.0f);
+                const unsigned key = hp < 0 ? 0u : ((u & 0x80000000u) ? ~u : (u | 0x80000000u));
+                const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+                if (kmax == 0u) break;
+                const unsigned pmin = __reduce_min_sync(0xffffffffu, key == kmax ? (unsigned)hp : 0xffffffffu);
+                const unsigned win = __ballot_sync(0xffffffffu, key == kmax && (unsigned)hp == pmin);
+                const float wv = __shfl_sync(0xffffffffu, hv, __ffs(win) - 1);
+                if (lane == k) { mypos = (int)pmin; myval = wv; }
+                if (lane == __ffs(win) - 1) {
+                    ++ptr;
+                    hp = ptr < nB ? lp_s[lane * kMaxBands + ptr] : -1;
+                    hv = ptr < nB ? lv_s[lane * kMaxBands + ptr] : -INFINITY;
+                }
+            }
+            float blk[9];
+#pragma unroll
+            for (int k9 = 0; k9 < 9; ++k9) blk[k9] = 0.0f;
+            if (mypos >= 0) {
+                const int i = mypos / a.nTheta, j = mypos - i * a.nTheta - j0;
+                const float* c0 = conv + (i + D0 - 1) * CCP + (j + D1 - 1);
+#pragma unroll
+                for (int r3 = 0; r3 < 3; ++r3)
+#pragma unroll
+                    for (int c3 = 0; c3 < 3; ++c3) blk[r3 * 3 + c3] = c0[r3 * CCP + c3];
+            }
+            // ranks: a slab entry counts the running entries ahead of it, a running entry the
+            // slab entries ahead of it; positions are unique, so the ranks are distinct
+            const float* ro = run + cur * kMaxBands * kBlk;
+            float* rn = run + (cur ^ 1) * kMaxBands * kBlk;
+            const float rv = lane < nB ? ro[lane * kBlk] : 0.0f;
+            const int rp = lane < nB ? __float_as_int(ro[lane * kBlk + 1]) : -1;
+            int rank_s = lane, rank_r = lane;
+            for (int k = 0; k < nB; ++k) {
+                const float ov = __shfl_sync(0xffffffffu, rv, k);
+                const int op = __shfl_sync(0xffffffffu, rp, k);
+                const float sv = __shfl_sync(0xffffffffu, myval, k);
+                const int sp = __shfl_sync(0xffffffffu, mypos, k);
+                if (op >= 0 && beats(ov, op, myval, mypos)) ++rank_s;
+                if (sp >= 0 && beats(sv, sp, rv, rp)) ++rank_r;
+            }
+            if (lane < nB && mypos >= 0 && rank_s < nB) {
+                float* d = rn + rank_s * kBlk;
+                d[0] = myval;
+                d[1] = __int_as_float(mypos);
+#pragma unroll
+                for (int k9 = 0; k9 < 9; ++k9) d[2 + k9] = blk[k9];
+            }
+            if (lane < nB && rp >= 0 && rank_r < nB) {
+                float* d = rn + rank_r * kBlk;
+                const float* s = ro + lane * kBlk;
+#pragma unroll
+                for (int k = 0; k < 11; ++k) d[k] = s[k];
+            }
+            // slots past the merged entries stay empty
+            const int nsl = __popc(__ballot_sync(0xffffffffu, lane < nB && mypos >= 0));
+            const int nrn = __popc(__ballot_sync(0xffffffffu, lane < nB && rp >= 0));
+            if (lane < nB && lane >= nsl + nrn) rn[lane * kBlk + 1] = __int_as_float(-1);
+            __syncwarp();
+        };
+
+        for (int s = 0; s < a.nslab; ++s) {
+            const int j0 = __ldg(a.slab_j + s), Ts = __ldg(a.slab_j + s + 1) - j0;
+            const int gbeg = __ldg(a.slab_g + s), ng = __ldg(a.slab_g + s + 1) - gbeg;
+            // (the previous slab's merge, below, reads only the warp lists and the conv region)
+            for (int i = tid; i < ng; i += kThreads) {
+                gst_s[i] = __ldg(a.gst + gbeg + i);
+                gtb_s[i] = __ldg(a.gtb + gbeg + i);
+            }
+            for (int i = tid; i < 2 * (kWarps + 1); i += kThreads) wofs_s[i] = __ldg(a.wofs + s * 2 * (kWarps + 1) + i);
+            __syncthreads();
+            if (s > 0 && warp == 0) {
+                slab_merge(__ldg(a.slab_j + s - 1));
+                cur ^= 1;
+            }
+
+            // ---- 1. Radon of the slab's columns, one ray per lane
+            {
+                const int g0 = wofs_s[warp], g1 = wofs_s[warp + 1];
+                const uint4* ip = a.lut + ((size_t)wofs_s[kWarps + 1 + warp] * 32 + lane);
+                uint4 ring[kRing];
+#pragma unroll
+                for (int k = 0; k < kRing; ++k) ring[k] = __ldg(ip + (size_t)k * 32);
+                ip += (size_t)kRing * 32;
+                int gi = g0, pc = 0;
+                unsigned gs = gi < g1 ? gst_s[gi] : 0u;
+                int t = (int)(gs & 0xFFFFu) * 32 + lane;
+                int cnt = gi < g1 ? __ldg(a.count + t) : 0;
+                unsigned isum = 0u;
+                float fsum = 0.0f;
+                while (gi < g1) {
+#pragma unroll
+                    for (int k = 0; k < kRing; ++k) {
+                        if (gi < g1) {
+                            const uint4 e = ring[k];
+                            ring[k] = __ldg(ip);
+                            ip += 32;
+                            const unsigned o[8] = {e.x & 0xFFFF, e.x >> 16, e.y & 0xFFFF, e.y >> 16,
+                                                   e.z & 0xFFFF, e.z >> 16, e.w & 0xFFFF, e.w >> 16};
+#pragma unroll
+                            for (int k8 = 0; k8 < 8; ++k8) {
+                                if (kInt) isum += (unsigned)pat[o[k8]];
+                                else fsum = __fadd_rn(fsum, (float)pat[o[k8]]);
+                            }
+                            if (++pc == (int)(gs >> 16)) {
+                                // ray ends: the mean of an empty ray is -1 (radon_fast.py:265)
+                                const float v = cnt > 0 ? __fdiv_rn(kInt ? (float)isum : fsum, (float)cnt) : -1.0f;
+                                const unsigned tb = gtb_s[gi];
+                                const int stride = (tb >> 22) & 1 ? -TBP : TBP;
+                                if (lane < (int)((tb >> 16) & 63)) tile[(int)(tb & 0xFFFFu) + lane * stride] = v;
+                                ++gi;
+                                pc = 0;
+                                isum = 0u;
+                                fsum = 0.0f;
+                                if (gi < g1) {
+                                    gs = gst_s[gi];
+                                    t = (int)(gs & 0xFFFFu) * 32 + lane;
+                                    cnt = __ldg(a.count + t);
+                                }
+                            }
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+
+            // ---- 2. rho padding rows of every buffer column
+            {
+                const int TB = Ts + 2 * (D1 + H1);
+                const int top = a.rho0, bot = a.rho0 + a.nRho;  // interior tile rows [top, bot)
+                const int npadrow = top + (a.TR - bot);
+                for (int k = tid; k < npadrow * TB; k += kThreads) {
+                    const int pr = k / TB, c = k - pr * TB;
+                    const int r = pr < top ? pr : bot + (pr - top);
+                    float v;
+                    if (r >= a.rpad_end) v = 0.0f;
+                    else v = tile[(r < top ? top : bot - 1) * TBP + c];
+                    tile[r * TBP + c] = v;
+                }
+            }
+            __syncthreads();
+
+            // ---- 3. LoG convolution, two separable passes (as the single-tile kernel)
+            const int CCs = Ts + 2 * D1;
+            {
+                constexpr int kSegA = 16;
+                const int nseg = (CCs + kSegA - 1) / kSegA;
+                for (int task = tid; task < a.TR * nseg; task += kThreads) {
+                    const int sg = task / a.TR, r = task - sg * a.TR;
+                    const int c0 = sg * kSegA < CCs - kSegA ? sg * kSegA : CCs - kSegA;
+                    const float* trow = tile + r * TBP + c0;
+                    float x[kSegA + K1 - 1];
+#pragma unroll
+                    for (int k = 0; k < kSegA + K1 - 1; ++k) x[k] = trow[k];
+                    float* hrow = conv + r * CCP + c0;
+#pragma unroll
+                    for (int j = 0; j < kSegA; ++j) {
+                        float hv = 0.0f;
+#pragma unroll
+                        for (int b = 0; b < K1; ++b) hv = fmaf(a.kw[b], x[j + 2 * H1 - b], hv);
+                        hrow[j] = hv;
+                    }
+                }
+            }
+            __syncthreads();
+            {
+                const int CR = a.CR;
+                const int nstrip = CCs >= kThreads ? 1 : (kThreads / CCs < (CR + 7) / 8 ? kThreads / CCs : (CR + 7) / 8);
+                const int L = (CR + nstrip - 1) / nstrip;
+                const int ntask = nstrip * CCs;
+                const int rounds = (ntask + kThreads - 1) / kThreads;
+                for (int rd = 0; rd < rounds; ++rd) {
+                    const int task = rd * kThreads + tid;
+                    const int st = task < ntask ? task / CCs : 0, cc = task < ntask ? task - st * CCs : 0;
+                    const int o0 = st * L, o1 = task < ntask ? (o0 + L < CR ? o0 + L : CR) : 0;
+                    float* hcol = conv + cc;
+                    // statistics columns: this slab's own theta columns
+                    const bool colstat = (unsigned)(cc - D1) < (unsigned)Ts;
+                    float w[K0], held[K0 - 1];
+#pragma unroll
+                    for (int k = 0; k < K0 - 1; ++k) {
+                        w[k] = o0 < o1 ? hcol[(o0 + k) * CCP] : 0.0f;
+                        held[k] = 0.0f;
+                    }
+                    for (int o = o0; o < o1; o += K0) {
+#pragma unroll
+                        for (int j = 0; j < K0; ++j) {
+                            const int oj = o + j;
+                            if (oj < o1) {
+                                w[(j + K0 - 1) % K0] = hcol[(oj + K0 - 1) * CCP];
+                                float acc = 0.0f;
+#pragma unroll
+                                for (int ka = 0; ka < K0; ++ka) acc = fmaf(a.ku[ka], w[(j + K0 - 1 - ka) % K0], acc);
+                                if (j < K0 - 1 && o == o0) held[j < K0 - 1 ? j : 0] = acc;
+                                else hcol[oj * CCP] = acc;
+                                if (colstat && (unsigned)(oj - D0) < (unsigned)stat_rows) {
+                                    smin = fminf(smin, acc);
+                                    ssum += acc;
+                                }
+                            }
+                        }
+                    }
+                    __syncthreads();
+#pragma unroll
+                    for (int k = 0; k < K0 - 1; ++k)
+                        if (o0 + k < o1) hcol[(o0 + k) * CCP] = held[k];
+                }
+            }
+            __syncthreads();
+
+            // ---- 4a. theta max of the conv rows the rho window needs (into the dead Radon tile)
+            float* tm = tile;
+            {
+                const int NR = a.nRho + 2 * D0;
+                const int nseg = (Ts + WIN - 1) / WIN;
+                for (int task = tid; task < NR * nseg; task += kThreads) {
+                    const int sg = task / NR, rr = task - sg * NR;
+                    const int jj = sg * WIN < Ts - WIN ? sg * WIN : Ts - WIN;
+                    const float* x = conv + rr * CCP + jj;
+                    float* o = tm + rr * MP + jj;
+                    float xv[2 * WIN - 1];
+#pragma unroll
+                    for (int k = 0; k < 2 * WIN - 1; ++k) xv[k] = x[k];
+#pragma unroll
+                    for (int k = WIN - 2; k >= 0; --k) xv[k] = fmaxf(xv[k], xv[k + 1]);
+                    float pm = -INFINITY;
+#pragma unroll
+                    for (int tt = 0; tt < WIN; ++tt) {
+                        if (tt > 0) pm = fmaxf(pm, xv[WIN - 1 + tt]);
+                        o[tt] = fmaxf(xv[tt], pm);
+                    }
+                }
+            }
+            __syncthreads();
+
+            // ---- 4b. rho max, exact equality, Radon mask; warp top-N lists
+            float lv = -INFINITY;
+            int lp = -1;
+            {
+                const int nrho = a.nRho;
+                const int nstrip = (Ts + 31) / 32;
+                const int nrowb = (nrho + kRowBlock - 1) / kRowBlock;
+                for (int task = warp; task < nstrip * nrowb; task += kWarps) {
+                    const int rb = task / nstrip, st = task - rb * nstrip;
+                    const int jl = 32 * st + lane;
+                    const bool colok = jl < Ts;
+                    const int j = colok ? jl : Ts - 1;
+                    const int i_first = rb * kRowBlock;
+                    const int i0 = i_first < nrho - kRowBlock ? i_first : nrho - kRowBlock;
+                    const float* tcol = tm + i0 * MP + j;
+                    float v[NV];
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) v[k] = tcol[k * MP];
+                    float suf[kRowBlock], pre[kRowBlock], core = -INFINITY;
+                    suf[kRowBlock - 1] = -INFINITY;
+#pragma unroll
+                    for (int o = kRowBlock - 2; o >= 0; --o) suf[o] = fmaxf(v[o], o + 1 <= kRowBlock - 2 ? suf[o + 1] : -INFINITY);
+#pragma unroll
+                    for (int k = kRowBlock - 1; k <= 2 * D0; ++k) core = fmaxf(core, v[k]);
+                    pre[0] = -INFINITY;
+#pragma unroll
+                    for (int o = 1; o < kRowBlock; ++o) pre[o] = fmaxf(pre[o - 1], v[2 * D0 + o]);
+                    const float* crow = conv + (i0 + D0) * CCP + j + D1;
+#pragma unroll
+                    for (int o = 0; o < kRowBlock; ++o) {
+                        const float m = fmaxf(fmaxf(suf[o], core), pre[o]);
+                        const int i = i0 + o;
+                        const float val = crow[o * CCP];
+                        const bool f = colok && i >= i_first && val == m && a.rdnmask[i * a.nTheta + j0 + j];
+                        unsigned bal = __ballot_sync(0xffffffffu, f);
+                        while (bal) {
+                            const int b = __ffs(bal) - 1;
+                            bal &= bal - 1;
+                            const float cv = __shfl_sync(0xffffffffu, val, b);
+                            list_insert(cv, i * a.nTheta + j0 + 32 * st + b, lv, lp, nB, lane);
+                        }
+                    }
+                }
+            }
+            if (lane < nB) {
+                lv_s[warp * kMaxBands + lane] = lv;
+                lp_s[warp * kMaxBands + lane] = lp;
+            }
+            __syncthreads();
+        }
+        // the last slab's peaks, then the statistics and the band fits
+        if (warp == 0) {
+            slab_merge(__ldg(a.slab_j + a.nslab - 1));
+            cur ^= 1;
+        }
+        {
+            float hi = ssum, lo = 0.0f, m = smin;
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+                const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+                const float s2 = __fadd_rn(hi, oh);
+                const float bb = __fsub_rn(s2, hi);
+                const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s2, bb)), __fsub_rn(oh, bb));
+                const float e2 = __fadd_rn(err, __fadd_rn(lo, ol));
+                hi = __fadd_rn(s2, e2);
+                lo = __fsub_rn(e2, __fsub_rn(hi, s2));
+                m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
+            }
+            if (lane == 0) { red_f[warp] = m; red_f[32 + warp] = hi; red_d[warp] = (double)lo; }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double sd = (double)red_f[32 + lane] + red_d[lane];
+            float m = red_f[lane];
+            for (int o = 16; o > 0; o >>= 1) {
+                sd += __shfl_down_sync(0xffffffffu, sd, o);
+                m = fminf(m, __shfl_down_sync(0xffffffffu, m, o));
+            }
+            sd = __shfl_sync(0xffffffffu, sd, 0);
+            m = __shfl_sync(0xffffffffu, m, 0);
+            const int stat_count = stat_rows * a.nTheta;
+            const float mean = (float)(sd / (double)stat_count);
+            if (lane < nB) {
+                const float* e = run + cur * kMaxBands * kBlk + lane * kBlk;
+                const int pos = __float_as_int(e[1]);
+                const bool has = pos >= 0;
+                int r = 0, c = 0;
+                float nn[9];
+#pragma unroll
+                for (int k9 = 0; k9 < 9; ++k9) nn[k9] = has ? e[2 + k9] : 0.0f;
+                if (has) {
+                    const int i = pos / a.nTheta;
+                    r = i + a.p0;
+                    c = (pos - i * a.nTheta) + a.p1;
+                }
+                band_fit_block<float, false>(has, r, c, nn, m, mean, a.kc, a.out, (a.out_offset + q) * nB + lane);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+}  // namespace ebsd
+
+// ------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------
+namespace ebsd {
+namespace {
+
+template <typename InT>
+void* slab_kernel(int k0, int k1) {
+    if (k0 == 5 && k1 == 5) return (void*)k_slab<InT, 5, 5>;
+    if (k0 == 7 && k1 == 7) return (void*)k_slab<InT, 7, 7>;
+    if (k0 == 9 && k1 == 9) return (void*)k_slab<InT, 9, 9>;
+    return nullptr;
+}
+
+void* pick_slab_kernel(int dtype, int k0, int k1) {
+    switch (dtype) {
+        case EBSD_U8: return slab_kernel<uint8_t>(k0, k1);
+        case EBSD_U16: return slab_kernel<uint16_t>(k0, k1);
+        case EBSD_F32: return slab_kernel<float>(k0, k1);
+    }
+    return nullptr;
+}
+
+// dynamic shared memory of k_slab, as the kernel carves it
+size_t slab_smem(size_t pat_elems, size_t esize, int TR, int TBP, int CCP, int maxg) {
+    size_t b = (pat_elems * esize + 15) & ~(size_t)15;
+    b += ((size_t)TR * TBP * 4 + 15) & ~(size_t)15;
+    b += ((size_t)TR * CCP * 4 + 15) & ~(size_t)15;
+    b += (size_t)kWarps * kMaxBands * 8 + 2 * kMaxBands * kBlk * 4 + 80 * 4 + 32 * 8 + 2 * (kWarps + 1) * 4;
+    b += (size_t)maxg * 8;
+    return b;
+}
+
+std::mutex g_slab_mtx;
+struct SlabAttr {
+    const void* fn;
+    int device, smem;
+};
+std::vector<SlabAttr> g_slab_attr;
+
+int slab_attr(const void* fn, int device, int smem) {
+    std::lock_guard<std::mutex> lk(g_slab_mtx);
+    for (SlabAttr& s : g_slab_attr)
+        if (s.fn == fn && s.device == device) {
+            if (smem > s.smem) {
+                EBSD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+                s.smem = smem;
+            }
+            return EBSD_OK;
+        }
+    EBSD_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    g_slab_attr.push_back(SlabAttr{fn, device, smem});
+    return EBSD_OK;
+}
+
+}  // namespace
+
+// Plan-time tables for the slab kernel.  The LUT groups are those of the single-tile kernel:
+// 32 neighbouring rho at one theta, slot s of every lane at image column (or row) base + s when
+// each ray of the group has at most one pixel per column (row), as the reference's sampling
+// gives (radon_fast.py:113-158); a group that fits neither keeps each ray's sorted order.
+int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
+    p->sg = SlabGeom{};
+    if (p->fg.ok_f32) return EBSD_OK;  // the single-tile kernel takes the plan
+    const int K0 = p->k0, K1 = p->k1;
+    const int D0 = K0, D1 = K1, H0 = K0 / 2, H1 = K1 / 2;
+    if (!(p->pk0 == 2 * K0 + 1 && p->pk1 == 2 * K1 + 1 && K0 == K1 && pick_slab_kernel(EBSD_U16, K0, K1) &&
+          p->sep && p->bg_mode == 0 && p->nRho >= kRowBlock && p->nTheta >= 4 * (D1 + H1) &&
+          p->p0 >= D0 + H0 && p->maxCount <= 255 && p->H <= 255 && p->W <= 255))
+        return EBSD_OK;
+    const int pitch = p->W + 1;
+    const size_t pat_elems = (size_t)p->H * pitch + 1;
+    if (pat_elems > 65535) return EBSD_OK;  // element offsets in 16 bits
+    // padded-frame rows as the single-tile kernel: tile rows [row0, row1), conv rows [crow0, crow1)
+    const int statR1 = std::min(p->R, p->Tp - p->p0);
+    const int crow0 = p->p0 - D0, crow1 = std::max(p->p0 + p->nRho + D0, statR1);
+    const int row0 = crow0 - H0, row1 = crow1 + H0;
+    const int TR = row1 - row0, CR = crow1 - crow0;
+    const int gpt = (p->nRho + 31) / 32;
+    const int halo = D1 + H1;
+    int dev_smem = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    // widest slab whose uint16 tiles fit; slabs of near-equal width
+    int nslab = 0, Ts = 0;
+    for (int ns = 2; ns <= p->nTheta; ++ns) {
+        const int ts = (p->nTheta + ns - 1) / ns;
+        if (ts < 2 * D1 + 1 || ts < 16) break;
+        const int TBP = (ts + 2 * halo) | 1, CCP = (ts + 2 * D1) | 1;
+        const int maxg = (ts + 2 * halo) * gpt;
+        if ((size_t)TR * TBP >= 65536) continue;
+        if (slab_smem(pat_elems, 2, TR, TBP, CCP, maxg) <= (size_t)dev_smem) {
+            nslab = ns;
+            Ts = ts;
+            break;
+        }
+    }
+    if (!nslab) return EBSD_OK;
+    SlabGeom g;
+    g.nslab = nslab;
+    g.Ts = Ts;
+    g.TR = TR;
+    g.TBP = (Ts + 2 * halo) | 1;
+    g.CCP = (Ts + 2 * D1) | 1;
+    g.MP = Ts | 1;
+    g.rho0 = p->p0 - row0;
+    g.rpad_end = p->R - row0;
+    g.CR = CR;
+    g.statR = statR1 - p->p0;
+    g.pitch = pitch;
+    g.maxg = (Ts + 2 * halo) * gpt;
+    g.smem[0] = (int)slab_smem(pat_elems, 1, TR, g.TBP, g.CCP, g.maxg);
+    g.smem[1] = (int)slab_smem(pat_elems, 2, TR, g.TBP, g.CCP, g.maxg);
+    g.smem[2] = (int)slab_smem(pat_elems, 4, TR, g.TBP, g.CCP, g.maxg);
+
+    // per source group (theta j, rho block b): chunks, and each lane's slot -> element offset
+    const int L = d->lut_len;
+    const int nsrc = p->nTheta * gpt;
+    const uint16_t zero = (uint16_t)(p->H * pitch);
+    std::vector<int> gch(nsrc, 1);
+    std::vector<std::vector<uint16_t>> gslots(nsrc);  // [chunk][lane][8]
+    std::vector<int32_t> count((size_t)nsrc * 32, 0);
+    std::vector<char> seen((size_t)std::max(p->W, p->H));
+    for (int gs = 0; gs < nsrc; ++gs) {
+        const int j = gs / gpt, i0 = (gs % gpt) * 32;
+        bool colok = true, rowok = true;
+        int xmin = 1 << 30, xmax = -1, ymin = 1 << 30, ymax = -1, maxc = 0;
+        for (int l = 0; l < 32 && i0 + l < p->nRho; ++l) {
+            const int64_t* ray = d->lut + ((size_t)(i0 + l) * p->nTheta + j) * L;
+            int c = 0;
+            while (c < L && ray[c] >= 0 && ray[c] < p->nPx) ++c;
+            count[(size_t)gs * 32 + l] = c;
+            maxc = std::max(maxc, c);
+            std::fill(seen.begin(), seen.end(), 0);
+            for (int k = 0; k < c; ++k) {
+                const int x = (int)(ray[k] % p->W);
+                if (seen[x]) colok = false;
+                seen[x] = 1;
+                xmin = std::min(xmin, x);
+                xmax = std::max(xmax, x);
+            }
+            std::fill(seen.begin(), seen.end(), 0);
+            for (int k = 0; k < c; ++k) {
+                const int y = (int)(ray[k] / p->W);
+                if (seen[y]) rowok = false;
+                seen[y] = 1;
+                ymin = std::min(ymin, y);
+                ymax = std::max(ymax, y);
+            }
+        }
+        int axis = 2, base = 0, nslot = maxc;
+        if (maxc == 0) {
+            nslot = 0;
+        } else if (colok) {
+            axis = 0;
+            base = xmin;
+            nslot = xmax - xmin + 1;
+        } else if (rowok) {
+            axis = 1;
+            base = ymin;
+            nslot = ymax - ymin + 1;
+        }
+        gch[gs] = std::max(1, (nslot + 7) / 8);
+        std::vector<uint16_t>& sl = gslots[gs];
+        sl.assign((size_t)gch[gs] * 32 * 8, zero);
+        for (int l = 0; l < 32 && i0 + l < p->nRho; ++l) {
+            const int64_t* ray = d->lut + ((size_t)(i0 + l) * p->nTheta + j) * L;
+            for (int k = 0; k < count[(size_t)gs * 32 + l]; ++k) {
+                const int idx = (int)ray[k], y = idx / p->W, x = idx - y * p->W;
+                const int slot = axis == 0 ? x - base : (axis == 1 ? y - base : k);
+                sl[((size_t)(slot / 8) * 32 + l) * 8 + slot % 8] = (uint16_t)(y * pitch + x);
+            }
+        }
+    }
+
+    // per slab: buffer columns [j0 - halo, j0 + ts + halo), groups balanced over the warps
+    std::vector<int32_t> slab_j(nslab + 1), slab_g(nslab + 1, 0), wofs;
+    std::vector<uint32_t> gst, gtb;
+    std::vector<uint16_t> lut;
+    for (int s = 0; s <= nslab; ++s) slab_j[s] = (int)((int64_t)p->nTheta * s / nslab);
+    int maxg = 0;
+    for (int s = 0; s < nslab; ++s) {
+        const int j0 = slab_j[s], ts = slab_j[s + 1] - j0, TB = ts + 2 * halo;
+        if (ts < 2 * D1 + 1) return EBSD_OK;
+        struct Grp {
+            int src;
+            uint32_t tb;
+        };
+        std::vector<Grp> grps;
+        for (int jb = 0; jb < TB; ++jb) {
+            const int jc = j0 - halo + jb;
+            const bool flip = jc < 0 || jc >= p->nTheta;
+            const int js = ((jc % p->nTheta) + p->nTheta) % p->nTheta;
+            for (int b = 0; b < gpt; ++b) {
+                const int nval = std::min(32, p->nRho - 32 * b);
+                const int row = g.rho0 + (flip ? p->nRho - 1 - 32 * b : 32 * b);
+                const uint32_t offs = (uint32_t)(row * g.TBP + jb);
+                grps.push_back(Grp{js * gpt + b, offs | ((uint32_t)nval << 16) | ((flip ? 1u : 0u) << 22)});
+            }
+        }
+        maxg = std::max(maxg, (int)grps.size());
+        std::vector<int> order(grps.size());
+        for (size_t k = 0; k < grps.size(); ++k) order[k] = (int)k;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return gch[grps[x].src] > gch[grps[y].src]; });
+        std::vector<std::vector<int>> wg(kWarps);
+        std::vector<long> wload(kWarps, 0);
+        for (int k : order) {
+            const int w = (int)(std::min_element(wload.begin(), wload.end()) - wload.begin());
+            wg[w].push_back(k);
+            wload[w] += gch[grps[k].src];
+        }
+        std::vector<int32_t> wo(2 * (kWarps + 1), 0);
+        int gcount = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            wo[w] = gcount;
+            wo[kWarps + 1 + w] = (int32_t)(lut.size() / (32 * 8));
+            for (int k : wg[w]) {
+                const Grp& gr = grps[k];
+                gst.push_back((uint32_t)gr.src | ((uint32_t)gch[gr.src] << 16));
+                gtb.push_back(gr.tb);
+                lut.insert(lut.end(), gslots[gr.src].begin(), gslots[gr.src].end());
+                ++gcount;
+            }
+            lut.insert(lut.end(), (size_t)kRing * 32 * 8, zero);  // the ring's unconditional loads
+        }
+        wo[kWarps] = gcount;
+        wo[2 * kWarps + 1] = (int32_t)(lut.size() / (32 * 8));
+        wofs.insert(wofs.end(), wo.begin(), wo.end());
+        slab_g[s + 1] = slab_g[s] + gcount;
+    }
+    if (maxg > g.maxg) return EBSD_OK;
+    // device tables: [gst][gtb][slab_g][slab_j][wofs][count], each part 16-byte aligned
+    std::vector<int32_t> tab;
+    auto part = [&](const int32_t* src, size_t cnt) {
+        const int32_t at = (int32_t)tab.size();
+        tab.insert(tab.end(), src, src + cnt);
+        while (tab.size() % 4) tab.push_back(0);
+        return at;
+    };
+    p->s_gst = part((const int32_t*)gst.data(), gst.size());
+    p->s_gtb = part((const int32_t*)gtb.data(), gtb.size());
+    p->s_slabg = part(slab_g.data(), slab_g.size());
+    p->s_slabj = part(slab_j.data(), slab_j.size());
+    p->s_wofs = part(wofs.data(), wofs.size());
+    p->s_count = part(count.data(), count.size());
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_stab, tab.size() * sizeof(int32_t)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_stab, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_slut, lut.size() * sizeof(uint16_t)));
+    EBSD_CUDA_TRY(cudaMemcpy(p->d_slut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    g.ok = g.smem[1] <= dev_smem;
+    g.ok_f32 = g.smem[2] <= dev_smem;
+    p->sg = g;
+    return EBSD_OK;
+}
+
+void slab_release(ebsd_plan_s* p) {
+    cudaFree(p->d_slut);
+    cudaFree(p->d_stab);
+    p->d_slut = nullptr;
+    p->d_stab = nullptr;
+    p->sg = SlabGeom{};
+}
+
+bool slab_serves(const ebsd_plan_s* p, int method, int dtype) {
+    if (method != EBSD_FUSED_F32 || !p->sg.ok || p->fg.ok_f32) return false;
+    return dtype != EBSD_F32 || p->sg.ok_f32;
+}
+
+int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
+                   int64_t out_offset, cudaStream_t st, int64_t* launches) {
+    if (n <= 0) return EBSD_OK;
+    void* fn = pick_slab_kernel(dtype, p->k0, p->k1);
+    if (!fn || !slab_serves(p, EBSD_FUSED_F32, dtype)) return EBSD_E_UNSUPPORTED;
+    const SlabGeom& g = p->sg;
+    const int smem = g.smem[dtype == EBSD_U8 ? 0 : (dtype == EBSD_U16 ? 1 : 2)];
+    int rc = slab_attr(fn, p->device, smem);
+    if (rc != EBSD_OK) return rc;
+    int sms = 0;
+    EBSD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+    SlabArgs a;
+    a.pats = d_pats;
+    a.n = n;
+    a.H = p->H;
+    a.W = p->W;
+    a.pitch = g.pitch;
+    a.lut = (const uint4*)p->d_slut;
+    a.gst = (const uint32_t*)(p->d_stab + p->s_gst);
+    a.gtb = (const uint32_t*)(p->d_stab + p->s_gtb);
+    a.slab_g = p->d_stab + p->s_slabg;
+    a.slab_j = p->d_stab + p->s_slabj;
+    a.wofs = p->d_stab + p->s_wofs;
+    a.count = p->d_stab + p->s_count;
+    a.nslab = g.nslab;
+    a.maxg = g.maxg;
+    a.nRho = p->nRho;
+    a.nTheta = p->nTheta;
+    a.nB = p->nB;
+    a.p0 = p->p0;
+    a.p1 = p->p1;
+    a.TR = g.TR;
+    a.TBP = g.TBP;
+    a.CCP = g.CCP;
+    a.MP = g.MP;
+    a.rho0 = g.rho0;
+    a.rpad_end = g.rpad_end;
+    a.CR = g.CR;
+    a.statR = g.statR;
+    for (int k = 0; k < 9; ++k) {
+        a.ku[k] = k < p->k0 ? p->h_ku[k] : 0.0f;
+        a.kw[k] = k < p->k1 ? p->h_kw[k] : 0.0f;
+    }
+    a.rdnmask = p->d_rdnmask;
+    a.kc = LabelConsts{p->p0, p->p1, p->nTheta, p->nRho, p->nB, p->d_theta, p->d_rho};
+    a.out = *out;
+    a.out_offset = out_offset;
+    void* args[] = {&a};
+    const int64_t grid = std::min<int64_t>(n, sms);
+    EBSD_CUDA_TRY(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kThreads), args, (size_t)smem, st));
+    band_epilogue_launch(*out, out_offset, n, p->nB, a.kc, sms, st);
+    *launches += 2;
+    return launch_status();
+}
+
+}  // namespace ebsd

@@ -1,0 +1,76 @@
+"""The fused path in theta slabs (csrc/slab.cu) for plans too large for the single on-chip tile.
+
+120x120 and 240x240 patterns with nRho = 1.5 * size (the mixed-size configuration's
+geometry; the padded Radon image of a 120x120 pattern is 202 x 202 cells, beyond one SM's
+shared memory next to its LoG image) run the FP32 fused method slab by slab.  The slab kernel
+follows the per-stage FP32 path's arithmetic: integer ray sums are exact, the mean is the
+correctly rounded quotient, the separable LoG keeps the per-stage multiply-add order, and the
+peak search and fit are the same -- so for integer patterns every band field equals the
+per-stage method's bit for bit, except normmax, whose per-pattern mean is reduced in another
+order (last-bit differences).  Float32 patterns sum in another order (rounding level).
+Against the FP64 method (plain64): integer peaks on >= 99.9% of bands, sub-pixel within 1e-3 px.
+"""
+import numpy as np
+import pytest
+
+import pyebsdindex_gb300 as pg
+from pyebsdindex_gb300 import synthetic as syn
+from pyebsdindex_gb300.accuracy import compare_records
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("max", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid")
+
+
+def plan(h, w, nrho, nbands=10, mask=True):
+    bd = pg.BandDetect(nTheta=180, nRho=nrho, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=nbands)
+    bd.band_detect_setup(patDim=(h, w), patternmask=syn.circular_mask(h, w) if mask else None)
+    return bd
+
+
+def patterns(n, h, w, dtype, seed, peak):
+    return syn.make_patterns(n, h, w, seed=seed, dtype=dtype, peak=peak, noise_frac=0.1)[0]
+
+
+@pytest.mark.parametrize("size,dtype,peak", [(120, np.uint16, 4000.0), (240, np.uint16, 4000.0),
+                                             (120, np.uint8, 200.0), (240, np.uint8, 200.0)])
+def test_slab_equals_per_stage(cuda, size, dtype, peak):
+    bd = plan(size, size, int(1.5 * size))
+    dp = bd._device_plan()
+    assert dp.supported("fused"), "the slab path should take this plan"
+    pats = patterns(96 if size == 240 else 256, size, size, dtype, 900 + size, peak)
+    a = bd.find_bands(pats, method="plain")
+    b = bd.find_bands(pats, method="fused")
+    for f in FIELDS:
+        assert a[f].tobytes() == b[f].tobytes(), f
+    np.testing.assert_allclose(a["normmax"], b["normmax"], rtol=1e-6)
+    c = compare_records(b, bd.find_bands(pats, method="plain64"))
+    print(size, np.dtype(dtype).name, "vs FP64:", c)
+    assert c["peak_frac"] >= 0.999 and c["aveloc_max"] <= 1e-3, c
+
+
+def test_slab_float_and_rectangular(cuda):
+    """float32 input and a non-square 100x150 pattern (nRho 150), no detector mask."""
+    bd = plan(100, 150, 150, nbands=9, mask=False)
+    assert bd._device_plan().supported("fused")
+    pats = patterns(128, 100, 150, np.uint16, 77, 3000.0).astype(np.float32) / np.float32(7.0)
+    a = bd.find_bands(pats, method="plain")
+    b = bd.find_bands(pats, method="fused")
+    c = compare_records(b, a)
+    assert c["peak_frac"] >= 0.999 and c["aveloc_max"] <= 1e-3 and c["max_rel"] <= 1e-5, c
+
+
+def test_slab_chunking_and_degenerate(cuda):
+    """Records do not depend on the chunking; all-zero and constant patterns give no valid band
+    (zero) and plateau bands (constant), as on the per-stage path."""
+    bd = plan(120, 120, 180)
+    pats = patterns(40, 120, 120, np.uint16, 31, 4000.0)
+    pats[3] = 0
+    pats[7] = 1000
+    whole = bd.find_bands(pats, method="fused")
+    parts = np.concatenate([bd.find_bands(pats[s:s + 7], method="fused") for s in range(0, 40, 7)])
+    for f in FIELDS + ("normmax",):
+        assert whole[f].tobytes() == parts[f].tobytes(), f
+    assert np.all(whole["valid"][3] == 0)
+    plain = bd.find_bands(pats[[7]], method="plain")
+    assert whole["valid"][7].tobytes() == plain["valid"][0].tobytes()
