@@ -76,6 +76,8 @@ def parse():
                     help="format of the file timed (EDAX UP1, Oxford .ebsp, ThermoFisher .pat)")
     ap.add_argument("--nlpar-file", action="store_true",
                     help="also time NLPAR's file interface (opt_lambda, calcnlpar) on a 400x500 UP1 scan")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-size (60/120/240 uint16) figure")
+    ap.add_argument("--mixed-patterns", type=int, default=300_000, help="patterns of the mixed-size step")
     ap.add_argument("--lambda-scan", action="store_true",
                     help="also time NLPAR's lambda optimisation on a 400x500 scan of 80x80 patterns")
     return ap.parse_args()
@@ -375,6 +377,92 @@ def time_indexing(outs, bd, N, stream, with_cpu, detect_ms):
     return res
 
 
+MIXED_SIZES = (60, 120, 240)
+
+
+def _mixed_part(args):
+    h, start, count = args
+    from pyebsdindex_gb300 import synthetic as syn
+    return syn.make_patterns(count, h, h, seed=3_000_000 + 1_000 * h, start=start, dtype=np.uint16, peak=4000.0,
+                             noise_frac=0.1)[0]
+
+
+def mixed_pools(ex, per_size):
+    """Seeded uint16 patterns (Poisson peak 4000 counts) per size of the mixed-size configuration."""
+    out = {}
+    for h in MIXED_SIZES:
+        parts = [(h, s, min(256, per_size - s)) for s in range(0, per_size, 256)]
+        out[h] = np.concatenate(list(ex.map(_mixed_part, parts)))
+    return out
+
+
+def time_mixed(pools, n_total, steps, dev):
+    """The mixed-size configuration: n_total uint16 patterns, one third each at 60x60, 120x120
+    and 240x240 (nRho 1.5 * size, nTheta 180, nBands 10, circular mask), one persistent fused
+    launch over all three sizes per step (MixedBandDetect / ebsd_find_bands_mixed), inputs
+    resident; then each size alone and the per-stage FP32 path for comparison, and the
+    accuracy of the mixed launch against the FP64 method (plain64) on 2,048 patterns per size."""
+    import torch
+    from pyebsdindex_gb300 import synthetic as syn
+    from pyebsdindex_gb300.band_detect import MixedBandDetect
+    from pyebsdindex_gb300.accuracy import compare_records
+    mb = MixedBandDetect(nBands=10, mask_for=syn.circular_mask)
+    each = n_total // len(MIXED_SIZES)
+    batches = {}
+    for h in MIXED_SIZES:
+        # tiled as int16 (torch's uint16 has few device operations), then viewed as uint16
+        pd = torch.from_numpy(pools[h].view(np.int16)).to(dev)
+        reps = (each + pd.shape[0] - 1) // pd.shape[0]
+        batches[(h, h)] = pd.repeat(reps, 1, 1)[:each].contiguous().view(torch.uint16)
+    st = torch.cuda.current_stream(dev)
+
+    def run(b):
+        return mb.find_bands_device(b, stream=st)
+    outs = run(batches)
+    torch.cuda.synchronize()
+    mixed = mb.last_mixed
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(st)
+    for _ in range(steps):
+        outs = run(batches)
+    ev[1].record(st)
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / steps
+    res = {"workload": f"{3 * each:,} uint16 patterns (Poisson peak 4000), one third each at 60x60 / 120x120 / "
+                       "240x240, nRho 1.5*size, nTheta 180, nBands 10; pools of distinct seeded patterns per size "
+                       f"({pools[60].shape[0]}) tiled",
+           "one_launch": mixed, "ms_per_step": ms, "patterns_per_s": 3 * each / ms * 1e3, "per_size": {}}
+    for h in MIXED_SIZES:
+        key = (h, h)
+        t = batches[key]
+        plan = mb.plan(h, h)._device_plan()
+        sub = {key: t}
+        run(sub)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        run(sub)
+        e1.record(st)
+        torch.cuda.synchronize()
+        entry = {"fused_patterns_per_s": t.shape[0] / e0.elapsed_time(e1) * 1e3}
+        npl = min(t.shape[0], 16384 if h < 240 else 4096)
+        po = {f: torch.empty((npl,) + tuple(v.shape[1:]), dtype=v.dtype, device=dev) for f, v in outs[key].items()}
+        plan.find_bands_device(t.data_ptr(), 1, npl, {f: v.data_ptr() for f, v in po.items()}, "plain", stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        e0.record(st)
+        plan.find_bands_device(t.data_ptr(), 1, npl, {f: v.data_ptr() for f, v in po.items()}, "plain", stream=st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        entry["plain_patterns_per_s"] = npl / e0.elapsed_time(e1) * 1e3
+        na = min(t.shape[0], 2048)
+        plan.find_bands_device(t.data_ptr(), 1, na, {f: v.data_ptr() for f, v in po.items()}, "plain64", stream=st.cuda_stream)
+        torch.cuda.synchronize()
+        entry["accuracy_vs_plain64"] = dict(compare_records({f: v[:na] for f, v in outs[key].items()},
+                                                            {f: v[:na] for f, v in po.items()}), patterns=na)
+        res["per_size"][str(h)] = entry
+    return res
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -413,6 +501,7 @@ def main():
     # the pattern pool is generated by spawned host processes before the GPU is touched
     ex = host_executor()
     pool = make_pool(args.pool, ex)
+    mpools = None if args.no_mixed else mixed_pools(ex, 1024)
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -634,6 +723,10 @@ def main():
     if rank == 0 and args.nlpar_file:
         nlpar_file = time_nlpar_file()
 
+    mixed = None
+    if mpools is not None and rank == 0:
+        mixed = time_mixed(mpools, args.mixed_patterns, max(2, min(args.steps, 5)), dev)
+
     indexing = None
     if not args.no_index:
         indexing = time_indexing(outs, bd, N, stream, rank == 0 and world == 1 and not args.no_cpu,
@@ -671,7 +764,7 @@ def main():
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "accuracy": acc,
             "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
-            "nlpar_lambda": nlpar_lambda, "nlpar_file": nlpar_file,
+            "nlpar_lambda": nlpar_lambda, "nlpar_file": nlpar_file, "mixed_sizes": mixed,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))

@@ -117,6 +117,19 @@ int ebsd_plan_reserve(ebsd_plan_t plan, int method, int64_t max_chunk);
 int ebsd_find_bands(ebsd_plan_t plan, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* d_out, int64_t chunk, void* stream);
 
+/* Mixed pattern sizes in one persistent launch: the FP32 fused method for up to 8 plans at
+ * once (e.g. one plan per detector size), plan k's d_pats[k] [n[k]][H_k][W_k] of `dtype`
+ * into d_out[k].  The reference runs one size per BandDetect plan and rebuilds the plan when
+ * the size changes (band_detect.py:138-155); here every persistent CTA strides over the
+ * patterns of all plans, each pattern detected in theta slabs with its plan's tables.  All
+ * plans live on one device and share the LoG size; each must report
+ * ebsd_method_supported(plan, EBSD_FUSED_F32) and qualify for the slab kernel (uint8 /
+ * uint16 input; float32 where its pattern tile fits), else EBSD_E_UNSUPPORTED.  Records equal
+ * those of ebsd_find_bands with EBSD_FUSED_F32 on each plan alone, up to the last bit of
+ * normmax.  Asynchronous on `stream`; allocates nothing. */
+int ebsd_find_bands_mixed(const ebsd_plan_t* plans, int nplans, int dtype, const void* const* d_pats,
+                          const int64_t* n, const ebsd_bands* d_out, void* stream);
+
 /* The same on HOST buffers: copies each chunk in, runs it and copies the bands out, with
  * two streams so copies overlap compute.  Pinned host memory gives overlapped copies;
  * pageable memory works but serialises.  Synchronous: returns when the outputs are
@@ -420,6 +433,50 @@ int ebsd_nlpar_apply64(const double* d_x, int32_t nrows, int32_t ncols, int32_t 
                        const double* d_w, int32_t sr, double* d_out, void* stream);
 int ebsd_nlpar_apply_t64(const double* d_g, int32_t nrows, int32_t ncols, int32_t npx,
                          const double* d_w, int32_t sr, double* d_out, void* stream);
+
+/* One axis of a separable filter with reflect padding (torch's "reflect": index -q reads q,
+ * L-1+q reads L-1-q; radius r < L): out[o] = sum_{t=-r..r} taps[t+r] in[refl(o+t)] along
+ * axis 0 (rows) or 1 (columns) of [n][H][W], or with adjoint = 1 the transpose of that map
+ * (a gather, no atomics).  fp64 selects double data and taps.  The background blur of the
+ * differentiable path: forward along x then y, its adjoint, and d/dsigma with the taps'
+ * derivative. */
+int ebsd_blur1d(int fp64, int adjoint, int axis, const void* d_in, int64_t n, int32_t H, int32_t W,
+                const void* d_taps, int32_t r, void* d_out, void* stream);
+
+/* Soft-argmax band sharpness of n LoG-filtered Radon images [n][ncell]: per image
+ * J_p = sum_i s_i c_i with s = softmax(c / tau) over the cells d_cells[ncm] (the Radon mask),
+ * into d_J[n] (float64), and the gradient dJ_p / dc_i = s_i (1 + (c_i - J_p) / tau) into
+ * d_grad (same layout as c; only the listed cells are written).  Sums in float64. */
+int ebsd_softargmax(int fp64, const void* d_c, int64_t n, int64_t ncell, const int32_t* d_cells,
+                    int32_t ncm, double tau, double* d_J, void* d_grad, void* stream);
+
+/* NLPAR noise sigma (NLPAR.sigma_numba, nlpar_cpu.py:753-796, nn = 1) with what its
+ * derivative needs: d_sig2 = sigma^2 (sigma rounded as the weights read it), d_arg = the 3x3
+ * neighbour whose SSD / (2 n) is the minimum (-1: none), d_nsig = that pair's count. */
+int ebsd_nlpar_sigma_arg(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+                         const int32_t* d_indices, int32_t nind, float datamax, int saturation_protect,
+                         float* d_sig2, int32_t* d_arg, float* d_nsig, void* stream);
+
+/* The window weights of ebsd_nlpar_weights from sigma^2 (d_sig2), plus the partial
+ * derivatives of each pair's normalised distance d = (S - n s) / (s sqrt(2 n))
+ * (nlpar_cpu.py:897-917): d_dS = dd/dS, d_dsig = dd/ds with s = sigma_p^2 + sigma_c^2; both 0
+ * at the centre, where d is replaced by 1e6 n, and where max(d - dthresh, 0) clamps. */
+int ebsd_nlpar_weights_d(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+                         const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
+                         float dthresh, const float* d_sig2, int saturation_protect, float* d_w, float* d_m,
+                         float* d_dS, float* d_dsig, void* stream);
+
+/* Backward of the weights for y = W(lambda, x) x given g = dL/dy: into d_gx the part of dL/dx
+ * that flows through the weights -- each pair's SSD over the masked pixels d_pmask[npx] where
+ * both values pass the 0.999 saturation test, and each pattern's noise sigma through its
+ * minimising pair (0.9961 test) -- and into d_glam[nrows*ncols] the per-pixel terms of
+ * dL/dlambda.  (W^T g, the direct part, is ebsd_nlpar_apply_t.)  d_scratch holds
+ * 3 * nrows*ncols*(2 sr + 1)^2 + nrows*ncols doubles.  fp64 selects double g, x and gx. */
+int ebsd_nlpar_weights_grad(int fp64, const void* d_g, const void* d_x, int32_t nrows, int32_t ncols,
+                            int32_t npx, int32_t sr, const float* d_w, const float* d_m, const float* d_dS,
+                            const float* d_dsig, double lam, const uint8_t* d_pmask, float datamax,
+                            int saturation_protect, const int32_t* d_arg, const float* d_nsig,
+                            double* d_scratch, double* d_glam, void* d_gx, void* stream);
 
 /* Per scan pixel p: sum_c dw_pc/dlambda (g_p . x_c) in float64 (d_out[nrows*ncols]); the sum
  * over p is dL/dlambda for L with dL/dy = g. */

@@ -77,6 +77,9 @@ def load():
         lib.ebsd_plan_reserve.restype = C.c_int
         lib.ebsd_find_bands.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, C.POINTER(Bands), C.c_int64, P]
         lib.ebsd_find_bands.restype = C.c_int
+        lib.ebsd_find_bands_mixed.argtypes = [C.POINTER(P), C.c_int, C.c_int, C.POINTER(P), C.POINTER(C.c_int64),
+                                              C.POINTER(Bands), P]
+        lib.ebsd_find_bands_mixed.restype = C.c_int
         lib.ebsd_find_bands_host.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, C.POINTER(Bands), C.c_int64]
         lib.ebsd_find_bands_host.restype = C.c_int
         lib.ebsd_find_bands_host_records.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, P, C.c_int32,
@@ -234,6 +237,20 @@ class DevicePlan:
         check(self._lib.ebsd_find_bands(self.handle, method_id(method), int(dtype), C.c_void_p(int(pats_ptr)),
                                         int(n), C.byref(b), int(chunk), C.c_void_p(int(stream))),
               "ebsd_find_bands")
+
+    @staticmethod
+    def find_bands_mixed(plans, dtype: int, pats_ptrs, counts, out_ptrs, stream=0):
+        """One persistent launch over several plans' device patterns (mixed pattern sizes):
+        plans[k] detects counts[k] patterns at pats_ptrs[k] into the device arrays out_ptrs[k]
+        (dicts of raw pointers), the FP32 fused method in theta slabs.  Asynchronous."""
+        lib = load()
+        k = len(plans)
+        hp = (C.c_void_p * k)(*[p.handle.value for p in plans])
+        pp = (C.c_void_p * k)(*[int(x) for x in pats_ptrs])
+        nn = (C.c_int64 * k)(*[int(x) for x in counts])
+        bb = (Bands * k)(*[Bands(**{f: C.c_void_p(int(o[f])) for f in BAND_FIELDS}) for o in out_ptrs])
+        check(lib.ebsd_find_bands_mixed(hp, k, int(dtype), pp, nn, bb, C.c_void_p(int(stream))),
+              "ebsd_find_bands_mixed")
 
     def close(self):
         if getattr(self, "handle", None) is not None and self.handle.value:

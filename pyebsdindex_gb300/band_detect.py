@@ -452,11 +452,16 @@ class MixedBandDetect:
     """Band detection over a batch of patterns of different sizes.
 
     The reference handles one pattern size per ``BandDetect`` plan (band_detect.py:138-155
-    rebuilds the plan when the size changes).  Here one plan is kept per size; a ragged batch is
-    split by size, every size group runs on its own plan and CUDA stream (the fused kernel where
-    its on-chip tile fits, the per-stage kernels otherwise), and the records come back in input
-    order.  uint16 patterns need a torch build with ``torch.uint16``; otherwise pass float32.  ``nRho`` for a size comes from ``nRho_for(H, W)`` (default 1.5 * min(H, W)).
+    rebuilds the plan when the size changes).  Here one plan is kept per size, and a batch
+    holding several sizes runs as ONE persistent fused launch over all of them
+    (``ebsd_find_bands_mixed``: every CTA strides over the patterns of every size, each
+    detected in theta slabs with its size's tables), up to eight sizes of one input type.
+    Other methods, or more sizes, run size by size, each on its own CUDA stream.  ``nRho`` for
+    a size comes from ``nRho_for(H, W)`` (default 1.5 * min(H, W)).  uint16 patterns need a
+    torch build with ``torch.uint16``; otherwise pass float32.
     """
+
+    MAX_MIXED = 8
 
     def __init__(self, nTheta=180, nRho_for=None, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=10,
                  mask_for=None, method="fused", gpu_id=0, **kwargs):
@@ -466,6 +471,7 @@ class MixedBandDetect:
         self.mask_for = mask_for
         self.kwargs = kwargs
         self.plans = {}
+        self.last_mixed = False  # whether the last call ran as one mixed-size launch
 
     def plan(self, h, w):
         key = (int(h), int(w))
@@ -482,43 +488,82 @@ class MixedBandDetect:
         return m if not m.startswith("fused") or bd._device_plan().supported(m) else "plain"
 
     def find_bands(self, patterns, method=None):
-        """patterns: sequence of [H, W] arrays (numpy or CUDA tensors), sizes mixed.
-        Returns an (n, nBands) record array in input order.  Size groups are launched on
-        separate CUDA streams without waiting for one another; results are gathered at the end."""
+        """patterns: sequence of [H, W] arrays (numpy, or CUDA tensors), sizes mixed.  Returns an
+        (n, nBands) record array in input order."""
         import torch
         groups = {}
         for k, p in enumerate(patterns):
             groups.setdefault(tuple(p.shape[-2:]), []).append(k)
-        out = np.zeros((len(patterns), self.nBands), dtype=record_dtype(10))
-        dev = torch.device("cuda", self.gpu_id)
-        u16 = getattr(torch, "uint16", None)
-        pending = []
+        batches = {}
         for key, idx in groups.items():
-            bd = self.plan(*key)
-            plan = bd._device_plan()
-            m = method or self.method_for(*key)
-            if m.startswith("fused") and not plan.supported(m):
-                m = "plain"
-            st = torch.cuda.Stream(device=dev)
-            with torch.cuda.stream(st):
-                batch = torch.stack([torch.as_tensor(patterns[k]) for k in idx]).to(dev, non_blocking=True)
-                if batch.dtype == torch.uint8:
-                    dt = _lib.EBSD_U8
-                elif u16 is not None and batch.dtype == u16:
-                    dt = _lib.EBSD_U16
-                else:
-                    batch = batch.to(torch.float32)
-                    dt = _lib.EBSD_F32
-                batch = batch.contiguous()
-                n, nB = len(idx), self.nBands
-                outs = {f: torch.empty((n, nB, 2) if f in ("maxloc", "aveloc") else (n, nB),
-                                       dtype=torch.int8 if f == "valid" else torch.float32, device=dev)
-                        for f in _lib.BAND_FIELDS}
-                plan.find_bands_device(batch.data_ptr(), dt, n, {f: v.data_ptr() for f, v in outs.items()}, m,
-                                       stream=st.cuda_stream)
-            pending.append((idx, outs, batch, st))
-        for idx, outs, _batch, st in pending:
-            st.synchronize()
-            for f, v in outs.items():
-                out[f][idx] = v.cpu().numpy()
+            first = patterns[idx[0]]
+            if type(first).__module__.startswith("torch"):
+                batches[key] = torch.stack([patterns[k] for k in idx])
+            else:
+                batches[key] = np.stack([np.asarray(patterns[k]) for k in idx])
+        recs = self.find_bands_grouped(batches, method=method)
+        out = np.zeros((len(patterns), self.nBands), dtype=record_dtype(10))
+        for key, idx in groups.items():
+            out[np.asarray(idx)] = recs[key]
         return out
+
+    def find_bands_device(self, batches, method=None, stream=None):
+        """batches: {(H, W): CUDA tensor [n, H, W]} (one input type) -> {(H, W): dict of device
+        band arrays}, asynchronous on ``stream`` (default: the current stream).  With the fused
+        method and at most eight sizes that the slab kernel takes, one launch serves them all."""
+        import torch
+        dev = torch.device("cuda", self.gpu_id)
+        st = stream if stream is not None else torch.cuda.current_stream(dev)
+        m = method or self.method
+        u16 = getattr(torch, "uint16", None)
+        ins, dts = {}, set()
+        for key, t in batches.items():
+            if t.dtype == torch.uint8:
+                dt = _lib.EBSD_U8
+            elif u16 is not None and t.dtype == u16:
+                dt = _lib.EBSD_U16
+            else:
+                t = t.to(torch.float32)
+                dt = _lib.EBSD_F32
+            ins[key] = (t.to(dev).contiguous(), dt)
+            dts.add(dt)
+        outs = {key: {f: torch.empty((t.shape[0], self.nBands, 2) if f in ("maxloc", "aveloc")
+                                     else (t.shape[0], self.nBands),
+                                     dtype=torch.int8 if f == "valid" else torch.float32, device=dev)
+                      for f in _lib.BAND_FIELDS} for key, (t, _) in ins.items()}
+        plans = {key: self.plan(*key)._device_plan() for key in ins}
+        mixed = (m in ("fused", "fused32") and len(dts) == 1 and 1 <= len(ins) <= self.MAX_MIXED
+                 and all(p.supported("fused") for p in plans.values()))
+        self.last_mixed = False
+        if mixed:
+            keys = list(ins)
+            try:
+                _lib.DevicePlan.find_bands_mixed([plans[k] for k in keys], dts.pop(), [ins[k][0].data_ptr() for k in keys],
+                                                 [ins[k][0].shape[0] for k in keys],
+                                                 [{f: v.data_ptr() for f, v in outs[k].items()} for k in keys],
+                                                 stream=st.cuda_stream)
+                self.last_mixed = True
+                return outs
+            except RuntimeError as e:
+                if "not supported" not in str(e):
+                    raise
+        for key, (t, dt) in ins.items():
+            mk = m if not m.startswith("fused") or plans[key].supported(m) else "plain"
+            plans[key].find_bands_device(t.data_ptr(), dt, t.shape[0], {f: v.data_ptr() for f, v in outs[key].items()},
+                                         mk, stream=st.cuda_stream)
+        return outs
+
+    def find_bands_grouped(self, batches, method=None):
+        """batches: {(H, W): [n, H, W] array (numpy or CUDA tensor)} -> {(H, W): record array}."""
+        import torch
+        tb = {k: (v if type(v).__module__.startswith("torch") else torch.from_numpy(np.ascontiguousarray(v)))
+              for k, v in batches.items()}
+        outs = self.find_bands_device(tb, method=method)
+        torch.cuda.synchronize(torch.device("cuda", self.gpu_id))
+        res = {}
+        for key, o in outs.items():
+            rec = np.zeros((o["valid"].shape[0], self.nBands), dtype=record_dtype(10))
+            for f in _lib.BAND_FIELDS:
+                rec[f] = o[f].cpu().numpy()
+            res[key] = rec
+        return res

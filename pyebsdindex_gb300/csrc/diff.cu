@@ -180,6 +180,332 @@ __global__ void k_nlpar_lam_grad(const T* __restrict__ g, const T* __restrict__ 
     }
 }
 
+// ---- Gaussian background blur: one axis of a separable filter with reflect padding ----------
+// Forward along `axis` (0: rows y, 1: columns x) of [n][H][W]:
+//   out[o] = sum_{t=-r..r} taps[t + r] in[refl(o + t)],   refl(q) = -q (q < 0), 2(L-1) - q (q >= L)
+// (torch's "reflect" padding followed by a correlation), and its adjoint
+//   out[i] = sum_o sum_t taps[t + r] v[o] [refl(o + t) == i]
+// as a gather: the direct terms o = i - t, the mirror of the low edge (o + t = -i, 1 <= i <= r)
+// and of the high edge (o + t = 2(L-1) - i, L-1-r <= i <= L-2).  Requires r < L.
+template <typename T>
+__global__ void k_blur1d(const T* __restrict__ in, T* __restrict__ out, int64_t total, int H, int W, int axis,
+                         const T* __restrict__ taps, int r) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int64_t p = idx / ((int64_t)H * W);
+    const int rem = (int)(idx - p * H * W), y = rem / W, x = rem - (rem / W) * W;
+    const int L = axis == 0 ? H : W, o = axis == 0 ? y : x, stride = axis == 0 ? W : 1;
+    const T* base = in + p * H * W + (axis == 0 ? x : y * W);
+    T acc = (T)0;
+    for (int t = -r; t <= r; ++t) {
+        int q = o + t;
+        q = q < 0 ? -q : (q >= L ? 2 * (L - 1) - q : q);
+        acc = fma(__ldg(taps + t + r), __ldg(base + (int64_t)q * stride), acc);
+    }
+    out[idx] = acc;
+}
+
+template <typename T>
+__global__ void k_blur1d_t(const T* __restrict__ v, T* __restrict__ out, int64_t total, int H, int W, int axis,
+                           const T* __restrict__ taps, int r) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int64_t p = idx / ((int64_t)H * W);
+    const int rem = (int)(idx - p * H * W), y = rem / W, x = rem - (rem / W) * W;
+    const int L = axis == 0 ? H : W, i = axis == 0 ? y : x, stride = axis == 0 ? W : 1;
+    const T* base = v + p * H * W + (axis == 0 ? x : y * W);
+    T acc = (T)0;
+    const int a0 = i - r > 0 ? i - r : 0, a1 = i + r < L - 1 ? i + r : L - 1;
+    for (int o = a0; o <= a1; ++o) acc = fma(__ldg(taps + (i - o) + r), __ldg(base + (int64_t)o * stride), acc);
+    if (i >= 1 && i <= r)
+        for (int o = 0; o <= r - i; ++o) acc = fma(__ldg(taps + (-i - o) + r), __ldg(base + (int64_t)o * stride), acc);
+    if (i <= L - 2 && i >= L - 1 - r)
+        for (int o = 2 * (L - 1) - i - r; o <= L - 1; ++o)
+            acc = fma(__ldg(taps + (2 * (L - 1) - i - o) + r), __ldg(base + (int64_t)o * stride), acc);
+    out[idx] = acc;
+}
+
+// ---- soft-argmax band sharpness ------------------------------------------------------------
+// Per pattern (one block): J_p = sum_i s_i c_i over the Radon-mask cells, s = softmax(c / tau),
+// and dJ_p / dc_i = s_i (1 + (c_i - J_p) / tau) (zero off the mask).  Sums in float64.
+template <typename T>
+__global__ void k_softargmax(const T* __restrict__ c, int64_t ncell, const int32_t* __restrict__ cells, int ncm,
+                             double inv_tau, double* __restrict__ Jp, T* __restrict__ grad) {
+    __shared__ double red[64];
+    const int64_t p = blockIdx.x;
+    const T* cp = c + p * ncell;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    double mx = -INFINITY;
+    for (int k = tid; k < ncm; k += blockDim.x) mx = fmax(mx, (double)cp[cells[k]] * inv_tau);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    if (lane == 0) red[warp] = mx;
+    __syncthreads();
+    if (tid == 0) {
+        double m = red[0];
+        for (int w = 1; w < nw; ++w) m = fmax(m, red[w]);
+        red[63] = m;
+    }
+    __syncthreads();
+    mx = red[63];
+    double s0 = 0.0, s1 = 0.0;
+    for (int k = tid; k < ncm; k += blockDim.x) {
+        const double v = (double)cp[cells[k]];
+        const double e = exp(v * inv_tau - mx);
+        s0 += e;
+        s1 += e * v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    __syncthreads();
+    if (lane == 0) { red[warp] = s0; red[32 + warp] = s1; }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0.0, b = 0.0;
+        for (int w = 0; w < nw; ++w) { a += red[w]; b += red[32 + w]; }
+        red[62] = a;
+        red[61] = b / a;
+        Jp[p] = b / a;
+    }
+    __syncthreads();
+    const double S0 = red[62], J = red[61];
+    T* gp = grad + p * ncell;
+    for (int k = tid; k < ncm; k += blockDim.x) {
+        const double v = (double)cp[cells[k]];
+        const double si = exp(v * inv_tau - mx) / S0;
+        gp[cells[k]] = (T)(si * (1.0 + (v - J) * inv_tau));
+    }
+}
+
+// ---- NLPAR weights as functions of the patterns ----------------------------------------------
+// sigma (nlpar_cpu.py:753-796, nn = 1) with the neighbour that attains the minimum and its pair
+// count: sig2 = sigma^2 as the weights use it, arg = that neighbour (-1: none), nsig = its count.
+__global__ void k_sigma_arg(const float* __restrict__ data, int nrows, int ncols, int npx,
+                            const int32_t* __restrict__ ind, int nind, float mxval, float* __restrict__ sig2,
+                            int* __restrict__ arg, float* __restrict__ nsig) {
+    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= nrows * ncols) return;
+    const int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+    float best = 1e24f, bn = 0.0f;
+    int ba = -1;
+    for (int k = 0; k < 9; ++k) {
+        if (k == 4) continue;
+        const int jn = j + k / 3 - 1, inn = i + k % 3 - 1;
+        if (jn < 0 || jn >= nrows || inn < 0 || inn >= ncols) continue;
+        const int nb = inn + ncols * jn;
+        float d2, n2;
+        pair_ssd(data + (int64_t)pix * npx, data + (int64_t)nb * npx, ind, nind, mxval, d2, n2);
+        n2 = __fadd_rn(n2, 1.0e-12f);
+        if (d2 >= 1.e-3f) {
+            const float s0 = __fdiv_rn(d2, __fmul_rn(n2, 2.0f));
+            if (s0 < best) { best = s0; ba = nb; bn = n2; }
+        }
+    }
+    const float sg = sqrtf(best);
+    sig2[pix] = __fmul_rn(sg, sg);
+    arg[pix] = ba;
+    nsig[pix] = bn;
+}
+
+// Window weights with the pieces of their derivative (one block per scan pixel, one thread per
+// slot): w (normalised), m = max(d - dthresh, 0), and for the normalised distance
+// d = (S - n s) / (s sqrt(2 n)) (s = sigma_p^2 + sigma_c^2): dS = dd/dS = 1 / (s sqrt(2 n)),
+// ds = dd/ds = -S / (s^2 sqrt(2 n)); both 0 at the centre slot and where d is set to 1e6 n.
+__global__ void k_nlpar_weights_d(const float* __restrict__ data, int nrows, int ncols, int npx,
+                                  const int32_t* __restrict__ ind, int nind, float mxval,
+                                  const float* __restrict__ sig2, float lam2, float dthresh, int sr,
+                                  float* __restrict__ wout, float* __restrict__ mout, float* __restrict__ dsout,
+                                  float* __restrict__ dgout) {
+    extern __shared__ float w_s[];
+    __shared__ float tot_s;
+    const int pix = blockIdx.x;
+    const int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+    int xs, xe, ys, ye;
+    window(i, sr, ncols, xs, xe);
+    window(j, sr, nrows, ys, ye);
+    const int wx = xe - xs, winsz = (2 * sr + 1) * (2 * sr + 1);
+    const int c = threadIdx.x;
+    float m = 0.0f, dS = 0.0f, dg = 0.0f;
+    if (c < winsz) {
+        const int nb = (xs + c % wx) + ncols * (ys + c / wx);
+        float w;
+        if (nb == pix) {
+            w = -1.0e6f;
+        } else {
+            float d2, n2;
+            pair_ssd(data + (int64_t)pix * npx, data + (int64_t)nb * npx, ind, nind, mxval, d2, n2);
+            const float ss = __fadd_rn(sig2[pix], sig2[nb]);
+            const float S = d2;
+            d2 = __fsub_rn(d2, __fmul_rn(n2, ss));
+            const float dnorm = __fmul_rn(ss, sqrtf(__fmul_rn(2.0f, n2)));
+            if (dnorm > 1.e-8f) {
+                w = __fdiv_rn(d2, dnorm);
+                dS = 1.0f / dnorm;
+                dg = -S / (ss * dnorm);
+            } else {
+                w = __fmul_rn(1e6f, n2);
+            }
+        }
+        m = fmaxf(__fsub_rn(w, dthresh), 0.0f);
+        if (!(w - dthresh > 0.0f)) { dS = 0.0f; dg = 0.0f; }  // clamped: no derivative
+        w_s[c] = expf(__fmul_rn(__fmul_rn(-1.0f, m), lam2));
+    }
+    __syncthreads();
+    if (c == 0) {
+        float t = 0.0f;
+        for (int k = 0; k < winsz; ++k) t = __fadd_rn(t, w_s[k]);
+        tot_s = t;
+    }
+    __syncthreads();
+    if (c < winsz) {
+        const int64_t o = (int64_t)pix * winsz + c;
+        wout[o] = __fdiv_rn(w_s[c], tot_s);
+        mout[o] = m;
+        dsout[o] = dS;
+        dgout[o] = dg;
+    }
+}
+
+// G[p][c] = g_p . x_c over all pattern pixels (float64 sums); one block per scan pixel, one warp
+// per window slot at a time.
+template <typename T>
+__global__ void k_nlpar_dots(const T* __restrict__ g, const T* __restrict__ x, int nrows, int ncols, int npx, int sr,
+                             double* __restrict__ G) {
+    const int p = blockIdx.x;
+    const int jp = p / ncols, ip = p - (p / ncols) * ncols;
+    int xs, xe, ys, ye;
+    window(ip, sr, ncols, xs, xe);
+    window(jp, sr, nrows, ys, ye);
+    const int wx = xe - xs, winsz = (2 * sr + 1) * (2 * sr + 1);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const T* gp = g + (int64_t)p * npx;
+    for (int c = warp; c < winsz; c += nw) {
+        const int nb = (xs + c % wx) + ncols * (ys + c / wx);
+        const T* xc = x + (int64_t)nb * npx;
+        double acc = 0.0;
+        for (int k = lane; k < npx; k += 32) acc += (double)__ldg(gp + k) * (double)__ldg(xc + k);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) G[(int64_t)p * winsz + c] = acc;
+    }
+}
+
+// Per scan pixel p: Gbar = sum_c w_pc G_pc; dJ/dd_pc = -(w_pc / lam^2) (G_pc - Gbar) where the
+// weight's exponent is not clamped; alpha = dJ/dd * dd/dS, beta = dJ/dd * dd/ds; and the lambda
+// term sum_c w_pc (2 m_pc / lam^3) (G_pc - Gbar).
+__global__ void k_nlpar_coef(const double* __restrict__ G, const float* __restrict__ w, const float* __restrict__ m,
+                             const float* __restrict__ dS, const float* __restrict__ dg, int npix, int winsz,
+                             double lam, double* __restrict__ alpha, double* __restrict__ beta,
+                             double* __restrict__ glam) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const int64_t o = (int64_t)p * winsz;
+    double gbar = 0.0;
+    for (int c = 0; c < winsz; ++c) gbar += (double)w[o + c] * G[o + c];
+    const double il2 = 1.0 / (lam * lam), c3 = 2.0 / (lam * lam * lam);
+    double gl = 0.0;
+    for (int c = 0; c < winsz; ++c) {
+        const double dg_ = G[o + c] - gbar;
+        const double a = -(double)w[o + c] * il2 * dg_;
+        alpha[o + c] = a * (double)dS[o + c];
+        beta[o + c] = a * (double)dg[o + c];
+        gl += (double)w[o + c] * c3 * (double)m[o + c] * dg_;
+    }
+    glam[p] = gl;
+}
+
+// gamma_q = dJ / d sigma_q^2 = sum of beta over the pairs that hold q (as window centre or as
+// neighbour); s_pc = sigma_p^2 + sigma_c^2 enters both.
+__global__ void k_nlpar_gamma(const double* __restrict__ beta, int nrows, int ncols, int sr,
+                              double* __restrict__ gamma) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrows * ncols) return;
+    const int winsz = (2 * sr + 1) * (2 * sr + 1), wx = 2 * sr + 1;
+    const int jq = q / ncols, iq = q - (q / ncols) * ncols;
+    double acc = 0.0;
+    for (int c = 0; c < winsz; ++c) acc += beta[(int64_t)q * winsz + c];
+    const int j0 = jq - 2 * sr < 0 ? 0 : jq - 2 * sr, j1 = jq + 2 * sr > nrows - 1 ? nrows - 1 : jq + 2 * sr;
+    const int i0 = iq - 2 * sr < 0 ? 0 : iq - 2 * sr, i1 = iq + 2 * sr > ncols - 1 ? ncols - 1 : iq + 2 * sr;
+    for (int jp = j0; jp <= j1; ++jp) {
+        int ys, ye;
+        window(jp, sr, nrows, ys, ye);
+        if (jq < ys || jq >= ye) continue;
+        for (int ip = i0; ip <= i1; ++ip) {
+            int xs, xe;
+            window(ip, sr, ncols, xs, xe);
+            if (iq < xs || iq >= xe) continue;
+            const int p = ip + ncols * jp;
+            if (p == q) continue;
+            acc += beta[(int64_t)p * winsz + (jq - ys) * wx + (iq - xs)];
+        }
+    }
+    gamma[q] = acc;
+}
+
+// dJ/dx_q[k] from the weights' dependence on the patterns: the pair SSDs of q's own window, of
+// the windows that hold q, and the noise sigma's minimising pair (q's own, and those of the
+// 3x3 neighbours whose minimum pairs with q).  Masked pixels only, each pair's saturation test.
+template <typename T>
+__global__ void k_nlpar_dx(const T* __restrict__ x, int nrows, int ncols, int npx, int sr,
+                           const uint8_t* __restrict__ pmask, float mxw, float mxs, const double* __restrict__ alpha,
+                           const double* __restrict__ gamma, const int* __restrict__ arg,
+                           const float* __restrict__ nsig, T* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (k >= npx) return;
+    double acc = 0.0;
+    if (pmask[k]) {
+        const int winsz = (2 * sr + 1) * (2 * sr + 1), wx = 2 * sr + 1;
+        const int jq = q / ncols, iq = q - (q / ncols) * ncols;
+        const double xq = (double)x[(int64_t)q * npx + k];
+        const bool qw = xq < (double)mxw, qs = xq < (double)mxs;
+        {
+            int xs, xe, ys, ye;
+            window(iq, sr, ncols, xs, xe);
+            window(jq, sr, nrows, ys, ye);
+            const int wq = xe - xs;
+            for (int c = 0; c < winsz; ++c) {
+                const int nb = (xs + c % wq) + ncols * (ys + c / wq);
+                if (nb == q) continue;
+                const double xc = (double)x[(int64_t)nb * npx + k];
+                if (qw && xc < (double)mxw) acc += 2.0 * alpha[(int64_t)q * winsz + c] * (xq - xc);
+            }
+        }
+        const int j0 = jq - 2 * sr < 0 ? 0 : jq - 2 * sr, j1 = jq + 2 * sr > nrows - 1 ? nrows - 1 : jq + 2 * sr;
+        const int i0 = iq - 2 * sr < 0 ? 0 : iq - 2 * sr, i1 = iq + 2 * sr > ncols - 1 ? ncols - 1 : iq + 2 * sr;
+        for (int jp = j0; jp <= j1; ++jp) {
+            int ys, ye;
+            window(jp, sr, nrows, ys, ye);
+            if (jq < ys || jq >= ye) continue;
+            for (int ip = i0; ip <= i1; ++ip) {
+                int xs, xe;
+                window(ip, sr, ncols, xs, xe);
+                if (iq < xs || iq >= xe) continue;
+                const int p = ip + ncols * jp;
+                if (p == q) continue;
+                const double xp = (double)x[(int64_t)p * npx + k];
+                if (qw && xp < (double)mxw) acc += 2.0 * alpha[(int64_t)p * winsz + (jq - ys) * wx + (iq - xs)] * (xq - xp);
+            }
+        }
+        // noise sigma: sigma_p^2 = SSD(p, arg_p) / (2 n_p)
+        const int aq = arg[q];
+        if (aq >= 0) {
+            const double xa = (double)x[(int64_t)aq * npx + k];
+            if (qs && xa < (double)mxs) acc += gamma[q] * (xq - xa) / (double)nsig[q];
+        }
+        for (int dj = -1; dj <= 1; ++dj)
+            for (int di = -1; di <= 1; ++di) {
+                const int jn = jq + dj, in_ = iq + di;
+                if ((dj == 0 && di == 0) || jn < 0 || jn >= nrows || in_ < 0 || in_ >= ncols) continue;
+                const int p = in_ + ncols * jn;
+                if (arg[p] != q) continue;
+                const double xp = (double)x[(int64_t)p * npx + k];
+                if (qs && xp < (double)mxs) acc += gamma[p] * (xq - xp) / (double)nsig[p];
+            }
+    }
+    out[(int64_t)q * npx + k] = (T)acc;
+}
+
 }  // namespace
 }  // namespace ebsd
 
@@ -264,6 +590,91 @@ int ebsd_nlpar_weights(const float* d_data, int32_t nrows, int32_t ncols, int32_
     k_nlpar_weights2<<<(unsigned)(nrows * ncols), ((winsz + 31) / 32) * 32, winsz * sizeof(float),
                        (cudaStream_t)stream>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma, lam2,
                                                dthresh, sr, d_w, d_m);
+    return launch_status();
+}
+
+int ebsd_blur1d(int fp64, int adjoint, int axis, const void* d_in, int64_t n, int32_t H, int32_t W,
+                const void* d_taps, int32_t r, void* d_out, void* stream) {
+    if (!d_in || !d_taps || !d_out || n < 0 || H <= 0 || W <= 0 || r < 0 || (axis != 0 && axis != 1) ||
+        r >= (axis == 0 ? H : W))
+        return EBSD_E_ARG;
+    const int64_t total = n * H * W;
+    if (total == 0) return EBSD_OK;
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (fp64) {
+        if (adjoint) k_blur1d_t<double><<<blocks, 256, 0, st>>>((const double*)d_in, (double*)d_out, total, H, W, axis, (const double*)d_taps, r);
+        else k_blur1d<double><<<blocks, 256, 0, st>>>((const double*)d_in, (double*)d_out, total, H, W, axis, (const double*)d_taps, r);
+    } else {
+        if (adjoint) k_blur1d_t<float><<<blocks, 256, 0, st>>>((const float*)d_in, (float*)d_out, total, H, W, axis, (const float*)d_taps, r);
+        else k_blur1d<float><<<blocks, 256, 0, st>>>((const float*)d_in, (float*)d_out, total, H, W, axis, (const float*)d_taps, r);
+    }
+    return launch_status();
+}
+
+int ebsd_softargmax(int fp64, const void* d_c, int64_t n, int64_t ncell, const int32_t* d_cells, int32_t ncm,
+                    double tau, double* d_J, void* d_grad, void* stream) {
+    if (!d_c || !d_cells || !d_J || !d_grad || n < 0 || ncell <= 0 || ncm <= 0 || ncm > ncell || !(tau > 0.0))
+        return EBSD_E_ARG;
+    if (n == 0) return EBSD_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (fp64) k_softargmax<double><<<(unsigned)n, 256, 0, st>>>((const double*)d_c, ncell, d_cells, ncm, 1.0 / tau, d_J, (double*)d_grad);
+    else k_softargmax<float><<<(unsigned)n, 256, 0, st>>>((const float*)d_c, ncell, d_cells, ncm, 1.0 / tau, d_J, (float*)d_grad);
+    return launch_status();
+}
+
+int ebsd_nlpar_sigma_arg(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
+                         int32_t nind, float datamax, int saturation_protect, float* d_sig2, int32_t* d_arg,
+                         float* d_nsig, void* stream) {
+    if (!d_data || !d_indices || !d_sig2 || !d_arg || !d_nsig || nrows <= 0 || ncols <= 0 || npx <= 0 || nind < 0 ||
+        nind > npx)
+        return EBSD_E_ARG;
+    const float mxval = saturation_protect ? datamax * 0.9961f : datamax + 1.0f;
+    const int npix = nrows * ncols;
+    k_sigma_arg<<<(unsigned)((npix + 127) / 128), 128, 0, (cudaStream_t)stream>>>(d_data, nrows, ncols, npx, d_indices,
+                                                                             nind, mxval, d_sig2, d_arg, d_nsig);
+    return launch_status();
+}
+
+int ebsd_nlpar_weights_d(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
+                         int32_t nind, float datamax, float lam, int32_t sr, float dthresh, const float* d_sig2,
+                         int saturation_protect, float* d_w, float* d_m, float* d_dS, float* d_dsig, void* stream) {
+    if (!d_data || !d_indices || !d_sig2 || !d_w || !d_m || !d_dS || !d_dsig || nrows <= 0 || ncols <= 0 ||
+        npx <= 0 || nind < 0 || nind > npx || sr < 0 || sr > 10 || !(lam > 0.0f) || 2 * sr + 1 > nrows ||
+        2 * sr + 1 > ncols)
+        return EBSD_E_ARG;
+    const float mxval = saturation_protect ? datamax * 0.999f : datamax + 1.0f;
+    const int winsz = (2 * sr + 1) * (2 * sr + 1);
+    k_nlpar_weights_d<<<(unsigned)(nrows * ncols), ((winsz + 31) / 32) * 32, winsz * sizeof(float),
+                        (cudaStream_t)stream>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sig2,
+                                                1.0f / (lam * lam), dthresh, sr, d_w, d_m, d_dS, d_dsig);
+    return launch_status();
+}
+
+int ebsd_nlpar_weights_grad(int fp64, const void* d_g, const void* d_x, int32_t nrows, int32_t ncols, int32_t npx,
+                            int32_t sr, const float* d_w, const float* d_m, const float* d_dS, const float* d_dsig,
+                            double lam, const uint8_t* d_pmask, float datamax, int saturation_protect,
+                            const int32_t* d_arg, const float* d_nsig, double* d_scratch, double* d_glam,
+                            void* d_gx, void* stream) {
+    if (!d_g || !d_x || !d_w || !d_m || !d_dS || !d_dsig || !d_pmask || !d_arg || !d_nsig || !d_scratch ||
+        !d_glam || !d_gx || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10 || !(lam > 0.0))
+        return EBSD_E_ARG;
+    const int npix = nrows * ncols, winsz = (2 * sr + 1) * (2 * sr + 1);
+    double* G = d_scratch;
+    double* alpha = G + (int64_t)npix * winsz;
+    double* beta = alpha + (int64_t)npix * winsz;
+    double* gamma = beta + (int64_t)npix * winsz;
+    cudaStream_t st = (cudaStream_t)stream;
+    const float mxw = saturation_protect ? datamax * 0.999f : datamax + 1.0f;
+    const float mxs = saturation_protect ? datamax * 0.9961f : datamax + 1.0f;
+    if (fp64) k_nlpar_dots<double><<<(unsigned)npix, 256, 0, st>>>((const double*)d_g, (const double*)d_x, nrows, ncols, npx, sr, G);
+    else k_nlpar_dots<float><<<(unsigned)npix, 256, 0, st>>>((const float*)d_g, (const float*)d_x, nrows, ncols, npx, sr, G);
+    k_nlpar_coef<<<(unsigned)((npix + 127) / 128), 128, 0, st>>>(G, d_w, d_m, d_dS, d_dsig, npix, winsz, lam, alpha,
+                                                                 beta, d_glam);
+    k_nlpar_gamma<<<(unsigned)((npix + 127) / 128), 128, 0, st>>>(beta, nrows, ncols, sr, gamma);
+    dim3 grid((unsigned)((npx + 127) / 128), (unsigned)npix);
+    if (fp64) k_nlpar_dx<double><<<grid, 128, 0, st>>>((const double*)d_x, nrows, ncols, npx, sr, d_pmask, mxw, mxs, alpha, gamma, d_arg, d_nsig, (double*)d_gx);
+    else k_nlpar_dx<float><<<grid, 128, 0, st>>>((const float*)d_x, nrows, ncols, npx, sr, d_pmask, mxw, mxs, alpha, gamma, d_arg, d_nsig, (float*)d_gx);
     return launch_status();
 }
 

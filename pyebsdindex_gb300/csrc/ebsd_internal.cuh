@@ -186,5 +186,10 @@ void slab_release(ebsd_plan_s* p);
 bool slab_serves(const ebsd_plan_s* p, int method, int dtype);
 int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
                    int64_t out_offset, cudaStream_t st, int64_t* launches);
+// mixed pattern sizes in one launch: up to 8 plans of one input type and LoG size
+constexpr int kMaxMixedPlans = 8;
+bool slab_mixable(const ebsd_plan_s* p, int dtype);
+int slab_run_mixed(ebsd_plan_s* const* plans, int nplans, int dtype, const void* const* d_pats, const int64_t* n,
+                   const ebsd_bands* out, cudaStream_t st, int64_t* launches);
 
 }  // namespace ebsd

@@ -683,6 +683,30 @@ int ebsd_find_bands(ebsd_plan_t p, int method, int dtype, const void* d_pats, in
     return EBSD_OK;
 }
 
+int ebsd_find_bands_mixed(const ebsd_plan_t* plans, int nplans, int dtype, const void* const* d_pats,
+                          const int64_t* n, const ebsd_bands* d_out, void* stream) {
+    if (!plans || !d_pats || !n || !d_out || nplans < 1 || nplans > kMaxMixedPlans) return EBSD_E_ARG;
+    if (dtype != EBSD_U8 && dtype != EBSD_U16 && dtype != EBSD_F32) return EBSD_E_DTYPE;
+    for (int k = 0; k < nplans; ++k) {
+        const ebsd_plan_s* p = plans[k];
+        if (!p || n[k] < 0 || (n[k] > 0 && !d_pats[k]) || !all_outputs(&d_out[k])) return EBSD_E_ARG;
+        if (p->device != plans[0]->device || p->k0 != plans[0]->k0 || p->k1 != plans[0]->k1) return EBSD_E_ARG;
+        if (!slab_mixable(p, dtype)) return EBSD_E_UNSUPPORTED;
+    }
+    // one plan's lock at a time would let two mixed calls interleave; lock in address order
+    std::vector<ebsd_plan_s*> order(plans, plans + nplans);
+    std::sort(order.begin(), order.end());
+    order.erase(std::unique(order.begin(), order.end()), order.end());
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (ebsd_plan_s* p : order) locks.emplace_back(p->mtx);
+    if (cudaSetDevice(plans[0]->device) != cudaSuccess) return EBSD_E_DEVICE;
+    std::vector<ebsd_plan_s*> ps(plans, plans + nplans);
+    int64_t launches = 0;
+    const int rc = slab_run_mixed(ps.data(), nplans, dtype, d_pats, n, d_out, (cudaStream_t)stream, &launches);
+    for (ebsd_plan_s* p : order) p->last_launches = launches;
+    return rc;
+}
+
 int ebsd_find_bands_host(ebsd_plan_t p, int method, int dtype, const void* h_pats, int64_t n,
                          const ebsd_bands* h_out, int64_t chunk) {
     if (!p || !h_out || n < 0) return EBSD_E_ARG;

@@ -73,6 +73,17 @@ struct SlabArgs {
     int64_t out_offset;
 };
 
+// One launch serves up to kMaxPlans plans of one input type and LoG size (mixed pattern sizes):
+// plan k's patterns are indices [start[k], start[k + 1]) of the launch, which the persistent
+// CTAs stride over, so every CTA takes patterns of every plan.  The arguments travel by value
+// in the launch parameters.
+constexpr int kMaxPlans = 8;
+struct MultiArgs {
+    SlabArgs plan[kMaxPlans];
+    int64_t start[kMaxPlans + 1];
+    int nplans;
+};
+
 __device__ __forceinline__ bool beats(float v, int p, float w, int q) {
     return v > w || (v == w && p < q);
 }
@@ -89,7 +100,7 @@ __device__ __forceinline__ void list_insert(float v, int pos, float& lv, int& lp
 }
 
 template <typename InT, int K0, int K1>
-__global__ void __launch_bounds__(kThreads, 1) k_slab(SlabArgs a) {
+__global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ MultiArgs ma) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int D0 = K0, D1 = K1;          // max-filter half windows (peakPad = 2*ksz + 1)
     constexpr int H1 = K1 / 2;               // LoG half width along theta
@@ -97,6 +108,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(SlabArgs a) {
     constexpr int NV = kRowBlock + 2 * D0;
     constexpr bool kInt = sizeof(InT) < 4;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+    for (int64_t qq = blockIdx.x; qq < ma.start[ma.nplans]; qq += gridDim.x) {
+    int pid = 0;
+    while (pid + 1 < ma.nplans && qq >= ma.start[pid + 1]) ++pid;
+    const SlabArgs& a = ma.plan[pid];
+    const int64_t q = qq - ma.start[pid];
     const int nB = a.nB, TBP = a.TBP, CCP = a.CCP, MP = a.MP;
 
     size_t off = 0;
@@ -123,7 +140,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(SlabArgs a) {
     unsigned* gtb_s = (unsigned*)(smem + off);
 
     const int stat_rows = a.statR;
-    for (int64_t q = blockIdx.x; q < a.n; q += gridDim.x) {
+    {
         // ---- the pattern into shared memory; one zero element after it (the LUT's pad slot)
         {
             const InT* gp = (const InT*)a.pats + q * (int64_t)a.H * a.W;
@@ -481,6 +498,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(SlabArgs a) {
         }
         __syncthreads();
     }
+    }  // patterns
 }
 
 }  // namespace
@@ -547,9 +565,10 @@ int slab_attr(const void* fn, int device, int smem) {
 // 32 neighbouring rho at one theta, slot s of every lane at image column (or row) base + s when
 // each ray of the group has at most one pixel per column (row), as the reference's sampling
 // gives (radon_fast.py:113-158); a group that fits neither keeps each ray's sorted order.
+// Built for every plan whose geometry qualifies: the single-plan path uses it when the single
+// tile does not fit, the mixed-size launch (ebsd_find_bands_mixed) for every plan.
 int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     p->sg = SlabGeom{};
-    if (p->fg.ok_f32) return EBSD_OK;  // the single-tile kernel takes the plan
     const int K0 = p->k0, K1 = p->k1;
     const int D0 = K0, D1 = K1, H0 = K0 / 2, H1 = K1 / 2;
     if (!(p->pk0 == 2 * K0 + 1 && p->pk1 == 2 * K1 + 1 && K0 == K1 && pick_slab_kernel(EBSD_U16, K0, K1) &&
@@ -570,7 +589,7 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
     // widest slab whose uint16 tiles fit; slabs of near-equal width
     int nslab = 0, Ts = 0;
-    for (int ns = 2; ns <= p->nTheta; ++ns) {
+    for (int ns = 1; ns <= p->nTheta; ++ns) {
         const int ts = (p->nTheta + ns - 1) / ns;
         if (ts < 2 * D1 + 1 || ts < 16) break;
         const int TBP = (ts + 2 * halo) | 1, CCP = (ts + 2 * D1) | 1;
@@ -753,17 +772,10 @@ bool slab_serves(const ebsd_plan_s* p, int method, int dtype) {
     return dtype != EBSD_F32 || p->sg.ok_f32;
 }
 
-int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
-                   int64_t out_offset, cudaStream_t st, int64_t* launches) {
-    if (n <= 0) return EBSD_OK;
-    void* fn = pick_slab_kernel(dtype, p->k0, p->k1);
-    if (!fn || !slab_serves(p, EBSD_FUSED_F32, dtype)) return EBSD_E_UNSUPPORTED;
+namespace {
+
+SlabArgs slab_args(const ebsd_plan_s* p, const void* d_pats, int64_t n, const ebsd_bands& out, int64_t out_offset) {
     const SlabGeom& g = p->sg;
-    const int smem = g.smem[dtype == EBSD_U8 ? 0 : (dtype == EBSD_U16 ? 1 : 2)];
-    int rc = slab_attr(fn, p->device, smem);
-    if (rc != EBSD_OK) return rc;
-    int sms = 0;
-    EBSD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
     SlabArgs a;
     a.pats = d_pats;
     a.n = n;
@@ -798,14 +810,69 @@ int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, con
     }
     a.rdnmask = p->d_rdnmask;
     a.kc = LabelConsts{p->p0, p->p1, p->nTheta, p->nRho, p->nB, p->d_theta, p->d_rho};
-    a.out = *out;
+    a.out = out;
     a.out_offset = out_offset;
-    void* args[] = {&a};
-    const int64_t grid = std::min<int64_t>(n, sms);
+    return a;
+}
+
+int smem_index(int dtype) { return dtype == EBSD_U8 ? 0 : (dtype == EBSD_U16 ? 1 : 2); }
+
+// One persistent launch over the plans' patterns, then each plan's float64 epilogue pass.
+int slab_launch(ebsd_plan_s* const* plans, int nplans, int dtype, const void* const* d_pats, const int64_t* n,
+                const ebsd_bands* out, const int64_t* out_offset, cudaStream_t st, int64_t* launches) {
+    const ebsd_plan_s* p0 = plans[0];
+    void* fn = pick_slab_kernel(dtype, p0->k0, p0->k1);
+    if (!fn) return EBSD_E_UNSUPPORTED;
+    MultiArgs ma;
+    std::memset(&ma, 0, sizeof(ma));
+    ma.nplans = nplans;
+    int smem = 0;
+    int64_t total = 0;
+    for (int k = 0; k < nplans; ++k) {
+        ma.start[k] = total;
+        ma.plan[k] = slab_args(plans[k], d_pats[k], n[k], out[k], out_offset[k]);
+        smem = std::max(smem, plans[k]->sg.smem[smem_index(dtype)]);
+        total += n[k];
+    }
+    ma.start[nplans] = total;
+    if (total == 0) return EBSD_OK;
+    int rc = slab_attr(fn, p0->device, smem);
+    if (rc != EBSD_OK) return rc;
+    int sms = 0;
+    EBSD_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p0->device));
+    void* args[] = {&ma};
+    const int64_t grid = std::min<int64_t>(total, sms);
     EBSD_CUDA_TRY(cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kThreads), args, (size_t)smem, st));
-    band_epilogue_launch(*out, out_offset, n, p->nB, a.kc, sms, st);
-    *launches += 2;
+    *launches += 1;
+    for (int k = 0; k < nplans; ++k) {
+        if (n[k] <= 0) continue;
+        const SlabArgs& a = ma.plan[k];
+        band_epilogue_launch(out[k], out_offset[k], n[k], plans[k]->nB, a.kc, sms, st);
+        *launches += 1;
+    }
     return launch_status();
+}
+
+}  // namespace
+
+int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
+                   int64_t out_offset, cudaStream_t st, int64_t* launches) {
+    if (n <= 0) return EBSD_OK;
+    if (!slab_serves(p, EBSD_FUSED_F32, dtype)) return EBSD_E_UNSUPPORTED;
+    ebsd_plan_s* plans[1] = {p};
+    const void* pats[1] = {d_pats};
+    return slab_launch(plans, 1, dtype, pats, &n, out, &out_offset, st, launches);
+}
+
+bool slab_mixable(const ebsd_plan_s* p, int dtype) {
+    return p->sg.ok && (dtype != EBSD_F32 || p->sg.ok_f32);
+}
+
+int slab_run_mixed(ebsd_plan_s* const* plans, int nplans, int dtype, const void* const* d_pats, const int64_t* n,
+                   const ebsd_bands* out, cudaStream_t st, int64_t* launches) {
+    if (nplans < 1 || nplans > kMaxPlans) return EBSD_E_ARG;
+    int64_t offs[kMaxPlans] = {};
+    return slab_launch(plans, nplans, dtype, d_pats, n, out, offs, st, launches);
 }
 
 }  // namespace ebsd

@@ -1,6 +1,7 @@
 """Mixed pattern sizes in one batch (60x60 / 120x120 / 240x240 uint16 at 4000 counts, nRho =
-1.5*size, nBands 10): per-size plans, results in input order, equal to running each size alone;
-and the precision study on it: FP16 Radon storage vs FP32 vs the FP64 GPU oracle."""
+1.5*size, nBands 10): per-size plans, one persistent launch over all sizes, results in input
+order, equal to running each size alone; and the precision study on it: FP16 Radon storage vs
+FP32 vs the FP64 GPU oracle."""
 import numpy as np
 import pytest
 
@@ -28,6 +29,7 @@ def test_mixed_sizes_equal_per_size_runs(cuda):
     pats = mixed_batch()
     mb = MixedBandDetect(nBands=10, mask_for=syn.circular_mask)
     rec = mb.find_bands(pats)
+    assert mb.last_mixed, "the three sizes should run as one mixed-size launch"
     assert rec.shape == (len(pats), 10)
     for h in (60, 120, 240):
         idx = [k for k, p in enumerate(pats) if p.shape[0] == h]
@@ -53,3 +55,21 @@ def test_mixed_precision_vs_fp64(cuda, h):
         c16 = compare(bd.find_bands(pats, method="fused16"), ref)
         print(h, "fused16 vs fp64", c16)
         assert c16["frac"] >= 0.98 and c16["aveloc_p50"] <= 2e-3, c16
+
+
+def test_mixed_uint16_one_launch(cuda):
+    """uint16 patterns of three sizes in unequal numbers through one launch (ebsd_find_bands_mixed):
+    every band field equals the single-size fused call's, normmax to its last bits."""
+    import torch
+    if getattr(torch, "uint16", None) is None:
+        pytest.skip("torch without uint16")
+    mb = MixedBandDetect(nBands=10, mask_for=syn.circular_mask)
+    batches = {(h, h): syn.make_patterns(n, h, h, seed=40 + h, dtype=np.uint16, peak=4000.0, noise_frac=0.1)[0]
+               for h, n in ((60, 301), (120, 77), (240, 19))}
+    recs = mb.find_bands_grouped(batches)
+    assert mb.last_mixed
+    for key, pats in batches.items():
+        alone = mb.plan(*key).find_bands(pats, method="fused")
+        for f in ("max", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
+            assert recs[key][f].tobytes() == alone[f].tobytes(), (key, f)
+        np.testing.assert_allclose(recs[key]["normmax"], alone["normmax"], rtol=1e-6)

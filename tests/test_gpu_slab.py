@@ -57,7 +57,7 @@ def test_slab_float_and_rectangular(cuda):
     a = bd.find_bands(pats, method="plain")
     b = bd.find_bands(pats, method="fused")
     c = compare_records(b, a)
-    assert c["peak_frac"] >= 0.999 and c["aveloc_max"] <= 1e-3 and c["max_rel"] <= 1e-5, c
+    assert c["peak_frac"] >= 0.999 and c["aveloc_max"] <= 1e-3 and c["max_rel"] <= 1e-4, c
 
 
 def test_slab_chunking_and_degenerate(cuda):
