@@ -78,6 +78,8 @@ def parse():
                     help="also time NLPAR's file interface (opt_lambda, calcnlpar) on a 400x500 UP1 scan")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-size (60/120/240 uint16) figure")
     ap.add_argument("--mixed-patterns", type=int, default=300_000, help="patterns of the mixed-size step")
+    ap.add_argument("--no-nlpar", action="store_true", help="skip the NLPAR -> detection figure")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiable-path figure")
     ap.add_argument("--lambda-scan", action="store_true",
                     help="also time NLPAR's lambda optimisation on a 400x500 scan of 80x80 patterns")
     return ap.parse_args()
@@ -377,6 +379,45 @@ def time_indexing(outs, bd, N, stream, with_cpu, detect_ms):
     return res
 
 
+def time_diff(dev):
+    """The differentiable configuration: 4096 patterns (a 64 x 64 scan, 120x120 float32, peak
+    50 counts), NLPAR radius 2 -> Gaussian background subtraction -> Radon (nTheta 180, nRho
+    180) -> LoG -> soft-argmax band sharpness; forward plus backward (dJ/dlambda, dJ/dsigma,
+    dJ/dx through every stage, the NLPAR weights' dependence on the patterns included)."""
+    import torch
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300 import diff, synthetic as syn
+    n_r = n_c = 64
+    hh = 120
+    bd = pg.BandDetect(nTheta=180, nRho=180, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=9)
+    bd.band_detect_setup(patDim=(hh, hh), patternmask=syn.circular_mask(hh, hh))
+    t0 = time.perf_counter()
+    obj = diff.BandSharpness(bd, n_r, n_c, searchradius=2, tau=2.0)
+    setup_s = time.perf_counter() - t0
+    scan = syn.voronoi_scan_rows(n_r, n_c, 0, n_r, ngrains=60, h=hh, w=hh, seed=9, peak_range=(50.0, 50.0))
+    x0 = torch.from_numpy(scan.reshape(n_r * n_c, hh * hh).astype(np.float32)).to(dev)
+
+    def step():
+        x = x0.clone().requires_grad_(True)
+        lam = torch.tensor(0.9, device=dev, requires_grad=True)
+        bgs = torch.tensor(6.0, device=dev, requires_grad=True)
+        J = obj(x, lam, bgs)
+        J.backward()
+        return J, lam.grad, bgs.grad
+    step()
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        J, gl, gs = step()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    return {"workload": "4096 x 120x120 float32 (64x64 scan, peak 50), NLPAR radius 2, background sigma, Radon "
+                        "nTheta 180 x nRho 180, LoG, soft-argmax; forward + backward",
+            "ms_forward_backward": ms, "patterns_per_s": n_r * n_c / ms * 1e3, "operator_setup_s": setup_s,
+            "J": float(J.detach()), "dJ_dlambda": float(gl), "dJ_dsigma": float(gs)}
+
+
 MIXED_SIZES = (60, 120, 240)
 
 
@@ -463,6 +504,87 @@ def time_mixed(pools, n_total, steps, dev):
     return res
 
 
+SCAN_ROWS, SCAN_COLS = 400, 500
+
+
+def _scan_part(args):
+    r0, r1 = args
+    from pyebsdindex_gb300 import synthetic as syn
+    return syn.voronoi_scan_rows(SCAN_ROWS, SCAN_COLS, r0, r1, ngrains=300, h=H, w=W, seed=5, peak_range=(30.0, 200.0))
+
+
+def nlpar_scan(ex):
+    """The NLPAR configuration's scan: 400 x 500 80x80 uint8 patterns from 300 seeded Voronoi
+    grains, per-pixel Poisson peak counts drawn from 30-200 (row blocks generated in parallel)."""
+    parts = [(r, min(r + 16, SCAN_ROWS)) for r in range(0, SCAN_ROWS, 16)]
+    return np.concatenate(list(ex.map(_scan_part, parts)))
+
+
+def time_nlpar_detect(scan, plan_bd, dev):
+    """NLPAR (radius 3, lambda 0.7, nlpar_cpu.py:821-936) on the 400 x 500 scan held on the
+    device, its average stored as uint8 straight from the averaging kernel (as the reference
+    writes its NLPAR output file, pat_flt2int 'clip'), then band detection (fused kernel) on it:
+    the pair's rate, each stage's time, and the same chain with a float32 intermediate."""
+    import torch
+    import pyebsdindex_gb300 as pg
+    from pyebsdindex_gb300 import _lib
+    from pyebsdindex_gb300.accuracy import compare_records
+    n = SCAN_ROWS * SCAN_COLS
+    x = torch.from_numpy(scan).to(dev).to(torch.float32).reshape(n, H, W)
+    nl = pg.NLPAR(lam=0.7, searchradius=3)
+    plan = plan_bd._device_plan(dev.index or 0)
+    st = torch.cuda.current_stream(dev)
+    outs = {f: torch.empty((n, NBANDS, 2) if f in ("maxloc", "aveloc") else (n, NBANDS),
+                           dtype=torch.int8 if f == "valid" else torch.float32, device=dev) for f in _lib.BAND_FIELDS}
+    outs32 = {f: torch.empty_like(v) for f, v in outs.items()}
+
+    def chain(out_dtype, o):
+        a = nl.calcnlpar_array(x, SCAN_ROWS, SCAN_COLS, reset_sigma=True, out_dtype=out_dtype)
+        b = torch.cuda.Event(enable_timing=True)
+        b.record(st)
+        dt = _lib.EBSD_U8 if out_dtype is np.uint8 else _lib.EBSD_F32
+        plan.find_bands_device(a.data_ptr(), dt, n, {f: v.data_ptr() for f, v in o.items()},
+                               "fused", stream=st.cuda_stream)
+        return a, b
+    chain(np.uint8, outs)  # warm-up
+    torch.cuda.synchronize()
+    e0, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    avg, e1 = chain(np.uint8, outs)
+    e2.record(st)
+    torch.cuda.synchronize()
+    total, t_nlpar = e0.elapsed_time(e2), e0.elapsed_time(e1)
+    f0, f2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    chain(np.float32, outs32)
+    torch.cuda.synchronize()
+    f0.record(st)
+    _, f1 = chain(np.float32, outs32)
+    f2.record(st)
+    torch.cuda.synchronize()
+    c = compare_records(outs, outs32)
+    return {"workload": "NLPAR radius 3, lambda 0.7 on a 400x500 scan of 80x80 uint8 patterns (300 Voronoi grains, "
+                        "peaks 30-200 counts), average stored uint8, then find_bands (nTheta 180, nRho 120, nBands 9)",
+            "patterns_per_s": n / total * 1e3, "ms": total, "nlpar_ms": t_nlpar, "detect_ms": total - t_nlpar,
+            "float32_intermediate": {"patterns_per_s": n / f0.elapsed_time(f2) * 1e3, "nlpar_ms": f0.elapsed_time(f1),
+                                     "detect_ms": f0.elapsed_time(f2) - f0.elapsed_time(f1)},
+            "uint8_vs_float32_intermediate": c}, avg
+
+
+def _nlpar_oracle_chain(sub):
+    """The oracle's NLPAR (restating nlpar_nb) of a sub-scan, stored uint8 as the reference's
+    writer does (clip, truncate), then the oracle's FFT restatement of find_bands."""
+    from oracle import band_oracle as bo, nlpar_oracle as no
+    from pyebsdindex_gb300 import synthetic as syn
+    r, c = sub.shape[0], sub.shape[1]
+    data = sub.reshape(r * c, H * W).astype(np.float32)
+    ind = np.nonzero(no.automask(H, W).ravel())[0]
+    sig = no.sigma(data, r, c, ind)
+    avg = no.nlpar(data, 0.7, 3, 0.0, sig, r, c, ind)
+    pats = np.clip(avg, 0, 255).astype(np.uint8).reshape(r * c, H, W)
+    plan = bo.Plan((H, W), NTHETA, NRHO, 1.0, 1.0, 0.1, NBANDS, mask=syn.circular_mask(H, W))
+    return bo.find_bands(plan, pats, conv="fft"), pats
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -502,6 +624,7 @@ def main():
     ex = host_executor()
     pool = make_pool(args.pool, ex)
     mpools = None if args.no_mixed else mixed_pools(ex, 1024)
+    scan = None if args.no_nlpar else nlpar_scan(ex)
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -727,6 +850,14 @@ def main():
     if mpools is not None and rank == 0:
         mixed = time_mixed(mpools, args.mixed_patterns, max(2, min(args.steps, 5)), dev)
 
+    nlpar_detect = None
+    if scan is not None and rank == 0:
+        nlpar_detect, _ = time_nlpar_detect(scan, bd, dev)
+
+    diffp = None
+    if not args.no_diff and rank == 0:
+        diffp = time_diff(dev)
+
     indexing = None
     if not args.no_index:
         indexing = time_indexing(outs, bd, N, stream, rank == 0 and world == 1 and not args.no_cpu,
@@ -748,6 +879,24 @@ def main():
                                                             pats_d[:no].cpu().numpy(), outs), patterns=no)
             except Exception as e:
                 acc["vs_oracle_fft"] = {"error": str(e)}
+        if nlpar_detect is not None:
+            # the oracle chain on the scan's top-left 32 x 32 block, against the device chain on
+            # the same block (NLPAR windows shift inward at a scan's edges)
+            try:
+                import pyebsdindex_gb300 as pg
+                from pyebsdindex_gb300.accuracy import compare_records
+                sub = scan.reshape(SCAN_ROWS, SCAN_COLS, H, W)[:32, :32]
+                ref, ref_pats = ex.submit(_nlpar_oracle_chain, sub).result()
+                nl = pg.NLPAR(lam=0.7, searchradius=3)
+                got_pats = nl.calcnlpar_array(sub.reshape(32 * 32, H, W), 32, 32, out_dtype=np.uint8)
+                got = bd.find_bands(got_pats, method="fused")
+                nlpar_detect["vs_oracle_chain"] = dict(
+                    compare_records(got, ref), patterns=32 * 32,
+                    pattern_pixels_differing=float(np.mean(got_pats != ref_pats)),
+                    oracle="nlpar_nb restatement -> clip/truncate uint8 -> find_bands restatement with FFT, 32x32 "
+                           "sub-scan")
+            except Exception as e:
+                nlpar_detect["vs_oracle_chain"] = {"error": str(e)}
     ex.shutdown()
 
     if rank == 0:
@@ -765,6 +914,7 @@ def main():
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "accuracy": acc,
             "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
             "nlpar_lambda": nlpar_lambda, "nlpar_file": nlpar_file, "mixed_sizes": mixed,
+            "nlpar_detect": nlpar_detect, "differentiable": diffp,
             "gpu_launches": launches_per_step * args.steps,
         }
         print(json.dumps(line))

@@ -107,6 +107,10 @@ int ebsd_plan_destroy(ebsd_plan_t plan);
  * in shared memory).  Returns 1 / 0, or a negative code. */
 int ebsd_method_supported(ebsd_plan_t plan, int method);
 
+/* The same for input of `dtype`: the theta-slab form of the fused FP32 method (plans too
+ * large for one on-chip tile) takes float32 input only where a float32 pattern tile fits. */
+int ebsd_method_supported_for(ebsd_plan_t plan, int method, int dtype);
+
 /* Reserves the per-plan workspace for chunks of up to max_chunk patterns so that later
  * calls allocate nothing.  Optional: find_bands reserves on first use. */
 int ebsd_plan_reserve(ebsd_plan_t plan, int method, int64_t max_chunk);
@@ -219,6 +223,15 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
                const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
                float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
                float* d_out, void* stream);
+
+/* ebsd_nlpar with the averaged patterns stored as `out_dtype`: EBSD_F32, or EBSD_U8 /
+ * EBSD_U16 as the reference writes NLPAR's output file (calcnlpar_cpu -> write_data with
+ * pat_flt2int 'clip', ebsd_pattern.py:118-182: clipped to the type's range, truncated), so that
+ * band detection reads its usual integer input straight from the averaging kernel. */
+int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+                   const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
+                   float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
+                   int out_dtype, void* d_out, void* stream);
 
 /* ---- band normals (Radon.radon2pole, radon_fast.py:314-397) ---------------------------- */
 #define EBSD_VENDOR_EDAX 0

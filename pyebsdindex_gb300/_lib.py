@@ -73,6 +73,8 @@ def load():
         lib.ebsd_plan_destroy.restype = C.c_int
         lib.ebsd_method_supported.argtypes = [P, C.c_int]
         lib.ebsd_method_supported.restype = C.c_int
+        lib.ebsd_method_supported_for.argtypes = [P, C.c_int, C.c_int]
+        lib.ebsd_method_supported_for.restype = C.c_int
         lib.ebsd_plan_reserve.argtypes = [P, C.c_int, C.c_int64]
         lib.ebsd_plan_reserve.restype = C.c_int
         lib.ebsd_find_bands.argtypes = [P, C.c_int, C.c_int, P, C.c_int64, C.POINTER(Bands), C.c_int64, P]
@@ -162,8 +164,11 @@ class DevicePlan:
         self.H, self.W, self.nBands = int(H), int(W), int(nBands)
         self.device = int(device)
 
-    def supported(self, method) -> bool:
-        return self._lib.ebsd_method_supported(self.handle, method_id(method)) == 1
+    def supported(self, method, dtype=None) -> bool:
+        """Whether ``method`` can run this plan (for input of ``dtype``, an EBSD_* code, if given)."""
+        if dtype is None:
+            return self._lib.ebsd_method_supported(self.handle, method_id(method)) == 1
+        return self._lib.ebsd_method_supported_for(self.handle, method_id(method), int(dtype)) == 1
 
     def reserve(self, method, max_chunk):
         check(self._lib.ebsd_plan_reserve(self.handle, method_id(method), int(max_chunk)), "ebsd_plan_reserve")

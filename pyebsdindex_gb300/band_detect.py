@@ -68,6 +68,12 @@ def _digest(*arrays):
     return h.hexdigest()
 
 
+def _input_code(pats):
+    """The EBSD_* input type find_bands hands the library for ``pats`` (numpy or torch)."""
+    name = str(getattr(pats, "dtype", "")).replace("torch.", "")
+    return {"uint8": _lib.EBSD_U8, "uint16": _lib.EBSD_U16}.get(name, _lib.EBSD_F32)
+
+
 def _large_inputs(*arrays):
     """The plan inputs above 1 MiB, as objects (compared by identity)."""
     return tuple(a for a in arrays if a is not None and np.asarray(a).nbytes > (1 << 20))
@@ -106,9 +112,11 @@ class GPUFindBands:
         self._gpu_plan_cache = (key, plan, large)
         return plan
 
-    def _pick_method(self, plan, method):
+    def _pick_method(self, plan, method, dtype=None):
+        """The method a call runs: the requested (or default) one, the per-stage FP32 method
+        where a fused kernel cannot take the plan (or the input type, ``dtype`` an EBSD_* code)."""
         m = self.default_method if method is None else method
-        if m in ("fused", "fused32", "fused16") and not plan.supported(m):
+        if m in ("fused", "fused32", "fused16") and not plan.supported(m, dtype):
             m = "plain"
         return m
 
@@ -132,7 +140,7 @@ class GPUFindBands:
         if self.patDim is None or tuple(np.asarray(self.patDim)[-2:]) != tuple(pats.shape[-2:]):
             self.band_detect_setup(patDim=pats.shape[-2:])
         plan = self._device_plan(gpu_id)
-        m = self._pick_method(plan, method)
+        m = self._pick_method(plan, method, _input_code(pats))
         chunk = int(chunksize) if (chunksize is not None and chunksize > 0) else 0
         if m.startswith("fused"):
             chunk = 0
@@ -206,7 +214,7 @@ class GPUFindBands:
         if self.patDim is None or tuple(np.asarray(self.patDim)[-2:]) != tuple(pats.shape[-2:]):
             self.band_detect_setup(patDim=pats.shape[-2:])
         plan = self._device_plan(gpu_id)
-        m = self._pick_method(plan, method)
+        m = self._pick_method(plan, method, _input_code(pats))
         pats = pats.to(torch.device("cuda", plan.device))
         dev_out = self._find_bands_dev(plan, pats, m, 0)
         normals = radon2pole_gpu(dev_out["theta"], dev_out["rho"], self.radonPlan.imDim, PC=PC, vendor=vendor)
@@ -382,70 +390,102 @@ class BandDetect(GPUFindBands):
             self.nBands = nBands
 
     def collect_background(self, fileobj=None, patsIn=None, nsample=None, method='randomStride', sigma=None):
-        """Mean pattern -> 2-D Gaussian-on-a-plane fit (band_detect.py:297-348).  File input
-        goes through the reference's pattern-file objects (``read_data``)."""
-        back = None
+        """The static background subtracted before the Radon (band_detect.py:297-348): the mean
+        of a sample of the patterns, smoothed by ``backsub_fit`` into a 2-D Gaussian on a tilted
+        plane.  The sample is every pattern when ``nsample`` covers them, else ``nsample`` drawn
+        at random without replacement ('randomStride') or every int(n / nsample)-th
+        ('evenStride').  Patterns come from ``patsIn`` ([n, H, W] or one [H, W]) or, failing
+        that, from a pattern file read in runs of consecutive patterns."""
+        mean = None
         if patsIn is not None:
-            p = np.expand_dims(patsIn, 0) if patsIn.ndim == 2 else patsIn
-            npats = p.shape[0]
-            nsample = npats if nsample is None else nsample
-            if npats <= nsample:
-                back = np.expand_dims(np.mean(p, axis=0), 0)
-            elif method.upper() == 'RANDOMSTRIDE':
-                back = np.mean(p[np.sort(np.random.choice(npats, size=nsample, replace=False)), :, :], axis=0)
-            elif method.upper() == 'EVENSTRIDE':
-                back = np.mean(p[np.arange(0, npats, int(npats / nsample)), :, :], axis=0)
-        if back is None and fileobj is not None:
-            if fileobj.version is None:
-                fileobj.read_header()
-            npats = fileobj.nPatterns
-            nsample = npats if (nsample is None or npats <= nsample) else nsample
-            if method.upper() == 'RANDOMSTRIDE':
-                stride = np.sort(np.random.choice(npats, size=nsample, replace=False))
-            else:
-                stride = np.arange(0, npats, int(npats / nsample), dtype=np.uint64)
-            acc = fileobj.read_data(convertToFloat=True, patStartCount=[stride[0], 1], returnArrayOnly=True)[0]
-            for i in stride[1:]:
-                acc += fileobj.read_data(convertToFloat=True, patStartCount=[i, 1], returnArrayOnly=True)[0]
-            back = acc / float(len(stride))
-        if back is not None:
-            back = self.backsub_fit(np.squeeze(back))
-        self.backgroundsub = back
+            stack = patsIn if patsIn.ndim == 3 else patsIn[np.newaxis]
+            n = stack.shape[0]
+            want = n if nsample is None else nsample
+            pick = None if n <= want else _sample_picks(n, want, method)
+            if n <= want:
+                mean = np.mean(stack, axis=0)
+            elif pick is not None:
+                mean = np.mean(stack[pick], axis=0)
+        if mean is None and fileobj is not None:
+            mean = _file_sample_mean(fileobj, nsample, method)
+        self.backgroundsub = None if mean is None else self.backsub_fit(np.squeeze(mean))
 
     def backsub_fit(self, back, mask=None):
-        """Least-squares fit of a 2-D Gaussian on a tilted plane to the mean pattern
-        (band_detect.py:350-408); falls back to the mean itself when the fit fails."""
-        def surface(x, y, a, x0, y0, sx, sy, c, d, e):
-            return a * np.exp(-((x - x0) ** 2) / (2.0 * sx ** 2) - ((y - y0) ** 2) / (2.0 * sy ** 2)) + c + d * x + e * y
-
-        nx, ny = back.shape[-1], back.shape[-2]
-        x = np.broadcast_to(np.arange(nx, dtype=float).reshape(1, nx), (ny, nx)).ravel()
-        y = np.broadcast_to(np.arange(ny, dtype=float), (nx, ny)).T.ravel()
+        """Smooth background model of a mean pattern (band_detect.py:350-408): a 2-D Gaussian on a
+        tilted plane fitted by least squares (scipy's curve_fit, started from a tenth of the
+        median-filtered range at the brightest pixel with widths of a sixth of the pattern) to
+        the 3x3 median-filtered pattern inside ``mask`` (default: the disc of radius 0.49 * H
+        about the centre), evaluated on the whole pattern, its mean removed.  If the fit does
+        not converge, the mean pattern itself, mean removed."""
+        ny, nx = back.shape[-2], back.shape[-1]
+        yy, xx = np.indices((ny, nx), dtype=float)
         if mask is None:
-            cx = (np.arange(nx) - nx * 0.5) ** 2
-            cy = (np.arange(ny) - ny * 0.5) ** 2
-            sel = np.sqrt(np.broadcast_to(cx.reshape(1, nx), (ny, nx)) + np.broadcast_to(cy, (nx, ny)).T) < (ny * 0.49)
-        else:
-            sel = mask
-        wh = np.nonzero(sel.ravel())[0]
-        xy = np.vstack((x[wh], y[wh]))
-        z = ndi.median_filter(np.squeeze(back), 3).ravel()[wh]
-        pk = np.unravel_index(back.argmax(), back.shape)
-        p0 = [(z.max() - z.min()) * 0.1, pk[1], pk[0], nx / 2.355, ny / 2.355, z.min(), 0, 0]
-        try:
-            popt, _ = opt.curve_fit(lambda M, *a: surface(M[0], M[1], *a), xy, z, p0)
-            fit = surface(x, y, *popt).reshape(ny, nx)
-        except RuntimeError:
+            mask = np.sqrt((xx - nx * 0.5) ** 2 + (yy - ny * 0.5) ** 2) < (ny * 0.49)
+        inside = np.asarray(mask).ravel() != 0
+        smooth = ndi.median_filter(np.squeeze(back), 3).ravel()[inside]
+        brightest = np.unravel_index(back.argmax(), back.shape)
+        start = [(smooth.max() - smooth.min()) * 0.1, brightest[1], brightest[0], nx / 2.355, ny / 2.355,
+                 smooth.min(), 0, 0]
+        fitted = _fit_gaussian_plane(xx.ravel(), yy.ravel(), inside, smooth, start)
+        model = back if fitted is None else fitted.reshape(ny, nx)
+        if fitted is None:
             print('Warning: no convergence on background gaussian fit ... using mean of the patterns.')
-            fit = back
-        fit -= np.mean(fit)
-        return fit
+        return model - np.mean(model)
 
     def _circmask(self, im):
         nx, ny = im.shape[-1], im.shape[-2]
         cx = (np.arange(nx) - nx * 0.5) ** 2
         cy = (np.arange(ny) - ny * 0.5) ** 2
         return np.sqrt(np.broadcast_to(cx.reshape(1, nx), (ny, nx)) + np.broadcast_to(cy, (nx, ny)).T)
+
+
+def _sample_picks(n, want, method):
+    """Indices of the background sample: ``want`` of ``n`` at random without replacement,
+    sorted ('randomStride'), or every int(n / want)-th ('evenStride'); None for another
+    method."""
+    kind = method.upper()
+    if kind == 'RANDOMSTRIDE':
+        return np.sort(np.random.choice(n, size=want, replace=False))
+    if kind == 'EVENSTRIDE':
+        return np.arange(0, n, int(n / want))
+    return None
+
+
+def _file_sample_mean(fileobj, nsample, method):
+    """Mean of the background sample of a pattern file: the sampled patterns read as float32
+    in runs of consecutive indices and summed one by one in index order."""
+    if fileobj.version is None:
+        fileobj.read_header()
+    n = int(fileobj.nPatterns)
+    want = n if (nsample is None or n <= nsample) else nsample
+    pick = _sample_picks(n, want, method)
+    if pick is None:
+        return None
+    pick = np.asarray(pick, dtype=np.int64)
+    breaks = np.nonzero(np.diff(pick) != 1)[0] + 1
+    total = None
+    for run in np.split(pick, breaks):
+        block = fileobj.read_data(convertToFloat=True, patStartCount=[int(run[0]), len(run)],
+                                  returnArrayOnly=True)[0]
+        for pat in block:
+            total = pat.copy() if total is None else total + pat
+    return total / float(len(pick))
+
+
+def _gaussian_plane(x, y, amp, x0, y0, sx, sy, c, d, e):
+    """amp * exp(-(x - x0)^2 / (2 sx^2) - (y - y0)^2 / (2 sy^2)) + c + d x + e y."""
+    return amp * np.exp(- ((x - x0) ** 2) / (2.0 * sx ** 2) - ((y - y0) ** 2) / (2.0 * sy ** 2)) + c + d * x + e * y
+
+
+def _fit_gaussian_plane(x, y, inside, z, start):
+    """Least-squares fit of ``_gaussian_plane`` to z at the pixels ``inside``; the fitted
+    surface on every pixel, or None when curve_fit does not converge."""
+    try:
+        params, _ = opt.curve_fit(lambda xy, *p: _gaussian_plane(xy[0], xy[1], *p),
+                                  np.vstack((x[inside], y[inside])), z, start)
+    except RuntimeError:
+        return None
+    return _gaussian_plane(x, y, *params)
 
 
 class MixedBandDetect:
@@ -482,10 +522,11 @@ class MixedBandDetect:
             self.plans[key] = bd
         return self.plans[key]
 
-    def method_for(self, h, w):
+    def method_for(self, h, w, dtype=None):
+        """The method a size runs (for input of ``dtype``, an EBSD_* code, if given)."""
         bd = self.plan(h, w)
         m = self.method
-        return m if not m.startswith("fused") or bd._device_plan().supported(m) else "plain"
+        return m if not m.startswith("fused") or bd._device_plan().supported(m, dtype) else "plain"
 
     def find_bands(self, patterns, method=None):
         """patterns: sequence of [H, W] arrays (numpy, or CUDA tensors), sizes mixed.  Returns an
@@ -532,13 +573,14 @@ class MixedBandDetect:
                                      dtype=torch.int8 if f == "valid" else torch.float32, device=dev)
                       for f in _lib.BAND_FIELDS} for key, (t, _) in ins.items()}
         plans = {key: self.plan(*key)._device_plan() for key in ins}
-        mixed = (m in ("fused", "fused32") and len(dts) == 1 and 1 <= len(ins) <= self.MAX_MIXED
-                 and all(p.supported("fused") for p in plans.values()))
+        dt0 = next(iter(dts)) if len(dts) == 1 else None
+        mixed = (m in ("fused", "fused32") and dt0 is not None and 1 <= len(ins) <= self.MAX_MIXED
+                 and all(p.supported("fused", dt0) for p in plans.values()))
         self.last_mixed = False
         if mixed:
             keys = list(ins)
             try:
-                _lib.DevicePlan.find_bands_mixed([plans[k] for k in keys], dts.pop(), [ins[k][0].data_ptr() for k in keys],
+                _lib.DevicePlan.find_bands_mixed([plans[k] for k in keys], dt0, [ins[k][0].data_ptr() for k in keys],
                                                  [ins[k][0].shape[0] for k in keys],
                                                  [{f: v.data_ptr() for f, v in outs[k].items()} for k in keys],
                                                  stream=st.cuda_stream)
@@ -548,7 +590,7 @@ class MixedBandDetect:
                 if "not supported" not in str(e):
                     raise
         for key, (t, dt) in ins.items():
-            mk = m if not m.startswith("fused") or plans[key].supported(m) else "plain"
+            mk = m if not m.startswith("fused") or plans[key].supported(m, dt) else "plain"
             plans[key].find_bands_device(t.data_ptr(), dt, t.shape[0], {f: v.data_ptr() for f, v in outs[key].items()},
                                          mk, stream=st.cuda_stream)
         return outs

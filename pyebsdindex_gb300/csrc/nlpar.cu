@@ -118,6 +118,19 @@ __global__ void k_nlpar_weights(const float* __restrict__ data, int nrows, int n
 __device__ __forceinline__ float wadd(float acc, float x, float w) { return __fadd_rn(acc, __fmul_rn(x, w)); }
 __device__ __forceinline__ double wadd(double acc, double x, double w) { return __dadd_rn(acc, __dmul_rn(x, w)); }
 
+// The averaged value as stored: float as is; an unsigned integer type as the reference's pattern
+// writer stores it (pat_flt2int with method 'clip', ebsd_pattern.py:118-182: clipped to the
+// type's range, then truncated toward zero by astype).
+template <typename O> __device__ __forceinline__ O store_as(float v);
+template <> __device__ __forceinline__ float store_as<float>(float v) { return v; }
+template <> __device__ __forceinline__ double store_as<double>(float v) { return (double)v; }
+template <> __device__ __forceinline__ uint8_t store_as<uint8_t>(float v) {
+    return (uint8_t)fminf(fmaxf(v, 0.0f), 255.0f);
+}
+template <> __device__ __forceinline__ uint16_t store_as<uint16_t>(float v) {
+    return (uint16_t)fminf(fmaxf(v, 0.0f), 65535.0f);
+}
+
 // out[pix][k] = sum over the window, in window order, of data[nb][k] * w[pix][c].
 template <typename T>
 __global__ void k_nlpar_average(const T* __restrict__ data, int nrows, int ncols, int npx,
@@ -137,6 +150,27 @@ __global__ void k_nlpar_average(const T* __restrict__ data, int nrows, int ncols
         for (int inn = xs; inn < xe; ++inn, ++c)
             acc = wadd(acc, __ldg(data + (int64_t)(inn + ncols * jn) * npx + k), __ldg(wp + c));
     out[(int64_t)pix * npx + k] = acc;
+}
+
+// The same, stored as O.
+template <typename O>
+__global__ void k_nlpar_average_to(const float* __restrict__ data, int nrows, int ncols, int npx,
+                                   const float* __restrict__ w, int sr, O* __restrict__ out) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int pix = blockIdx.y;
+    if (k >= npx) return;
+    int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+    int xs, xe, ys, ye;
+    window(i, sr, ncols, xs, xe);
+    window(j, sr, nrows, ys, ye);
+    int winsz = (2 * sr + 1) * (2 * sr + 1);
+    const float* wp = w + (int64_t)pix * winsz;
+    float acc = 0.0f;
+    int c = 0;
+    for (int jn = ys; jn < ye; ++jn)
+        for (int inn = xs; inn < xe; ++inn, ++c)
+            acc = wadd(acc, __ldg(data + (int64_t)(inn + ncols * jn) * npx + k), __ldg(wp + c));
+    out[(int64_t)pix * npx + k] = store_as<O>(acc);
 }
 
 // ---- tiled kernels: one block per 32 neighbouring scan pixels of one scan row ------------
@@ -242,11 +276,12 @@ __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_tiled(
     }
 }
 
-// Weighted window sum (k_nlpar_average's order) for 32 scan pixels x 32 pattern pixels per step.
-template <typename T>
+// Weighted window sum (k_nlpar_average's order) for 32 scan pixels x 32 pattern pixels per step,
+// stored as O (float, or clipped and truncated to uint8 / uint16 -- the detection input).
+template <typename T, typename O = T>
 __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_average_tiled(
         const T* __restrict__ data, int nrows, int ncols, int npx, const T* __restrict__ w, int sr,
-        T* __restrict__ out) {
+        O* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* sm = (T*)smraw;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileX + tx;
@@ -282,7 +317,7 @@ __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_average_tiled(
                     const T* srow = S + (r * ncx + (xs - cx0)) * kSP + tx;
                     for (int cc = 0; cc < wn; ++cc, ++c) acc = wadd(acc, srow[cc * kSP], wp[c]);
                 }
-                out[(int64_t)(y * ncols + x0 + px) * npx + k0 + tx] = acc;
+                out[(int64_t)(y * ncols + x0 + px) * npx + k0 + tx] = store_as<O>(acc);
             }
         }
     }
@@ -493,6 +528,14 @@ int ebsd_nlpar_lambda_metric(const float* d_d2, int32_t nrows, int32_t ncols, in
 int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
                int32_t nind, float datamax, float lam, int32_t sr, float dthresh, const float* d_sigma,
                int saturation_protect, float* d_work, float* d_out, void* stream) {
+    return ebsd_nlpar_out(d_data, nrows, ncols, npx, d_indices, nind, datamax, lam, sr, dthresh, d_sigma,
+                          saturation_protect, d_work, EBSD_F32, d_out, stream);
+}
+
+int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
+                   int32_t nind, float datamax, float lam, int32_t sr, float dthresh, const float* d_sigma,
+                   int saturation_protect, float* d_work, int out_dtype, void* d_out, void* stream) {
+    if (out_dtype != EBSD_F32 && out_dtype != EBSD_U8 && out_dtype != EBSD_U16) return EBSD_E_DTYPE;
     if (!d_data || !d_indices || !d_sigma || !d_work || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 ||
         nind < 0 || nind > npx || sr < 0 || sr > 10 || !(lam > 0.0f))
         return EBSD_E_ARG;
@@ -509,7 +552,15 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, c
                                                              d_sigma, lam2, dthresh, sr, d_work);
         int rc = launch_status();
         if (rc != EBSD_OK) return rc;
-        k_nlpar_average_tiled<float><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr, d_out);
+        if (out_dtype == EBSD_U8)
+            k_nlpar_average_tiled<float, uint8_t><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr,
+                                                                              (uint8_t*)d_out);
+        else if (out_dtype == EBSD_U16)
+            k_nlpar_average_tiled<float, uint16_t><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr,
+                                                                               (uint16_t*)d_out);
+        else
+            k_nlpar_average_tiled<float><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr,
+                                                                     (float*)d_out);
         return launch_status();
     }
     k_nlpar_weights<<<(unsigned)(nrows * ncols), bs, winsz * sizeof(float), st>>>(
@@ -517,7 +568,12 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, c
     int rc = launch_status();
     if (rc != EBSD_OK) return rc;
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
-    k_nlpar_average<float><<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, d_out);
+    if (out_dtype == EBSD_U8)
+        k_nlpar_average_to<uint8_t><<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, (uint8_t*)d_out);
+    else if (out_dtype == EBSD_U16)
+        k_nlpar_average_to<uint16_t><<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, (uint16_t*)d_out);
+    else
+        k_nlpar_average<float><<<grid, 256, 0, st>>>(d_data, nrows, ncols, npx, d_work, sr, (float*)d_out);
     return launch_status();
 }
 

@@ -642,6 +642,16 @@ int ebsd_method_supported(ebsd_plan_t p, int method) {
     return EBSD_E_ARG;
 }
 
+int ebsd_method_supported_for(ebsd_plan_t p, int method, int dtype) {
+    if (!p) return EBSD_E_ARG;
+    if (dtype != EBSD_U8 && dtype != EBSD_U16 && dtype != EBSD_F32) return EBSD_E_DTYPE;
+    if (is_plain(method)) return 1;
+    if (!is_fused(method)) return EBSD_E_ARG;
+    if (!fused_supported(p, method)) return 0;
+    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) return slab_serves(p, method, dtype) ? 1 : 0;
+    return 1;
+}
+
 int ebsd_plan_reserve(ebsd_plan_t p, int method, int64_t max_chunk) {
     if (!p || max_chunk <= 0) return EBSD_E_ARG;
     int rc = check_method(p, method);

@@ -117,46 +117,39 @@ class EBSDPatterns:
 
 
 def pat_flt2int(patterns, typeout=None, method='clip', scalevalue=0.98, maxScale=None):
-    """Patterns to an unsigned integer type (ebsd_pattern.py:118-182): 'clip' to the type's
-    range (capped at maxScale), 'fullscale' (min to 0, the max -- or maxScale -- to
-    scalevalue * the type's maximum, rounded) or 'scale' (negative minimum lifted to 0, then as
-    'fullscale').  A floating typeout returns the patterns cast."""
-    pats = patterns.patterns if isinstance(patterns, EBSDPatterns) else patterns
-    if pats.ndim == 2:
-        pats = pats.reshape(1, pats.shape[0], pats.shape[1])
-    shp = pats.shape
-    maxp, minp = pats.max(), pats.min()
+    """Patterns [n, H, W] (or one [H, W]) as an unsigned integer type (ebsd_pattern.py:118-182).
+    ``typeout`` None picks uint16 when the largest value is above 258, else uint8; a floating
+    type returns the patterns cast to it.  Methods: 'clip' -- clipped to [0, top] (top the
+    type's largest value, or maxScale if smaller), truncated by the cast; 'fullscale' -- the
+    minimum moved to 0, then scaled so that maxScale (default: the largest value) maps to
+    scalevalue * top, clipped and rounded; 'scale' -- a negative minimum lifted to 0, then
+    scaled the same way and rounded.  Another method gives zeros."""
+    arr = patterns.patterns if isinstance(patterns, EBSDPatterns) else patterns
+    if arr.ndim == 2:
+        arr = arr.reshape(1, arr.shape[0], arr.shape[1])
+    lo_val, hi_val = arr.min(), arr.max()
     if typeout is None:
-        typeout = np.uint8
-        if maxp > 258:
-            typeout = np.uint16
+        typeout = np.uint16 if hi_val > 258 else np.uint8
     if isinstance(typeout(0), np.floating):
-        return pats.astype(typeout)
-    minval, maxval = 0, 255
+        return arr.astype(typeout)
+    top = 65535 if isinstance(typeout(0), np.uint16) else 255
     if isinstance(typeout(0), np.uint16):
-        typeout, minval, maxval = np.uint16, 0, 65535
-    patsout = np.zeros(shp, dtype=typeout)
+        typeout = np.uint16
     if method == 'clip':
-        if maxScale is not None:
-            maxval = min(maxScale, maxval)
-        patsout[:, :, :] = pats.clip(minval, maxval).astype(dtype=typeout)
-    elif method == 'fullscale':
-        temp = pats.astype(np.float32) - minp
-        if maxScale is None:
-            maxScale = temp.max()
-        temp *= scalevalue * maxval / maxScale
-        temp = np.around(temp.clip(0, maxval))
-        patsout[:, :, :] = temp.astype(typeout)
-    elif method == 'scale':
-        temp = pats.astype(np.float32)
-        if minp < minval:
-            temp += minval - minp
-        if maxScale is None:
-            maxScale = temp.max()
-        temp *= scalevalue * maxval / maxScale
-        temp = np.around(temp)
-        patsout[:, :, :] = temp.astype(typeout)
-    return patsout
+        ceiling = top if maxScale is None else min(maxScale, top)
+        return np.ascontiguousarray(arr.clip(0, ceiling).astype(typeout))
+    if method not in ('fullscale', 'scale'):
+        return np.zeros(arr.shape, dtype=typeout)
+    work = arr.astype(np.float32)
+    if method == 'fullscale':
+        work = work - lo_val
+    elif lo_val < 0:
+        work += 0 - lo_val
+    peak = work.max() if maxScale is None else maxScale
+    work *= scalevalue * top / peak
+    if method == 'fullscale':
+        work = work.clip(0, top)
+    return np.ascontiguousarray(np.around(work).astype(typeout))
 
 
 class EBSDPatternFile:
@@ -203,59 +196,66 @@ class EBSDPatternFile:
         return copy.deepcopy(self)
 
     def read_data(self, path=None, convertToFloat=False, patStartCount=[0, -1], returnArrayOnly=False):
-        """ebsd_pattern.py:236-329: a run [start, count] (count -1: to the end) or a slab
-        [[col, row], [ncol, nrow]] (negative sizes: to the edge), clamped to the file."""
+        """Patterns from the file (ebsd_pattern.py:236-329), as float32 with ``convertToFloat``.
+        ``patStartCount``: a run [start, count] (count -1: to the end, 0: one pattern) or a slab
+        [[col, row], [ncol, nrow]] of the scan (a negative size: to the edge), clamped to the
+        file.  Returns (patterns, xy locations), or with ``returnArrayOnly`` False an
+        ``EBSDPatterns`` that also carries the file's scan attributes and the request."""
         if path is not None:
             self.set_filepath(path)
             self.read_header()
         if self.version is None:
             self.read_header()
         typeout = np.float32 if convertToFloat else self.filedatatype
-        pse = np.asarray(patStartCount, dtype=np.int64)
-        if pse.ndim == 1:
-            patStart = np.int64(pse[0])
-            nPatToRead = np.int64(pse[-1])
-            if nPatToRead == -1:
-                nPatToRead = np.int64(self.nPatterns - patStart)
-            if nPatToRead == 0:
-                nPatToRead = 1
-            if (patStart + nPatToRead) > self.nPatterns:
-                nPatToRead = np.int64(self.nPatterns - patStart)
-            readpats, xyloc = self.pat_reader(patStart, nPatToRead)
-            patterns = readpats.astype(typeout)
+        req = np.asarray(patStartCount, dtype=np.int64)
+        if req.ndim == 1:
+            start, count = self._clamp_run(req[0], req[-1])
+            raw, xyloc = self.pat_reader(start, count)
+            patterns, origin, extent = raw.astype(typeout), start, count
         else:
-            colstart, ncolread = np.int64(pse[0, 0]), np.int64(pse[1, 0])
-            rowstart, nrowread = np.int64(pse[0, 1]), np.int64(pse[1, 1])
-            patStart = [colstart, rowstart]
-            if ncolread < 0:
-                ncolread = np.int64(self.nCols - colstart)
-            if nrowread < 0:
-                nrowread = np.int64(self.nRows - rowstart)
-            if (colstart + ncolread) > self.nCols:
-                ncolread = np.int64(self.nCols - colstart)
-            if (rowstart + nrowread) > self.nRows:
-                nrowread = np.int64(self.nRows - rowstart)
-            nrowread, ncolread = np.uint64(nrowread), np.uint64(ncolread)
-            nPatToRead = [ncolread, nrowread]
-            patterns = np.zeros([np.int64(ncolread * nrowread), self.patternH, self.patternW], dtype=typeout)
-            xyloc = np.zeros([np.int64(ncolread * nrowread), 2], dtype=np.float32)
-            for i in range(int(nrowread)):
-                pstart = np.int64(np.int64(np.int64(rowstart + i) * self.nCols) + colstart)
-                pt, xy = self.read_data(convertToFloat=convertToFloat, patStartCount=[pstart, ncolread],
-                                        returnArrayOnly=True)
-                patterns[np.int64(i * ncolread):np.int64((i + 1) * ncolread)] = pt
-                xyloc[np.int64(i * ncolread):np.int64((i + 1) * ncolread)] = xy
+            origin, extent, patterns, xyloc = self._read_slab(req, typeout, convertToFloat)
         if returnArrayOnly:
             return patterns, xyloc
         out = EBSDPatterns()
         out.vendor, out.file, out.filetype = self.vendor, Path(self.filepath).expanduser(), self.filetype
         out.patternW, out.patternH = self.patternW, self.patternH
         out.nFileCols, out.nFileRows = np.uint64(self.nCols), np.uint64(self.nRows)
-        out.nPatterns = np.array(nPatToRead)
+        out.nPatterns = np.array(extent)
         out.hexflag, out.xStep, out.yStep = self.hexflag, self.xStep, self.yStep
-        out.patStart = np.array(patStart)
+        out.patStart = np.array(origin)
         out.patterns, out.xyLocations = patterns, xyloc
         return out
+
+    def _clamp_run(self, start, count):
+        """A run request clamped to the file: count -1 reads to the end, 0 reads one pattern."""
+        start, count = np.int64(start), np.int64(count)
+        if count == -1:
+            count = np.int64(self.nPatterns - start)
+        if count == 0:
+            count = np.int64(1)
+        if start + count > self.nPatterns:
+            count = np.int64(self.nPatterns - start)
+        return start, count
+
+    def _read_slab(self, req, typeout, convertToFloat):
+        """A [[col, row], [ncol, nrow]] block of the scan, one run read per scan row."""
+        col0, row0 = np.int64(req[0, 0]), np.int64(req[0, 1])
+        ncol, nrow = np.int64(req[1, 0]), np.int64(req[1, 1])
+        ncol = np.int64(self.nCols - col0) if ncol < 0 else ncol
+        nrow = np.int64(self.nRows - row0) if nrow < 0 else nrow
+        ncol = min(ncol, np.int64(self.nCols - col0))
+        nrow = min(nrow, np.int64(self.nRows - row0))
+        ncol, nrow = np.uint64(ncol), np.uint64(nrow)
+        total = np.int64(ncol * nrow)
+        patterns = np.zeros([total, self.patternH, self.patternW], dtype=typeout)
+        xyloc = np.zeros([total, 2], dtype=np.float32)
+        width = int(ncol)
+        for r in range(int(nrow)):
+            first = np.int64(np.int64(np.int64(row0 + r) * self.nCols) + col0)
+            pats, xy = self.read_data(convertToFloat=convertToFloat, patStartCount=[first, ncol], returnArrayOnly=True)
+            patterns[r * width:(r + 1) * width] = pats
+            xyloc[r * width:(r + 1) * width] = xy
+        return [col0, row0], [ncol, nrow], patterns, xyloc
 
     def write_data(self, newpatterns=None, patStartCount=[0, -1], writeHead=False, flt2int='clip', scalevalue=0.98,
                    maxScale=None):

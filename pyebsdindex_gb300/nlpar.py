@@ -84,6 +84,10 @@ def _bind():
                                    C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_void_p]
         lib.ebsd_nlpar.restype = C.c_int
+        lib.ebsd_nlpar_out.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
+                                       C.c_float, C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_int, C.c_void_p,
+                                       C.c_int, C.c_void_p, C.c_void_p]
+        lib.ebsd_nlpar_out.restype = C.c_int
         lib.ebsd_nlpar_sigma_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                               C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int, C.c_void_p,
                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -241,10 +245,13 @@ class NLPAR:
         return vals
 
     def calcnlpar_array(self, data, nrows=None, ncols=None, lam=None, searchradius=None, dthresh=None,
-                        saturation_protect=None, sigma=None, reset_sigma=False):
-        """NLPAR-averaged patterns, same shape as ``data``, float32.  ``sigma`` (or a previously
-        computed ``self.sigma``) is reused unless ``reset_sigma``; else it is estimated first,
-        as calcnlpar_cpu does (nlpar_cpu.py:486-493)."""
+                        saturation_protect=None, sigma=None, reset_sigma=False, out_dtype=None):
+        """NLPAR-averaged patterns, same shape as ``data``.  ``sigma`` (or a previously computed
+        ``self.sigma``) is reused unless ``reset_sigma``; else it is estimated first, as
+        calcnlpar_cpu does (nlpar_cpu.py:486-493).  ``out_dtype``: float32 (default), or
+        np.uint8 / np.uint16 -- the averaged values stored as the reference writes its NLPAR
+        output file (pat_flt2int 'clip': clipped to the type's range, truncated), straight from
+        the averaging kernel, e.g. as the input of band detection on the device."""
         import torch
         lib = _bind()
         if lam is not None:
@@ -269,12 +276,26 @@ class NLPAR:
         self.sigma = sig.cpu().numpy()
         sr = int(self.searchradius)
         work = torch.empty((nrows * ncols, (2 * sr + 1) ** 2), dtype=torch.float32, device=dev)
-        out = torch.empty_like(t)
-        _lib.check(lib.ebsd_nlpar(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
-                                  float(t.max().item()), float(np.float32(self.lam)), sr, float(np.float32(self.dthresh)),
-                                  sig.data_ptr(), int(bool(sp)), work.data_ptr(), out.data_ptr(), stream),
-                   "ebsd_nlpar")
+        odt = np.dtype(np.float32 if out_dtype is None else out_dtype)
+        if odt == np.float32:
+            out, code = torch.empty_like(t), _lib.EBSD_F32
+        elif odt == np.uint8:
+            out, code = torch.empty(t.shape, dtype=torch.uint8, device=dev), _lib.EBSD_U8
+        elif odt == np.uint16:
+            # torch's uint16 has few device operations: allocated as int16, viewed as uint16
+            out, code = torch.empty(t.shape, dtype=torch.int16, device=dev), _lib.EBSD_U16
+        else:
+            raise TypeError(f"out_dtype {odt} (float32, uint8 or uint16)")
+        _lib.check(lib.ebsd_nlpar_out(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
+                                      float(t.max().item()), float(np.float32(self.lam)), sr,
+                                      float(np.float32(self.dthresh)), sig.data_ptr(), int(bool(sp)),
+                                      work.data_ptr(), code, out.data_ptr(), stream), "ebsd_nlpar_out")
         out = out.reshape(shape)
+        if odt == np.uint16:
+            # torch's uint16 has few operations: returned as a uint16 view where torch has the type
+            if not is_torch:
+                return out.cpu().numpy().view(np.uint16)
+            return out.view(torch.uint16) if hasattr(torch, "uint16") else out
         return out if is_torch else out.cpu().numpy()
 
     # -- the reference's file interface (nlpar_cpu.py:81-92, :94-281, :283-540, :542-677) ------

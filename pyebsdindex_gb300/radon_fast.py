@@ -130,55 +130,61 @@ class Radon:
 
     def radon2pole(self, bandData, PC=None, vendor='EDAX'):
         """Band (theta, rho) -> unit plane normal in the detector frame (radon_fast.py:314-397,
-        Krieger Lassen 1994 eq. 3.1.6): the band is the detector line through
-        ``p = rho*(cos, sin) + centre`` with direction ``(-sin, cos)``; its plane normal is
-        ``r x (p - t)`` with ``t`` the source point scaled per vendor convention."""
+        Krieger Lassen 1994 eq. 3.1.6).  The band is the detector line through the foot point
+        p = (rho cos, rho sin) + image centre with direction r = (-sin, cos, 0) (origin at the
+        bottom-left pixel); its plane normal is r x (p - t) for the vendor's source point t
+        (``source_points``).  float32 throughout, each product rounded before its difference as
+        the reference's np.cross rounds it, so the normals equal the reference's bit for bit."""
         if PC is None:
-            PC = np.array([0.471659, 0.675044, 0.630139])
-        ven = str.upper(vendor)
-        nPats, nBands = bandData.shape[0], bandData.shape[1]
-        theta = bandData['theta'][:]
-        rho = bandData['rho'][:]
-        st, ct = np.sin(theta), np.cos(theta)
-        pc = np.asarray(PC, dtype=np.float32).copy()
-        if ven != 'EMSOFT':
-            if pc.ndim < 2:
-                pc = np.tile(pc, nPats).reshape(nPats, 3)
-            elif pc.shape[0] != nPats:
-                pc = np.tile(pc[0, :], nPats).reshape(nPats, 3)
-            t = pc
-        else:
-            if pc.ndim < 2:
-                pc = np.tile(pc, nPats).reshape(nPats, 4)
-            elif pc.shape[0] != nPats:
-                pc = np.tile(pc[0, :], nPats).reshape(nPats, 4)
-            t = pc[:, 0:3]
-            t[:, 2] /= pc[:, 3]
-        dimf = np.array(self.imDim, dtype=np.float32)
-        if ven == 'EDAX':
-            t *= np.array([dimf[1], dimf[0], -np.min(dimf[0:2])])
-        if ven == 'OXFORD':
-            t *= np.array([dimf[1], dimf[1], -dimf[1]])
-        if ven == 'EMSOFT':
-            t[:, 0] *= -1.0
-            t += np.array([dimf[1] / 2.0, dimf[0] / 2.0, 0.0])
-            t[:, 2] *= -1.0
-        if ven in ('KIKUCHIPY', 'BRUKER'):
-            t *= np.array([dimf[1], dimf[0], -dimf[0]])
-            t[:, 1] = dimf[0] - t[:, 1]
-        t = np.tile(t.reshape(nPats, 1, 3), (1, nBands, 1))
-        r = np.zeros((nPats, nBands, 3), dtype=np.float32)
-        r[:, :, 0] = -1 * st
-        r[:, :, 1] = ct
-        p = np.zeros((nPats, nBands, 3), dtype=np.float32)
-        p[:, :, 0] = rho * ct
-        p[:, :, 1] = rho * st
-        p[:, :, 0] += dimf[1] * 0.5
-        p[:, :, 1] += dimf[0] * 0.5
-        n = np.cross(r.reshape(nPats * nBands, 3), (p - t).reshape(nPats * nBands, 3))
-        nrm = np.linalg.norm(n, axis=1).clip(1e-12)
-        n /= nrm.reshape(nPats * nBands, 1)
-        return n.reshape(nPats, nBands, 3)
+            PC = DEFAULT_PC
+        theta = np.asarray(bandData['theta'])
+        rho = np.asarray(bandData['rho'])
+        n_pat = theta.shape[0]
+        t = source_points(PC, n_pat, self.imDim, vendor)[:, None, :]    # [n_pat, 1, 3]
+        s, c = np.sin(theta), np.cos(theta)
+        rows, cols = np.asarray(self.imDim, dtype=np.float32)[:2]
+        # p - t, component by component (p lies in the detector plane)
+        v0 = (rho * c + cols * 0.5) - t[..., 0]
+        v1 = (rho * s + rows * 0.5) - t[..., 1]
+        zero = np.zeros_like(s)
+        v2 = zero - t[..., 2]
+        ns = -1 * s
+        normal = np.stack([c * v2 - zero * v1, zero * v0 - ns * v2, ns * v1 - c * v0], axis=-1)
+        flat = normal.reshape(-1, 3)
+        flat /= np.linalg.norm(flat, axis=1).clip(1e-12).reshape(-1, 1)
+        return flat.reshape(normal.shape)
+
+
+DEFAULT_PC = np.array([0.471659, 0.675044, 0.630139])
+
+
+def source_points(PC, n_pat, imDim, vendor='EDAX'):
+    """Source point t [n_pat, 3] (float32) of each pattern in the detector frame of
+    ``Radon.radon2pole`` from its pattern centre, per vendor convention (radon_fast.py:348-378):
+    EDAX (x W, y H, z -min(H, W)); Oxford (x, y, z scaled by W, z negated); EMsoft ((xpc, ypc,
+    L, pixel size): x negated, shifted by the image centre, z = -L / pixel size); kikuchipy and
+    Bruker (x W, y H, z -H, y measured from the top).  One pattern centre serves every pattern
+    unless one is given per pattern."""
+    ven = str.upper(vendor)
+    width = 4 if ven == 'EMSOFT' else 3
+    pc = np.asarray(PC, dtype=np.float32)
+    if pc.ndim < 2 or pc.shape[0] != n_pat:
+        pc = np.broadcast_to((pc if pc.ndim < 2 else pc[0])[:width], (n_pat, width))
+    pc = np.array(pc, dtype=np.float32)
+    rows, cols = np.asarray(imDim, dtype=np.float32)[:2]
+    if ven == 'EMSOFT':
+        t = pc[:, 0:3]
+        t[:, 2] /= pc[:, 3]
+        t[:, 0] *= -1.0
+        t += np.array([cols / 2.0, rows / 2.0, 0.0])
+        t[:, 2] *= -1.0
+        return t
+    scale = {'EDAX': (cols, rows, -np.min([rows, cols])), 'OXFORD': (cols, cols, -cols),
+             'KIKUCHIPY': (cols, rows, -rows), 'BRUKER': (cols, rows, -rows)}.get(ven)
+    t = pc if scale is None else pc * np.array(scale)
+    if ven in ('KIKUCHIPY', 'BRUKER'):
+        t[:, 1] = rows - t[:, 1]
+    return t
 
 
 VENDORS = {"EDAX": 0, "OXFORD": 1, "EMSOFT": 2, "KIKUCHIPY": 3, "BRUKER": 4}

@@ -15,7 +15,7 @@ from __future__ import annotations
 import numpy as np
 
 __all__ = ["fcc_plane_normals", "random_quaternions", "quat_to_matrix", "circular_mask",
-           "make_patterns", "voronoi_scan"]
+           "make_patterns", "voronoi_scan", "voronoi_scan_rows"]
 
 
 def fcc_plane_normals():
@@ -142,3 +142,32 @@ def voronoi_scan(nrows, ncols, ngrains=300, h=80, w=80, seed=0, peak_range=(30.0
         lam = peaks[i] * base[gid[i]]
         out[i] = (np.clip(g.poisson(lam), 0, 255) * mk).astype(np.uint8)
     return out, gid.reshape(nrows, ncols)
+
+
+def voronoi_scan_rows(nrows, ncols, r0, r1, ngrains=300, h=80, w=80, seed=0, peak_range=(30.0, 200.0),
+                      pc=(0.46, 0.70, 0.64)):
+    """Rows [r0, r1) of a seeded Voronoi-grain scan (grains, orientations and per-pixel peak
+    counts as ``voronoi_scan`` draws them from ``seed``), with the Poisson noise of each row
+    block drawn from its own stream ``(seed, r0)`` so that blocks can be generated in parallel.
+    Returns uint8 patterns [(r1 - r0) * ncols, h, w]."""
+    g = np.random.default_rng(seed)
+    seeds = g.random((ngrains, 2)) * np.array([nrows, ncols])
+    gq = random_quaternions(g, ngrains)
+    peaks = g.uniform(peak_range[0], peak_range[1], size=nrows * ncols)
+    rr, cc = np.mgrid[r0:r1, 0:ncols]
+    pts = np.stack([rr.ravel(), cc.ravel()], -1).astype(np.float64)
+    gid = np.empty(pts.shape[0], dtype=np.int64)
+    for s in range(0, pts.shape[0], 4096):
+        d = ((pts[s:s + 4096, None, :] - seeds[None]) ** 2).sum(-1)
+        gid[s:s + 4096] = d.argmin(1)
+    used = np.unique(gid)
+    base = np.zeros((ngrains, h, w))
+    base[used] = _render(gq[used], h, w, pc, 1.5, 0.5, np.zeros(len(used), dtype=bool))
+    base[used] /= base[used].reshape(len(used), -1).max(axis=1).reshape(len(used), 1, 1)
+    mk = circular_mask(h, w)
+    noise = np.random.default_rng([seed, r0])
+    out = np.empty((pts.shape[0], h, w), dtype=np.uint8)
+    for i in range(pts.shape[0]):
+        lam = peaks[r0 * ncols + i] * base[gid[i]]
+        out[i] = (np.clip(noise.poisson(lam), 0, 255) * mk).astype(np.uint8)
+    return out

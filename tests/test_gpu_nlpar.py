@@ -68,3 +68,25 @@ def test_nlpar_rejects_oversized_window(cuda):
     nl = pg.NLPAR(lam=0.7, searchradius=3)
     with pytest.raises(RuntimeError, match="invalid argument"):
         nl.calcnlpar_array(pats, 4, 4)
+
+
+@pytest.mark.parametrize("out_dtype", [np.uint8, np.uint16])
+def test_nlpar_integer_output_is_the_reference_writers_conversion(cuda, out_dtype):
+    """The averaging kernel's integer output equals the float32 average clipped to the type's
+    range and truncated, as the reference's pattern writer stores NLPAR output (pat_flt2int
+    'clip', ebsd_pattern.py:118-182) -- bit for bit, and band detection reads it directly."""
+    import pyebsdindex_gb300 as pg
+    pats, _ = syn.voronoi_scan(12, 14, ngrains=6, h=40, w=40, seed=8, peak_range=(60.0, 250.0))
+    nl = pg.NLPAR(lam=0.7, searchradius=3)
+    f = nl.calcnlpar_array(pats, 12, 14)
+    g = nl.calcnlpar_array(pats, 12, 14, out_dtype=out_dtype)
+    hi = np.iinfo(out_dtype).max
+    assert g.dtype == out_dtype
+    assert np.array_equal(g, np.clip(f, 0, hi).astype(out_dtype))
+    if out_dtype is np.uint8:
+        bd = pg.BandDetect(nTheta=180, nRho=60, tSigma=1.0, rSigma=1.0, rhoMaskFrac=0.1, nBands=8)
+        bd.band_detect_setup(patDim=(40, 40), patternmask=syn.circular_mask(40, 40))
+        a = bd.find_bands(g, method="fused")
+        b = bd.find_bands(np.clip(f, 0, 255).astype(np.uint8), method="fused")
+        for k in ("max", "maxloc", "aveloc", "valid"):
+            assert a[k].tobytes() == b[k].tobytes(), k
