@@ -227,11 +227,14 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
 /* ebsd_nlpar with the averaged patterns stored as `out_dtype`: EBSD_F32, or EBSD_U8 /
  * EBSD_U16 as the reference writes NLPAR's output file (calcnlpar_cpu -> write_data with
  * pat_flt2int 'clip', ebsd_pattern.py:118-182: clipped to the type's range, truncated), so that
- * band detection reads its usual integer input straight from the averaging kernel. */
+ * band detection reads its usual integer input straight from the averaging kernel.
+ * d_centre_offset (NULL: none) [nrows*ncols] is added to each pixel's own window weight before
+ * the normalisation -- nlpar_nb's diff_offset addition (nlpar_cpu.py:880-925), which the
+ * caller computes per pixel. */
 int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
                    const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
                    float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
-                   int out_dtype, void* d_out, void* stream);
+                   int out_dtype, void* d_out, const float* d_centre_offset, void* stream);
 
 /* ---- band normals (Radon.radon2pole, radon_fast.py:314-397) ---------------------------- */
 #define EBSD_VENDOR_EDAX 0

@@ -104,8 +104,32 @@ def window_bounds(i, sr, n):
     return start, end
 
 
-def nlpar(data, lam, sr, dthresh, sig, nrows, ncols, indices, saturation_protect=True):
-    """Weighted neighbour average of every scan pixel, nlpar_cpu.py:821-936."""
+def diff_offsets(nrows, ncols, sr, diff_offset, calclim=None):
+    """The per-pixel addition to the centre weight that nlpar_nb makes with a non-zero
+    diff_offset (nlpar_cpu.py:880-925), as its loops run one after another: one array of
+    per-slot additions (diff_step, float32) for the whole call; pixels of the calculated block
+    ``calclim`` = (col0, row0, ncol, nrow) visited column by column, rows inner; at each pixel
+    every window slot is visited in window order -- the pixel's own slot gains diff_offset, every
+    other slot is set to 0 -- and the pixel's own slot value is added to its centre weight."""
+    c0, r0, nc, nr = calclim if calclim is not None else (0, 0, ncols, nrows)
+    winsz = (2 * sr + 1) ** 2
+    step = np.zeros(winsz, dtype=np.float32)
+    off = np.zeros((nrows, ncols), dtype=np.float32)
+    for i in range(c0, c0 + nc):
+        xs, xe = window_bounds(i, sr, ncols)
+        for j in range(r0, r0 + nr):
+            ys, ye = window_bounds(j, sr, nrows)
+            own = (j - ys) * (xe - xs) + (i - xs)
+            keep = step[own]
+            step[:] = 0
+            step[own] = f32(keep + f32(diff_offset))
+            off[j, i] = step[own]
+    return off
+
+
+def nlpar(data, lam, sr, dthresh, sig, nrows, ncols, indices, saturation_protect=True, centre_offset=None):
+    """Weighted neighbour average of every scan pixel, nlpar_cpu.py:821-936; ``centre_offset``
+    [nrows, ncols] is added to each pixel's own weight (``diff_offsets``)."""
     data = np.asarray(data, dtype=np.float32)
     lam = f32(lam)
     lam2 = f32(1.0) / (lam * lam)
@@ -136,6 +160,9 @@ def nlpar(data, lam, sr, dthresh, sig, nrows, ncols, indices, saturation_protect
     w = np.where(centre, f32(-1.0e6), d2).astype(np.float32)
     w = np.maximum((w - dthresh).astype(np.float32), f32(0.0))
     w = np.exp((f32(-1.0) * w * lam2).astype(np.float32)).astype(np.float32)
+    if centre_offset is not None:
+        co = np.asarray(centre_offset, dtype=np.float32).ravel()
+        w = np.where(centre, (w + co[:, None]).astype(np.float32), w).astype(np.float32)
     tot = np.zeros(npx, dtype=np.float32)
     for c in range(winsz):
         tot = (tot + w[:, c]).astype(np.float32)

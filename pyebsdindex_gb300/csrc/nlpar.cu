@@ -74,7 +74,7 @@ __global__ void k_nlpar_sigma(const float* __restrict__ data, int nrows, int nco
 __global__ void k_nlpar_weights(const float* __restrict__ data, int nrows, int ncols, int npx,
                                 const int32_t* __restrict__ ind, int nind, float mxval,
                                 const float* __restrict__ sigma, float lam2, float dthresh, int sr,
-                                float* __restrict__ wout) {
+                                float* __restrict__ wout, const float* __restrict__ coff = nullptr) {
     extern __shared__ float w_s[];
     __shared__ float tot_s;
     int pix = blockIdx.x;
@@ -103,6 +103,7 @@ __global__ void k_nlpar_weights(const float* __restrict__ data, int nrows, int n
         }
         w = fmaxf(__fsub_rn(w, dthresh), 0.0f);
         w = expf(__fmul_rn(__fmul_rn(-1.0f, w), lam2));
+        if (coff && nb == pix) w = __fadd_rn(w, coff[pix]);  // diff_offset's centre addition
         w_s[c] = w;
     }
     __syncthreads();
@@ -188,7 +189,7 @@ template <int MP>
 __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_tiled(
         const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind,
         int nind, float mxval, const float* __restrict__ sigma, float lam2, float dthresh, int sr,
-        float* __restrict__ wout) {
+        float* __restrict__ wout, const float* __restrict__ coff) {
     extern __shared__ float sm[];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileX + tx;
     const int y = blockIdx.y, x0 = blockIdx.x * kTileX;
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_tiled(
             }
             w = fmaxf(__fsub_rn(w, dthresh), 0.0f);
             w = expf(__fmul_rn(__fmul_rn(-1.0f, w), lam2));
+            if (coff && nb == pix) w = __fadd_rn(w, coff[pix]);  // diff_offset's centre addition
             W[tx * winsz + c] = w;
         }
     }
@@ -529,12 +531,13 @@ int ebsd_nlpar(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, c
                int32_t nind, float datamax, float lam, int32_t sr, float dthresh, const float* d_sigma,
                int saturation_protect, float* d_work, float* d_out, void* stream) {
     return ebsd_nlpar_out(d_data, nrows, ncols, npx, d_indices, nind, datamax, lam, sr, dthresh, d_sigma,
-                          saturation_protect, d_work, EBSD_F32, d_out, stream);
+                          saturation_protect, d_work, EBSD_F32, d_out, nullptr, stream);
 }
 
 int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
                    int32_t nind, float datamax, float lam, int32_t sr, float dthresh, const float* d_sigma,
-                   int saturation_protect, float* d_work, int out_dtype, void* d_out, void* stream) {
+                   int saturation_protect, float* d_work, int out_dtype, void* d_out,
+                   const float* d_centre_offset, void* stream) {
     if (out_dtype != EBSD_F32 && out_dtype != EBSD_U8 && out_dtype != EBSD_U16) return EBSD_E_DTYPE;
     if (!d_data || !d_indices || !d_sigma || !d_work || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 ||
         nind < 0 || nind > npx || sr < 0 || sr > 10 || !(lam > 0.0f))
@@ -549,7 +552,7 @@ int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t np
     const size_t wsm = tiled_smem(sr, ncols, sizeof(float), true), asm_ = tiled_smem(sr, ncols, sizeof(float), false);
     if (sr <= 3 && wsm <= 48 * 1024 && asm_ <= 48 * 1024) {
         k_nlpar_weights_tiled<4><<<tgrid, tblock, wsm, st>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval,
-                                                             d_sigma, lam2, dthresh, sr, d_work);
+                                                             d_sigma, lam2, dthresh, sr, d_work, d_centre_offset);
         int rc = launch_status();
         if (rc != EBSD_OK) return rc;
         if (out_dtype == EBSD_U8)
@@ -564,7 +567,7 @@ int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t np
         return launch_status();
     }
     k_nlpar_weights<<<(unsigned)(nrows * ncols), bs, winsz * sizeof(float), st>>>(
-        d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma, lam2, dthresh, sr, d_work);
+        d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sigma, lam2, dthresh, sr, d_work, d_centre_offset);
     int rc = launch_status();
     if (rc != EBSD_OK) return rc;
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));

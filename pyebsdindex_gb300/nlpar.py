@@ -86,7 +86,7 @@ def _bind():
         lib.ebsd_nlpar.restype = C.c_int
         lib.ebsd_nlpar_out.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
                                        C.c_float, C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_int, C.c_void_p,
-                                       C.c_int, C.c_void_p, C.c_void_p]
+                                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.ebsd_nlpar_out.restype = C.c_int
         lib.ebsd_nlpar_sigma_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                               C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int, C.c_void_p,
@@ -97,6 +97,60 @@ def _bind():
         lib.ebsd_nlpar_lambda_metric.restype = C.c_int
         lib._nlpar_bound = True
     return lib
+
+
+class _Tile:
+    """One scan tile of an NLPAR file run: rows [r0, r0 + nr) x columns [c0, c0 + nc) are read;
+    the interior rows [ir0, ir0 + inr) x columns [ic0, ic0 + inc) of it are written."""
+    __slots__ = ("r0", "nr", "c0", "nc", "ir0", "inr", "ic0", "inc")
+
+    def __init__(self, r0, nr, c0, nc, ir0, inr, ic0, inc):
+        self.r0, self.nr, self.c0, self.nc = r0, nr, c0, nc
+        self.ir0, self.inr, self.ic0, self.inc = ir0, inr, ic0, inc
+
+
+def _halo_tiles(rows, cols, sr):
+    """The tiles of ``scan_tiles``' row and column ranges, row by row; each drops ``sr`` halo
+    rows / columns on every side it shares with a neighbouring tile (nlpar_cpu.py:400-426)."""
+    nrt, nct = len(rows), len(cols)
+    for a in range(nrt):
+        r0, r1 = int(rows[a, 0]), int(rows[a, 1])
+        top = sr if a > 0 else 0
+        bottom = (r1 - r0) - sr if a < nrt - 1 else r1 - r0
+        for b in range(nct):
+            c0, c1 = int(cols[b, 0]), int(cols[b, 1])
+            left = sr if b > 0 else 0
+            right = (c1 - c0) - sr if b < nct - 1 else c1 - c0
+            yield _Tile(r0, r1 - r0, c0, c1 - c0, top, bottom - top, left, right - left)
+
+
+def _diff_offsets(nrows, ncols, sr, diff_offset, block):
+    """nlpar_nb's centre-weight additions for a non-zero diff_offset (nlpar_cpu.py:880-925), as
+    its loops run one after another over the computed block (col0, row0, ncol, nrow) of a tile:
+    one float32 array of per-slot additions lives for the whole call; the pixels are visited
+    column by column (rows inner), and each visit adds diff_offset to the pixel's own window slot
+    and zeroes all others.  So a pixel's addition is diff_offset summed (in float32) over the run
+    of consecutive visits, ending with it, whose own slot is the same.  Returns [nrows, ncols]
+    float32 (0 outside the block)."""
+    c0, r0, nc, nr = block
+    wn = 2 * sr + 1
+    cols = np.arange(c0, c0 + nc)
+    rows = np.arange(r0, r0 + nr)
+    xs = np.array([window_start(i, sr, ncols) for i in cols])
+    ys = np.array([window_start(j, sr, nrows) for j in rows])
+    own = ((rows - ys)[None, :] * wn + (cols - xs)[:, None]).ravel()  # visit order: column-major
+    cuts = np.nonzero(np.diff(own) != 0)[0] + 1
+    adds = np.concatenate([np.add.accumulate(np.full(len(run), diff_offset, dtype=np.float32))
+                           for run in np.split(own, cuts)])
+    out = np.zeros((nrows, ncols), dtype=np.float32)
+    out[r0:r0 + nr, c0:c0 + nc] = adds.reshape(nc, nr).T
+    return out
+
+
+def window_start(i, sr, n):
+    """First index of the (2 sr + 1)-wide search window of position i along a scan axis of n,
+    shifted inward at the edges (nlpar_cpu.py:872-878)."""
+    return max(i - sr, 0) - max(i + sr - (n - 1), 0)
 
 
 class NLPAR:
@@ -245,13 +299,16 @@ class NLPAR:
         return vals
 
     def calcnlpar_array(self, data, nrows=None, ncols=None, lam=None, searchradius=None, dthresh=None,
-                        saturation_protect=None, sigma=None, reset_sigma=False, out_dtype=None):
+                        saturation_protect=None, sigma=None, reset_sigma=False, out_dtype=None,
+                        centre_offset=None):
         """NLPAR-averaged patterns, same shape as ``data``.  ``sigma`` (or a previously computed
         ``self.sigma``) is reused unless ``reset_sigma``; else it is estimated first, as
         calcnlpar_cpu does (nlpar_cpu.py:486-493).  ``out_dtype``: float32 (default), or
         np.uint8 / np.uint16 -- the averaged values stored as the reference writes its NLPAR
         output file (pat_flt2int 'clip': clipped to the type's range, truncated), straight from
-        the averaging kernel, e.g. as the input of band detection on the device."""
+        the averaging kernel, e.g. as the input of band detection on the device.
+        ``centre_offset`` [nrows, ncols]: added to each pixel's own window weight (the
+        diff_offset additions of nlpar_nb)."""
         import torch
         lib = _bind()
         if lam is not None:
@@ -286,10 +343,17 @@ class NLPAR:
             out, code = torch.empty(t.shape, dtype=torch.int16, device=dev), _lib.EBSD_U16
         else:
             raise TypeError(f"out_dtype {odt} (float32, uint8 or uint16)")
+        coff = None
+        if centre_offset is not None:
+            coff = torch.as_tensor(np.asarray(centre_offset, dtype=np.float32) if not torch.is_tensor(centre_offset)
+                                   else centre_offset, device=dev).to(torch.float32).reshape(-1).contiguous()
+            if coff.numel() != nrows * ncols:
+                raise ValueError("centre_offset holds one value per scan pixel")
         _lib.check(lib.ebsd_nlpar_out(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
                                       float(t.max().item()), float(np.float32(self.lam)), sr,
                                       float(np.float32(self.dthresh)), sig.data_ptr(), int(bool(sp)),
-                                      work.data_ptr(), code, out.data_ptr(), stream), "ebsd_nlpar_out")
+                                      work.data_ptr(), code, out.data_ptr(),
+                                      None if coff is None else coff.data_ptr(), stream), "ebsd_nlpar_out")
         out = out.reshape(shape)
         if odt == np.uint16:
             # torch's uint16 has few operations: returned as a uint16 view where torch has the type
@@ -428,173 +492,174 @@ class NLPAR:
         """sigma_numba with nn = 1 over one tile (nlpar_cpu.py:486-490)."""
         return np.asarray(self.calcsigma_array(data, nrows, ncols, saturation_protect=saturation_protect))
 
-    def _tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma):
-        """nlpar_nb over one tile with the tile's merged sigma (nlpar_cpu.py:496-509); the
-        object's own parameters and sigma are left as they were."""
+    def _tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma, centre_offset=None):
+        """nlpar_nb over one tile with the tile's merged sigma (nlpar_cpu.py:496-509) and, with a
+        diff_offset, the per-pixel centre-weight additions; the object's own parameters and
+        sigma are left as they were."""
         keep = (self.lam, self.searchradius, self.dthresh, self.sigma)
         try:
             return np.asarray(self.calcnlpar_array(data, nrows, ncols, lam=lam, searchradius=sr, dthresh=dthresh,
-                                                   saturation_protect=saturation_protect, sigma=sigma))
+                                                   saturation_protect=saturation_protect, sigma=sigma,
+                                                   centre_offset=centre_offset))
         finally:
             self.lam, self.searchradius, self.dthresh, self.sigma = keep
 
     def backsub(self, data):
-        """NLPAR.backsub (nlpar_cpu.py:679-734): a 2-D Gaussian on a plane fitted by least squares
-        (scipy's curve_fit) to the mean of the patterns [n, H, W] over the mask, its mean removed,
-        subtracted from every pattern in place; the plain mean pattern when the fit does not
-        converge.  Host preprocessing of a tile, as in the reference."""
-        import scipy.optimize as opt
-
-        def surface(x, y, a, x0, y0, sx, sy, c, d, e):
-            return a * np.exp(- ((x - x0) ** 2) / (2.0 * sx ** 2) - ((y - y0) ** 2) / (2.0 * sy ** 2)) + c + d * x + e * y
-
-        def model(M, *p):
-            return surface(M[0], M[1], *p)
-
-        back = np.mean(data, axis=0)
+        """Subtract a smooth background from every pattern of ``data`` [n, H, W] in place
+        (nlpar_cpu.py:679-734): a 2-D Gaussian on a tilted plane fitted by least squares to the
+        patterns' mean over the mask (started from the full range of the masked mean at its
+        brightest pixel, widths of a sixth of the pattern), its own mean removed; the plain
+        mean pattern, mean removed, when the fit does not converge.  Host preprocessing of a
+        tile, as in the reference."""
+        from .band_detect import _fit_gaussian_plane
+        mean = np.mean(data, axis=0)
         ny, nx = data.shape[-2], data.shape[-1]
-        x = np.broadcast_to(np.arange(nx, dtype=float).reshape(1, nx), (ny, nx)).ravel()
-        y = np.broadcast_to(np.arange(ny, dtype=float), (nx, ny)).T.ravel()
         if self.mask is None:
             self.mask = self.makeautomask(ny, nx) if self.automask is True else np.ones((ny, nx), np.uint8)
-        wh = np.nonzero(np.asarray(self.mask).ravel())[0]
-        z = back.ravel()[wh]
-        peak = np.unravel_index(back.argmax(), back.shape)
-        p0 = [(z.max() - z.min()), peak[1], peak[0], nx / 2.355, ny / 2.355, z.min(), 0, 0]
-        try:
-            popt, _ = opt.curve_fit(model, np.vstack((x[wh], y[wh])), z, p0)
-            fit = surface(x, y, *popt).reshape(ny, nx)
-        except RuntimeError:
+        inside = np.asarray(self.mask).ravel() != 0
+        z = mean.ravel()[inside]
+        yy, xx = np.indices((ny, nx), dtype=float)
+        brightest = np.unravel_index(mean.argmax(), mean.shape)
+        start = [z.max() - z.min(), brightest[1], brightest[0], nx / 2.355, ny / 2.355, z.min(), 0, 0]
+        fitted = _fit_gaussian_plane(xx.ravel(), yy.ravel(), inside, z, start)
+        if fitted is None:
             print('Warning: no convergence on back subtract ... using mean of the patterns.')
-            fit = back
-        fit -= np.mean(fit)
-        data -= fit
+            model = mean
+        else:
+            model = fitted.reshape(ny, nx)
+        data -= model - np.mean(model)
         return data
 
     def calcnlpar(self, chunksize=0, searchradius=None, lam=None, dthresh=None, saturation_protect=None,
                   automask=None, stem_scale=None, filename=None, fileout=None, reset_sigma=False, backsub=False,
                   rescale=False, verbose=2, diff_offset=None, **kwargs):
-        """NLPAR.calcnlpar_cpu (nlpar_cpu.py:283-540) on the input file, written to the output
-        file (``setoutfile``); returns the output path.  The scan goes in tiles of about
-        ``chunksize`` bytes (0: the reference's default) with ``searchradius`` rows and columns
-        of halo, in the reference's order: per tile, its sigma merged into ``self.sigma`` by
-        minimum (unless a sigma is already set, e.g. by ``opt_lambda``), the average over the
-        tile, the tile's interior clipped to the output file's pixel type and written."""
-        if searchradius is not None:
-            self.searchradius = searchradius
-        sr = int(self._first(self.searchradius))
-        if lam is not None:
-            self.lam = lam
-        lam = np.float32(self._first(self.lam))
-        if dthresh is not None:
-            self.dthresh = dthresh
-        dthresh = np.float32(self._first(self.dthresh))
-        if diff_offset is not None:
-            self.diff_offset = diff_offset
-        if float(self._first(self.diff_offset)) != 0.0:
-            raise NotImplementedError("diff_offset other than 0 is not built")
-        if saturation_protect is not None:
-            self.saturation_protect = saturation_protect
-        sp = bool(self._first(self.saturation_protect))
-        if automask is not None:
-            self.automask = automask
-        if stem_scale is not None:
-            self.stem_scale = stem_scale
-        stem = bool(self._first(self.stem_scale))
+        """NLPAR.calcnlpar_cpu (nlpar_cpu.py:283-540) on the input file, into the output file
+        (``setoutfile``); returns the output path.
+
+        The scan is processed in tiles of about ``chunksize`` bytes (0: the reference's default
+        of a quarter of host memory, at most 32 GB), each read with ``searchradius`` rows and
+        columns of halo from its neighbours, in the reference's order.  Per tile: optionally
+        square-rooted above the file's minimum (``stem_scale``) and background-subtracted
+        (``backsub``); its noise sigma merged into ``self.sigma`` by minimum unless a sigma is
+        already set (e.g. by ``opt_lambda``); the weighted average on the device (with
+        ``diff_offset``, its centre-weight additions); the interior kept, squared back
+        (``stem_scale``) or stretched to the output type's range (``rescale``), and written
+        clipped to the output file's pixel type.  The output file's data minimum and maximum
+        are set from what was written.  With ``reset_sigma`` the sigma is estimated anew (the
+        reference's calcnlpar_cpu fails with reset_sigma set)."""
+        params = self._run_parameters(searchradius, lam, dthresh, saturation_protect, automask, stem_scale,
+                                      diff_offset)
+        sr, stem = params["sr"], params["stem"]
         if filename is not None:
             self.setfile(filepath=filename)
-        patternfile = self.getinfileobj()
-        if patternfile is None:
+        src = self.getinfileobj()
+        if src is None:
             raise ValueError("no input file: NLPAR(filename), setfile(path) or filename=")
-        self.setoutfile(patternfile, filepath=fileout)
-        patternfileout = self.getoutfileobj()
+        self.setoutfile(src, filepath=fileout)
+        dst = self.getoutfileobj()
         nrows, ncols = np.int64(self.nrows), np.int64(self.ncols)
-        if patternfileout.nCols is None:
-            patternfileout.nCols = ncols
-        if patternfileout.nRows is None:
-            patternfileout.nRows = nrows
-        pwidth, pheight = int(patternfile.patternW), int(patternfile.patternH)
-        cols, rows = scan_tiles([pwidth, pheight], int(ncols), int(nrows), self._target_bytes(chunksize),
+        dst.nCols = ncols if dst.nCols is None else dst.nCols
+        dst.nRows = nrows if dst.nRows is None else dst.nRows
+        width, height = int(src.patternW), int(src.patternH)
+        cols, rows = scan_tiles([width, height], int(ncols), int(nrows), self._target_bytes(chunksize),
                                 col_overlap=sr, row_overlap=sr)
         if self.automask is True and self.mask is None:
-            self.mask = self.makeautomask(pheight, pwidth)
+            self.mask = self.makeautomask(height, width)
         if self.mask is None:
-            self.mask = np.ones((pheight, pwidth), dtype=np.uint8)
-        calcsigma = False
-        if self.sigma is None or reset_sigma:
-            calcsigma = True
-            self.sigma = np.zeros((nrows, ncols), dtype=np.float32) + 1e24
-        if np.asarray(self.sigma).size == 1:
-            self.sigma = np.zeros((nrows, ncols), dtype=np.float32) + np.asarray(self.sigma).ravel()[0]
-            calcsigma = False
-        shp = np.asarray(self.sigma).shape
-        if shp[0] != nrows and shp[1] != ncols:
-            self.sigma = np.zeros((nrows, ncols), dtype=np.float32) + 1e24
-            calcsigma = True
-        self.sigma = np.asarray(self.sigma, dtype=np.float32)
-        sigma = self.sigma
-        mxval = None
-        if rescale:
-            if np.issubdtype(patternfileout.filedatatype, np.integer):
-                mxval = np.iinfo(patternfileout.filedatatype).max
-            else:
-                rescale = False
-        datamin = None
-        if stem:
-            full, _ = patternfile.read_data(patStartCount=[[0, 0], [int(ncols), int(nrows)]], convertToFloat=True,
-                                            returnArrayOnly=True)
-            datamin = np.float32(full.min())
-            del full
+            self.mask = np.ones((height, width), dtype=np.uint8)
+        estimate = self._scan_sigma(int(nrows), int(ncols), reset_sigma)
+        top = None
+        if rescale and np.issubdtype(dst.filedatatype, np.integer):
+            top = np.iinfo(dst.filedatatype).max
+        floor = self._file_minimum(src, rows, cols) if stem else None
         if verbose >= 1:
             print("lambda:", self.lam, "search radius:", self.searchradius, "dthresh:", self.dthresh)
-        nrc, ncc = len(rows), len(cols)
-        ndone = 0
-        for rowchunk in range(nrc):
-            rstart, rend = int(rows[rowchunk, 0]), int(rows[rowchunk, 1])
-            nrowchunk = rend - rstart
-            rstartcalc = sr if rowchunk > 0 else 0
-            rendcalc = nrowchunk - sr if rowchunk < nrc - 1 else nrowchunk
-            nrowcalc = rendcalc - rstartcalc
-            for colchunk in range(ncc):
-                cstart, cend = int(cols[colchunk, 0]), int(cols[colchunk, 1])
-                ncolchunk = cend - cstart
-                cstartcalc = sr if colchunk > 0 else 0
-                cendcalc = ncolchunk - sr if colchunk < ncc - 1 else ncolchunk
-                ncolcalc = cendcalc - cstartcalc
-                data, _ = patternfile.read_data(patStartCount=[[cstart, rstart], [ncolchunk, nrowchunk]],
-                                                convertToFloat=True, returnArrayOnly=True)
-                if stem:
-                    data = np.sqrt(data.astype(np.float32) - datamin).astype(np.float32)
-                if backsub:
-                    data = self.backsub(data)
-                if calcsigma:
-                    sigchunk = self._tile_sigma(data, nrowchunk, ncolchunk, sp)
-                    sigchunk = np.minimum(sigma[rstart:rend, cstart:cend], sigchunk)
-                    sigma[rstart:rend, cstart:cend] = sigchunk
-                else:
-                    sigchunk = sigma[rstart:rend, cstart:cend]
-                out = self._tile_nlpar(data, nrowchunk, ncolchunk, lam, sr, dthresh, sp,
-                                       np.ascontiguousarray(sigchunk))
-                out = out.reshape(nrowchunk, ncolchunk, -1)[rstartcalc:rstartcalc + nrowcalc,
-                                                            cstartcalc:cstartcalc + ncolcalc, :]
-                if stem:
-                    out = out ** 2 + datamin
-                out = out.reshape(nrowcalc * ncolcalc, pheight, pwidth)
-                if rescale:
-                    for i in range(out.shape[0]):
-                        temp = out[i]
-                        temp -= temp.min()
-                        temp *= np.float32(mxval) / temp.max()
-                        out[i] = temp
-                patternfileout.write_data(newpatterns=out,
-                                          patStartCount=[[np.int64(cstart + cstartcalc), np.int64(rstart + rstartcalc)],
-                                                         [ncolcalc, nrowcalc]], flt2int='clip', scalevalue=1.0)
-                ndone += 1
-                if verbose >= 2:
-                    print("tiles complete: ", ndone, "/", nrc * ncc, sep='', end='\r')
+        lo_written, hi_written = np.inf, -np.inf
+        tiles = list(_halo_tiles(rows, cols, sr))
+        for done, t in enumerate(tiles, 1):
+            data, _ = src.read_data(patStartCount=[[t.c0, t.r0], [t.nc, t.nr]], convertToFloat=True,
+                                    returnArrayOnly=True)
+            if stem:
+                data = np.sqrt(data.astype(np.float32) - floor).astype(np.float32)
+            if backsub:
+                data = self.backsub(data)
+            window_sigma = self._merge_tile_sigma(data, t, estimate, params["sp"])
+            centre = None
+            if params["diff_offset"] != 0.0:
+                centre = _diff_offsets(t.nr, t.nc, sr, params["diff_offset"], (t.ic0, t.ir0, t.inc, t.inr))
+            avg = self._tile_nlpar(data, t.nr, t.nc, params["lam"], sr, params["dthresh"], params["sp"],
+                                   window_sigma, centre)
+            out = avg.reshape(t.nr, t.nc, -1)[t.ir0:t.ir0 + t.inr, t.ic0:t.ic0 + t.inc, :]
+            if stem:
+                out = out ** 2 + floor
+            out = out.reshape(t.inr * t.inc, height, width)
+            if top is not None:
+                for pat in out:
+                    pat -= pat.min()
+                    pat *= np.float32(top) / pat.max()
+            lo_written, hi_written = min(lo_written, np.min(out)), max(hi_written, np.max(out))
+            dst.write_data(newpatterns=out, patStartCount=[[np.int64(t.c0 + t.ic0), np.int64(t.r0 + t.ir0)],
+                                                           [np.int64(t.inc), np.int64(t.inr)]],
+                           flt2int='clip', scalevalue=1.0)
+            if verbose >= 2:
+                print("tiles complete: ", done, "/", len(tiles), sep='', end='\r')
         if verbose >= 2:
             print('', end='')
-        return str(patternfileout.filepath)
+        dst.datamin, dst.datamax = lo_written, hi_written
+        dst.write_datamaxmin()
+        return str(dst.filepath)
+
+    def _run_parameters(self, searchradius, lam, dthresh, saturation_protect, automask, stem_scale, diff_offset):
+        """Update the object's parameters from the given ones; the scalars a run uses."""
+        for name, value in (("searchradius", searchradius), ("lam", lam), ("dthresh", dthresh),
+                            ("saturation_protect", saturation_protect), ("automask", automask),
+                            ("stem_scale", stem_scale), ("diff_offset", diff_offset)):
+            if value is not None:
+                setattr(self, name, value)
+        return {"sr": int(self._first(self.searchradius)), "lam": np.float32(self._first(self.lam)),
+                "dthresh": np.float32(self._first(self.dthresh)),
+                "sp": bool(self._first(self.saturation_protect)), "stem": bool(self._first(self.stem_scale)),
+                "diff_offset": np.float32(self._first(self.diff_offset))}
+
+    def _scan_sigma(self, nrows, ncols, reset):
+        """Prepare ``self.sigma`` for a run over an nrows x ncols scan (nlpar_cpu.py:365-389);
+        True when it is to be estimated tile by tile.  An unset (or reset) sigma starts at 1e24
+        everywhere and is estimated; one value is spread over the scan and kept; an array whose
+        rows and columns both differ from the scan's is replaced and estimated."""
+        sig = None if reset else self.sigma
+        estimate = sig is None
+        if estimate:
+            sig = np.full((nrows, ncols), 1e24, dtype=np.float32)
+        elif np.asarray(sig).size == 1:
+            sig = np.full((nrows, ncols), np.asarray(sig).ravel()[0], dtype=np.float32)
+        shape = np.asarray(sig).shape
+        if shape[0] != nrows and shape[1] != ncols:
+            sig, estimate = np.full((nrows, ncols), 1e24, dtype=np.float32), True
+        self.sigma = np.asarray(sig, dtype=np.float32)
+        return estimate
+
+    def _merge_tile_sigma(self, data, t, estimate, sp):
+        """The sigma a tile's windows use: when estimating, the tile's own sigma merged into
+        ``self.sigma`` by minimum (nlpar_cpu.py:486-493); else ``self.sigma`` over the tile."""
+        block = self.sigma[t.r0:t.r0 + t.nr, t.c0:t.c0 + t.nc]
+        if estimate:
+            block[...] = np.minimum(block, self._tile_sigma(data, t.nr, t.nc, sp))
+        return np.ascontiguousarray(block)
+
+    def _file_minimum(self, src, rows, cols):
+        """The input file's smallest value (nlpar_cpu.py:948-969): the file's stored limits, or a
+        pass over the scan tile by tile; stored on the file object."""
+        src.read_datamaxmin()
+        if src.datamin is None or src.datamax is None:
+            lo, hi = np.inf, -np.inf
+            for r0, r1 in rows:
+                for c0, c1 in cols:
+                    data, _ = src.read_data(patStartCount=[[int(c0), int(r0)], [int(c1 - c0), int(r1 - r0)]],
+                                            convertToFloat=True, returnArrayOnly=True)
+                    lo, hi = min(lo, data.min()), max(hi, data.max())
+            src.datamin, src.datamax = lo, hi
+            src.write_datamaxmin()
+        return src.datamin
 
     def auto_nlpar(self, filename=None, fileout=None, lindex=1, **kwargs):
         """opt_lambda, then calcnlpar with the lambda of target weight ``lindex`` unless ``lam``

@@ -36,25 +36,28 @@ def test_one_tile_equals_the_array_form(cuda, tmp_path):
     assert read_all(out).tobytes() == pat_flt2int(want, typeout=np.uint8).tobytes()
 
 
-def test_tiles_follow_the_oracle(cuda, tmp_path, monkeypatch):
+@pytest.mark.parametrize("diff_offset", [0.0, 0.3])
+def test_tiles_follow_the_oracle(cuda, tmp_path, monkeypatch, diff_offset):
+    """Several tiles, with and without a diff_offset (the centre-weight additions)."""
     src = voronoi_file(tmp_path, 11, 13, 24, 62)
     nl = NLPAR(src, lam=0.8, searchradius=2)
-    got = nl.calcnlpar(chunksize=80_000, fileout=os.path.join(tmp_path, "g.up1"), verbose=0)
+    got = nl.calcnlpar(chunksize=80_000, fileout=os.path.join(tmp_path, "g.up1"), verbose=0, diff_offset=diff_offset)
     sig_dev = nl.sigma.copy()
 
     def tile_sigma(self, data, nrows, ncols, saturation_protect):
         ind = np.asarray(np.asarray(self.mask).ravel().nonzero()[0], np.int64)
         return no.sigma(data.reshape(nrows * ncols, -1), nrows, ncols, ind, saturation_protect)
 
-    def tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma):
+    def tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma, centre_offset=None):
         ind = np.asarray(np.asarray(self.mask).ravel().nonzero()[0], np.int64)
         return no.nlpar(data.reshape(nrows * ncols, -1), lam, sr, dthresh, sigma, nrows, ncols, ind,
-                        saturation_protect).reshape(data.shape)
+                        saturation_protect, centre_offset=centre_offset).reshape(data.shape)
 
     monkeypatch.setattr(NLPAR, "_tile_sigma", tile_sigma)
     monkeypatch.setattr(NLPAR, "_tile_nlpar", tile_nlpar)
     ref = NLPAR(src, lam=0.8, searchradius=2)
-    want = ref.calcnlpar(chunksize=80_000, fileout=os.path.join(tmp_path, "w.up1"), verbose=0)
+    want = ref.calcnlpar(chunksize=80_000, fileout=os.path.join(tmp_path, "w.up1"), verbose=0,
+                         diff_offset=diff_offset)
     assert sig_dev.tobytes() == ref.sigma.tobytes()
     a, b = read_all(got).astype(np.int16), read_all(want).astype(np.int16)
     assert np.abs(a - b).max() <= 1

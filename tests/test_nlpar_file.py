@@ -38,10 +38,10 @@ def oracle_tiles(monkeypatch):
         ind = np.asarray(np.asarray(self.mask).ravel().nonzero()[0], np.int64)
         return no.sigma(data.reshape(nrows * ncols, -1), nrows, ncols, ind, saturation_protect)
 
-    def tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma):
+    def tile_nlpar(self, data, nrows, ncols, lam, sr, dthresh, saturation_protect, sigma, centre_offset=None):
         ind = np.asarray(np.asarray(self.mask).ravel().nonzero()[0], np.int64)
         out = no.nlpar(data.reshape(nrows * ncols, -1), lam, sr, dthresh, sigma, nrows, ncols, ind,
-                       saturation_protect)
+                       saturation_protect, centre_offset=centre_offset)
         return out.reshape(data.shape)
 
     monkeypatch.setattr(NLPAR, "_tile_sigma", tile_sigma)
@@ -225,6 +225,32 @@ def test_calcnlpar_options_match_reference(tmp_path, ref, oracle_tiles, built_li
         warnings.simplefilter("ignore")
         rn.calcnlpar_cpu(fileout=theirs, chunksize=40_000, verbose=0, **opts)
     assert open(mine, "rb").read() == open(theirs, "rb").read()
+
+
+def test_diff_offset_matches_reference(tmp_path, ref, oracle_tiles, built_lib):
+    """A non-zero diff_offset: the centre-weight additions nlpar_nb accumulates over its serial
+    visit order (per tile, over the computed block), in one tile and in several."""
+    from pyebsdindex_gb300.nlpar import NLPAR
+    pats = scan(9, 11, 16, 29)
+    src = write("up1", str(tmp_path), pats, 9, 11)
+    for chunk in (0, 60_000):
+        mine, theirs = os.path.join(tmp_path, "m.up1"), os.path.join(tmp_path, "t.up1")
+        NLPAR(src, lam=0.8, searchradius=2).calcnlpar(fileout=mine, chunksize=chunk, diff_offset=0.3, verbose=0)
+        rn = ref.nlpar_cpu.NLPAR(src, lam=0.8, searchradius=2)
+        with warnings.catch_warnings(), np.errstate(all="ignore"):
+            warnings.simplefilter("ignore")
+            rn.calcnlpar_cpu(fileout=theirs, chunksize=chunk, diff_offset=np.float32(0.3), verbose=0)
+        assert open(mine, "rb").read() == open(theirs, "rb").read(), chunk
+
+
+def test_diff_offsets_equal_the_oracles():
+    """The product's vectorised centre-weight additions equal the oracle's step-by-step
+    restatement of nlpar_nb's loops (itself checked against the reference above)."""
+    from pyebsdindex_gb300.nlpar import _diff_offsets
+    for nrows, ncols, sr, block in ((7, 9, 2, (0, 0, 9, 7)), (12, 10, 3, (3, 2, 5, 8)), (6, 6, 1, (1, 1, 4, 4))):
+        a = _diff_offsets(nrows, ncols, sr, np.float32(0.37), block)
+        b = no.diff_offsets(nrows, ncols, sr, np.float32(0.37), block)
+        assert a.tobytes() == b.tobytes()
 
 
 def test_backsub_matches_reference(tmp_path, ref, oracle_tiles, built_lib):
