@@ -108,6 +108,11 @@ def load():
         return lib
 
 
+def version() -> str:
+    """The library's version string (ebsd_version)."""
+    return load().ebsd_version().decode()
+
+
 def check(code: int, what: str = "ebsdgpu"):
     if code != 0:
         msg = load().ebsd_strerror(code).decode()

@@ -221,14 +221,18 @@ class GPUFindBands:
         soa = {k: v.cpu().numpy() for k, v in dev_out.items()}
         return self._records(soa, int(pats.shape[0])), normals.cpu().numpy()
 
-    def autotune(self, sample, method=None, gpu_id=None):
+    def autotune(self, sample, method=None, gpu_id=None, cache=None):
         """Time the record-identical variants of the fused kernel (one, two, four or eight patterns per
         block pass) on ``sample`` ([n, H, W] numpy or torch, uint8/uint16/float32) and keep
         the faster in the device plan for later ``find_bands`` calls.  No counterpart in the
-        reference.  Returns the chosen patterns per pass."""
+        reference.  Returns the chosen patterns per pass.
+
+        ``cache``: None (default) times every call; a JSON file name, or True for
+        ``tuning.default_path()``, keeps the decision per GPU, library version, plan geometry,
+        input type and method (``tuning.TuningCache``): a call whose key is stored applies the
+        stored choice without timing, a new key is timed and stored."""
         import torch
         plan = self._device_plan(gpu_id)
-        m = self._pick_method(plan, method)
         dev = torch.device("cuda", plan.device)
         t = sample if type(sample).__module__.startswith("torch") else torch.from_numpy(np.ascontiguousarray(sample))
         if t.ndim == 2:
@@ -241,9 +245,38 @@ class GPUFindBands:
         else:
             t = t.to(torch.float32)
             dt = _lib.EBSD_F32
+        m = self._pick_method(plan, method, dt)
+        store = key = None
+        if cache is not None and cache is not False:
+            from . import tuning
+            store = tuning.TuningCache(cache)
+            key = self._tuning_key(plan, m, dt)
+            hit = store.get(key)
+            if hit is not None and int(hit.get("patterns_per_pass", 0)) in (1, 2, 4, 8):
+                ppp = int(hit["patterns_per_pass"])
+                plan.set_patterns_per_pass(ppp)
+                return ppp
         t = t.to(dev).contiguous()
         stream = torch.cuda.current_stream(dev).cuda_stream
-        return plan.autotune(t.data_ptr(), dt, int(t.shape[0]), m, stream=stream)
+        ppp = plan.autotune(t.data_ptr(), dt, int(t.shape[0]), m, stream=stream)
+        if store is not None:
+            store.put(key, {"patterns_per_pass": int(ppp), "timed_patterns": int(t.shape[0])})
+        return ppp
+
+    def _tuning_key(self, plan, method, dtype):
+        """The tuning-cache key of this plan on its GPU (tuning.plan_key)."""
+        import torch
+        from . import tuning
+        props = torch.cuda.get_device_properties(plan.device)
+        lut = self.radonPlan.indexPlan
+        if getattr(self, "_tuning_lut", (None, None))[0] is not lut:
+            self._tuning_lut = (lut, tuning.lut_digest(lut))
+        return tuning.plan_key(gpu=props.name, sms=props.multi_processor_count, library=_lib.version(),
+                               shape=np.asarray(self.patDim)[-2:], dtype=dtype, method=method,
+                               nTheta=self.nTheta, nRho=self.nRho, nBands=self.nBands,
+                               kernel_shape=np.shape(self.kernel)[-2:], padding=np.asarray(self.padding),
+                               peakPad=np.asarray(self.peakPad), lut=self._tuning_lut[1],
+                               background=self.backgroundsub is not None)
 
     def _records(self, soa, nP):
         out = np.zeros((nP, int(self.nBands)), dtype=self.dataType)

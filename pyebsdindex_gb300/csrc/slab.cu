@@ -11,7 +11,9 @@
 //              column (or row) order -- exact integers for uint8/uint16 patterns -- and the
 //              mean as a correctly rounded quotient (rdn_loops, radon_fast.py:281-310).
 //              Columns beyond theta 0 / 180 deg are the theta-wrapped rays written rho-flipped,
-//              as band_detect.py:573-575 pads the Radon image.
+//              as band_detect.py:573-575 pads the Radon image.  Neighbouring slabs share
+//              2 * (D1 + H1) Radon columns: they move to the front of the tile after the conv's
+//              theta pass, and every slab but the first computes only the columns after them.
 //   2. pad     rho padding rows: the first / last interior row, zero from row R on
 //              (band_detect.py:578-580 and the FFT convolution's zero extension).
 //   3. conv    two-pass separable LoG (theta taps along rows, rho taps down columns in place)
@@ -61,7 +63,7 @@ struct SlabArgs {
     int nslab, maxg;
     int nRho, nTheta, nB;
     int p0, p1;
-    int TR, TBP, CCP, MP;      // Radon tile rows, Radon / conv / theta-max pitches
+    int TR, TBP, CCP, MP;      // Radon tile rows, Radon / conv / theta-max pitches (MP = TBP)
     int rho0;                  // tile row of interior row 0 (p0 - row0)
     int rpad_end;              // tile rows from here on are zero (padded row R)
     int CR;                    // conv rows
@@ -106,6 +108,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
     constexpr int H1 = K1 / 2;               // LoG half width along theta
     constexpr int WIN = 2 * D1 + 1;
     constexpr int NV = kRowBlock + 2 * D0;
+    constexpr int kCarry = 2 * (D1 + H1);    // Radon columns shared by neighbouring slabs
     constexpr bool kInt = sizeof(InT) < 4;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -328,6 +331,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                 }
             }
             __syncthreads();
+            // the Radon columns the next slab shares with this one (its left halo and the first
+            // halo-width of its own columns) move to the front of the tile; the next slab's
+            // Radon phase computes only the columns after them
+            if (s + 1 < a.nslab) {
+                for (int k = tid; k < a.TR * kCarry; k += kThreads) {
+                    const int r = k / kCarry, c = k - r * kCarry;
+                    tile[r * TBP + c] = tile[r * TBP + Ts + c];
+                }
+            }
             {
                 const int CR = a.CR;
                 const int nstrip = CCs >= kThreads ? 1 : (kThreads / CCs < (CR + 7) / 8 ? kThreads / CCs : (CR + 7) / 8);
@@ -373,8 +385,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
             }
             __syncthreads();
 
-            // ---- 4a. theta max of the conv rows the rho window needs (into the dead Radon tile)
-            float* tm = tile;
+            // ---- 4a. theta max of the conv rows the rho window needs (into the dead Radon tile,
+            // after the carried columns)
+            float* tm = tile + kCarry;
             {
                 const int NR = a.nRho + 2 * D0;
                 const int nseg = (Ts + WIN - 1) / WIN;
@@ -591,7 +604,7 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     int nslab = 0, Ts = 0;
     for (int ns = 1; ns <= p->nTheta; ++ns) {
         const int ts = (p->nTheta + ns - 1) / ns;
-        if (ts < 2 * D1 + 1 || ts < 16) break;
+        if (ts < 2 * D1 + 1 || ts < 16 || ts < 2 * halo) break;
         const int TBP = (ts + 2 * halo) | 1, CCP = (ts + 2 * D1) | 1;
         const int maxg = (ts + 2 * halo) * gpt;
         if ((size_t)TR * TBP >= 65536) continue;
@@ -608,7 +621,7 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     g.TR = TR;
     g.TBP = (Ts + 2 * halo) | 1;
     g.CCP = (Ts + 2 * D1) | 1;
-    g.MP = Ts | 1;
+    g.MP = g.TBP;  // the theta-max rows sit in the Radon tile after the carried columns
     g.rho0 = p->p0 - row0;
     g.rpad_end = p->R - row0;
     g.CR = CR;
@@ -687,13 +700,14 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     int maxg = 0;
     for (int s = 0; s < nslab; ++s) {
         const int j0 = slab_j[s], ts = slab_j[s + 1] - j0, TB = ts + 2 * halo;
-        if (ts < 2 * D1 + 1) return EBSD_OK;
+        if (ts < 2 * D1 + 1 || ts < 2 * halo) return EBSD_OK;
         struct Grp {
             int src;
             uint32_t tb;
         };
         std::vector<Grp> grps;
-        for (int jb = 0; jb < TB; ++jb) {
+        // slabs after the first take their first 2 * halo columns from the previous slab
+        for (int jb = s > 0 ? 2 * halo : 0; jb < TB; ++jb) {
             const int jc = j0 - halo + jb;
             const bool flip = jc < 0 || jc >= p->nTheta;
             const int js = ((jc % p->nTheta) + p->nTheta) % p->nTheta;

@@ -454,7 +454,8 @@ class NLPAR:
         """NLPAR.calcsigma_cpu (nlpar_cpu.py:186-281) on the input file: sigma [nrows, ncols]
         and the normalised neighbour distances d2 and counts n2 [nrows, ncols, 9], per scan tile
         of about ``chunksize`` bytes (0: the reference's default), merged as the reference
-        merges them.  The scan is read once and held on the device."""
+        merges them.  The scan is read once and held on the device as float32: host and device
+        memory must hold 4 * nrows * ncols * H * W bytes (the reference reads tile by tile)."""
         if int(nn) != 1:
             raise NotImplementedError("only nn = 1 (the reference's default) is built")
         self.sigmann = 1
@@ -472,7 +473,8 @@ class NLPAR:
                    saturation_protect=None, automask=None, stem_scale=None, **kwargs):
         """NLPAR.opt_lambda_cpu (nlpar_cpu.py:94-184) on the input file: the lambda values for
         the target weights (``opt_lambda_array`` on the file's scan), their median in ``lam``
-        when ``autoupdate``."""
+        when ``autoupdate``.  Like ``calcsigma``, holds the whole scan as float32 on the host and
+        the device (4 * nrows * ncols * H * W bytes)."""
         if saturation_protect is not None:
             self.saturation_protect = saturation_protect
         if automask is not None:

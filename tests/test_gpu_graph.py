@@ -72,6 +72,33 @@ def test_autotune_choice_does_not_change_records(cuda):
     np.testing.assert_allclose(plain["normmax"], after["normmax"], rtol=1e-6)
 
 
+def test_autotune_decision_cache(cuda, tmp_path, monkeypatch):
+    """A decision stored by one plan is applied to an equal plan without timing; records match."""
+    import torch
+    path = tmp_path / "tuning.json"
+    pats = syn.make_patterns(1024, 80, 80, seed=16, noise_frac=0.1)[0]
+    bd = make_bd()
+    ppp = bd.autotune(torch.from_numpy(pats), method="fused", cache=path)
+    assert ppp in (1, 2, 4, 8)
+    assert len(__import__("json").loads(path.read_text())["entries"]) == 1
+    ref = bd.find_bands(pats, method="fused")
+    bd2 = make_bd()
+    plan2 = bd2._device_plan()
+
+    def timed(*a, **k):
+        raise AssertionError("a cached decision must not be timed again")
+    monkeypatch.setattr(plan2, "autotune", timed)
+    assert bd2.autotune(torch.from_numpy(pats), method="fused", cache=path) == ppp
+    got = bd2.find_bands(pats, method="fused")
+    for f in FIELDS:
+        assert got[f].tobytes() == ref[f].tobytes(), f
+    # another geometry is a new key: timed and added beside the first
+    bd3 = make_bd(h=60, nRho=90)
+    p3 = bd3.autotune(torch.from_numpy(syn.make_patterns(512, 60, 60, seed=17)[0]), method="fused", cache=path)
+    assert p3 in (1, 2, 4, 8)
+    assert len(__import__("json").loads(path.read_text())["entries"]) == 2
+
+
 @pytest.mark.parametrize("dtype", [np.uint16, np.float32])
 def test_autotune_single_variant_dtypes(cuda, dtype):
     import torch
