@@ -236,6 +236,22 @@ int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t np
                    float dthresh, const float* d_sigma, int saturation_protect, float* d_work,
                    int out_dtype, void* d_out, const float* d_centre_offset, void* stream);
 
+/* Noise sigma (optional), weights and average of ebsd_nlpar_out in one call for search radii
+ * 1 <= sr <= 3, with each unordered pair's distance summed once: the squared difference of a
+ * pair is symmetric bit for bit, so a pixel's window slot at offset -o reads the sum its
+ * neighbour made for +o (slots beyond +-sr, which only windows shifted inward at the scan edges
+ * have, are summed directly).  The results equal ebsd_nlpar_sigma + ebsd_nlpar_out bit for bit.
+ * compute_sigma = 1: d_sigma [nrows*ncols] is written (NLPAR.sigma_numba, nn = 1, from the same
+ * pass over the patterns); 0: d_sigma is read.  d_work (8-byte aligned): nrows*ncols*(W + 2 F + 8)
+ * + 2 E W + 1 floats, W = (2 sr + 1)^2, F = sr (2 sr + 1) + sr, E = 2 sr (nrows + ncols - 2 sr)
+ * (the edge pixels, whose windows are shifted inward).  EBSD_E_UNSUPPORTED where the staged
+ * tiles pass 48 KB. */
+int ebsd_nlpar_pairs_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx,
+                         const int32_t* d_indices, int32_t nind, float datamax, float lam, int32_t sr,
+                         float dthresh, float* d_sigma, int compute_sigma, int saturation_protect,
+                         float* d_work, int out_dtype, void* d_out, const float* d_centre_offset,
+                         void* stream);
+
 /* ---- band normals (Radon.radon2pole, radon_fast.py:314-397) ---------------------------- */
 #define EBSD_VENDOR_EDAX 0
 #define EBSD_VENDOR_OXFORD 1

@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_PKG, "libebsdgpu.so")
 
 EBSD_U8, EBSD_U16, EBSD_F32 = 0, 1, 2
 EBSD_PLAIN_F32, EBSD_PLAIN_F64, EBSD_FUSED_F32, EBSD_FUSED_F16 = 0, 1, 2, 3
+EBSD_E_UNSUPPORTED = -5  # include/ebsdgpu.h
 
 METHODS = {
     "plain": EBSD_PLAIN_F32, "plain32": EBSD_PLAIN_F32, "plain_f32": EBSD_PLAIN_F32,

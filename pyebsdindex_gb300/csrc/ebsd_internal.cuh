@@ -68,6 +68,8 @@ struct ebsd_plan_s {
     int32_t* d_lut32 = nullptr;    // same when H*W >= 65535
     int32_t* d_count = nullptr;    // [nRays]
     uint8_t* d_rdnmask = nullptr;  // [nRays]
+    uint32_t* d_rdnbits = nullptr; // [nTheta][rdn_words]: bit (i & 31) of word i >> 5 = rdnmask[i][j]
+    int rdn_words = 0;             // (nRho + 31) / 32 + 1: a word past the last, for two-word reads
     float* d_kernel = nullptr;     // [k0*k1]
     std::vector<float> h_kernel;   // host copy of the taps (fused-kernel parameters)
     // separable LoG: taps[a][b] = ku[a] * kw[b] to within two float32 ulps of the largest tap

@@ -67,6 +67,8 @@ struct FusedArgs {
     float ksum;                // sum of the kernel taps (FP16 centring correction)
     const float* wimg;         // [nPx] pixel weights whose dot product is the Radon mean
     const uint8_t* rdnmask;    // [nRho][nTheta]
+    const uint32_t* rdnbits;   // [nTheta][rdnw] the same as bit columns
+    int rdnw;
     int bg_mode;
     const double* bg;
     const float* bgf;
@@ -825,6 +827,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                 const int j = colok ? jl : nT - 1;
                 const int i_first = rb * kRowBlock;
                 const int i0 = i_first < nrho - kRowBlock ? i_first : nrho - kRowBlock;
+                // Radon-mask bits of rows i0 .. i0 + kRowBlock - 1 (issued before the tile loads)
+                const uint32_t* mb = a.rdnbits + (size_t)j * a.rdnw + (i0 >> 5);
+                const unsigned mbits = __funnelshift_r(__ldg(mb), __ldg(mb + 1), i0 & 31);
                 const float* tcol = tm + i0 * MP + j;
                 float v[NV];
 #pragma unroll
@@ -845,7 +850,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                     const float m = fmaxf(fmaxf(suf[o], core), pre[o]);
                     const int i = i0 + o;
                     const float val = crow[o * CP];
-                    const bool f = colok && i >= i_first && val == m && a.rdnmask[i * nT + j];
+                    const bool f = colok && i >= i_first && val == m && ((mbits >> o) & 1u);
                     unsigned bal = __ballot_sync(0xffffffffu, f);
                     while (bal) {
                         const int b = __ffs(bal) - 1;
@@ -1334,6 +1339,8 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
     }
     a.wimg = p->d_fray;
     a.rdnmask = p->d_rdnmask;
+    a.rdnbits = p->d_rdnbits;
+    a.rdnw = p->rdn_words;
     a.bg_mode = p->bg_mode;
     a.bg = p->d_bg;
     a.bgf = p->d_bgf;

@@ -184,6 +184,11 @@ constexpr int kChunk = 32;  // pixel values per staged pattern per step
 constexpr int kSP = kChunk + 1;  // staged row pitch (odd: lanes on different patterns, no conflicts)
 constexpr int kTy = 16;     // threadIdx.y extent (blockDim = 32 x 16)
 
+// Scan rows whose windows are shifted inward (rows within sr of the top or bottom edge), and
+// columns likewise: their windows reach past +-sr.
+__device__ __forceinline__ bool edge_row(int y, int sr, int nrows) { return y < sr || y >= nrows - sr; }
+__device__ __forceinline__ bool edge_col(int x, int sr, int ncols) { return x < sr || x >= ncols - sr; }
+
 // Distance weights of NLPAR.nlpar_nb (nlpar_cpu.py:866-927) for window slots c = ty + 16 j.
 template <int MP>
 __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_tiled(
@@ -280,12 +285,14 @@ __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_tiled(
 
 // Weighted window sum (k_nlpar_average's order) for 32 scan pixels x 32 pattern pixels per step,
 // stored as O (float, or clipped and truncated to uint8 / uint16 -- the detection input).
-template <typename T, typename O = T>
+// SR > 0 fixes the search radius at compile time (unrolled window loops); 0 reads sr.
+template <typename T, typename O, int SR>
 __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_average_tiled(
-        const T* __restrict__ data, int nrows, int ncols, int npx, const T* __restrict__ w, int sr,
+        const T* __restrict__ data, int nrows, int ncols, int npx, const T* __restrict__ w, int sr_arg,
         O* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char smraw[];
     T* sm = (T*)smraw;
+    const int sr = SR > 0 ? SR : sr_arg;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileX + tx;
     const int y = blockIdx.y, x0 = blockIdx.x * kTileX;
     const int wn = 2 * sr + 1, winsz = wn * wn;
@@ -293,30 +300,87 @@ __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_average_tiled(
     window(y, sr, nrows, ys, ye);
     const int cx0 = x0 - 2 * sr > 0 ? x0 - 2 * sr : 0;
     const int cx1 = x0 + kTileX + 2 * sr < ncols ? x0 + kTileX + 2 * sr : ncols;
-    const int ncx = cx1 - cx0, nstage = wn * ncx;
-    T* S = sm;                 // [nstage][kSP]
-    T* Wt = sm + nstage * kSP; // [kTileX][winsz]
+    const int ncx = cx1 - cx0;
+    T* S = sm;                      // [wn rows][ncx][kSP]
+    // [kTileX][WP]: each pixel's weights at a 16-byte aligned row of WP = winsz rounded up to 4,
+    // read four at a time (one broadcast load for four window slots)
+    const int WP = (winsz + 3) & ~3;
+    T* Wt = sm + ((wn * ncx * kSP + 3) & ~3);
     const int npix_tile = ncols - x0 < kTileX ? ncols - x0 : kTileX;
     for (int i = tid; i < npix_tile * winsz; i += kTileX * kTy)
-        Wt[i] = w[(int64_t)(y * ncols + x0) * winsz + i];
+        Wt[(i / winsz) * WP + i % winsz] = w[(int64_t)(y * ncols + x0) * winsz + i];
+    // this thread's scan pixels: the neighbours px = 2 ty + m (kTileX = 2 kTy), and their
+    // windows' first staged column
+    constexpr int kPx = kTileX / kTy;
+    int xsc[kPx];
+#pragma unroll
+    for (int m = 0; m < kPx; ++m) {
+        const int px = kPx * ty + m;
+        int xs, xe;
+        window(px < npix_tile ? x0 + px : x0, sr, ncols, xs, xe);
+        xsc[m] = xs - cx0;
+    }
+    // neighbouring windows one column apart share all but one column of staged values
+    const bool shared_cols = SR > 0 && kPx == 2 && kPx * ty + 1 < npix_tile && xsc[1] == xsc[0] + 1;
     for (int k0 = 0; k0 < npx; k0 += kChunk) {
         const int kn = npx - k0 < kChunk ? npx - k0 : kChunk;
         __syncthreads();
-        for (int st = ty; st < nstage; st += kTy) {
-            const int r = st / ncx, cc = st - r * ncx;
-            const int64_t pat = (int64_t)(ys + r) * ncols + (cx0 + cc);
-            S[st * kSP + tx] = tx < kn ? data[pat * npx + k0 + tx] : (T)0;
+#pragma unroll
+        for (int r = 0; r < (SR > 0 ? 2 * SR + 1 : 1); ++r) {
+            const int rr0 = SR > 0 ? r : 0, rr1 = SR > 0 ? r + 1 : wn;
+            for (int rr = rr0; rr < rr1; ++rr) {
+                const int64_t prow = (int64_t)(ys + rr) * ncols + cx0;
+                for (int cc = ty; cc < ncx; cc += kTy)
+                    S[(rr * ncx + cc) * kSP + tx] = tx < kn ? data[(prow + cc) * npx + k0 + tx] : (T)0;
+            }
         }
         __syncthreads();
-        if (tx < kn) {
-            for (int px = ty; px < npix_tile; px += kTy) {
-                int xs, xe;
-                window(x0 + px, sr, ncols, xs, xe);
-                const T* wp = Wt + px * winsz;
+        if (tx >= kn) continue;
+        if (SR > 0 && shared_cols) {
+            // both pixels at once: each staged value loaded once for the two sums
+            constexpr int WN = 2 * SR + 1, WS = WN * WN;
+            const T* s0 = S + xsc[0] * kSP + tx;
+            const T* wpa = Wt + (kPx * ty) * WP;
+            const T* wpb = wpa + WP;
+            T acc0 = (T)0, acc1 = (T)0;
+#pragma unroll
+            for (int c4 = 0; c4 < WS; c4 += 4) {
+                T wa[4], wb[4];
+                if (sizeof(T) == 4) {
+                    const float4 a4 = *(const float4*)(wpa + c4), b4 = *(const float4*)(wpb + c4);
+                    wa[0] = a4.x; wa[1] = a4.y; wa[2] = a4.z; wa[3] = a4.w;
+                    wb[0] = b4.x; wb[1] = b4.y; wb[2] = b4.z; wb[3] = b4.w;
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        wa[t] = c4 + t < WS ? wpa[c4 + t] : (T)0;
+                        wb[t] = c4 + t < WS ? wpb[c4 + t] : (T)0;
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int c = c4 + t;
+                    if (c < WS) {
+                        const int r = c / WN, cc = c % WN;
+                        acc0 = wadd(acc0, s0[(r * ncx + cc) * kSP], wa[t]);
+                        acc1 = wadd(acc1, s0[(r * ncx + cc + 1) * kSP], wb[t]);
+                    }
+                }
+            }
+            const int64_t o = (int64_t)(y * ncols + x0 + kPx * ty) * npx + k0 + tx;
+            out[o] = store_as<O>(acc0);
+            out[o + npx] = store_as<O>(acc1);
+            continue;
+        }
+#pragma unroll
+        for (int m = 0; m < kPx; ++m) {
+            const int px = kPx * ty + m;
+            if (px < npix_tile) {
+                const T* wp = Wt + px * WP;
                 T acc = (T)0;
                 int c = 0;
                 for (int r = 0; r < wn; ++r) {
-                    const T* srow = S + (r * ncx + (xs - cx0)) * kSP + tx;
+                    const T* srow = S + (r * ncx + xsc[m]) * kSP + tx;
                     for (int cc = 0; cc < wn; ++cc, ++c) acc = wadd(acc, srow[cc * kSP], wp[c]);
                 }
                 out[(int64_t)(y * ncols + x0 + px) * npx + k0 + tx] = store_as<O>(acc);
@@ -325,10 +389,382 @@ __global__ void __launch_bounds__(kTileX * kTy) k_nlpar_average_tiled(
     }
 }
 
+template <typename T, typename O>
+void launch_average_tiled(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const T* data, int nrows, int ncols,
+                          int npx, const T* w, int sr, O* out) {
+    switch (sr) {
+        case 1: k_nlpar_average_tiled<T, O, 1><<<grid, block, smem, st>>>(data, nrows, ncols, npx, w, sr, out); break;
+        case 2: k_nlpar_average_tiled<T, O, 2><<<grid, block, smem, st>>>(data, nrows, ncols, npx, w, sr, out); break;
+        case 3: k_nlpar_average_tiled<T, O, 3><<<grid, block, smem, st>>>(data, nrows, ncols, npx, w, sr, out); break;
+        default: k_nlpar_average_tiled<T, O, 0><<<grid, block, smem, st>>>(data, nrows, ncols, npx, w, sr, out);
+    }
+}
+
+// ---- pair kernels: each unordered pair's distance computed once ---------------------------
+// The squared difference of a pair is symmetric bit for bit ((a - b)^2 == (b - a)^2 in float,
+// and the saturation test is symmetric), so pixel p's distance to neighbour q is the same
+// float sum whichever of the two computes it.  k_nlpar_pairs computes, for every scan pixel,
+// the sums of the nF = sr (2 sr + 1) + sr "forward" offsets (dy, dx) -- dy > 0, or dy == 0 and
+// dx > 0, |dy|, |dx| <= sr -- in the reference's pixel order; a pixel's window slot at offset
+// -o reads the sum its neighbour computed for o.  Slots beyond +-sr, which only the windows
+// shifted inward at the scan edges have, are summed directly from memory.  With kSig the
+// kernel also sums the four forward 3x3 neighbours under sigma_numba's saturation level, from
+// which k_nlpar_sigma_pairs takes the noise sigma without another pass over the patterns.
+constexpr int kPairTy = 8;  // threadIdx.y extent of k_nlpar_pairs (blockDim = 32 x 8)
+
+__device__ __forceinline__ int fwd_count(int sr) { return sr * (2 * sr + 1) + sr; }
+__device__ __forceinline__ void fwd_offset(int f, int sr, int& dy, int& dx) {
+    if (f < sr) {
+        dy = 0;
+        dx = f + 1;
+    } else {
+        const int g = f - sr, w = 2 * sr + 1;
+        dy = 1 + g / w;
+        dx = g - (dy - 1) * w - sr;
+    }
+}
+__device__ __forceinline__ int fwd_index(int dy, int dx, int sr) {
+    return dy == 0 ? dx - 1 : sr + (dy - 1) * (2 * sr + 1) + (dx + sr);
+}
+
+template <int MPF, bool kSig>
+__global__ void __launch_bounds__(kTileX * kPairTy) k_nlpar_pairs(
+        const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind,
+        int nind, float mxval, float mxsig, int sr, float2* __restrict__ pairs, float2* __restrict__ sigp) {
+    extern __shared__ float sm[];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int y = blockIdx.y, x0 = blockIdx.x * kTileX;
+    const int nF = fwd_count(sr);
+    const int nr = (y + sr < nrows ? y + sr : nrows - 1) - y + 1;  // staged scan rows y .. y + nr - 1
+    const int cx0 = x0 - sr > 0 ? x0 - sr : 0;
+    const int cx1 = x0 + kTileX + sr < ncols ? x0 + kTileX + sr : ncols;
+    const int ncx = cx1 - cx0;
+    float* S = sm;  // [nr][ncx][kSP]
+    const int x = x0 + tx;
+    const bool px_ok = x < ncols;
+    const int self = (px_ok ? x : ncols - 1) - cx0;
+    int slot[MPF];
+    bool ok[MPF];
+#pragma unroll
+    for (int j = 0; j < MPF; ++j) {
+        const int f = ty + kPairTy * j;
+        int dy = 0, dx = 0;
+        if (f < nF) fwd_offset(f, sr, dy, dx);
+        ok[j] = px_ok && f < nF && x + dx >= 0 && x + dx < ncols && y + dy < nrows;
+        slot[j] = ok[j] ? dy * ncx + (x + dx - cx0) : self;
+    }
+    // sigma's four forward 3x3 neighbours sit at f = 0, 2 sr - 1, 2 sr, 2 sr + 1 (warp-uniform ty)
+    const int sk = ty == 0 ? 0 : (ty == 2 * sr - 1 ? 1 : (ty == 2 * sr ? 2 : (ty == 2 * sr + 1 ? 3 : -1)));
+    const bool near = kSig && sk >= 0 && ok[0];
+    float d[MPF], n[MPF], ds = 0.0f, ns = 0.0f;
+#pragma unroll
+    for (int j = 0; j < MPF; ++j) {
+        d[j] = 0.0f;
+        n[j] = 0.0f;
+    }
+    for (int q0 = 0; q0 < nind; q0 += kChunk) {
+        const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
+        const int k = tx < qn ? __ldg(ind + q0 + tx) : 0;
+        __syncthreads();  // the previous chunk has been consumed
+        for (int r = 0; r < nr; ++r) {
+            const float* prow = data + ((int64_t)(y + r) * ncols + cx0) * npx + k;
+            float* srow = S + r * ncx * kSP + tx;
+            for (int cc = ty; cc < ncx; cc += kPairTy) srow[cc * kSP] = tx < qn ? __ldg(prow + (int64_t)cc * npx) : 0.0f;
+        }
+        __syncthreads();
+        for (int qq = 0; qq < qn; ++qq) {
+            const float xv = S[self * kSP + qq];
+#pragma unroll
+            for (int j = 0; j < MPF; ++j) {
+                const float yv = S[slot[j] * kSP + qq];
+                if (yv < mxval && xv < mxval) {  // pair_ssd's order: count, difference, square
+                    n[j] = __fadd_rn(n[j], 1.0f);
+                    const float t = __fsub_rn(xv, yv);
+                    d[j] = __fadd_rn(d[j], __fmul_rn(t, t));
+                }
+                if (kSig && j == 0 && near && yv < mxsig && xv < mxsig) {
+                    ns = __fadd_rn(ns, 1.0f);
+                    const float t = __fsub_rn(xv, yv);
+                    ds = __fadd_rn(ds, __fmul_rn(t, t));
+                }
+            }
+        }
+    }
+    const int64_t pix = (int64_t)y * ncols + x;
+#pragma unroll
+    for (int j = 0; j < MPF; ++j)
+        if (ok[j]) pairs[pix * nF + ty + kPairTy * j] = make_float2(d[j], n[j]);
+    if (near) sigp[pix * 4 + sk] = make_float2(ds, ns);
+}
+
+// sigma_numba (nn = 1) from the pair sums: min over the clipped 3x3 neighbourhood of
+// SSD / (2 n) for SSD >= 1e-3 (the count starts at 1e-12, which the first add absorbs).
+__global__ void k_nlpar_sigma_pairs(const float2* __restrict__ sigp, int nrows, int ncols, float* __restrict__ sigma) {
+    const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= (int64_t)nrows * ncols) return;
+    const int j = (int)(pix / ncols), i = (int)(pix - (int64_t)j * ncols);
+    // forward 3x3 offsets in sigp order, and their mirrors
+    const int fdy[4] = {0, 1, 1, 1}, fdx[4] = {1, -1, 0, 1};
+    float s0 = 1e24f;
+    for (int k = 0; k < 8; ++k) {
+        const int kk = k & 3;
+        const int dy = k < 4 ? fdy[kk] : -fdy[kk], dx = k < 4 ? fdx[kk] : -fdx[kk];
+        const int jn = j + dy, inn = i + dx;
+        if (jn < 0 || jn >= nrows || inn < 0 || inn >= ncols) continue;
+        const float2 e = k < 4 ? sigp[pix * 4 + kk] : sigp[((int64_t)jn * ncols + inn) * 4 + kk];
+        const float n2 = e.y > 0.0f ? e.y : 1.0e-12f;
+        if (e.x >= 1.e-3f) s0 = fminf(s0, __fdiv_rn(e.x, __fmul_rn(n2, 2.0f)));
+    }
+    sigma[pix] = sqrtf(s0);
+}
+
+// The window weights of k_nlpar_weights_tiled from the pair sums (slots c = ty + 16 j), for the
+// pixels whose windows are centred; the edge pixels take k_nlpar_weights_edge.
+template <int MP>
+__global__ void __launch_bounds__(kTileX * kTy) k_nlpar_weights_pairs(
+        const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind,
+        int nind, float mxval, const float2* __restrict__ pairs, const float* __restrict__ sigma, float lam2,
+        float dthresh, int sr, float* __restrict__ wout, const float* __restrict__ coff) {
+    __shared__ float W[kTileX * 49];
+    __shared__ float T[kTileX];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTileX + tx;
+    const int y = blockIdx.y, x0 = blockIdx.x * kTileX;
+    if (edge_row(y, sr, nrows)) return;
+    const int wn = 2 * sr + 1, winsz = wn * wn, nF = fwd_count(sr);
+    int ys, ye;
+    window(y, sr, nrows, ys, ye);
+    const int x = x0 + tx;
+    const bool px_ok = x < ncols && !edge_col(x, sr, ncols);
+    int xs, xe;
+    window(x < ncols ? x : ncols - 1, sr, ncols, xs, xe);
+    const int64_t pix = (int64_t)y * ncols + (x < ncols ? x : ncols - 1);
+#pragma unroll
+    for (int j = 0; j < MP; ++j) {
+        const int c = ty + kTy * j;
+        if (c < winsz && px_ok) {
+            const int jn = ys + c / wn, inn = xs + c % wn;
+            const int64_t nb = (int64_t)jn * ncols + inn;
+            const int dy = jn - y, dx = inn - x;
+            float w;
+            if (nb == pix) {
+                w = -1.0e6f;
+            } else {
+                float d2, n2;
+                if (dy >= -sr && dy <= sr && dx >= -sr && dx <= sr) {
+                    const float2 e = (dy > 0 || (dy == 0 && dx > 0)) ? pairs[pix * nF + fwd_index(dy, dx, sr)]
+                                                                    : pairs[nb * nF + fwd_index(-dy, -dx, sr)];
+                    d2 = e.x;
+                    n2 = e.y;
+                } else {  // (not reached: the windows of these blocks are centred)
+                    pair_ssd(data + pix * npx, data + nb * npx, ind, nind, mxval, 0.0f, d2, n2);
+                }
+                float s0 = sigma[pix], s1 = sigma[nb];
+                s0 = __fmul_rn(s0, s0);
+                s1 = __fmul_rn(s1, s1);
+                const float ss = __fadd_rn(s0, s1);
+                d2 = __fsub_rn(d2, __fmul_rn(n2, ss));
+                const float dnorm = __fmul_rn(ss, sqrtf(__fmul_rn(2.0f, n2)));
+                w = dnorm > 1.e-8f ? __fdiv_rn(d2, dnorm) : __fmul_rn(1e6f, n2);
+            }
+            w = fmaxf(__fsub_rn(w, dthresh), 0.0f);
+            w = expf(__fmul_rn(__fmul_rn(-1.0f, w), lam2));
+            if (coff && nb == pix) w = __fadd_rn(w, coff[pix]);  // diff_offset's centre addition
+            W[tx * winsz + c] = w;
+        }
+    }
+    __syncthreads();
+    if (ty == 0 && px_ok) {
+        float t = 0.0f;
+        for (int c = 0; c < winsz; ++c) t = __fadd_rn(t, W[tx * winsz + c]);
+        T[tx] = t;
+    }
+    __syncthreads();
+    for (int i = tid; i < kTileX * winsz; i += kTileX * kTy) {
+        const int px = i / winsz, c = i - px * winsz;
+        if (x0 + px < ncols && !edge_col(x0 + px, sr, ncols))
+            wout[((int64_t)y * ncols + x0 + px) * winsz + c] = __fdiv_rn(W[px * winsz + c], T[px]);
+    }
+}
+
+// ---- edge pixels: windows shifted inward, reaching past +-sr ----------------------------------
+// Edge pixels are those of the sr top and bottom rows, and the sr left and right columns of the
+// other rows; index: top rows, bottom rows, then per middle row its 2 sr edge columns.  Their
+// raw window sums (SSD, count per slot, in the reference's pixel order) are computed by two
+// kernels that split the slots over many blocks, then k_nlpar_weights_edge turns them into
+// normalised weights, one block per edge pixel.
+__device__ __forceinline__ int64_t edge_index(int y, int x, int sr, int nrows, int ncols) {
+    if (y < sr) return (int64_t)y * ncols + x;
+    if (y >= nrows - sr) return (int64_t)(sr + y - (nrows - sr)) * ncols + x;
+    return (int64_t)2 * sr * ncols + (int64_t)(y - sr) * 2 * sr + (x < sr ? x : sr + x - (ncols - sr));
+}
+
+// Edge rows: blockIdx.y picks the row (the sr top rows, then the sr bottom rows), blockIdx.x 32
+// neighbouring pixels (one per lane), blockIdx.z a range of kTy window slots (one per thread row).
+// All pixels of the row share the window rows; the patterns of those rows in the columns the
+// block's windows touch are staged.
+__global__ void __launch_bounds__(kTileX * kTy) k_nlpar_edge_rows(
+        const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind, int nind,
+        float mxval, int sr, float2* __restrict__ raw) {
+    extern __shared__ float sm[];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int wn = 2 * sr + 1, winsz = wn * wn;
+    const int y = blockIdx.y < sr ? blockIdx.y : nrows - 2 * sr + blockIdx.y;
+    const int x0 = blockIdx.x * kTileX;
+    int ys, ye;
+    window(y, sr, nrows, ys, ye);
+    const int cx0 = x0 - 2 * sr > 0 ? x0 - 2 * sr : 0;
+    const int cx1 = x0 + kTileX + 2 * sr < ncols ? x0 + kTileX + 2 * sr : ncols;
+    const int ncx = cx1 - cx0;
+    float* S = sm;  // [wn][ncx][kSP]
+    const int x = x0 + tx;
+    const int c = blockIdx.z * kTy + ty;
+    const bool ok = x < ncols && c < winsz;
+    int xs, xe;
+    window(x < ncols ? x : ncols - 1, sr, ncols, xs, xe);
+    const int self = (y - ys) * ncx + ((x < ncols ? x : ncols - 1) - cx0);
+    const int nbs = ok ? (c / wn) * ncx + (xs + c % wn - cx0) : self;
+    float d = 0.0f, n = 0.0f;
+    for (int q0 = 0; q0 < nind; q0 += kChunk) {
+        const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
+        const int k = tx < qn ? __ldg(ind + q0 + tx) : 0;
+        __syncthreads();
+        for (int r = 0; r < wn; ++r) {
+            const float* prow = data + ((int64_t)(ys + r) * ncols + cx0) * npx + k;
+            float* srow = S + r * ncx * kSP + tx;
+            for (int cc = ty; cc < ncx; cc += kTy) srow[cc * kSP] = tx < qn ? __ldg(prow + (int64_t)cc * npx) : 0.0f;
+        }
+        __syncthreads();
+        for (int qq = 0; qq < qn; ++qq) {
+            const float xv = S[self * kSP + qq], yv = S[nbs * kSP + qq];
+            if (yv < mxval && xv < mxval) {  // pair_ssd's order: count, difference, square
+                n = __fadd_rn(n, 1.0f);
+                const float t = __fsub_rn(xv, yv);
+                d = __fadd_rn(d, __fmul_rn(t, t));
+            }
+        }
+    }
+    if (ok) raw[edge_index(y, x, sr, nrows, ncols) * winsz + c] = make_float2(d, n);
+}
+
+// Edge columns of the middle rows: blockIdx.y the side, blockIdx.x 32 neighbouring rows (one per
+// lane), blockIdx.z a range of kTy (edge column, window slot) combinations.  All edge pixels of
+// one side share the window columns [0, 2 sr] (or the last 2 sr + 1).
+__global__ void __launch_bounds__(kTileX * kTy) k_nlpar_edge_cols(
+        const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind, int nind,
+        float mxval, int sr, float2* __restrict__ raw) {
+    extern __shared__ float sm[];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int wn = 2 * sr + 1, winsz = wn * wn;
+    const int nri = nrows - 2 * sr;
+    const int y0 = sr + blockIdx.x * kTileX;
+    const int nrow = nri - blockIdx.x * kTileX < kTileX ? nri - blockIdx.x * kTileX : kTileX;
+    const int side = blockIdx.y;
+    const int colbase = side ? ncols - wn : 0;
+    const int xe0 = side ? ncols - sr : 0;
+    const int nrs = nrow + 2 * sr;
+    float* S = sm;  // [nrs][wn][kSP]
+    const int idx = blockIdx.z * kTy + ty;
+    const bool ok = tx < nrow && idx < sr * winsz;
+    const int e = ok ? idx / winsz : 0, c = ok ? idx - e * winsz : 0;
+    const int self = ((ok ? tx : 0) + sr) * wn + (xe0 + e - colbase);
+    const int nbs = ok ? (tx + c / wn) * wn + c % wn : self;
+    float d = 0.0f, n = 0.0f;
+    for (int q0 = 0; q0 < nind; q0 += kChunk) {
+        const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
+        const int k = tx < qn ? __ldg(ind + q0 + tx) : 0;
+        __syncthreads();
+        for (int r = ty; r < nrs; r += kTy) {
+            const float* prow = data + ((int64_t)(y0 - sr + r) * ncols + colbase) * npx + k;
+            float* srow = S + r * wn * kSP + tx;
+            for (int cc = 0; cc < wn; ++cc) srow[cc * kSP] = tx < qn ? __ldg(prow + (int64_t)cc * npx) : 0.0f;
+        }
+        __syncthreads();
+        for (int qq = 0; qq < qn; ++qq) {
+            const float xv = S[self * kSP + qq], yv = S[nbs * kSP + qq];
+            if (yv < mxval && xv < mxval) {  // pair_ssd's order: count, difference, square
+                n = __fadd_rn(n, 1.0f);
+                const float t = __fsub_rn(xv, yv);
+                d = __fadd_rn(d, __fmul_rn(t, t));
+            }
+        }
+    }
+    if (ok) raw[edge_index(y0 + tx, xe0 + e, sr, nrows, ncols) * winsz + c] = make_float2(d, n);
+}
+
+// Normalised window weights of the edge pixels from their raw sums: one block (64 threads) per
+// edge pixel, the arithmetic of k_nlpar_weights_tiled.
+__global__ void k_nlpar_weights_edge(const float2* __restrict__ raw, int nrows, int ncols, int sr,
+                                     const float* __restrict__ sigma, float lam2, float dthresh,
+                                     float* __restrict__ wout, const float* __restrict__ coff) {
+    __shared__ float W[64];
+    __shared__ float T;
+    const int wn = 2 * sr + 1, winsz = wn * wn;
+    const int64_t b = blockIdx.x;
+    // edge index -> pixel
+    int y, x;
+    const int64_t top = (int64_t)sr * ncols;
+    if (b < 2 * top) {
+        const int64_t r = b / ncols;
+        y = (int)(r < sr ? r : nrows - 2 * sr + r);
+        x = (int)(b - r * ncols);
+    } else {
+        const int64_t m = b - 2 * top;
+        y = sr + (int)(m / (2 * sr));
+        const int e = (int)(m - (int64_t)(y - sr) * 2 * sr);
+        x = e < sr ? e : ncols - 2 * sr + e;
+    }
+    int ys, ye, xs, xe;
+    window(y, sr, nrows, ys, ye);
+    window(x, sr, ncols, xs, xe);
+    const int64_t pix = (int64_t)y * ncols + x;
+    const int c = threadIdx.x;
+    if (c < winsz) {
+        const int64_t nb = (int64_t)(ys + c / wn) * ncols + (xs + c % wn);
+        float w;
+        if (nb == pix) {
+            w = -1.0e6f;
+        } else {
+            const float2 e2 = raw[b * winsz + c];
+            float s0 = sigma[pix], s1 = sigma[nb];
+            s0 = __fmul_rn(s0, s0);
+            s1 = __fmul_rn(s1, s1);
+            const float ss = __fadd_rn(s0, s1);
+            const float d2 = __fsub_rn(e2.x, __fmul_rn(e2.y, ss));
+            const float dnorm = __fmul_rn(ss, sqrtf(__fmul_rn(2.0f, e2.y)));
+            w = dnorm > 1.e-8f ? __fdiv_rn(d2, dnorm) : __fmul_rn(1e6f, e2.y);
+        }
+        w = fmaxf(__fsub_rn(w, dthresh), 0.0f);
+        w = expf(__fmul_rn(__fmul_rn(-1.0f, w), lam2));
+        if (coff && nb == pix) w = __fadd_rn(w, coff[pix]);  // diff_offset's centre addition
+        W[c] = w;
+    }
+    __syncthreads();
+    if (c == 0) {
+        float t = 0.0f;
+        for (int k = 0; k < winsz; ++k) t = __fadd_rn(t, W[k]);
+        T = t;
+    }
+    __syncthreads();
+    if (c < winsz) wout[pix * winsz + c] = __fdiv_rn(W[c], T);
+}
+
+size_t edge_rows_smem(int sr, int ncols) {
+    const int ncx = std::min(ncols, kTileX + 4 * sr);
+    return (size_t)(2 * sr + 1) * ncx * kSP * sizeof(float);
+}
+size_t edge_cols_smem(int sr) { return (size_t)(kTileX + 2 * sr) * (2 * sr + 1) * kSP * sizeof(float); }
+
+size_t pairs_smem(int sr, int ncols) {
+    const int ncx = std::min(ncols, kTileX + 2 * sr);
+    return (size_t)(sr + 1) * ncx * kSP * sizeof(float);
+}
+
 size_t tiled_smem(int sr, int ncols, size_t elem, bool weights) {
     const int wn = 2 * sr + 1;
     const int ncx = std::min(ncols, kTileX + 4 * sr);
-    size_t b = (size_t)wn * ncx * kSP * elem + (size_t)kTileX * wn * wn * elem;
+    // staged rows (rounded up to 4 elements), then the pixels' weights at rows of winsz
+    // rounded up to 4
+    size_t b = (((size_t)wn * ncx * kSP + 3) & ~(size_t)3) * elem + (size_t)kTileX * ((wn * wn + 3) & ~3) * elem;
     if (weights) b += kTileX * sizeof(float);
     return b;
 }
@@ -556,14 +992,14 @@ int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t np
         int rc = launch_status();
         if (rc != EBSD_OK) return rc;
         if (out_dtype == EBSD_U8)
-            k_nlpar_average_tiled<float, uint8_t><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr,
-                                                                              (uint8_t*)d_out);
+            launch_average_tiled<float, uint8_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, d_work, sr,
+                                                 (uint8_t*)d_out);
         else if (out_dtype == EBSD_U16)
-            k_nlpar_average_tiled<float, uint16_t><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr,
-                                                                               (uint16_t*)d_out);
+            launch_average_tiled<float, uint16_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, d_work, sr,
+                                                  (uint16_t*)d_out);
         else
-            k_nlpar_average_tiled<float><<<tgrid, tblock, asm_, st>>>(d_data, nrows, ncols, npx, d_work, sr,
-                                                                     (float*)d_out);
+            launch_average_tiled<float, float>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, d_work, sr,
+                                               (float*)d_out);
         return launch_status();
     }
     k_nlpar_weights<<<(unsigned)(nrows * ncols), bs, winsz * sizeof(float), st>>>(
@@ -580,6 +1016,83 @@ int ebsd_nlpar_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t np
     return launch_status();
 }
 
+int ebsd_nlpar_pairs_out(const float* d_data, int32_t nrows, int32_t ncols, int32_t npx, const int32_t* d_indices,
+                         int32_t nind, float datamax, float lam, int32_t sr, float dthresh, float* d_sigma,
+                         int compute_sigma, int saturation_protect, float* d_work, int out_dtype, void* d_out,
+                         const float* d_centre_offset, void* stream) {
+    if (out_dtype != EBSD_F32 && out_dtype != EBSD_U8 && out_dtype != EBSD_U16) return EBSD_E_DTYPE;
+    if (!d_data || !d_indices || !d_sigma || !d_work || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 ||
+        nind < 0 || nind > npx || sr < 1 || sr > 3 || !(lam > 0.0f))
+        return EBSD_E_ARG;
+    if (2 * sr + 1 > nrows || 2 * sr + 1 > ncols) return EBSD_E_ARG;  // window must fit the scan
+    const size_t psm = pairs_smem(sr, ncols), asm_ = tiled_smem(sr, ncols, sizeof(float), false);
+    if (psm > 48 * 1024 || asm_ > 48 * 1024 || edge_rows_smem(sr, ncols) > 48 * 1024 || edge_cols_smem(sr) > 48 * 1024)
+        return EBSD_E_UNSUPPORTED;
+    const float mxval = saturation_protect ? datamax * 0.999f : datamax + 1.0f;
+    const float mxsig = saturation_protect ? datamax * 0.9961f : datamax + 1.0f;
+    const float lam2 = 1.0f / (lam * lam);
+    const int64_t npix = (int64_t)nrows * ncols;
+    const int winsz = (2 * sr + 1) * (2 * sr + 1), nF = sr * (2 * sr + 1) + sr;
+    float* w = d_work;
+    // the pair sums start at the next even float after the weights (8-byte aligned float2;
+    // d_work itself is at least 8-byte aligned)
+    if ((uintptr_t)d_work % 8 != 0) return EBSD_E_ARG;
+    float2* pairs = (float2*)(d_work + ((npix * winsz + 1) & ~(int64_t)1));
+    float2* sigp = pairs + npix * nF;
+    cudaStream_t st = (cudaStream_t)stream;
+    const dim3 pgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), pblock(kTileX, kPairTy);
+    const int mpf = (nF + kPairTy - 1) / kPairTy;
+#define EBSD_PAIRS(M, SG)                                                                                     \
+    k_nlpar_pairs<M, SG><<<pgrid, pblock, psm, st>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, sr, \
+                                                     pairs, sigp)
+    if (compute_sigma) {
+        if (mpf == 1) EBSD_PAIRS(1, true);
+        else if (mpf == 2) EBSD_PAIRS(2, true);
+        else EBSD_PAIRS(3, true);
+    } else {
+        if (mpf == 1) EBSD_PAIRS(1, false);
+        else if (mpf == 2) EBSD_PAIRS(2, false);
+        else EBSD_PAIRS(3, false);
+    }
+#undef EBSD_PAIRS
+    int rc = launch_status();
+    if (rc != EBSD_OK) return rc;
+    if (compute_sigma) {
+        k_nlpar_sigma_pairs<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(sigp, nrows, ncols, d_sigma);
+        if ((rc = launch_status()) != EBSD_OK) return rc;
+    }
+    const dim3 tgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), tblock(kTileX, kTy);
+    k_nlpar_weights_pairs<4><<<tgrid, tblock, 0, st>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval, pairs,
+                                                       d_sigma, lam2, dthresh, sr, w, d_centre_offset);
+    if ((rc = launch_status()) != EBSD_OK) return rc;
+    {
+        // edge pixels: raw window sums (rows, then the middle rows' columns), then their weights
+        float2* raw = sigp + npix * 4;
+        const int nri = nrows - 2 * sr;
+        const unsigned zr = (unsigned)((winsz + kTy - 1) / kTy), zc = (unsigned)((sr * winsz + kTy - 1) / kTy);
+        k_nlpar_edge_rows<<<dim3((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)(2 * sr), zr), tblock,
+                            edge_rows_smem(sr, ncols), st>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval, sr, raw);
+        if ((rc = launch_status()) != EBSD_OK) return rc;
+        if (nri > 0) {
+            k_nlpar_edge_cols<<<dim3((unsigned)((nri + kTileX - 1) / kTileX), 2u, zc), tblock, edge_cols_smem(sr), st>>>(
+                d_data, nrows, ncols, npx, d_indices, nind, mxval, sr, raw);
+            if ((rc = launch_status()) != EBSD_OK) return rc;
+        }
+        const int64_t nedge = (int64_t)2 * sr * ncols + (int64_t)nri * 2 * sr;
+        k_nlpar_weights_edge<<<(unsigned)nedge, 64, 0, st>>>(raw, nrows, ncols, sr, d_sigma, lam2, dthresh, w,
+                                                             d_centre_offset);
+        if ((rc = launch_status()) != EBSD_OK) return rc;
+    }
+    if (out_dtype == EBSD_U8)
+        launch_average_tiled<float, uint8_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (uint8_t*)d_out);
+    else if (out_dtype == EBSD_U16)
+        launch_average_tiled<float, uint16_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr,
+                                              (uint16_t*)d_out);
+    else
+        launch_average_tiled<float, float>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (float*)d_out);
+    return launch_status();
+}
+
 int ebsd_nlpar_apply(const float* d_x, int32_t nrows, int32_t ncols, int32_t npx, const float* d_w, int32_t sr,
                      float* d_out, void* stream) {
     if (!d_x || !d_w || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10 || 2 * sr + 1 > nrows ||
@@ -588,7 +1101,8 @@ int ebsd_nlpar_apply(const float* d_x, int32_t nrows, int32_t ncols, int32_t npx
     const size_t asm_ = tiled_smem(sr, ncols, sizeof(float), false);
     if (asm_ <= 48 * 1024) {
         const dim3 tgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), tblock(kTileX, kTy);
-        k_nlpar_average_tiled<float><<<tgrid, tblock, asm_, (cudaStream_t)stream>>>(d_x, nrows, ncols, npx, d_w, sr, d_out);
+        launch_average_tiled<float, float>(tgrid, tblock, asm_, (cudaStream_t)stream, d_x, nrows, ncols, npx, d_w, sr,
+                                           d_out);
         return launch_status();
     }
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));

@@ -30,6 +30,7 @@ void free_plan_tables(ebsd_plan_s* p) {
     cudaFree(p->d_lut32);
     cudaFree(p->d_count);
     cudaFree(p->d_rdnmask);
+    cudaFree(p->d_rdnbits);
     cudaFree(p->d_kernel);
     cudaFree(p->d_kernel64);
     cudaFree(p->d_ksep);
@@ -575,6 +576,16 @@ int ebsd_plan_create(const ebsd_plan_desc* d, int device, ebsd_plan_t* out) {
     }
     if (rc == EBSD_OK) rc = upload(&p->d_count, count.data(), count.size());
     if (rc == EBSD_OK) rc = upload(&p->d_rdnmask, d->rdnmask, (size_t)nRays);
+    {
+        // the Radon mask as bit columns: a peak task reads the mask of its rows with one
+        // funnel shift of two words, loaded ahead of its tile loads
+        p->rdn_words = (p->nRho + 31) / 32 + 1;
+        std::vector<uint32_t> bits((size_t)p->nTheta * p->rdn_words, 0u);
+        for (int i = 0; i < p->nRho; ++i)
+            for (int j = 0; j < p->nTheta; ++j)
+                if (d->rdnmask[(size_t)i * p->nTheta + j]) bits[(size_t)j * p->rdn_words + (i >> 5)] |= 1u << (i & 31);
+        if (rc == EBSD_OK) rc = upload(&p->d_rdnbits, bits.data(), bits.size());
+    }
     if (rc == EBSD_OK) rc = upload(&p->d_kernel, d->kernel, (size_t)p->k0 * p->k1);
     p->h_kernel.assign(d->kernel, d->kernel + (size_t)p->k0 * p->k1);
     {

@@ -70,6 +70,8 @@ struct SlabArgs {
     int statR;                 // statistics rows (conv rows [D0, D0 + statR))
     float ku[9], kw[9];
     const uint8_t* rdnmask;
+    const uint32_t* rdnbits;   // [nTheta][rdnw] the Radon mask as bit columns
+    int rdnw;
     LabelConsts kc;
     ebsd_bands out;
     int64_t out_offset;
@@ -425,6 +427,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                     const int j = colok ? jl : Ts - 1;
                     const int i_first = rb * kRowBlock;
                     const int i0 = i_first < nrho - kRowBlock ? i_first : nrho - kRowBlock;
+                    // Radon-mask bits of rows i0 .. i0 + kRowBlock - 1 (issued before the tile loads)
+                    const uint32_t* mb = a.rdnbits + (size_t)(j0 + j) * a.rdnw + (i0 >> 5);
+                    const unsigned mbits = __funnelshift_r(__ldg(mb), __ldg(mb + 1), i0 & 31);
                     const float* tcol = tm + i0 * MP + j;
                     float v[NV];
 #pragma unroll
@@ -444,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                         const float m = fmaxf(fmaxf(suf[o], core), pre[o]);
                         const int i = i0 + o;
                         const float val = crow[o * CCP];
-                        const bool f = colok && i >= i_first && val == m && a.rdnmask[i * a.nTheta + j0 + j];
+                        const bool f = colok && i >= i_first && val == m && ((mbits >> o) & 1u);
                         unsigned bal = __ballot_sync(0xffffffffu, f);
                         while (bal) {
                             const int b = __ffs(bal) - 1;
@@ -823,6 +828,8 @@ SlabArgs slab_args(const ebsd_plan_s* p, const void* d_pats, int64_t n, const eb
         a.kw[k] = k < p->k1 ? p->h_kw[k] : 0.0f;
     }
     a.rdnmask = p->d_rdnmask;
+    a.rdnbits = p->d_rdnbits;
+    a.rdnw = p->rdn_words;
     a.kc = LabelConsts{p->p0, p->p1, p->nTheta, p->nRho, p->nB, p->d_theta, p->d_rho};
     a.out = out;
     a.out_offset = out_offset;

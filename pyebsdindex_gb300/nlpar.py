@@ -88,6 +88,10 @@ def _bind():
                                        C.c_float, C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_int, C.c_void_p,
                                        C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         lib.ebsd_nlpar_out.restype = C.c_int
+        lib.ebsd_nlpar_pairs_out.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int32,
+                                             C.c_float, C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_int, C.c_int,
+                                             C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.ebsd_nlpar_pairs_out.restype = C.c_int
         lib.ebsd_nlpar_sigma_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                               C.c_int32, C.c_int32, C.c_void_p, C.c_int32, C.c_int, C.c_void_p,
                                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -320,6 +324,11 @@ class NLPAR:
         sp = self.saturation_protect if saturation_protect is None else saturation_protect
         t, ind, nrows, ncols, shape, is_torch, dev = self._prepare(data, nrows, ncols)
         stream = torch.cuda.current_stream(dev).cuda_stream
+        dmax = float(t.max().item())
+        sr = int(self.searchradius)
+        # radii 1..3: sigma, weights and average in one call that sums each unordered pair once
+        pairs = 1 <= sr <= 3
+        compute_sigma = False
         if sigma is not None:
             sig = torch.as_tensor(np.asarray(sigma, dtype=np.float32) if not isinstance(sigma, torch.Tensor) else sigma,
                                   device=dev).to(torch.float32).reshape(nrows, ncols).contiguous()
@@ -327,12 +336,15 @@ class NLPAR:
             sig = torch.as_tensor(np.asarray(self.sigma, dtype=np.float32), device=dev)
         else:
             sig = torch.empty((nrows, ncols), dtype=torch.float32, device=dev)
-            _lib.check(lib.ebsd_nlpar_sigma(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
-                                            float(t.max().item()), int(bool(sp)), sig.data_ptr(), stream),
-                       "ebsd_nlpar_sigma")
-        self.sigma = sig.cpu().numpy()
-        sr = int(self.searchradius)
-        work = torch.empty((nrows * ncols, (2 * sr + 1) ** 2), dtype=torch.float32, device=dev)
+            compute_sigma = True
+            if not pairs:
+                _lib.check(lib.ebsd_nlpar_sigma(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
+                                                dmax, int(bool(sp)), sig.data_ptr(), stream), "ebsd_nlpar_sigma")
+        winsz = (2 * sr + 1) ** 2
+        nfwd = sr * (2 * sr + 1) + sr
+        nedge = 2 * sr * (nrows + ncols - 2 * sr)
+        work = torch.empty(nrows * ncols * (winsz + (2 * nfwd + 8 if pairs else 0)) + (2 * nedge * winsz if pairs else 0)
+                           + 1, dtype=torch.float32, device=dev)
         odt = np.dtype(np.float32 if out_dtype is None else out_dtype)
         if odt == np.float32:
             out, code = torch.empty_like(t), _lib.EBSD_F32
@@ -349,11 +361,25 @@ class NLPAR:
                                    else centre_offset, device=dev).to(torch.float32).reshape(-1).contiguous()
             if coff.numel() != nrows * ncols:
                 raise ValueError("centre_offset holds one value per scan pixel")
-        _lib.check(lib.ebsd_nlpar_out(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
-                                      float(t.max().item()), float(np.float32(self.lam)), sr,
-                                      float(np.float32(self.dthresh)), sig.data_ptr(), int(bool(sp)),
-                                      work.data_ptr(), code, out.data_ptr(),
-                                      None if coff is None else coff.data_ptr(), stream), "ebsd_nlpar_out")
+        lam32, dth32 = float(np.float32(self.lam)), float(np.float32(self.dthresh))
+        rc = -1
+        if pairs:
+            rc = lib.ebsd_nlpar_pairs_out(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(), dmax,
+                                          lam32, sr, dth32, sig.data_ptr(), int(compute_sigma), int(bool(sp)),
+                                          work.data_ptr(), code, out.data_ptr(),
+                                          None if coff is None else coff.data_ptr(), stream)
+            if rc != _lib.EBSD_E_UNSUPPORTED:
+                _lib.check(rc, "ebsd_nlpar_pairs_out")
+        if rc != 0:
+            # the per-slot kernels (radii beyond 3, or staged tiles too large for the pair kernels)
+            if compute_sigma and pairs:
+                _lib.check(lib.ebsd_nlpar_sigma(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(),
+                                                dmax, int(bool(sp)), sig.data_ptr(), stream), "ebsd_nlpar_sigma")
+            _lib.check(lib.ebsd_nlpar_out(t.data_ptr(), nrows, ncols, t.shape[1], ind.data_ptr(), ind.numel(), dmax,
+                                          lam32, sr, dth32, sig.data_ptr(), int(bool(sp)), work.data_ptr(), code,
+                                          out.data_ptr(), None if coff is None else coff.data_ptr(), stream),
+                       "ebsd_nlpar_out")
+        self.sigma = sig.cpu().numpy()
         out = out.reshape(shape)
         if odt == np.uint16:
             # torch's uint16 has few operations: returned as a uint16 view where torch has the type
