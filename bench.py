@@ -456,6 +456,8 @@ def time_mixed(pools, n_total, steps, dev):
         reps = (each + pd.shape[0] - 1) // pd.shape[0]
         batches[(h, h)] = pd.repeat(reps, 1, 1)[:each].contiguous().view(torch.uint16)
     st = torch.cuda.current_stream(dev)
+    # the slab width of every size, autotuned on a sample of that size before the timed steps
+    tuned = mb.autotune({k: v[:4096 if k[0] < 240 else 1024] for k, v in batches.items()}, stream=st)
 
     def run(b):
         return mb.find_bands_device(b, stream=st)
@@ -472,7 +474,9 @@ def time_mixed(pools, n_total, steps, dev):
     res = {"workload": f"{3 * each:,} uint16 patterns (Poisson peak 4000), one third each at 60x60 / 120x120 / "
                        "240x240, nRho 1.5*size, nTheta 180, nBands 10; pools of distinct seeded patterns per size "
                        f"({pools[60].shape[0]}) tiled",
-           "one_launch": mixed, "ms_per_step": ms, "patterns_per_s": 3 * each / ms * 1e3, "per_size": {}}
+           "one_launch": mixed, "ms_per_step": ms, "patterns_per_s": 3 * each / ms * 1e3,
+           "autotuned_slabs": {f"{k[0]}x{k[1]}": {"slabs": v["slabs"], "ms_per_sample": v["ms"]} for k, v in tuned.items()},
+           "per_size": {}}
     for h in MIXED_SIZES:
         key = (h, h)
         t = batches[key]
@@ -668,6 +672,7 @@ def main():
     ppp = "rule: 8 for uint8 without background"
     if not args.no_autotune:
         ppp = plan.autotune(pats_d.data_ptr(), _lib.EBSD_U8, min(N, 16384), method, stream=stream.cuda_stream)
+    radon_tile = plan.get_tile()
     plan.reserve(method, N)
 
     def launch(st):
@@ -916,7 +921,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": WORKLOAD,
                        "method": method, "patterns_per_step": N, "distinct_patterns": len(pool),
-                       "patterns_per_block_pass": ppp, "cuda_graph": graph is not None,
+                       "patterns_per_block_pass": ppp, "radon_tile": radon_tile, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "accuracy": acc,
             "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,

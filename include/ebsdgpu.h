@@ -157,11 +157,15 @@ int64_t ebsd_last_launch_count(ebsd_plan_t plan);
 
 /* Autotuner -- no counterpart in the reference, whose OpenCL path sizes its work by fixed
  * rules (band_detect_cl.py:252-286).  Times the fused-kernel variants that give identical
- * records for (method, dtype) -- one, two, four or eight patterns per block pass -- on the caller's
- * device-resident sample d_pats [n][H][W] and keeps the faster in the plan for later calls.
- * Writes the choice to *patterns_per_pass (may be NULL); 1 when only one variant applies
- * (per-stage methods, uint16/float32 input, a fitted background, FP16 storage).
- * Synchronous on `stream`; allocates temporary outputs. */
+ * records for (method, dtype) on the caller's device-resident sample d_pats [n][H][W] and keeps
+ * the fastest in the plan for later calls.  The variants are the Radon tile shapes the plan
+ * can take: the whole padded Radon image as one tile with one, two, four or eight patterns per
+ * block pass (uint8 input), and, for EBSD_FUSED_F32, theta slabs -- the widest slabs that fit
+ * and up to three narrower slab counts.  Writes the patterns per pass of the choice to
+ * *patterns_per_pass (may be NULL; 1 for slabs and where only one pass width applies:
+ * per-stage methods, uint16/float32 input, a fitted background, FP16 storage); the tile
+ * shape is read back with ebsd_plan_get_tile.  Synchronous on `stream`; allocates temporary
+ * outputs. */
 int ebsd_plan_autotune(ebsd_plan_t plan, int method, int dtype, const void* d_pats, int64_t n,
                        void* stream, int* patterns_per_pass);
 
@@ -169,6 +173,28 @@ int ebsd_plan_autotune(ebsd_plan_t plan, int method, int dtype, const void* d_pa
  * a call allows), or 0 for the rule (the most a call allows).  For callers that tuned
  * offline; no counterpart in the reference.  Records do not depend on the choice. */
 int ebsd_plan_set_patterns_per_pass(ebsd_plan_t plan, int patterns_per_pass);
+
+/* The plan's Radon tile shape for EBSD_FUSED_F32 calls (no counterpart in the reference). */
+typedef struct {
+    int tile;               /* 1: the whole padded Radon image as one tile (when it fits);
+                               2: theta slabs; 0: neither fits (per-stage methods only) */
+    int patterns_per_pass;  /* one tile, uint8 input: 1, 2, 4 or 8 as pinned, 0 the rule */
+    int slabs;              /* slab count of the plan's slab tables (0: the plan has none) */
+    int slab_columns;       /* output theta columns of the widest slab */
+    int slabs_min;          /* widest slabs that fit */
+    int slabs_max;          /* narrowest slabs that still hold the filters' theta reach */
+    int single_fits;        /* 1 when the one-tile kernel can take the plan */
+} ebsd_tile_info;
+
+int ebsd_plan_get_tile(ebsd_plan_t plan, ebsd_tile_info* info);
+
+/* Pins the Radon tile shape for later EBSD_FUSED_F32 calls: tile 1 one tile, 2 theta slabs,
+ * 0 the rule (one tile when it fits); slabs = the slab count for the slab tables, in
+ * [slabs_min, slabs_max], or 0 for the widest.  The slab tables also serve
+ * ebsd_find_bands_mixed.  EBSD_E_UNSUPPORTED for a shape the plan cannot take.  Waits for
+ * the device when it rebuilds the slab tables.  For callers that tuned offline; records do not
+ * depend on the choice. */
+int ebsd_plan_set_tile(ebsd_plan_t plan, int tile, int slabs);
 
 /* Band detection that allocates nothing -- no counterpart in the reference, which always
  * allocates per chunk (band_detect.py:425, band_detect_cl.py:252-286).  For callers that may

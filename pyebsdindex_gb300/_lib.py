@@ -41,6 +41,12 @@ class PlanDesc(C.Structure):
     ]
 
 
+class TileInfo(C.Structure):
+    _fields_ = [("tile", C.c_int), ("patterns_per_pass", C.c_int), ("slabs", C.c_int),
+                ("slab_columns", C.c_int), ("slabs_min", C.c_int), ("slabs_max", C.c_int),
+                ("single_fits", C.c_int)]
+
+
 class Bands(C.Structure):
     _fields_ = [
         ("max", C.c_void_p), ("normmax", C.c_void_p), ("maxloc", C.c_void_p), ("avemax", C.c_void_p),
@@ -101,6 +107,10 @@ def load():
         lib.ebsd_plan_host_input_in_place.restype = C.c_int
         lib.ebsd_plan_set_patterns_per_pass.argtypes = [P, C.c_int]
         lib.ebsd_plan_set_patterns_per_pass.restype = C.c_int
+        lib.ebsd_plan_get_tile.argtypes = [P, C.POINTER(TileInfo)]
+        lib.ebsd_plan_get_tile.restype = C.c_int
+        lib.ebsd_plan_set_tile.argtypes = [P, C.c_int, C.c_int]
+        lib.ebsd_plan_set_tile.restype = C.c_int
         lib.ebsd_strerror.argtypes = [C.c_int]
         lib.ebsd_strerror.restype = C.c_char_p
         lib.ebsd_version.argtypes = []
@@ -186,6 +196,19 @@ class DevicePlan:
         """Pin the fused kernel's patterns per block pass (1, 2, 4, 8; 0 = rule)."""
         check(self._lib.ebsd_plan_set_patterns_per_pass(self.handle, int(ppp)), "ebsd_plan_set_patterns_per_pass")
 
+    def get_tile(self) -> dict:
+        """The Radon tile shape FP32 fused calls take (``ebsd_plan_get_tile``): ``tile`` 1 one
+        tile, 2 theta slabs, 0 neither; ``patterns_per_pass`` (0 = rule), ``slabs`` (the slab
+        tables' count), ``slab_columns``, ``slabs_min`` / ``slabs_max``, ``single_fits``."""
+        t = TileInfo()
+        check(self._lib.ebsd_plan_get_tile(self.handle, C.byref(t)), "ebsd_plan_get_tile")
+        return {f: int(getattr(t, f)) for f, _ in TileInfo._fields_}
+
+    def set_tile(self, tile: int, slabs: int = 0):
+        """Pin the Radon tile shape: ``tile`` 1 one tile, 2 theta slabs, 0 the rule; ``slabs``
+        the slab count (0 = the widest that fit)."""
+        check(self._lib.ebsd_plan_set_tile(self.handle, int(tile), int(slabs)), "ebsd_plan_set_tile")
+
     def set_host_input(self, mode: int):
         """Pinned host input: -1 read in place on coherent CPU-GPU links (default), 0 copy, 1 in place."""
         check(self._lib.ebsd_plan_set_host_input(self.handle, int(mode)), "ebsd_plan_set_host_input")
@@ -197,8 +220,10 @@ class DevicePlan:
         return r == 1
 
     def autotune(self, pats_ptr: int, dtype: int, n: int, method, stream=0) -> int:
-        """Time the record-identical kernel variants on a device-resident sample and keep the
-        faster in the plan; returns the chosen patterns per block pass (1, 2, 4 or 8)."""
+        """Time the record-identical kernel variants (Radon tile shapes: one tile with 1, 2, 4
+        or 8 patterns per block pass, theta slabs of several widths) on a device-resident sample
+        and keep the fastest in the plan; returns the chosen patterns per block pass (1, 2, 4 or
+        8; 1 for slabs).  ``get_tile()`` reads the chosen shape."""
         ppp = C.c_int(0)
         check(self._lib.ebsd_plan_autotune(self.handle, method_id(method), int(dtype), C.c_void_p(int(pats_ptr)),
                                            int(n), C.c_void_p(int(stream)), C.byref(ppp)), "ebsd_plan_autotune")

@@ -222,10 +222,13 @@ class GPUFindBands:
         return self._records(soa, int(pats.shape[0])), normals.cpu().numpy()
 
     def autotune(self, sample, method=None, gpu_id=None, cache=None):
-        """Time the record-identical variants of the fused kernel (one, two, four or eight patterns per
-        block pass) on ``sample`` ([n, H, W] numpy or torch, uint8/uint16/float32) and keep
-        the faster in the device plan for later ``find_bands`` calls.  No counterpart in the
-        reference.  Returns the chosen patterns per pass.
+        """Time the record-identical variants of the fused kernel on ``sample`` ([n, H, W]
+        numpy or torch, uint8/uint16/float32) and keep the fastest in the device plan for later
+        ``find_bands`` calls.  The variants are Radon tile shapes: the whole padded Radon image
+        as one tile with one, two, four or eight patterns per block pass, and theta slabs of
+        several widths (``DevicePlan.get_tile`` reads the choice back; it is also kept in
+        ``self.tuned``).  No counterpart in the reference.  Returns the chosen patterns per
+        pass (1 for slabs).
 
         ``cache``: None (default) times every call; a JSON file name, or True for
         ``tuning.default_path()``, keeps the decision per GPU, library version, plan geometry,
@@ -254,13 +257,25 @@ class GPUFindBands:
             hit = store.get(key)
             if hit is not None and int(hit.get("patterns_per_pass", 0)) in (1, 2, 4, 8):
                 ppp = int(hit["patterns_per_pass"])
-                plan.set_patterns_per_pass(ppp)
-                return ppp
+                tile, slabs = int(hit.get("tile", 0)), int(hit.get("slabs", 0))
+                try:
+                    if tile in (1, 2):
+                        plan.set_tile(tile, slabs if tile == 2 else 0)
+                    plan.set_patterns_per_pass(ppp)
+                except RuntimeError:
+                    hit = None  # a shape this plan cannot take: tune afresh
+                if hit is not None:
+                    self.tuned = dict(plan.get_tile(), patterns_per_pass=ppp, cached=True)
+                    return ppp
         t = t.to(dev).contiguous()
         stream = torch.cuda.current_stream(dev).cuda_stream
         ppp = plan.autotune(t.data_ptr(), dt, int(t.shape[0]), m, stream=stream)
+        info = plan.get_tile()
+        self.tuned = dict(info, patterns_per_pass=int(ppp), cached=False)
         if store is not None:
-            store.put(key, {"patterns_per_pass": int(ppp), "timed_patterns": int(t.shape[0])})
+            store.put(key, {"patterns_per_pass": int(ppp), "tile": info["tile"],
+                            "slabs": info["slabs"] if info["tile"] == 2 else 0,
+                            "timed_patterns": int(t.shape[0])})
         return ppp
 
     def _tuning_key(self, plan, method, dtype):
@@ -472,6 +487,21 @@ class BandDetect(GPUFindBands):
         return np.sqrt(np.broadcast_to(cx.reshape(1, nx), (ny, nx)) + np.broadcast_to(cy, (nx, ny)).T)
 
 
+def _device_input(t, dev):
+    """(contiguous CUDA tensor on ``dev``, EBSD_* input code) for a pattern batch: uint8 and
+    uint16 as they are, anything else as float32."""
+    import torch
+    u16 = getattr(torch, "uint16", None)
+    if t.dtype == torch.uint8:
+        dt = _lib.EBSD_U8
+    elif u16 is not None and t.dtype == u16:
+        dt = _lib.EBSD_U16
+    else:
+        t = t.to(torch.float32)
+        dt = _lib.EBSD_F32
+    return t.to(dev).contiguous(), dt
+
+
 def _sample_picks(n, want, method):
     """Indices of the background sample: ``want`` of ``n`` at random without replacement,
     sorted ('randomStride'), or every int(n / want)-th ('evenStride'); None for another
@@ -589,22 +619,11 @@ class MixedBandDetect:
         dev = torch.device("cuda", self.gpu_id)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
         m = method or self.method
-        u16 = getattr(torch, "uint16", None)
         ins, dts = {}, set()
         for key, t in batches.items():
-            if t.dtype == torch.uint8:
-                dt = _lib.EBSD_U8
-            elif u16 is not None and t.dtype == u16:
-                dt = _lib.EBSD_U16
-            else:
-                t = t.to(torch.float32)
-                dt = _lib.EBSD_F32
-            ins[key] = (t.to(dev).contiguous(), dt)
-            dts.add(dt)
-        outs = {key: {f: torch.empty((t.shape[0], self.nBands, 2) if f in ("maxloc", "aveloc")
-                                     else (t.shape[0], self.nBands),
-                                     dtype=torch.int8 if f == "valid" else torch.float32, device=dev)
-                      for f in _lib.BAND_FIELDS} for key, (t, _) in ins.items()}
+            ins[key] = _device_input(t, dev)
+            dts.add(ins[key][1])
+        outs = {key: self._device_outputs(t.shape[0], dev) for key, (t, _) in ins.items()}
         plans = {key: self.plan(*key)._device_plan() for key in ins}
         dt0 = next(iter(dts)) if len(dts) == 1 else None
         mixed = (m in ("fused", "fused32") and dt0 is not None and 1 <= len(ins) <= self.MAX_MIXED
@@ -627,6 +646,52 @@ class MixedBandDetect:
             plans[key].find_bands_device(t.data_ptr(), dt, t.shape[0], {f: v.data_ptr() for f, v in outs[key].items()},
                                          mk, stream=st.cuda_stream)
         return outs
+
+    def _device_outputs(self, n, dev):
+        import torch
+        return {f: torch.empty((n, self.nBands, 2) if f in ("maxloc", "aveloc") else (n, self.nBands),
+                               dtype=torch.int8 if f == "valid" else torch.float32, device=dev)
+                for f in _lib.BAND_FIELDS}
+
+    def autotune(self, batches, stream=None, max_extra=3):
+        """Choose each size's theta-slab width for the one-launch mixed path.  For every size in
+        ``batches`` ({(H, W): CUDA tensor [n, H, W]}, a sample of each), the slab counts from
+        the widest slabs that fit to ``max_extra`` narrower ones are timed on that size alone
+        (the slab kernel, CUDA events on ``stream``, best of two runs after a warm-up), and the
+        fastest count's tables are kept in the size's plan (``ebsd_plan_set_tile``); calls of
+        one size keep the rule (one tile when it fits).  Records do not depend on the choice.
+        No counterpart in the reference.  Returns {(H, W): {"slabs": count, "ms": {count: ms}}}."""
+        import torch
+        dev = torch.device("cuda", self.gpu_id)
+        st = stream if stream is not None else torch.cuda.current_stream(dev)
+        chosen = {}
+        for key, t in batches.items():
+            t, dt = _device_input(t, dev)
+            plan = self.plan(*key)._device_plan()
+            info = plan.get_tile()
+            if info["slabs"] == 0 or not plan.supported("fused", dt):
+                continue
+            outs = {f: v.data_ptr() for f, v in self._device_outputs(t.shape[0], dev).items()}
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            times = {}
+            try:
+                for ns in range(info["slabs_min"], min(info["slabs_max"], info["slabs_min"] + max_extra) + 1):
+                    plan.set_tile(2, ns)
+                    best = None
+                    for rep in range(3):
+                        e0.record(st)
+                        plan.find_bands_device(t.data_ptr(), dt, t.shape[0], outs, "fused", stream=st.cuda_stream)
+                        e1.record(st)
+                        e1.synchronize()
+                        if rep > 0:
+                            ms = e0.elapsed_time(e1)
+                            best = ms if best is None else min(best, ms)
+                    times[ns] = best
+            finally:
+                pick = min(times, key=times.get) if times else 0
+                plan.set_tile(0, pick)
+            chosen[key] = {"slabs": pick, "ms": times}
+        return chosen
 
     def find_bands_grouped(self, batches, method=None):
         """batches: {(H, W): [n, H, W] array (numpy or CUDA tensor)} -> {(H, W): record array}."""

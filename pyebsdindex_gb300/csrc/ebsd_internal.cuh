@@ -44,6 +44,21 @@ struct SlabGeom {
     int TR = 0, TBP = 0, CCP = 0, MP = 0, rho0 = 0, rpad_end = 0, CR = 0, statR = 0;
     int pitch = 0;              // pattern tile row pitch (elements)
     int smem[3] = {0, 0, 0};    // dynamic shared memory bytes per dtype (uint8, uint16, float32)
+    int nslab_min = 0, nslab_max = 0;  // slab counts whose tiles fit (nslab_min: the widest slabs)
+};
+
+// Host copy of the slab kernel's per-source-group LUT slots (one group = 32 neighbouring rho at
+// one theta), kept with the plan so that the slab count can be changed after plan creation
+// (ebsd_plan_set_tile, ebsd_plan_autotune) without the reference's lookup table.
+struct SlabSource {
+    int gpt = 0, nsrc = 0;
+    int TR = 0, CR = 0, rho0 = 0, rpad_end = 0, statR = 0, pitch = 0;
+    size_t pat_elems = 0;
+    uint16_t zero = 0;                 // element offset of the tile's zero element
+    std::vector<int> gch;              // [nsrc] 8-slot chunks per group
+    std::vector<size_t> goff;          // [nsrc] first slot of the group in `slots`
+    std::vector<uint16_t> slots;       // per group: [chunk][lane][8] element offsets
+    std::vector<int32_t> count;        // [nsrc * 32] entries per ray
 };
 
 struct Workspace {
@@ -101,6 +116,10 @@ struct ebsd_plan_s {
     uint16_t* d_slut = nullptr;    // per-slab, per-warp LUT streams (pattern element offsets)
     int32_t* d_stab = nullptr;     // [gst][gtb][slab_g][slab_j][wofs][count]
     int32_t s_gst = 0, s_gtb = 0, s_slabg = 0, s_slabj = 0, s_wofs = 0, s_count = 0;  // offsets into d_stab
+    ebsd::SlabSource* ssrc = nullptr;  // host slots for re-layout (slab.cu)
+    // FP32 fused calls that both kernels can serve: 0 rule (the single tile when it fits),
+    // 1 the single tile, 2 theta slabs (ebsd_plan_set_tile, ebsd_plan_autotune)
+    int tile_mode = 0;
 
     // ---- workspaces ----
     std::mutex mtx;
@@ -183,8 +202,13 @@ int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, i
 
 // Theta-slab fused path: slab.cu -----------------------------------------------------------
 int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d);
+// Rebuild the slab tables for nslab slabs (0: the widest slabs that fit); EBSD_E_UNSUPPORTED
+// when the plan has no slab tables or nslab is out of [nslab_min, nslab_max].  Waits for the
+// device before it frees the old tables.
+int slab_relayout(ebsd_plan_s* p, int nslab);
 void slab_release(ebsd_plan_s* p);
-// the slab kernel serves this (method, dtype): FP32 method, plan too large for the single tile
+// the slab kernel serves this (method, dtype): FP32 method, and the plan too large for the
+// single tile or set to theta slabs (tile_mode 2)
 bool slab_serves(const ebsd_plan_s* p, int method, int dtype);
 int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
                    int64_t out_offset, cudaStream_t st, int64_t* launches);

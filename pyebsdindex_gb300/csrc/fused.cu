@@ -1265,10 +1265,8 @@ int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
     if (n <= 0) return EBSD_OK;
-    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) {
-        if (!slab_serves(p, method, dtype)) return EBSD_E_UNSUPPORTED;
-        return slab_run_chunk(p, dtype, d_pats, n, out, out_offset, st, launches);
-    }
+    if (slab_serves(p, method, dtype)) return slab_run_chunk(p, dtype, d_pats, n, out, out_offset, st, launches);
+    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) return EBSD_E_UNSUPPORTED;
     const int pack = fused_patterns_per_pass(p, method, dtype, n);
     void* fn = pick_kernel(method, dtype, p->k0, p->k1, pack, p->nTheta);
     if (!fn) return EBSD_E_UNSUPPORTED;

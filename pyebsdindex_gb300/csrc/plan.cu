@@ -659,7 +659,8 @@ int ebsd_method_supported_for(ebsd_plan_t p, int method, int dtype) {
     if (is_plain(method)) return 1;
     if (!is_fused(method)) return EBSD_E_ARG;
     if (!fused_supported(p, method)) return 0;
-    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) return slab_serves(p, method, dtype) ? 1 : 0;
+    if (slab_serves(p, method, dtype)) return 1;
+    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) return 0;
     return 1;
 }
 
@@ -835,6 +836,36 @@ int ebsd_plan_set_patterns_per_pass(ebsd_plan_t p, int ppp) {
     return EBSD_OK;
 }
 
+int ebsd_plan_set_tile(ebsd_plan_t p, int tile, int slabs) {
+    if (!p || tile < 0 || tile > 2 || slabs < 0) return EBSD_E_ARG;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    if (tile == 1 && !p->fg.ok_f32) return EBSD_E_UNSUPPORTED;
+    if ((tile == 2 || slabs > 0) && !p->sg.ok) return EBSD_E_UNSUPPORTED;
+    if (p->sg.ok) {
+        if (cudaSetDevice(p->device) != cudaSuccess) return EBSD_E_DEVICE;
+        const int rc = slab_relayout(p, slabs);
+        if (rc != EBSD_OK) return rc;
+    }
+    p->tile_mode = tile;
+    return EBSD_OK;
+}
+
+int ebsd_plan_get_tile(ebsd_plan_t p, ebsd_tile_info* info) {
+    if (!p || !info) return EBSD_E_ARG;
+    std::lock_guard<std::mutex> lk(p->mtx);
+    ebsd_tile_info t;
+    std::memset(&t, 0, sizeof(t));
+    t.single_fits = p->fg.ok_f32 ? 1 : 0;
+    t.tile = p->fg.ok_f32 ? (p->tile_mode == 2 && p->sg.ok ? 2 : 1) : (p->sg.ok ? 2 : 0);
+    t.patterns_per_pass = p->fused_ppp > 0 ? p->fused_ppp : 0;
+    t.slabs = p->sg.ok ? p->sg.nslab : 0;
+    t.slab_columns = p->sg.ok ? p->sg.Ts : 0;
+    t.slabs_min = p->sg.ok ? p->sg.nslab_min : 0;
+    t.slabs_max = p->sg.ok ? p->sg.nslab_max : 0;
+    *info = t;
+    return EBSD_OK;
+}
+
 int ebsd_plan_autotune(ebsd_plan_t p, int method, int dtype, const void* d_pats, int64_t n,
                        void* stream, int* patterns_per_pass) {
     if (!p || n <= 0 || !d_pats) return EBSD_E_ARG;
@@ -850,13 +881,40 @@ int ebsd_plan_autotune(ebsd_plan_t p, int method, int dtype, const void* d_pats,
     }
     rc = reserve(p, method, n);
     if (rc != EBSD_OK) return rc;
+    // the candidates, which give identical records: the single tile with 8, 4, 2 or 1 patterns
+    // per block pass, and theta slabs from the widest that fit to three more
+    struct Cand {
+        int tile, v;  // tile 1: v = patterns per pass; tile 2: v = slab count
+    };
+    std::vector<Cand> cands;
+    const int old_mode = p->tile_mode, old_slabs = p->sg.ok ? p->sg.nslab : 0;
     p->fused_ppp = -1;
-    const int maxp = fused_patterns_per_pass(p, method, dtype, n);
-    if (maxp == 1) {  // one variant only
-        if (patterns_per_pass) *patterns_per_pass = 1;
-        return EBSD_OK;
+    const bool single = method != EBSD_FUSED_F32 || p->fg.ok_f32;
+    if (single) {
+        p->tile_mode = 1;
+        const int maxp = fused_patterns_per_pass(p, method, dtype, n);
+        for (int ppp = maxp; ppp >= 1; ppp /= 2) cands.push_back(Cand{1, ppp});
     }
-    // time the variants (they give identical records) on the caller's sample
+    if (method == EBSD_FUSED_F32 && p->sg.ok && (dtype != EBSD_F32 || p->sg.ok_f32))
+        for (int ns = p->sg.nslab_min; ns <= std::min(p->sg.nslab_max, p->sg.nslab_min + 3); ++ns)
+            cands.push_back(Cand{2, ns});
+    auto apply = [&](const Cand& c) -> int {
+        if (c.tile == 1) {
+            p->tile_mode = 1;
+            p->fused_ppp = c.v;
+            return EBSD_OK;
+        }
+        p->tile_mode = 2;
+        p->fused_ppp = -1;
+        return slab_relayout(p, c.v);
+    };
+    if (cands.size() <= 1) {  // one variant only
+        if (!cands.empty()) rc = apply(cands[0]);
+        if (!single || cands.empty()) p->tile_mode = old_mode;
+        if (patterns_per_pass) *patterns_per_pass = cands.empty() || cands[0].tile != 1 ? 1 : cands[0].v;
+        return rc;
+    }
+    // time the variants on the caller's sample
     const size_t nb = (size_t)n * p->nB;
     char* buf = nullptr;
     EBSD_CUDA_TRY(cudaMalloc((void**)&buf, nb * (10 * sizeof(float) + 1) + 256));
@@ -872,12 +930,12 @@ int ebsd_plan_autotune(ebsd_plan_t p, int method, int dtype, const void* d_pats,
     dev.valid = (int8_t*)(dev.rho + nb);
     cudaEvent_t ev[2] = {nullptr, nullptr};
     float best_ms = 0.0f;
-    int best = maxp;
+    size_t best = 0;
     int64_t launches = 0;
     for (int i = 0; i < 2 && rc == EBSD_OK; ++i)
         if (cudaEventCreate(&ev[i]) != cudaSuccess) rc = EBSD_E_LAUNCH;
-    for (int ppp = maxp; ppp >= 1 && rc == EBSD_OK; ppp /= 2) {
-        p->fused_ppp = ppp;
+    for (size_t ci = 0; ci < cands.size() && rc == EBSD_OK; ++ci) {
+        rc = apply(cands[ci]);
         float ms_min = 0.0f;
         for (int rep = 0; rep < 3 && rc == EBSD_OK; ++rep) {  // first pass warms up
             if (cudaEventRecord(ev[0], st) != cudaSuccess) { rc = EBSD_E_LAUNCH; break; }
@@ -891,16 +949,23 @@ int ebsd_plan_autotune(ebsd_plan_t p, int method, int dtype, const void* d_pats,
             cudaEventElapsedTime(&ms, ev[0], ev[1]);
             if (rep > 0 && (rep == 1 || ms < ms_min)) ms_min = ms;
         }
-        if (rc == EBSD_OK && (ppp == maxp || ms_min < best_ms)) {
+        if (rc == EBSD_OK && (ci == 0 || ms_min < best_ms)) {
             best_ms = ms_min;
-            best = ppp;
+            best = ci;
         }
     }
     for (int i = 0; i < 2; ++i)
         if (ev[i]) cudaEventDestroy(ev[i]);
     cudaFree(buf);
-    p->fused_ppp = rc == EBSD_OK ? best : -1;
-    if (rc == EBSD_OK && patterns_per_pass) *patterns_per_pass = best;
+    if (rc == EBSD_OK) {
+        rc = apply(cands[best]);
+        if (rc == EBSD_OK && patterns_per_pass) *patterns_per_pass = cands[best].tile == 1 ? cands[best].v : 1;
+    } else {
+        // back to the settings before the call
+        p->fused_ppp = -1;
+        p->tile_mode = old_mode;
+        if (old_slabs) slab_relayout(p, old_slabs);
+    }
     return rc;
 }
 

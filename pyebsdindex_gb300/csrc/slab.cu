@@ -579,12 +579,161 @@ int slab_attr(const void* fn, int device, int smem) {
 
 }  // namespace
 
+namespace {
+
+// Slab geometry for nslab slabs of the plan's theta range, or false when the slabs are too
+// narrow for the filters' reach or their tiles do not fit (uint16 pattern tile).
+bool slab_geom_for(const ebsd_plan_s* p, const SlabSource& src, int nslab, int dev_smem, SlabGeom* out) {
+    const int D1 = p->k1, H1 = p->k1 / 2, halo = D1 + H1;
+    if (nslab < 1 || nslab > p->nTheta) return false;
+    const int ts = (p->nTheta + nslab - 1) / nslab;
+    // every slab (widths differ by at most one column) must hold the filters' reach
+    const int tmin = p->nTheta / nslab;
+    if (tmin < 2 * D1 + 1 || tmin < 16 || tmin < 2 * halo) return false;
+    SlabGeom g;
+    g.nslab = nslab;
+    g.Ts = ts;
+    g.TR = src.TR;
+    g.TBP = (ts + 2 * halo) | 1;
+    g.CCP = (ts + 2 * D1) | 1;
+    if ((size_t)g.TR * g.TBP >= 65536) return false;
+    g.MP = g.TBP;  // the theta-max rows sit in the Radon tile after the carried columns
+    g.rho0 = src.rho0;
+    g.rpad_end = src.rpad_end;
+    g.CR = src.CR;
+    g.statR = src.statR;
+    g.pitch = src.pitch;
+    g.maxg = (ts + 2 * halo) * src.gpt;
+    g.smem[0] = (int)slab_smem(src.pat_elems, 1, g.TR, g.TBP, g.CCP, g.maxg);
+    g.smem[1] = (int)slab_smem(src.pat_elems, 2, g.TR, g.TBP, g.CCP, g.maxg);
+    g.smem[2] = (int)slab_smem(src.pat_elems, 4, g.TR, g.TBP, g.CCP, g.maxg);
+    if (g.smem[1] > dev_smem) return false;
+    g.ok = 1;
+    g.ok_f32 = g.smem[2] <= dev_smem;
+    *out = g;
+    return true;
+}
+
+// Device tables of the geometry g: per slab, buffer columns [j0 - halo, j0 + ts + halo), the
+// slab's 32-ray groups balanced over the warps (longest first, each to the least-loaded warp).
+int slab_upload(ebsd_plan_s* p, const SlabSource& src, SlabGeom g) {
+    const int D1 = p->k1, H1 = p->k1 / 2, halo = D1 + H1;
+    const int nslab = g.nslab, gpt = src.gpt;
+    std::vector<int32_t> slab_j(nslab + 1), slab_g(nslab + 1, 0), wofs;
+    std::vector<uint32_t> gst, gtb;
+    std::vector<uint16_t> lut;
+    for (int s = 0; s <= nslab; ++s) slab_j[s] = (int)((int64_t)p->nTheta * s / nslab);
+    int maxg = 0;
+    for (int s = 0; s < nslab; ++s) {
+        const int j0 = slab_j[s], ts = slab_j[s + 1] - j0, TB = ts + 2 * halo;
+        if (ts < 2 * D1 + 1 || ts < 2 * halo) return EBSD_E_UNSUPPORTED;
+        struct Grp {
+            int src;
+            uint32_t tb;
+        };
+        std::vector<Grp> grps;
+        // slabs after the first take their first 2 * halo columns from the previous slab
+        for (int jb = s > 0 ? 2 * halo : 0; jb < TB; ++jb) {
+            const int jc = j0 - halo + jb;
+            const bool flip = jc < 0 || jc >= p->nTheta;
+            const int js = ((jc % p->nTheta) + p->nTheta) % p->nTheta;
+            for (int b = 0; b < gpt; ++b) {
+                const int nval = std::min(32, p->nRho - 32 * b);
+                const int row = g.rho0 + (flip ? p->nRho - 1 - 32 * b : 32 * b);
+                const uint32_t offs = (uint32_t)(row * g.TBP + jb);
+                grps.push_back(Grp{js * gpt + b, offs | ((uint32_t)nval << 16) | ((flip ? 1u : 0u) << 22)});
+            }
+        }
+        maxg = std::max(maxg, (int)grps.size());
+        std::vector<int> order(grps.size());
+        for (size_t k = 0; k < grps.size(); ++k) order[k] = (int)k;
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int x, int y) { return src.gch[grps[x].src] > src.gch[grps[y].src]; });
+        std::vector<std::vector<int>> wg(kWarps);
+        std::vector<long> wload(kWarps, 0);
+        for (int k : order) {
+            const int w = (int)(std::min_element(wload.begin(), wload.end()) - wload.begin());
+            wg[w].push_back(k);
+            wload[w] += src.gch[grps[k].src];
+        }
+        std::vector<int32_t> wo(2 * (kWarps + 1), 0);
+        int gcount = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            wo[w] = gcount;
+            wo[kWarps + 1 + w] = (int32_t)(lut.size() / (32 * 8));
+            for (int k : wg[w]) {
+                const Grp& gr = grps[k];
+                gst.push_back((uint32_t)gr.src | ((uint32_t)src.gch[gr.src] << 16));
+                gtb.push_back(gr.tb);
+                const uint16_t* sl = src.slots.data() + src.goff[gr.src];
+                lut.insert(lut.end(), sl, sl + (size_t)src.gch[gr.src] * 32 * 8);
+                ++gcount;
+            }
+            lut.insert(lut.end(), (size_t)kRing * 32 * 8, src.zero);  // the ring's unconditional loads
+        }
+        wo[kWarps] = gcount;
+        wo[2 * kWarps + 1] = (int32_t)(lut.size() / (32 * 8));
+        wofs.insert(wofs.end(), wo.begin(), wo.end());
+        slab_g[s + 1] = slab_g[s] + gcount;
+    }
+    if (maxg > g.maxg) return EBSD_E_UNSUPPORTED;
+    // device tables: [gst][gtb][slab_g][slab_j][wofs][count], each part 16-byte aligned
+    std::vector<int32_t> tab;
+    auto part = [&](const int32_t* a, size_t cnt) {
+        const int32_t at = (int32_t)tab.size();
+        tab.insert(tab.end(), a, a + cnt);
+        while (tab.size() % 4) tab.push_back(0);
+        return at;
+    };
+    const int32_t o_gst = part((const int32_t*)gst.data(), gst.size());
+    const int32_t o_gtb = part((const int32_t*)gtb.data(), gtb.size());
+    const int32_t o_slabg = part(slab_g.data(), slab_g.size());
+    const int32_t o_slabj = part(slab_j.data(), slab_j.size());
+    const int32_t o_wofs = part(wofs.data(), wofs.size());
+    const int32_t o_count = part(src.count.data(), src.count.size());
+    int32_t* d_tab = nullptr;
+    uint16_t* d_lut = nullptr;
+    EBSD_CUDA_TRY(cudaMalloc((void**)&d_tab, tab.size() * sizeof(int32_t)));
+    if (cudaMalloc((void**)&d_lut, lut.size() * sizeof(uint16_t)) != cudaSuccess ||
+        cudaMemcpy(d_tab, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d_lut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d_tab);
+        cudaFree(d_lut);
+        return EBSD_E_NOMEM;
+    }
+    // launches already queued may still read the old tables
+    if (p->d_stab || p->d_slut) {
+        EBSD_CUDA_TRY(cudaDeviceSynchronize());
+        cudaFree(p->d_slut);
+        cudaFree(p->d_stab);
+    }
+    p->d_stab = d_tab;
+    p->d_slut = d_lut;
+    p->s_gst = o_gst;
+    p->s_gtb = o_gtb;
+    p->s_slabg = o_slabg;
+    p->s_slabj = o_slabj;
+    p->s_wofs = o_wofs;
+    p->s_count = o_count;
+    p->sg = g;
+    return EBSD_OK;
+}
+
+int device_smem_optin(int device) {
+    int dev_smem = 0;
+    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    return dev_smem;
+}
+
+}  // namespace
+
 // Plan-time tables for the slab kernel.  The LUT groups are those of the single-tile kernel:
 // 32 neighbouring rho at one theta, slot s of every lane at image column (or row) base + s when
 // each ray of the group has at most one pixel per column (row), as the reference's sampling
 // gives (radon_fast.py:113-158); a group that fits neither keeps each ray's sorted order.
 // Built for every plan whose geometry qualifies: the single-plan path uses it when the single
-// tile does not fit, the mixed-size launch (ebsd_find_bands_mixed) for every plan.
+// tile does not fit (or the plan is set to slabs), the mixed-size launch
+// (ebsd_find_bands_mixed) for every plan.  The widest slabs that fit are laid out first.
 int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     p->sg = SlabGeom{};
     const int K0 = p->k0, K1 = p->k1;
@@ -593,57 +742,54 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
           p->sep && p->bg_mode == 0 && p->nRho >= kRowBlock && p->nTheta >= 4 * (D1 + H1) &&
           p->p0 >= D0 + H0 && p->maxCount <= 255 && p->H <= 255 && p->W <= 255))
         return EBSD_OK;
-    const int pitch = p->W + 1;
-    const size_t pat_elems = (size_t)p->H * pitch + 1;
-    if (pat_elems > 65535) return EBSD_OK;  // element offsets in 16 bits
+    SlabSource* src = new SlabSource;
+    src->pitch = p->W + 1;
+    src->pat_elems = (size_t)p->H * src->pitch + 1;
+    if (src->pat_elems > 65535) {  // element offsets in 16 bits
+        delete src;
+        return EBSD_OK;
+    }
     // padded-frame rows as the single-tile kernel: tile rows [row0, row1), conv rows [crow0, crow1)
     const int statR1 = std::min(p->R, p->Tp - p->p0);
     const int crow0 = p->p0 - D0, crow1 = std::max(p->p0 + p->nRho + D0, statR1);
     const int row0 = crow0 - H0, row1 = crow1 + H0;
-    const int TR = row1 - row0, CR = crow1 - crow0;
-    const int gpt = (p->nRho + 31) / 32;
-    const int halo = D1 + H1;
-    int dev_smem = 0;
-    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
-    // widest slab whose uint16 tiles fit; slabs of near-equal width
-    int nslab = 0, Ts = 0;
-    for (int ns = 1; ns <= p->nTheta; ++ns) {
-        const int ts = (p->nTheta + ns - 1) / ns;
-        if (ts < 2 * D1 + 1 || ts < 16 || ts < 2 * halo) break;
-        const int TBP = (ts + 2 * halo) | 1, CCP = (ts + 2 * D1) | 1;
-        const int maxg = (ts + 2 * halo) * gpt;
-        if ((size_t)TR * TBP >= 65536) continue;
-        if (slab_smem(pat_elems, 2, TR, TBP, CCP, maxg) <= (size_t)dev_smem) {
-            nslab = ns;
-            Ts = ts;
-            break;
-        }
-    }
-    if (!nslab) return EBSD_OK;
+    src->TR = row1 - row0;
+    src->CR = crow1 - crow0;
+    src->rho0 = p->p0 - row0;
+    src->rpad_end = p->R - row0;
+    src->statR = statR1 - p->p0;
+    src->gpt = (p->nRho + 31) / 32;
+    const int gpt = src->gpt;
+
+    // the slab counts whose tiles fit
+    const int dev_smem = device_smem_optin(p->device);
     SlabGeom g;
-    g.nslab = nslab;
-    g.Ts = Ts;
-    g.TR = TR;
-    g.TBP = (Ts + 2 * halo) | 1;
-    g.CCP = (Ts + 2 * D1) | 1;
-    g.MP = g.TBP;  // the theta-max rows sit in the Radon tile after the carried columns
-    g.rho0 = p->p0 - row0;
-    g.rpad_end = p->R - row0;
-    g.CR = CR;
-    g.statR = statR1 - p->p0;
-    g.pitch = pitch;
-    g.maxg = (Ts + 2 * halo) * gpt;
-    g.smem[0] = (int)slab_smem(pat_elems, 1, TR, g.TBP, g.CCP, g.maxg);
-    g.smem[1] = (int)slab_smem(pat_elems, 2, TR, g.TBP, g.CCP, g.maxg);
-    g.smem[2] = (int)slab_smem(pat_elems, 4, TR, g.TBP, g.CCP, g.maxg);
+    int nmin = 0, nmax = 0;
+    for (int ns = 1; ns <= p->nTheta; ++ns) {
+        SlabGeom t;
+        if (!slab_geom_for(p, *src, ns, dev_smem, &t)) {
+            if (nmin) break;
+            continue;
+        }
+        if (!nmin) {
+            nmin = ns;
+            g = t;
+        }
+        nmax = ns;
+    }
+    if (!nmin) {
+        delete src;
+        return EBSD_OK;
+    }
 
     // per source group (theta j, rho block b): chunks, and each lane's slot -> element offset
     const int L = d->lut_len;
     const int nsrc = p->nTheta * gpt;
-    const uint16_t zero = (uint16_t)(p->H * pitch);
-    std::vector<int> gch(nsrc, 1);
-    std::vector<std::vector<uint16_t>> gslots(nsrc);  // [chunk][lane][8]
-    std::vector<int32_t> count((size_t)nsrc * 32, 0);
+    src->nsrc = nsrc;
+    src->zero = (uint16_t)(p->H * src->pitch);
+    src->gch.assign(nsrc, 1);
+    src->goff.assign(nsrc, 0);
+    src->count.assign((size_t)nsrc * 32, 0);
     std::vector<char> seen((size_t)std::max(p->W, p->H));
     for (int gs = 0; gs < nsrc; ++gs) {
         const int j = gs / gpt, i0 = (gs % gpt) * 32;
@@ -653,7 +799,7 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
             const int64_t* ray = d->lut + ((size_t)(i0 + l) * p->nTheta + j) * L;
             int c = 0;
             while (c < L && ray[c] >= 0 && ray[c] < p->nPx) ++c;
-            count[(size_t)gs * 32 + l] = c;
+            src->count[(size_t)gs * 32 + l] = c;
             maxc = std::max(maxc, c);
             std::fill(seen.begin(), seen.end(), 0);
             for (int k = 0; k < c; ++k) {
@@ -684,98 +830,43 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
             base = ymin;
             nslot = ymax - ymin + 1;
         }
-        gch[gs] = std::max(1, (nslot + 7) / 8);
-        std::vector<uint16_t>& sl = gslots[gs];
-        sl.assign((size_t)gch[gs] * 32 * 8, zero);
+        src->gch[gs] = std::max(1, (nslot + 7) / 8);
+        src->goff[gs] = src->slots.size();
+        src->slots.resize(src->slots.size() + (size_t)src->gch[gs] * 32 * 8, src->zero);
+        uint16_t* sl = src->slots.data() + src->goff[gs];
         for (int l = 0; l < 32 && i0 + l < p->nRho; ++l) {
             const int64_t* ray = d->lut + ((size_t)(i0 + l) * p->nTheta + j) * L;
-            for (int k = 0; k < count[(size_t)gs * 32 + l]; ++k) {
+            for (int k = 0; k < src->count[(size_t)gs * 32 + l]; ++k) {
                 const int idx = (int)ray[k], y = idx / p->W, x = idx - y * p->W;
                 const int slot = axis == 0 ? x - base : (axis == 1 ? y - base : k);
-                sl[((size_t)(slot / 8) * 32 + l) * 8 + slot % 8] = (uint16_t)(y * pitch + x);
+                sl[((size_t)(slot / 8) * 32 + l) * 8 + slot % 8] = (uint16_t)(y * src->pitch + x);
             }
         }
     }
-
-    // per slab: buffer columns [j0 - halo, j0 + ts + halo), groups balanced over the warps
-    std::vector<int32_t> slab_j(nslab + 1), slab_g(nslab + 1, 0), wofs;
-    std::vector<uint32_t> gst, gtb;
-    std::vector<uint16_t> lut;
-    for (int s = 0; s <= nslab; ++s) slab_j[s] = (int)((int64_t)p->nTheta * s / nslab);
-    int maxg = 0;
-    for (int s = 0; s < nslab; ++s) {
-        const int j0 = slab_j[s], ts = slab_j[s + 1] - j0, TB = ts + 2 * halo;
-        if (ts < 2 * D1 + 1 || ts < 2 * halo) return EBSD_OK;
-        struct Grp {
-            int src;
-            uint32_t tb;
-        };
-        std::vector<Grp> grps;
-        // slabs after the first take their first 2 * halo columns from the previous slab
-        for (int jb = s > 0 ? 2 * halo : 0; jb < TB; ++jb) {
-            const int jc = j0 - halo + jb;
-            const bool flip = jc < 0 || jc >= p->nTheta;
-            const int js = ((jc % p->nTheta) + p->nTheta) % p->nTheta;
-            for (int b = 0; b < gpt; ++b) {
-                const int nval = std::min(32, p->nRho - 32 * b);
-                const int row = g.rho0 + (flip ? p->nRho - 1 - 32 * b : 32 * b);
-                const uint32_t offs = (uint32_t)(row * g.TBP + jb);
-                grps.push_back(Grp{js * gpt + b, offs | ((uint32_t)nval << 16) | ((flip ? 1u : 0u) << 22)});
-            }
-        }
-        maxg = std::max(maxg, (int)grps.size());
-        std::vector<int> order(grps.size());
-        for (size_t k = 0; k < grps.size(); ++k) order[k] = (int)k;
-        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return gch[grps[x].src] > gch[grps[y].src]; });
-        std::vector<std::vector<int>> wg(kWarps);
-        std::vector<long> wload(kWarps, 0);
-        for (int k : order) {
-            const int w = (int)(std::min_element(wload.begin(), wload.end()) - wload.begin());
-            wg[w].push_back(k);
-            wload[w] += gch[grps[k].src];
-        }
-        std::vector<int32_t> wo(2 * (kWarps + 1), 0);
-        int gcount = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            wo[w] = gcount;
-            wo[kWarps + 1 + w] = (int32_t)(lut.size() / (32 * 8));
-            for (int k : wg[w]) {
-                const Grp& gr = grps[k];
-                gst.push_back((uint32_t)gr.src | ((uint32_t)gch[gr.src] << 16));
-                gtb.push_back(gr.tb);
-                lut.insert(lut.end(), gslots[gr.src].begin(), gslots[gr.src].end());
-                ++gcount;
-            }
-            lut.insert(lut.end(), (size_t)kRing * 32 * 8, zero);  // the ring's unconditional loads
-        }
-        wo[kWarps] = gcount;
-        wo[2 * kWarps + 1] = (int32_t)(lut.size() / (32 * 8));
-        wofs.insert(wofs.end(), wo.begin(), wo.end());
-        slab_g[s + 1] = slab_g[s] + gcount;
+    g.nslab_min = nmin;
+    g.nslab_max = nmax;
+    const int rc = slab_upload(p, *src, g);
+    if (rc != EBSD_OK) {
+        delete src;
+        p->sg = SlabGeom{};
+        // a plan whose slab layout cannot be built keeps the other paths
+        return rc == EBSD_E_UNSUPPORTED ? EBSD_OK : rc;
     }
-    if (maxg > g.maxg) return EBSD_OK;
-    // device tables: [gst][gtb][slab_g][slab_j][wofs][count], each part 16-byte aligned
-    std::vector<int32_t> tab;
-    auto part = [&](const int32_t* src, size_t cnt) {
-        const int32_t at = (int32_t)tab.size();
-        tab.insert(tab.end(), src, src + cnt);
-        while (tab.size() % 4) tab.push_back(0);
-        return at;
-    };
-    p->s_gst = part((const int32_t*)gst.data(), gst.size());
-    p->s_gtb = part((const int32_t*)gtb.data(), gtb.size());
-    p->s_slabg = part(slab_g.data(), slab_g.size());
-    p->s_slabj = part(slab_j.data(), slab_j.size());
-    p->s_wofs = part(wofs.data(), wofs.size());
-    p->s_count = part(count.data(), count.size());
-    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_stab, tab.size() * sizeof(int32_t)));
-    EBSD_CUDA_TRY(cudaMemcpy(p->d_stab, tab.data(), tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
-    EBSD_CUDA_TRY(cudaMalloc((void**)&p->d_slut, lut.size() * sizeof(uint16_t)));
-    EBSD_CUDA_TRY(cudaMemcpy(p->d_slut, lut.data(), lut.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
-    g.ok = g.smem[1] <= dev_smem;
-    g.ok_f32 = g.smem[2] <= dev_smem;
-    p->sg = g;
+    p->ssrc = src;
     return EBSD_OK;
+}
+
+int slab_relayout(ebsd_plan_s* p, int nslab) {
+    if (!p->ssrc || !p->sg.ok) return EBSD_E_UNSUPPORTED;
+    const int nmin = p->sg.nslab_min, nmax = p->sg.nslab_max;
+    if (nslab == 0) nslab = nmin;
+    if (nslab < nmin || nslab > nmax) return EBSD_E_UNSUPPORTED;
+    if (nslab == p->sg.nslab) return EBSD_OK;
+    SlabGeom g;
+    if (!slab_geom_for(p, *p->ssrc, nslab, device_smem_optin(p->device), &g)) return EBSD_E_UNSUPPORTED;
+    g.nslab_min = nmin;
+    g.nslab_max = nmax;
+    return slab_upload(p, *p->ssrc, g);
 }
 
 void slab_release(ebsd_plan_s* p) {
@@ -784,11 +875,14 @@ void slab_release(ebsd_plan_s* p) {
     p->d_slut = nullptr;
     p->d_stab = nullptr;
     p->sg = SlabGeom{};
+    delete p->ssrc;
+    p->ssrc = nullptr;
 }
 
 bool slab_serves(const ebsd_plan_s* p, int method, int dtype) {
-    if (method != EBSD_FUSED_F32 || !p->sg.ok || p->fg.ok_f32) return false;
-    return dtype != EBSD_F32 || p->sg.ok_f32;
+    if (method != EBSD_FUSED_F32 || !p->sg.ok) return false;
+    if (dtype == EBSD_F32 && !p->sg.ok_f32) return false;
+    return !p->fg.ok_f32 || p->tile_mode == 2;
 }
 
 namespace {

@@ -1,7 +1,8 @@
 """Persisted autotuner decisions.
 
-``BandDetect.autotune`` times the record-identical variants of the fused kernel (one, two,
-four or eight patterns per block pass) on a sample.  With ``cache=`` the decision is stored in
+``BandDetect.autotune`` times the record-identical variants of the fused kernel -- Radon tile
+shapes: the whole padded Radon image as one tile with one, two, four or eight patterns per block
+pass, and theta slabs of several widths -- on a sample.  With ``cache=`` the decision is stored in
 a JSON file keyed by everything that can change it -- the GPU (name and SM count), the
 library version, the pattern shape and input type, the Radon geometry (nTheta, nRho, nBands,
 LoG size, padding, a digest of the lookup table, background) and the method -- and a later
@@ -9,7 +10,9 @@ call with the same key applies the stored choice without timing anything.  The r
 no autotuner; its nearest counterpart sizes GPU chunks from the device's memory
 (``__optimizegpuchunk__``, _ebsd_index_parallel.py:768-828) each run.
 
-File layout: ``{"format": 1, "entries": {key: {"patterns_per_pass": p, "timed_patterns": n}}}``.
+File layout: ``{"format": 1, "entries": {key: {"patterns_per_pass": p, "tile": t, "slabs": s,
+"timed_patterns": n}}}`` (tile 1: one tile, 2: theta slabs, s slabs; entries written before the
+tile shape was tuned hold the patterns per pass alone and keep the plan's rule for the shape).
 Writes merge with what the file holds and replace it atomically, so processes that tune
 different plans can share one file.
 """

@@ -54,3 +54,12 @@ def test_plan_create_rejects_bad_descriptors(built_lib):
     d = _lib.PlanDesc()
     d.H = 0
     assert lib.ebsd_plan_create(ctypes.byref(d), 0, ctypes.byref(h)) == -1
+
+
+def test_tile_entries_reject_null_arguments(built_lib):
+    from pyebsdindex_gb300 import _lib
+    lib = _lib.load()
+    info = _lib.TileInfo()
+    assert lib.ebsd_plan_get_tile(None, ctypes.byref(info)) == -1
+    assert lib.ebsd_plan_set_tile(None, 1, 0) == -1
+    assert lib.ebsd_plan_set_patterns_per_pass(None, 1) == -1
