@@ -424,16 +424,19 @@ MIXED_SIZES = (60, 120, 240)
 def _mixed_part(args):
     h, start, count = args
     from pyebsdindex_gb300 import synthetic as syn
-    return syn.make_patterns(count, h, h, seed=3_000_000 + 1_000 * h, start=start, dtype=np.uint16, peak=4000.0,
-                             noise_frac=0.1)[0]
+    pats, _, noise_only = syn.make_patterns(count, h, h, seed=3_000_000 + 1_000 * h, start=start, dtype=np.uint16,
+                                            peak=4000.0, noise_frac=0.1)
+    return pats, noise_only
 
 
 def mixed_pools(ex, per_size):
-    """Seeded uint16 patterns (Poisson peak 4000 counts) per size of the mixed-size configuration."""
+    """Seeded uint16 patterns (Poisson peak 4000 counts) per size of the mixed-size configuration,
+    with the flags of the noise-only patterns: {h: (patterns, noise_only)}."""
     out = {}
     for h in MIXED_SIZES:
         parts = [(h, s, min(256, per_size - s)) for s in range(0, per_size, 256)]
-        out[h] = np.concatenate(list(ex.map(_mixed_part, parts)))
+        got = list(ex.map(_mixed_part, parts))
+        out[h] = (np.concatenate([g[0] for g in got]), np.concatenate([g[1] for g in got]))
     return out
 
 
@@ -441,18 +444,22 @@ def time_mixed(pools, n_total, steps, dev):
     """The mixed-size configuration: n_total uint16 patterns, one third each at 60x60, 120x120
     and 240x240 (nRho 1.5 * size, nTheta 180, nBands 10, circular mask), one persistent fused
     launch over all three sizes per step (MixedBandDetect / ebsd_find_bands_mixed), inputs
-    resident; then each size alone and the per-stage FP32 path for comparison, and the
-    accuracy of the mixed launch against the FP64 method (plain64) on 2,048 patterns per size."""
+    resident, each size's slab width autotuned first; then each size alone and the per-stage
+    FP32 path for comparison; and, on each size's pool of distinct patterns, the accuracy of the
+    mixed launch and of FP16 Radon storage (where a kernel has it) against the FP64 method
+    (plain64), with the FCC orientations indexed from each set of records compared with those
+    from the FP64 records."""
     import torch
     from pyebsdindex_gb300 import synthetic as syn
     from pyebsdindex_gb300.band_detect import MixedBandDetect
-    from pyebsdindex_gb300.accuracy import compare_records
+    from pyebsdindex_gb300 import _lib
+    from pyebsdindex_gb300.accuracy import compare_records, orientation_agreement
     mb = MixedBandDetect(nBands=10, mask_for=syn.circular_mask)
     each = n_total // len(MIXED_SIZES)
     batches = {}
     for h in MIXED_SIZES:
         # tiled as int16 (torch's uint16 has few device operations), then viewed as uint16
-        pd = torch.from_numpy(pools[h].view(np.int16)).to(dev)
+        pd = torch.from_numpy(pools[h][0].view(np.int16)).to(dev)
         reps = (each + pd.shape[0] - 1) // pd.shape[0]
         batches[(h, h)] = pd.repeat(reps, 1, 1)[:each].contiguous().view(torch.uint16)
     st = torch.cuda.current_stream(dev)
@@ -473,7 +480,7 @@ def time_mixed(pools, n_total, steps, dev):
     ms = ev[0].elapsed_time(ev[1]) / steps
     res = {"workload": f"{3 * each:,} uint16 patterns (Poisson peak 4000), one third each at 60x60 / 120x120 / "
                        "240x240, nRho 1.5*size, nTheta 180, nBands 10; pools of distinct seeded patterns per size "
-                       f"({pools[60].shape[0]}) tiled",
+                       f"({pools[60][0].shape[0]}) tiled",
            "one_launch": mixed, "ms_per_step": ms, "patterns_per_s": 3 * each / ms * 1e3,
            "autotuned_slabs": {f"{k[0]}x{k[1]}": {"slabs": v["slabs"], "ms_per_sample": v["ms"]} for k, v in tuned.items()},
            "per_size": {}}
@@ -499,13 +506,60 @@ def time_mixed(pools, n_total, steps, dev):
         e1.record(st)
         torch.cuda.synchronize()
         entry["plain_patterns_per_s"] = npl / e0.elapsed_time(e1) * 1e3
-        na = min(t.shape[0], 2048)
+        na = min(t.shape[0], pools[h][0].shape[0])
         plan.find_bands_device(t.data_ptr(), 1, na, {f: v.data_ptr() for f, v in po.items()}, "plain64", stream=st.cuda_stream)
         torch.cuda.synchronize()
         entry["accuracy_vs_plain64"] = dict(compare_records({f: v[:na] for f, v in outs[key].items()},
                                                             {f: v[:na] for f, v in po.items()}), patterns=na)
+        ref64 = {f: v[:na].clone() for f, v in po.items()}
+        # FP16 Radon storage, where a plan's FP16 tile fits on chip (the single-tile kernel)
+        if plan.supported("fused16", _lib.EBSD_U16):
+            plan.find_bands_device(t.data_ptr(), _lib.EBSD_U16, na, {f: v.data_ptr() for f, v in po.items()}, "fused16",
+                                   stream=st.cuda_stream)
+            torch.cuda.synchronize()
+            f16 = {f: v[:na].clone() for f, v in po.items()}
+            entry["fused16_accuracy_vs_plain64"] = dict(compare_records(f16, ref64), patterns=na)
+        else:
+            f16 = None
+            entry["fused16_accuracy_vs_plain64"] = ("no FP16-storage kernel at this size: the single-tile FP16 kernel "
+                                                    "does not fit on chip and the theta-slab kernel stores FP32")
+        # indexing agreement: FCC orientations (triplet voting on the device) from these records
+        # against those from the FP64 method's records, over the patterns that carry bands (the
+        # noise-only tenth has no orientation to agree on)
+        rho_max = mb.plan(h, h).rhoMax
+        bands = ~pools[h][1][:na]
+        q64, n64 = index_records(ref64, h, rho_max, st)
+        q32, n32 = index_records({f: v[:na] for f, v in outs[key].items()}, h, rho_max, st)
+        entry["indexing_vs_plain64"] = {"fused": orientation_agreement(q32[bands], n32[bands], q64[bands], n64[bands])}
+        if f16 is not None:
+            q16, n16 = index_records(f16, h, rho_max, st)
+            entry["indexing_vs_plain64"]["fused16"] = orientation_agreement(q16[bands], n16[bands], q64[bands],
+                                                                            n64[bands])
         res["per_size"][str(h)] = entry
     return res
+
+
+_INDEXER = None
+
+
+def index_records(recs, h, rho_max, stream):
+    """FCC orientations (quaternions, nMatch; numpy) of device band records of h x h patterns:
+    band normals (PC 0.46, 0.70, 0.64, EDAX), band weights (the plan's rhoMax) and triplet
+    voting on the device."""
+    global _INDEXER
+    from pyebsdindex_gb300 import radon_fast, tripletvote as tv
+    if _INDEXER is None:
+        d = np.load(VOTE_LIBRARY)
+        params = json.loads(str(d["params"]))
+        lib = {k[4:]: d[k] for k in d.files if k.startswith("lib_")}
+        _INDEXER = tv.BandIndexer(lib=lib, angTol=params["angTol"], nband_earlyexit=params["nband_earlyexit"],
+                                  simpleqweights=params["simpleqweights"])
+    normals = radon_fast.radon2pole_gpu(recs["theta"], recs["rho"], (h, h), PC=[0.46, 0.70, 0.64], vendor="EDAX",
+                                        stream=stream.cuda_stream)
+    adj, _, _ = tv.band_intensity_gpu(recs["max"], recs["normmax"], recs["theta"], recs["rho"], recs["valid"],
+                                      rho_max, stream=stream.cuda_stream)
+    out = _INDEXER.bandindex_device(normals, adj, stream=stream.cuda_stream)
+    return out["quat"].cpu().numpy().astype(np.float64), out["nmatch"].cpu().numpy()
 
 
 SCAN_ROWS, SCAN_COLS = 400, 500
@@ -627,7 +681,7 @@ def main():
     # the pattern pool is generated by spawned host processes before the GPU is touched
     ex = host_executor()
     pool = make_pool(args.pool, ex)
-    mpools = None if args.no_mixed else mixed_pools(ex, 1024)
+    mpools = None if args.no_mixed else mixed_pools(ex, 2048)
     scan = None if args.no_nlpar else nlpar_scan(ex)
     import torch
     rank, world, local = dist_env()
@@ -767,7 +821,8 @@ def main():
         torch.cuda.synchronize()
         acc = {"vs_plain64": dict(compare_records({k: v[:na] for k, v in outs.items()}, ref64), patterns=na),
                "bar": "integer peaks identical on >= 99.9% of bands, aveloc within 1e-3 Radon px"}
-        del ref64
+    else:
+        ref64 = None
 
     # end to end through the drop-in call: BandDetect.find_bands(numpy uint8 [N, 80, 80]) ->
     # the reference's (N, nBands) record array (band_detect.py:411, dtype :110-115); every
@@ -825,7 +880,7 @@ def main():
         del host, hout, host_np
 
     # the other methods on the same device-resident input, for the batched-vs-plain comparison
-    variants = {}
+    variants, variants_acc = {}, {}
     if not args.no_variants:
         # separate outputs: `outs` keeps the timed method's records for the indexing below
         vouts = {k: torch.empty_like(v) for k, v in outs.items()}
@@ -844,8 +899,16 @@ def main():
             b.record(stream)
             torch.cuda.synchronize()
             variants[vm] = vn * 2 / (a.elapsed_time(b) / 1000.0)
+            if ref64 is not None and vm != "plain":
+                from pyebsdindex_gb300.accuracy import compare_records
+                na = ref64["valid"].shape[0]
+                variants_acc[vm] = dict(compare_records({k: v[:na] for k, v in vouts.items()}, ref64), patterns=na)
         variants[method] = value / world
+        if "plain" in variants:
+            variants["batched_over_plain_fp32"] = {m: variants[m] / variants["plain"] for m in ("fused", "fused16")
+                                                   if m in variants}
         del vouts
+    ref64 = None
 
     file_e2e = None
     if rank == 0 and not args.no_file:
@@ -924,7 +987,8 @@ def main():
                        "patterns_per_block_pass": ppp, "radon_tile": radon_tile, "cuda_graph": graph is not None,
                        "l2": "input 6.4 GB > L2, no flush", "parallelism": f"replicas x{world}"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "accuracy": acc,
-            "variants_patterns_per_s": variants, "indexing": indexing, "file_e2e": file_e2e,
+            "variants_patterns_per_s": variants, "variants_accuracy_vs_plain64": variants_acc,
+            "indexing": indexing, "file_e2e": file_e2e,
             "nlpar_lambda": nlpar_lambda, "nlpar_file": nlpar_file, "mixed_sizes": mixed,
             "nlpar_detect": nlpar_detect, "differentiable": diffp,
             "gpu_launches": launches_per_step * args.steps,

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["compare_records"]
+__all__ = ["compare_records", "cubic_misorientation_deg", "orientation_agreement"]
 
 _FIELDS = ("max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid")
 
@@ -75,4 +75,65 @@ def compare_records(got, ref):
     else:
         out.update({"aveloc_max": 0.0, "aveloc_p99": 0.0, "aveloc_p50": 0.0, "within_1e-3": 1.0,
                     "max_rel": 0.0, "theta_max": 0.0, "rho_max": 0.0})
+    return out
+
+
+def _cubic_rotations():
+    """The 24 proper rotations of the cube as unit quaternions (w, x, y, z): the identity, the
+    half turns about the three axes, the quarter turns about them (both senses), the half turns
+    about the six face diagonals and the third turns about the four body diagonals."""
+    h = np.sqrt(0.5)
+    q = [(1.0, 0.0, 0.0, 0.0)]
+    for a in range(3):
+        e = np.zeros(3)
+        e[a] = 1.0
+        q.append((0.0, *e))                       # half turn
+        q.append((h, *(h * e)))                   # quarter turns
+        q.append((h, *(-h * e)))
+    for a, b in ((0, 1), (0, 2), (1, 2)):
+        for s in (1.0, -1.0):
+            e = np.zeros(3)
+            e[a], e[b] = h, s * h
+            q.append((0.0, *e))                   # half turns about face diagonals
+    for sx in (1.0, -1.0):
+        for sy in (1.0, -1.0):
+            for sz in (1.0, -1.0):
+                q.append((0.5, 0.5 * sx, 0.5 * sy, 0.5 * sz))  # third turns
+    return np.asarray(q, dtype=np.float64)
+
+
+def _qprod(a, b):
+    aw, ax, ay, az = np.moveaxis(a, -1, 0)
+    bw, bx, by, bz = np.moveaxis(b, -1, 0)
+    return np.stack([aw * bw - ax * bx - ay * by - az * bz, aw * bx + ax * bw + ay * bz - az * by,
+                     aw * by - ax * bz + ay * bw + az * bx, aw * bz + ax * by - ay * bx + az * bw], axis=-1)
+
+
+def cubic_misorientation_deg(q1, q2):
+    """Smallest rotation angle (degrees) taking orientation q1 to q2 ([n, 4] quaternions) under
+    cubic crystal symmetry.  Either frame convention is covered: an equivalent of q is q s or
+    s q for a symmetry rotation s, and the rotation angle of a product does not change under
+    cyclic permutation, so the candidates are conj(q1) q2 s and q2 conj(q1) s."""
+    q1 = np.asarray(q1, dtype=np.float64)
+    q2 = np.asarray(q2, dtype=np.float64)
+    g = _cubic_rotations()[None]
+    c1 = q1 * np.array([1.0, -1.0, -1.0, -1.0])
+    wa = np.abs(_qprod(_qprod(c1, q2)[:, None, :], g)[..., 0]).max(-1)
+    wb = np.abs(_qprod(_qprod(q2, c1)[:, None, :], g)[..., 0]).max(-1)
+    return np.degrees(2.0 * np.arccos(np.clip(np.maximum(wa, wb), -1.0, 1.0)))
+
+
+def orientation_agreement(q_got, nmatch_got, q_ref, nmatch_ref, tol_deg=0.01):
+    """Agreement of two indexings of the same patterns (cubic phase): of the patterns that both
+    index (at least three matched bands), the fraction whose orientations differ by at most
+    ``tol_deg`` degrees, with the largest and 99th-percentile misorientation."""
+    g = np.asarray(nmatch_got) >= 3
+    r = np.asarray(nmatch_ref) >= 3
+    both = g & r
+    out = {"patterns": int(len(g)), "indexed_got": float(g.mean()) if len(g) else 1.0,
+           "indexed_ref": float(r.mean()) if len(r) else 1.0, "both_indexed": int(both.sum())}
+    if both.any():
+        m = cubic_misorientation_deg(np.asarray(q_got)[both], np.asarray(q_ref)[both])
+        out.update({"within_tol": float(np.mean(m <= tol_deg)), "tol_deg": tol_deg,
+                    "mis_max_deg": float(m.max()), "mis_p99_deg": float(np.percentile(m, 99))})
     return out

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_band_epilogue(ebsd_bands out, int64_t n
 // kNT > 0: nTheta fixed at compile time, so every tile pitch is a constant (0: runtime).
 template <typename InT, typename S, int K0, int K1, int kPack, int kNT>
 __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
-    static_assert(kPack == 1 || (sizeof(S) == 4 && sizeof(InT) == 1), "packed modes: uint8 input, FP32 tile");
+    static_assert(kPack == 1 || sizeof(InT) == 1, "packed modes: uint8 input");
     static_assert(kPack == 1 || kPack == 2 || kPack == 4 || kPack == 8, "1, 2, 4 or 8 patterns per pass");
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int D0 = K0;  // rho half-window of the max filter (peakPad = 2*ksz + 1)
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                     v = load_pixel<InT>(gp, i, a.bg_mode, a.bg, a.bgf);
                     pat[y * a.pitch + x] = v;
                 }
-                if (kHalf) {
+                if (kHalf && kPack == 1) {
                     wsum = fmaf(a.wimg[i], v, wsum);
                     pmin = fminf(pmin, v);
                     pmax = fmaxf(pmax, v);
@@ -284,36 +284,69 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
         }
         // FP16 storage keeps (value - m) * s: m = mean of the Radon interior (exact by
         // linearity: sum_px w[px] * p[px]), s = power of two keeping |value - m| * s < 2^14.
-        float cen = 0.0f, scl = 1.0f, inv_scl = 1.0f;
-        if (kHalf) {
-            double dw = (double)wsum;
+        // Pattern k of the unit keeps its m and s in red_f[64 + 2k], red_f[65 + 2k] (the conv
+        // statistics use red_f[0..63] only).
+        auto centre_scale = [&](float ws, float mn, float mx, int slot) {
+            double dw = (double)ws;
             for (int o = 16; o > 0; o >>= 1) {
                 dw += __shfl_down_sync(0xffffffffu, dw, o);
-                pmin = fminf(pmin, __shfl_down_sync(0xffffffffu, pmin, o));
-                pmax = fmaxf(pmax, __shfl_down_sync(0xffffffffu, pmax, o));
+                mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, o));
+                mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
             }
-            if (lane == 0) { red_d[warp] = dw; red_f[warp] = pmin; red_f[32 + warp] = pmax; }
+            if (lane == 0) { red_d[warp] = dw; red_f[warp] = mn; red_f[32 + warp] = mx; }
             __syncthreads();
             if (warp == 0) {
                 dw = red_d[lane];
-                pmin = red_f[lane];
-                pmax = red_f[32 + lane];
+                mn = red_f[lane];
+                mx = red_f[32 + lane];
                 for (int o = 16; o > 0; o >>= 1) {
                     dw += __shfl_down_sync(0xffffffffu, dw, o);
-                    pmin = fminf(pmin, __shfl_down_sync(0xffffffffu, pmin, o));
-                    pmax = fmaxf(pmax, __shfl_down_sync(0xffffffffu, pmax, o));
+                    mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, o));
+                    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
                 }
                 if (lane == 0) {
                     float m = (float)dw;
-                    float amax = fmaxf(fabsf(pmax - m), fabsf(pmin - m));
+                    float amax = fmaxf(fabsf(mx - m), fabsf(mn - m));
                     int e = 0;
                     frexpf(fmaxf(amax, 1e-30f), &e);  // amax < 2^e
-                    red_f[64] = m;
-                    red_f[65] = ldexpf(1.0f, 14 - e);
+                    red_f[64 + 2 * slot] = m;
+                    red_f[65 + 2 * slot] = ldexpf(1.0f, 14 - e);
                 }
             }
+            __syncthreads();
+        };
+        float cen = 0.0f, scl = 1.0f, inv_scl = 1.0f;
+        if (kHalf && kPack == 1) {
+            centre_scale(wsum, pmin, pmax, 0);
+        } else if (kHalf) {
+            // packed units: each pattern's weighted sum, minimum and maximum from the packed
+            // tile, with the thread-to-pixel order and multiply-adds of the one-pattern pass
+            __syncthreads();
+            for (int k = 0; k < npk; ++k) {
+                float ws = 0.0f, mn = -1.0f, mx = -1.0f;
+                for (int y = warp; y < a.H; y += kWarps) {
+                    for (int x = lane; x < a.W; x += 32) {
+                        unsigned b;
+                        if (kPack == 8) {
+                            const uint2 w = ((const uint2*)pat)[y * a.pitch + x];
+                            b = ((k < 4 ? w.x : w.y) >> (8 * (k & 3))) & 0xFFu;
+                        } else if (kPack == 4) {
+                            const uint2 w = ((const uint2*)pat)[y * a.pitch + x];
+                            b = ((k < 2 ? w.x : w.y) >> (16 * (k & 1))) & 0xFFFFu;
+                        } else {
+                            b = (((const unsigned*)pat)[y * a.pitch + x] >> (16 * k)) & 0xFFFFu;
+                        }
+                        const float v = (float)b;
+                        ws = fmaf(a.wimg[y * a.W + x], v, ws);
+                        mn = fminf(mn, v);
+                        mx = fmaxf(mx, v);
+                    }
+                }
+                centre_scale(ws, mn, mx, k);
+            }
+        } else {
+            __syncthreads();
         }
-        __syncthreads();
         if (kHalf) {
             cen = red_f[64];
             scl = red_f[65];
@@ -400,6 +433,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                             if (kPack > 1) {
                                 const float fc = (float)cnt;
                                 v = cnt > 0 ? div_int_exact(isum & 0xFFFFu, fc, rc) : -1.0f;
+                                if (kHalf) v = (v - cen) * scl;
                                 st_keep(scratch + t, cnt > 0 ? div_int_exact(isum >> 16, fc, rc) : -1.0f, keep);
                                 if (kPack >= 4) {
                                     st_keep(scratch + a.nRaysPad + t, cnt > 0 ? div_int_exact(isum2 & 0xFFFFu, fc, rc) : -1.0f, keep);
@@ -551,6 +585,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
 
         for (int sub = 0; sub < npk; ++sub) {
         const int64_t q = q0 + sub;
+        if (kHalf && kPack > 1 && sub > 0) {  // this pattern's FP16 centre and scale
+            cen = red_f[64 + 2 * sub];
+            scl = red_f[65 + 2 * sub];
+            inv_scl = 1.0f / scl;
+        }
         // ---- 3. pad the tile around the interior ----
         // padding cell list (plan table): low half = destination tile cell, high half = source
         // tile cell, 0xFFFF = zero (rows below the padded array, the convolution's zero fill).
@@ -583,14 +622,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused(FusedArgs a) {
                         const int j4 = ((it + u * kRel) & 7) * 4;
                         const int nval = (int)(tb[u] >> 16);
                         S* dst = tile + (tb[u] & 0xFFFFu) + j4 * TP;
-                        if (j4 + 0 < nval) dst[0] = v[u].x;
-                        if (j4 + 1 < nval) dst[TP] = v[u].y;
-                        if (j4 + 2 < nval) dst[2 * TP] = v[u].z;
-                        if (j4 + 3 < nval) dst[3 * TP] = v[u].w;
+                        if (kHalf) {
+                            v[u].x = (v[u].x - cen) * scl;
+                            v[u].y = (v[u].y - cen) * scl;
+                            v[u].z = (v[u].z - cen) * scl;
+                            v[u].w = (v[u].w - cen) * scl;
+                        }
+                        if (j4 + 0 < nval) dst[0] = to_store<S>(v[u].x);
+                        if (j4 + 1 < nval) dst[TP] = to_store<S>(v[u].y);
+                        if (j4 + 2 < nval) dst[2 * TP] = to_store<S>(v[u].z);
+                        if (j4 + 3 < nval) dst[3 * TP] = to_store<S>(v[u].w);
                     }
                 }
                 asm volatile("bar.sync 1, %0;" ::"r"(kThreads - 32) : "memory");  // warps 1.. only
-                pad_cells(tid - 32, kThreads - 32, to_store<S>(0.0f));
+                pad_cells(tid - 32, kThreads - 32, to_store<S>(kHalf ? -cen * scl : 0.0f));
             }
         } else {
             pad_cells(tid, kThreads, to_store<S>(kHalf ? -cen * scl : 0.0f));
@@ -906,13 +951,21 @@ void* kernel_ptr(int k0, int k1, int nTheta) {
     return nullptr;
 }
 
+// FP16 storage, packed uint8 units: the 5x5 LoG only (other kernel shapes run one pattern per pass)
+template <int P>
+void* kernel_ptr_half_packed(int k0, int k1, int nTheta) {
+    if (k0 == 5 && k1 == 5 && nTheta == 180) return (void*)k_fused<uint8_t, __half, 5, 5, P, 180>;
+    if (k0 == 5 && k1 == 5) return (void*)k_fused<uint8_t, __half, 5, 5, P, 0>;
+    return nullptr;
+}
+
 void* pick_kernel(int method, int dtype, int k0, int k1, int pack, int nTheta) {
     bool h = method == EBSD_FUSED_F16;
     switch (dtype) {
         case EBSD_U8:
-            if (pack == 8 && !h) return kernel_ptr<uint8_t, float, 8>(k0, k1, nTheta);
-            if (pack == 4 && !h) return kernel_ptr<uint8_t, float, 4>(k0, k1, nTheta);
-            if (pack == 2 && !h) return kernel_ptr<uint8_t, float, 2>(k0, k1, nTheta);
+            if (pack == 8) return h ? kernel_ptr_half_packed<8>(k0, k1, nTheta) : kernel_ptr<uint8_t, float, 8>(k0, k1, nTheta);
+            if (pack == 4) return h ? kernel_ptr_half_packed<4>(k0, k1, nTheta) : kernel_ptr<uint8_t, float, 4>(k0, k1, nTheta);
+            if (pack == 2) return h ? kernel_ptr_half_packed<2>(k0, k1, nTheta) : kernel_ptr<uint8_t, float, 2>(k0, k1, nTheta);
             return h ? kernel_ptr<uint8_t, __half, 1>(k0, k1, nTheta) : kernel_ptr<uint8_t, float, 1>(k0, k1, nTheta);
         case EBSD_U16:
             return h ? kernel_ptr<uint16_t, __half, 1>(k0, k1, nTheta) : kernel_ptr<uint16_t, float, 1>(k0, k1, nTheta);
@@ -926,9 +979,10 @@ void* pick_kernel(int method, int dtype, int k0, int k1, int pack, int nTheta) {
 // pixels; four or eight per pass also need the 8-byte-element tile and its LUT (fg.quad).
 // Returns the largest patterns-per-pass the call may use (1, 2 or 8).
 int max_pack(const ebsd_plan_s* p, int method, int dtype, int64_t n) {
-    if (!(dtype == EBSD_U8 && method == EBSD_FUSED_F32 && p->fg.ok_f32 && p->bg_mode == 0 && p->maxCount <= 257 &&
-          n >= 2))
-        return 1;
+    const bool tile_ok = (method == EBSD_FUSED_F32 && p->fg.ok_f32) ||
+                         // FP16 storage: packed kernels are built for the 5x5 LoG only
+                         (method == EBSD_FUSED_F16 && p->fg.ok && p->k0 == 5 && p->k1 == 5);
+    if (!(dtype == EBSD_U8 && tile_ok && p->bg_mode == 0 && p->maxCount <= 257 && n >= 2)) return 1;
     return p->fg.quad && p->d_flut8 ? 8 : 2;
 }
 
@@ -1248,7 +1302,7 @@ void band_epilogue_launch(const ebsd_bands& out, int64_t out_offset, int64_t n, 
 
 // packed-mode scratch: (patterns per pass - 1) rows of parked ray means per resident CTA
 size_t fused_workspace_bytes(const ebsd_plan_s* p, int method, int64_t) {
-    if (method != EBSD_FUSED_F32 || !p->fg.ok_f32) return 0;
+    if (!((method == EBSD_FUSED_F32 && p->fg.ok_f32) || (method == EBSD_FUSED_F16 && p->fg.ok))) return 0;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
     const int rows = p->fg.quad ? 7 : 1;

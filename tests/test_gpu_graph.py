@@ -124,6 +124,27 @@ def test_patterns_per_pass_variants_give_identical_records(cuda, h, nRho):
         plan.set_patterns_per_pass(3)
 
 
+@pytest.mark.parametrize("h,nRho", [(80, 120), (60, 90)])
+def test_fp16_storage_pass_widths_give_identical_records(cuda, h, nRho):
+    """FP16 Radon storage with 2, 4 or 8 uint8 patterns per block pass: the ray sums are exact
+    integers, the mean the correctly rounded quotient, and each pattern's centre and scale come
+    from its own pixels in the one-pattern pass's order -- so every record equals the
+    one-pattern pass's bit for bit."""
+    bd = make_bd(h=h, nRho=nRho)
+    plan = bd._device_plan()
+    assert plan.supported("fused16")
+    pats = syn.make_patterns(203, h, h, seed=21, noise_frac=0.1)[0]
+    pats[5] = 0  # an all-zero pattern inside a packed unit
+    recs = []
+    for ppp in (1, 2, 4, 8, 0):
+        plan.set_patterns_per_pass(ppp)
+        recs.append(bd.find_bands(pats, method="fused16"))
+    plan.set_patterns_per_pass(0)
+    for r in recs[1:]:
+        for f in FIELDS:
+            assert r[f].tobytes() == recs[0][f].tobytes(), f
+
+
 def test_non_separable_kernel_uses_2d_taps_in_both_paths(cuda):
     """A plan whose LoG taps are not rank-1 (here: perturbed off-centre taps) convolves with
     the 2-D taps; fused and per-stage records stay identical, and differ from the separable
