@@ -471,17 +471,27 @@ def time_mixed(pools, n_total, steps, dev):
     outs = run(batches)
     torch.cuda.synchronize()
     mixed = mb.last_mixed
+    # one persistent launch over all sizes (and the per-size float64 epilogues), captured once in
+    # a CUDA graph writing the same outputs, then replayed per step
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(st)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph, stream=side):
+        mb.find_bands_device(batches, stream=side, out=outs)
+    torch.cuda.synchronize()
+    graph.replay()
+    torch.cuda.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     ev[0].record(st)
     for _ in range(steps):
-        outs = run(batches)
+        graph.replay()
     ev[1].record(st)
     torch.cuda.synchronize()
     ms = ev[0].elapsed_time(ev[1]) / steps
     res = {"workload": f"{3 * each:,} uint16 patterns (Poisson peak 4000), one third each at 60x60 / 120x120 / "
                        "240x240, nRho 1.5*size, nTheta 180, nBands 10; pools of distinct seeded patterns per size "
                        f"({pools[60][0].shape[0]}) tiled",
-           "one_launch": mixed, "ms_per_step": ms, "patterns_per_s": 3 * each / ms * 1e3,
+           "one_launch": mixed, "cuda_graph": True, "ms_per_step": ms, "patterns_per_s": 3 * each / ms * 1e3,
            "autotuned_slabs": {f"{k[0]}x{k[1]}": {"slabs": v["slabs"], "ms_per_sample": v["ms"]} for k, v in tuned.items()},
            "per_size": {}}
     for h in MIXED_SIZES:
@@ -512,17 +522,22 @@ def time_mixed(pools, n_total, steps, dev):
         entry["accuracy_vs_plain64"] = dict(compare_records({f: v[:na] for f, v in outs[key].items()},
                                                             {f: v[:na] for f, v in po.items()}), patterns=na)
         ref64 = {f: v[:na].clone() for f, v in po.items()}
-        # FP16 Radon storage, where a plan's FP16 tile fits on chip (the single-tile kernel)
-        if plan.supported("fused16", _lib.EBSD_U16):
+        # FP16 Radon storage: the single-tile kernel where its FP16 tile fits, else theta slabs
+        # (re-laid to the widest slabs whose FP16 tile fits, then put back for the FP32 path)
+        tile_fp32 = plan.get_tile()
+        if mb.plan(h, h)._pick_method(plan, "fused16", _lib.EBSD_U16) == "fused16":
             plan.find_bands_device(t.data_ptr(), _lib.EBSD_U16, na, {f: v.data_ptr() for f, v in po.items()}, "fused16",
                                    stream=st.cuda_stream)
             torch.cuda.synchronize()
             f16 = {f: v[:na].clone() for f, v in po.items()}
-            entry["fused16_accuracy_vs_plain64"] = dict(compare_records(f16, ref64), patterns=na)
+            t16 = plan.get_tile()
+            entry["fused16_accuracy_vs_plain64"] = dict(compare_records(f16, ref64), patterns=na,
+                                                        kernel="one tile" if t16["single_fits"] else
+                                                        f"{t16['slabs']} theta slabs")
         else:
             f16 = None
-            entry["fused16_accuracy_vs_plain64"] = ("no FP16-storage kernel at this size: the single-tile FP16 kernel "
-                                                    "does not fit on chip and the theta-slab kernel stores FP32")
+            entry["fused16_accuracy_vs_plain64"] = "no FP16-storage kernel for this plan"
+        plan.set_tile(0, tile_fp32["slabs"])
         # indexing agreement: FCC orientations (triplet voting on the device) from these records
         # against those from the FP64 method's records, over the patterns that carry bands (the
         # noise-only tenth has no orientation to agree on)

@@ -184,6 +184,9 @@ typedef struct {
     int slabs_min;          /* widest slabs that fit */
     int slabs_max;          /* narrowest slabs that still hold the filters' theta reach */
     int single_fits;        /* 1 when the one-tile kernel can take the plan */
+    int slabs_fp16;         /* 1 when the current slab tables also take EBSD_FUSED_F16 (integer
+                               patterns, 5x5 LoG): its theta-max rows need room beside the 16-bit
+                               tile, so the widest slabs may leave none (240x240: from 10 slabs) */
 } ebsd_tile_info;
 
 int ebsd_plan_get_tile(ebsd_plan_t plan, ebsd_tile_info* info);

@@ -44,7 +44,7 @@ class PlanDesc(C.Structure):
 class TileInfo(C.Structure):
     _fields_ = [("tile", C.c_int), ("patterns_per_pass", C.c_int), ("slabs", C.c_int),
                 ("slab_columns", C.c_int), ("slabs_min", C.c_int), ("slabs_max", C.c_int),
-                ("single_fits", C.c_int)]
+                ("single_fits", C.c_int), ("slabs_fp16", C.c_int)]
 
 
 class Bands(C.Structure):

@@ -114,8 +114,22 @@ class GPUFindBands:
 
     def _pick_method(self, plan, method, dtype=None):
         """The method a call runs: the requested (or default) one, the per-stage FP32 method
-        where a fused kernel cannot take the plan (or the input type, ``dtype`` an EBSD_* code)."""
+        where a fused kernel cannot take the plan (or the input type, ``dtype`` an EBSD_* code).
+
+        FP16 storage on a plan that runs in theta slabs needs room for its theta-max rows beside
+        the 16-bit tile, which the widest slabs may not leave (240x240: 10 slabs instead of 9):
+        the slab tables are then re-laid to the widest slabs that take it, and FP32 calls run
+        those slabs too until ``set_tile`` changes them."""
         m = self.default_method if method is None else method
+        if m == "fused16" and dtype in (None, _lib.EBSD_U8, _lib.EBSD_U16) and not plan.supported(m, dtype):
+            info = plan.get_tile()
+            if info["slabs"] and not info["single_fits"] and not info["slabs_fp16"]:
+                for ns in range(info["slabs"] + 1, info["slabs_max"] + 1):
+                    plan.set_tile(0, ns)
+                    if plan.supported(m, dtype):
+                        break
+                else:
+                    plan.set_tile(0, info["slabs"])
         if m in ("fused", "fused32", "fused16") and not plan.supported(m, dtype):
             m = "plain"
         return m
@@ -611,10 +625,13 @@ class MixedBandDetect:
             out[np.asarray(idx)] = recs[key]
         return out
 
-    def find_bands_device(self, batches, method=None, stream=None):
+    def find_bands_device(self, batches, method=None, stream=None, out=None):
         """batches: {(H, W): CUDA tensor [n, H, W]} (one input type) -> {(H, W): dict of device
         band arrays}, asynchronous on ``stream`` (default: the current stream).  With the fused
-        method and at most eight sizes that the slab kernel takes, one launch serves them all."""
+        method and at most eight sizes that the slab kernel takes, one launch serves them all.
+        ``out``: the dict a previous call returned, written again instead of new arrays (the
+        same sizes and counts) -- with it the call allocates nothing and can be captured in a
+        CUDA graph (after a first call has set the kernels up)."""
         import torch
         dev = torch.device("cuda", self.gpu_id)
         st = stream if stream is not None else torch.cuda.current_stream(dev)
@@ -623,7 +640,12 @@ class MixedBandDetect:
         for key, t in batches.items():
             ins[key] = _device_input(t, dev)
             dts.add(ins[key][1])
-        outs = {key: self._device_outputs(t.shape[0], dev) for key, (t, _) in ins.items()}
+        if out is not None:
+            if set(out) != set(ins) or any(out[k]["valid"].shape[0] != ins[k][0].shape[0] for k in ins):
+                raise ValueError("out must be a previous result for the same sizes and counts")
+            outs = out
+        else:
+            outs = {key: self._device_outputs(t.shape[0], dev) for key, (t, _) in ins.items()}
         plans = {key: self.plan(*key)._device_plan() for key in ins}
         dt0 = next(iter(dts)) if len(dts) == 1 else None
         mixed = (m in ("fused", "fused32") and dt0 is not None and 1 <= len(ins) <= self.MAX_MIXED

@@ -44,7 +44,12 @@ struct SlabGeom {
     int TR = 0, TBP = 0, CCP = 0, MP = 0, rho0 = 0, rpad_end = 0, CR = 0, statR = 0;
     int pitch = 0;              // pattern tile row pitch (elements)
     int smem[3] = {0, 0, 0};    // dynamic shared memory bytes per dtype (uint8, uint16, float32)
+    int regb = 0;               // bytes of the FP32 Radon-tile region
     int nslab_min = 0, nslab_max = 0;  // slab counts whose tiles fit (nslab_min: the widest slabs)
+    // FP16 Radon storage (integer patterns, 5x5 LoG): theta-max rows of pitch MP16 (tmb16
+    // bytes) before the 16-bit tile; region regb16 bytes; shared memory per dtype (uint8, uint16)
+    int ok16 = 0, MP16 = 0, tmb16 = 0, regb16 = 0;
+    int smem16[2] = {0, 0};
 };
 
 // Host copy of the slab kernel's per-source-group LUT slots (one group = 32 neighbouring rho at
@@ -117,6 +122,7 @@ struct ebsd_plan_s {
     int32_t* d_stab = nullptr;     // [gst][gtb][slab_g][slab_j][wofs][count]
     int32_t s_gst = 0, s_gtb = 0, s_slabg = 0, s_slabj = 0, s_wofs = 0, s_count = 0;  // offsets into d_stab
     ebsd::SlabSource* ssrc = nullptr;  // host slots for re-layout (slab.cu)
+    float* d_swimg = nullptr;      // [nPx] slab plans' pixel weights: sum_px w*pixel = Radon mean (FP16 centring)
     // FP32 fused calls that both kernels can serve: 0 rule (the single tile when it fits),
     // 1 the single tile, 2 theta slabs (ebsd_plan_set_tile, ebsd_plan_autotune)
     int tile_mode = 0;
@@ -207,10 +213,11 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d);
 // device before it frees the old tables.
 int slab_relayout(ebsd_plan_s* p, int nslab);
 void slab_release(ebsd_plan_s* p);
-// the slab kernel serves this (method, dtype): FP32 method, and the plan too large for the
-// single tile or set to theta slabs (tile_mode 2)
+// the slab kernel serves this (method, dtype): the FP32 method when the plan is too large for
+// the single tile or set to theta slabs (tile_mode 2); FP16 storage (uint8 / uint16, 5x5 LoG)
+// when the single FP16 tile does not fit
 bool slab_serves(const ebsd_plan_s* p, int method, int dtype);
-int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
+int slab_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
                    int64_t out_offset, cudaStream_t st, int64_t* launches);
 // mixed pattern sizes in one launch: up to 8 plans of one input type and LoG size
 constexpr int kMaxMixedPlans = 8;

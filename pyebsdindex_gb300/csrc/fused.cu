@@ -1282,8 +1282,10 @@ void fused_release(ebsd_plan_s* p) {
 }
 
 int fused_supported(const ebsd_plan_s* p, int method) {
-    // plans too large for the single tile run the FP32 method in theta slabs (slab.cu)
+    // plans too large for the single tile run the FP32 method in theta slabs (slab.cu), and FP16
+    // storage there when the FP16 slab tile fits (integer patterns)
     if (method == EBSD_FUSED_F32 && !p->fg.ok_f32 && p->sg.ok) return 1;
+    if (method == EBSD_FUSED_F16 && !p->fg.ok && p->sg.ok && p->sg.ok16) return 1;
     if (!p->fg.ok) return 0;
     if (method == EBSD_FUSED_F32) return p->fg.ok_f32;
     return method == EBSD_FUSED_F16;
@@ -1319,8 +1321,8 @@ int fused_patterns_per_pass(const ebsd_plan_s* p, int method, int dtype, int64_t
 int fused_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n,
                     const ebsd_bands* out, int64_t out_offset, cudaStream_t st, int64_t* launches) {
     if (n <= 0) return EBSD_OK;
-    if (slab_serves(p, method, dtype)) return slab_run_chunk(p, dtype, d_pats, n, out, out_offset, st, launches);
-    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) return EBSD_E_UNSUPPORTED;
+    if (slab_serves(p, method, dtype)) return slab_run_chunk(p, method, dtype, d_pats, n, out, out_offset, st, launches);
+    if ((method == EBSD_FUSED_F32 && !p->fg.ok_f32) || !p->fg.ok) return EBSD_E_UNSUPPORTED;
     const int pack = fused_patterns_per_pass(p, method, dtype, n);
     void* fn = pick_kernel(method, dtype, p->k0, p->k1, pack, p->nTheta);
     if (!fn) return EBSD_E_UNSUPPORTED;

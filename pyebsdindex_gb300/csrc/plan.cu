@@ -660,7 +660,7 @@ int ebsd_method_supported_for(ebsd_plan_t p, int method, int dtype) {
     if (!is_fused(method)) return EBSD_E_ARG;
     if (!fused_supported(p, method)) return 0;
     if (slab_serves(p, method, dtype)) return 1;
-    if (method == EBSD_FUSED_F32 && !p->fg.ok_f32) return 0;
+    if ((method == EBSD_FUSED_F32 && !p->fg.ok_f32) || !p->fg.ok) return 0;
     return 1;
 }
 
@@ -862,6 +862,7 @@ int ebsd_plan_get_tile(ebsd_plan_t p, ebsd_tile_info* info) {
     t.slab_columns = p->sg.ok ? p->sg.Ts : 0;
     t.slabs_min = p->sg.ok ? p->sg.nslab_min : 0;
     t.slabs_max = p->sg.ok ? p->sg.nslab_max : 0;
+    t.slabs_fp16 = p->sg.ok && p->sg.ok16 && p->d_swimg ? 1 : 0;
     *info = t;
     return EBSD_OK;
 }
@@ -889,7 +890,7 @@ int ebsd_plan_autotune(ebsd_plan_t p, int method, int dtype, const void* d_pats,
     std::vector<Cand> cands;
     const int old_mode = p->tile_mode, old_slabs = p->sg.ok ? p->sg.nslab : 0;
     p->fused_ppp = -1;
-    const bool single = method != EBSD_FUSED_F32 || p->fg.ok_f32;
+    const bool single = method == EBSD_FUSED_F32 ? p->fg.ok_f32 != 0 : p->fg.ok != 0;
     if (single) {
         p->tile_mode = 1;
         const int maxp = fused_patterns_per_pass(p, method, dtype, n);

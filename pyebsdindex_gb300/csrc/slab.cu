@@ -32,6 +32,7 @@
 #include "ebsd_internal.cuh"
 #include "label.cuh"
 
+#include <cuda_fp16.h>
 #include <algorithm>
 #include <cfloat>
 #include <cstring>
@@ -63,7 +64,10 @@ struct SlabArgs {
     int nslab, maxg;
     int nRho, nTheta, nB;
     int p0, p1;
-    int TR, TBP, CCP, MP;      // Radon tile rows, Radon / conv / theta-max pitches (MP = TBP)
+    int TR, TBP, CCP, MP;      // Radon tile rows, Radon / conv / theta-max pitches (FP32 tile: MP = TBP)
+    int regb, tmb;             // bytes of the Radon-tile region; FP16 tile: theta-max rows first (tmb bytes)
+    const float* wimg;         // FP16 tile: [H * W] pixel weights whose dot product is the Radon mean
+    float ksum;                // FP16 tile: sum of the LoG taps (the centring correction)
     int rho0;                  // tile row of interior row 0 (p0 - row0)
     int rpad_end;              // tile rows from here on are zero (padded row R)
     int CR;                    // conv rows
@@ -88,6 +92,12 @@ struct MultiArgs {
     int nplans;
 };
 
+template <typename S> __device__ __forceinline__ S slab_store(float v);
+template <> __device__ __forceinline__ float slab_store<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half slab_store<__half>(float v) { return __float2half_rn(v); }
+__device__ __forceinline__ float slab_load(float v) { return v; }
+__device__ __forceinline__ float slab_load(__half v) { return __half2float(v); }
+
 __device__ __forceinline__ bool beats(float v, int p, float w, int q) {
     return v > w || (v == w && p < q);
 }
@@ -103,7 +113,9 @@ __device__ __forceinline__ void list_insert(float v, int pos, float& lv, int& lp
     }
 }
 
-template <typename InT, int K0, int K1>
+// S: Radon tile storage -- float, or __half holding (value - m) * s with m the pattern's Radon
+// mean and s a power of two (FP16 storage, as the single-tile kernel's; FP32 conv and fit).
+template <typename InT, typename S, int K0, int K1>
 __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ MultiArgs ma) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int D0 = K0, D1 = K1;          // max-filter half windows (peakPad = 2*ksz + 1)
@@ -112,6 +124,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
     constexpr int NV = kRowBlock + 2 * D0;
     constexpr int kCarry = 2 * (D1 + H1);    // Radon columns shared by neighbouring slabs
     constexpr bool kInt = sizeof(InT) < 4;
+    constexpr bool kHalf = sizeof(S) == 2;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
     for (int64_t qq = blockIdx.x; qq < ma.start[ma.nplans]; qq += gridDim.x) {
@@ -124,8 +137,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
     size_t off = 0;
     InT* pat = (InT*)(smem + off);
     off += ((size_t)(a.H * a.pitch + 1) * sizeof(InT) + 15) & ~(size_t)15;
-    float* tile = (float*)(smem + off);  // Radon slab; later the theta-max rows
-    off += ((size_t)a.TR * TBP * sizeof(float) + 15) & ~(size_t)15;
+    // Radon slab; the theta-max rows sit after the carried columns of its rows (FP32), or
+    // before the tile (FP16: tmb bytes)
+    S* tile = (S*)(smem + off + (kHalf ? a.tmb : 0));
+    float* tm = kHalf ? (float*)(smem + off) : (float*)tile + kCarry;
+    off += (size_t)a.regb;
     float* conv = (float*)(smem + off);  // TR rows: the two-pass convolution's theta pass
     off += ((size_t)a.TR * CCP * sizeof(float) + 15) & ~(size_t)15;
     float* lv_s = (float*)(smem + off);
@@ -152,6 +168,48 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
             for (int y = warp; y < a.H; y += kWarps)
                 for (int x = lane; x < a.W; x += 32) pat[y * a.pitch + x] = gp[y * a.W + x];
             if (tid == 0) pat[a.H * a.pitch] = (InT)0;
+        }
+        // FP16 tile: the pattern's Radon mean m (by linearity, sum_px w[px] p[px]) and a power
+        // of two s keeping |value - m| s < 2^14, as the single-tile kernel computes them
+        float cen = 0.0f, scl = 1.0f, inv_scl = 1.0f;
+        if (kHalf) {
+            float ws = 0.0f, mn = -1.0f, mx = -1.0f;  // -1: value of an empty ray
+            for (int y = warp; y < a.H; y += kWarps)
+                for (int x = lane; x < a.W; x += 32) {
+                    const float v = (float)pat[y * a.pitch + x];
+                    ws = fmaf(a.wimg[y * a.W + x], v, ws);
+                    mn = fminf(mn, v);
+                    mx = fmaxf(mx, v);
+                }
+            double dw = (double)ws;
+            for (int o = 16; o > 0; o >>= 1) {
+                dw += __shfl_down_sync(0xffffffffu, dw, o);
+                mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, o));
+                mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+            }
+            if (lane == 0) { red_d[warp] = dw; red_f[warp] = mn; red_f[32 + warp] = mx; }
+            __syncthreads();
+            if (warp == 0) {
+                dw = red_d[lane];
+                mn = red_f[lane];
+                mx = red_f[32 + lane];
+                for (int o = 16; o > 0; o >>= 1) {
+                    dw += __shfl_down_sync(0xffffffffu, dw, o);
+                    mn = fminf(mn, __shfl_down_sync(0xffffffffu, mn, o));
+                    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+                }
+                if (lane == 0) {
+                    const float m = (float)dw;
+                    int e = 0;
+                    frexpf(fmaxf(fmaxf(fabsf(mx - m), fabsf(mn - m)), 1e-30f), &e);
+                    red_f[64] = m;
+                    red_f[65] = ldexpf(1.0f, 14 - e);
+                }
+            }
+            __syncthreads();
+            cen = red_f[64];
+            scl = red_f[65];
+            inv_scl = 1.0f / scl;  // exact: scl is a power of two
         }
         float smin = INFINITY, ssum = 0.0f;
         int cur = 0;  // running list buffer
@@ -274,10 +332,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                             }
                             if (++pc == (int)(gs >> 16)) {
                                 // ray ends: the mean of an empty ray is -1 (radon_fast.py:265)
-                                const float v = cnt > 0 ? __fdiv_rn(kInt ? (float)isum : fsum, (float)cnt) : -1.0f;
+                                float v = cnt > 0 ? __fdiv_rn(kInt ? (float)isum : fsum, (float)cnt) : -1.0f;
+                                if (kHalf) v = (v - cen) * scl;
                                 const unsigned tb = gtb_s[gi];
                                 const int stride = (tb >> 22) & 1 ? -TBP : TBP;
-                                if (lane < (int)((tb >> 16) & 63)) tile[(int)(tb & 0xFFFFu) + lane * stride] = v;
+                                if (lane < (int)((tb >> 16) & 63)) tile[(int)(tb & 0xFFFFu) + lane * stride] = slab_store<S>(v);
                                 ++gi;
                                 pc = 0;
                                 isum = 0u;
@@ -302,8 +361,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                 for (int k = tid; k < npadrow * TB; k += kThreads) {
                     const int pr = k / TB, c = k - pr * TB;
                     const int r = pr < top ? pr : bot + (pr - top);
-                    float v;
-                    if (r >= a.rpad_end) v = 0.0f;
+                    S v;
+                    if (r >= a.rpad_end) v = slab_store<S>(kHalf ? -cen * scl : 0.0f);
                     else v = tile[(r < top ? top : bot - 1) * TBP + c];
                     tile[r * TBP + c] = v;
                 }
@@ -318,10 +377,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                 for (int task = tid; task < a.TR * nseg; task += kThreads) {
                     const int sg = task / a.TR, r = task - sg * a.TR;
                     const int c0 = sg * kSegA < CCs - kSegA ? sg * kSegA : CCs - kSegA;
-                    const float* trow = tile + r * TBP + c0;
+                    const S* trow = tile + r * TBP + c0;
                     float x[kSegA + K1 - 1];
 #pragma unroll
-                    for (int k = 0; k < kSegA + K1 - 1; ++k) x[k] = trow[k];
+                    for (int k = 0; k < kSegA + K1 - 1; ++k) x[k] = slab_load(trow[k]);
                     float* hrow = conv + r * CCP + c0;
 #pragma unroll
                     for (int j = 0; j < kSegA; ++j) {
@@ -370,6 +429,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
                                 float acc = 0.0f;
 #pragma unroll
                                 for (int ka = 0; ka < K0; ++ka) acc = fmaf(a.ku[ka], w[(j + K0 - 1 - ka) % K0], acc);
+                                if (kHalf) acc = fmaf(a.ksum, cen, acc * inv_scl);
                                 if (j < K0 - 1 && o == o0) held[j < K0 - 1 ? j : 0] = acc;
                                 else hcol[oj * CCP] = acc;
                                 if (colstat && (unsigned)(oj - D0) < (unsigned)stat_rows) {
@@ -388,8 +448,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_slab(const __grid_constant__ Mu
             __syncthreads();
 
             // ---- 4a. theta max of the conv rows the rho window needs (into the dead Radon tile,
-            // after the carried columns)
-            float* tm = tile + kCarry;
+            // after the carried columns; FP16 tile: into the rows before it)
             {
                 const int NR = a.nRho + 2 * D0;
                 const int nseg = (Ts + WIN - 1) / WIN;
@@ -530,13 +589,20 @@ namespace {
 
 template <typename InT>
 void* slab_kernel(int k0, int k1) {
-    if (k0 == 5 && k1 == 5) return (void*)k_slab<InT, 5, 5>;
-    if (k0 == 7 && k1 == 7) return (void*)k_slab<InT, 7, 7>;
-    if (k0 == 9 && k1 == 9) return (void*)k_slab<InT, 9, 9>;
+    if (k0 == 5 && k1 == 5) return (void*)k_slab<InT, float, 5, 5>;
+    if (k0 == 7 && k1 == 7) return (void*)k_slab<InT, float, 7, 7>;
+    if (k0 == 9 && k1 == 9) return (void*)k_slab<InT, float, 9, 9>;
     return nullptr;
 }
 
-void* pick_slab_kernel(int dtype, int k0, int k1) {
+void* pick_slab_kernel(int dtype, int k0, int k1, bool half = false) {
+    // FP16 Radon storage: integer patterns and the 5x5 LoG
+    if (half) {
+        if (k0 != 5 || k1 != 5) return nullptr;
+        if (dtype == EBSD_U8) return (void*)k_slab<uint8_t, __half, 5, 5>;
+        if (dtype == EBSD_U16) return (void*)k_slab<uint16_t, __half, 5, 5>;
+        return nullptr;
+    }
     switch (dtype) {
         case EBSD_U8: return slab_kernel<uint8_t>(k0, k1);
         case EBSD_U16: return slab_kernel<uint16_t>(k0, k1);
@@ -545,11 +611,13 @@ void* pick_slab_kernel(int dtype, int k0, int k1) {
     return nullptr;
 }
 
-// dynamic shared memory of k_slab, as the kernel carves it
-size_t slab_smem(size_t pat_elems, size_t esize, int TR, int TBP, int CCP, int maxg) {
-    size_t b = (pat_elems * esize + 15) & ~(size_t)15;
-    b += ((size_t)TR * TBP * 4 + 15) & ~(size_t)15;
-    b += ((size_t)TR * CCP * 4 + 15) & ~(size_t)15;
+size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// dynamic shared memory of k_slab, as the kernel carves it (regb: the Radon-tile region)
+size_t slab_smem(size_t pat_elems, size_t esize, size_t regb, int TR, int CCP, int maxg) {
+    size_t b = align16(pat_elems * esize);
+    b += regb;
+    b += align16((size_t)TR * CCP * 4);
     b += (size_t)kWarps * kMaxBands * 8 + 2 * kMaxBands * kBlk * 4 + 80 * 4 + 32 * 8 + 2 * (kWarps + 1) * 4;
     b += (size_t)maxg * 8;
     return b;
@@ -604,12 +672,23 @@ bool slab_geom_for(const ebsd_plan_s* p, const SlabSource& src, int nslab, int d
     g.statR = src.statR;
     g.pitch = src.pitch;
     g.maxg = (ts + 2 * halo) * src.gpt;
-    g.smem[0] = (int)slab_smem(src.pat_elems, 1, g.TR, g.TBP, g.CCP, g.maxg);
-    g.smem[1] = (int)slab_smem(src.pat_elems, 2, g.TR, g.TBP, g.CCP, g.maxg);
-    g.smem[2] = (int)slab_smem(src.pat_elems, 4, g.TR, g.TBP, g.CCP, g.maxg);
+    g.regb = (int)align16((size_t)g.TR * g.TBP * 4);
+    g.smem[0] = (int)slab_smem(src.pat_elems, 1, g.regb, g.TR, g.CCP, g.maxg);
+    g.smem[1] = (int)slab_smem(src.pat_elems, 2, g.regb, g.TR, g.CCP, g.maxg);
+    g.smem[2] = (int)slab_smem(src.pat_elems, 4, g.regb, g.TR, g.CCP, g.maxg);
     if (g.smem[1] > dev_smem) return false;
     g.ok = 1;
     g.ok_f32 = g.smem[2] <= dev_smem;
+    // FP16 tile (5x5 LoG): the theta-max rows (nRho + 2 D0 rows of an odd pitch >= Ts) first,
+    // then the 16-bit Radon tile
+    if (p->k0 == 5 && p->k1 == 5) {
+        g.MP16 = ts | 1;
+        g.tmb16 = (int)align16((size_t)(p->nRho + 2 * p->k0) * g.MP16 * 4);
+        g.regb16 = g.tmb16 + (int)align16((size_t)g.TR * g.TBP * 2);
+        g.smem16[0] = (int)slab_smem(src.pat_elems, 1, g.regb16, g.TR, g.CCP, g.maxg);
+        g.smem16[1] = (int)slab_smem(src.pat_elems, 2, g.regb16, g.TR, g.CCP, g.maxg);
+        g.ok16 = g.smem16[1] <= dev_smem;
+    }
     *out = g;
     return true;
 }
@@ -845,6 +924,34 @@ int slab_prepare(ebsd_plan_s* p, const ebsd_plan_desc* d) {
     }
     g.nslab_min = nmin;
     g.nslab_max = nmax;
+    if (p->k0 == 5 && p->k1 == 5) {
+        // pixel weights of the FP16 centring (built for every slab count: the widest slabs may
+        // leave no room for an FP16 tile, narrower ones do): the mean over non-empty rays of the ray means is
+        // sum_px w[px] * pixel[px] with w[px] = sum over the rays through px of 1 / (count * rays)
+        int nonempty = 0;
+        for (int32_t c : src->count) nonempty += c > 0;
+        std::vector<double> w(p->nPx, 0.0);
+        for (int gs = 0; gs < nsrc; ++gs)
+            for (int l = 0; l < 32; ++l) {
+                const int c = src->count[(size_t)gs * 32 + l];
+                if (c <= 0) continue;
+                const double f = 1.0 / ((double)c * nonempty);
+                for (int ch = 0; ch < src->gch[gs]; ++ch)
+                    for (int k = 0; k < 8; ++k) {
+                        const uint16_t o = src->slots[src->goff[gs] + ((size_t)ch * 32 + l) * 8 + k];
+                        if (o == src->zero) continue;
+                        w[(size_t)(o / src->pitch) * p->W + o % src->pitch] += f;
+                    }
+            }
+        std::vector<float> wf(w.begin(), w.end());
+        if (cudaMalloc((void**)&p->d_swimg, wf.size() * sizeof(float)) != cudaSuccess ||
+            cudaMemcpy(p->d_swimg, wf.data(), wf.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaFree(p->d_swimg);
+            p->d_swimg = nullptr;
+            delete src;
+            return EBSD_E_NOMEM;
+        }
+    }
     const int rc = slab_upload(p, *src, g);
     if (rc != EBSD_OK) {
         delete src;
@@ -872,6 +979,8 @@ int slab_relayout(ebsd_plan_s* p, int nslab) {
 void slab_release(ebsd_plan_s* p) {
     cudaFree(p->d_slut);
     cudaFree(p->d_stab);
+    cudaFree(p->d_swimg);
+    p->d_swimg = nullptr;
     p->d_slut = nullptr;
     p->d_stab = nullptr;
     p->sg = SlabGeom{};
@@ -880,16 +989,29 @@ void slab_release(ebsd_plan_s* p) {
 }
 
 bool slab_serves(const ebsd_plan_s* p, int method, int dtype) {
-    if (method != EBSD_FUSED_F32 || !p->sg.ok) return false;
+    if (!p->sg.ok) return false;
+    if (method == EBSD_FUSED_F16)  // FP16 storage: plans the single FP16 tile cannot take
+        return !p->fg.ok && p->sg.ok16 && p->d_swimg && (dtype == EBSD_U8 || dtype == EBSD_U16);
+    if (method != EBSD_FUSED_F32) return false;
     if (dtype == EBSD_F32 && !p->sg.ok_f32) return false;
     return !p->fg.ok_f32 || p->tile_mode == 2;
 }
 
 namespace {
 
-SlabArgs slab_args(const ebsd_plan_s* p, const void* d_pats, int64_t n, const ebsd_bands& out, int64_t out_offset) {
+SlabArgs slab_args(const ebsd_plan_s* p, const void* d_pats, int64_t n, const ebsd_bands& out, int64_t out_offset,
+                   bool half) {
     const SlabGeom& g = p->sg;
     SlabArgs a;
+    a.regb = half ? g.regb16 : g.regb;
+    a.tmb = half ? g.tmb16 : 0;
+    a.wimg = p->d_swimg;
+    {
+        double su = 0.0, sw = 0.0;
+        for (float v : p->h_ku) su += v;
+        for (float v : p->h_kw) sw += v;
+        a.ksum = (float)(su * sw);
+    }
     a.pats = d_pats;
     a.n = n;
     a.H = p->H;
@@ -912,7 +1034,7 @@ SlabArgs slab_args(const ebsd_plan_s* p, const void* d_pats, int64_t n, const eb
     a.TR = g.TR;
     a.TBP = g.TBP;
     a.CCP = g.CCP;
-    a.MP = g.MP;
+    a.MP = half ? g.MP16 : g.MP;
     a.rho0 = g.rho0;
     a.rpad_end = g.rpad_end;
     a.CR = g.CR;
@@ -932,11 +1054,16 @@ SlabArgs slab_args(const ebsd_plan_s* p, const void* d_pats, int64_t n, const eb
 
 int smem_index(int dtype) { return dtype == EBSD_U8 ? 0 : (dtype == EBSD_U16 ? 1 : 2); }
 
+int slab_smem_for(const ebsd_plan_s* p, int dtype, bool half) {
+    return half ? p->sg.smem16[dtype == EBSD_U8 ? 0 : 1] : p->sg.smem[smem_index(dtype)];
+}
+
 // One persistent launch over the plans' patterns, then each plan's float64 epilogue pass.
 int slab_launch(ebsd_plan_s* const* plans, int nplans, int dtype, const void* const* d_pats, const int64_t* n,
-                const ebsd_bands* out, const int64_t* out_offset, cudaStream_t st, int64_t* launches) {
+                const ebsd_bands* out, const int64_t* out_offset, cudaStream_t st, int64_t* launches,
+                bool half = false) {
     const ebsd_plan_s* p0 = plans[0];
-    void* fn = pick_slab_kernel(dtype, p0->k0, p0->k1);
+    void* fn = pick_slab_kernel(dtype, p0->k0, p0->k1, half);
     if (!fn) return EBSD_E_UNSUPPORTED;
     MultiArgs ma;
     std::memset(&ma, 0, sizeof(ma));
@@ -945,8 +1072,8 @@ int slab_launch(ebsd_plan_s* const* plans, int nplans, int dtype, const void* co
     int64_t total = 0;
     for (int k = 0; k < nplans; ++k) {
         ma.start[k] = total;
-        ma.plan[k] = slab_args(plans[k], d_pats[k], n[k], out[k], out_offset[k]);
-        smem = std::max(smem, plans[k]->sg.smem[smem_index(dtype)]);
+        ma.plan[k] = slab_args(plans[k], d_pats[k], n[k], out[k], out_offset[k], half);
+        smem = std::max(smem, slab_smem_for(plans[k], dtype, half));
         total += n[k];
     }
     ma.start[nplans] = total;
@@ -970,13 +1097,13 @@ int slab_launch(ebsd_plan_s* const* plans, int nplans, int dtype, const void* co
 
 }  // namespace
 
-int slab_run_chunk(ebsd_plan_s* p, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
+int slab_run_chunk(ebsd_plan_s* p, int method, int dtype, const void* d_pats, int64_t n, const ebsd_bands* out,
                    int64_t out_offset, cudaStream_t st, int64_t* launches) {
     if (n <= 0) return EBSD_OK;
-    if (!slab_serves(p, EBSD_FUSED_F32, dtype)) return EBSD_E_UNSUPPORTED;
+    if (!slab_serves(p, method, dtype)) return EBSD_E_UNSUPPORTED;
     ebsd_plan_s* plans[1] = {p};
     const void* pats[1] = {d_pats};
-    return slab_launch(plans, 1, dtype, pats, &n, out, &out_offset, st, launches);
+    return slab_launch(plans, 1, dtype, pats, &n, out, &out_offset, st, launches, method == EBSD_FUSED_F16);
 }
 
 bool slab_mixable(const ebsd_plan_s* p, int dtype) {

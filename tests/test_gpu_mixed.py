@@ -72,3 +72,40 @@ def test_mixed_uint16_one_launch(cuda):
         for f in ("max", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
             assert recs[key][f].tobytes() == alone[f].tobytes(), (key, f)
         np.testing.assert_allclose(recs[key]["normmax"], alone["normmax"], rtol=1e-6)
+
+
+def test_mixed_one_launch_in_a_cuda_graph(cuda):
+    """The mixed-size launch writing a previous call's outputs is captured in a CUDA graph; a
+    replay on new patterns in the same input buffers equals a direct call on them."""
+    import torch
+    if getattr(torch, "uint16", None) is None:
+        pytest.skip("torch without uint16")
+    dev = torch.device("cuda", 0)
+    mb = MixedBandDetect(nBands=10, mask_for=syn.circular_mask)
+
+    def batch(seed):
+        return {(h, h): torch.from_numpy(syn.make_patterns(n, h, h, seed=seed + h, dtype=np.uint16, peak=4000.0,
+                                                           noise_frac=0.1)[0].view(np.int16)).to(dev).view(torch.uint16)
+                for h, n in ((60, 64), (120, 32), (240, 8))}
+    bufs = batch(500)
+    outs = mb.find_bands_device(bufs)
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        mb.find_bands_device(bufs, stream=side, out=outs)
+    torch.cuda.synchronize()
+    new = batch(900)
+    for k in bufs:
+        bufs[k].copy_(new[k])
+    g.replay()
+    torch.cuda.synchronize()
+    got = {k: {f: v.cpu().numpy() for f, v in o.items()} for k, o in outs.items()}
+    ref = mb.find_bands_device(new)
+    torch.cuda.synchronize()
+    for k in bufs:
+        for f in ("max", "normmax", "maxloc", "avemax", "aveloc", "width", "theta", "rho", "valid"):
+            assert got[k][f].tobytes() == ref[k][f].cpu().numpy().tobytes(), (k, f)
+    with pytest.raises(ValueError):
+        mb.find_bands_device({(60, 60): bufs[(60, 60)]}, out=outs)
