@@ -400,6 +400,122 @@ void launch_average_tiled(dim3 grid, dim3 block, size_t smem, cudaStream_t st, c
     }
 }
 
+// Weighted window sum, register-blocked along the scan row (search radius SR fixed).  A block
+// takes RP neighbouring scan pixels of one row and 4 * kRbThreads pattern values; each thread
+// holds the RP pixels' sums for four consecutive pattern values and streams the window rows'
+// RP + 2 SR columns once: a loaded value feeds every pixel whose window holds its column, and a
+// broadcast weight feeds the four values.  Each sum adds its window slots in window order
+// (rows, then columns) as fadd(acc, fmul(value, weight)) from zero -- the order and rounding of
+// k_nlpar_average -- so the result equals the tiled kernel's bit for bit.  Needs npx % 4 == 0
+// and 16-byte aligned data.
+constexpr int kRbThreads = 128;
+constexpr int kRbPix = 8;
+
+template <typename O> __device__ __forceinline__ void store4(O* dst, const float* v);
+template <> __device__ __forceinline__ void store4<float>(float* dst, const float* v) {
+    *(float4*)dst = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <> __device__ __forceinline__ void store4<uint8_t>(uint8_t* dst, const float* v) {
+    *(uint32_t*)dst = (uint32_t)store_as<uint8_t>(v[0]) | ((uint32_t)store_as<uint8_t>(v[1]) << 8) |
+                      ((uint32_t)store_as<uint8_t>(v[2]) << 16) | ((uint32_t)store_as<uint8_t>(v[3]) << 24);
+}
+template <> __device__ __forceinline__ void store4<uint16_t>(uint16_t* dst, const float* v) {
+    *(uint2*)dst = make_uint2((uint32_t)store_as<uint16_t>(v[0]) | ((uint32_t)store_as<uint16_t>(v[1]) << 16),
+                              (uint32_t)store_as<uint16_t>(v[2]) | ((uint32_t)store_as<uint16_t>(v[3]) << 16));
+}
+
+template <typename O, int SR>
+__global__ void __launch_bounds__(kRbThreads) k_nlpar_average_rb(const float* __restrict__ data, int nrows, int ncols,
+                                                                  int npx, const float* __restrict__ w,
+                                                                  O* __restrict__ out) {
+    constexpr int WN = 2 * SR + 1, WS = WN * WN, RP = kRbPix, NC = RP + 2 * SR;
+    __shared__ float ws[RP * WS];
+    const int y = blockIdx.z, p0 = blockIdx.y * RP;
+    const int np = ncols - p0 < RP ? ncols - p0 : RP;
+    for (int i = threadIdx.x; i < np * WS; i += kRbThreads) ws[i] = w[(int64_t)(y * ncols + p0) * WS + i];
+    __syncthreads();
+    const int k = (blockIdx.x * kRbThreads + threadIdx.x) * 4;
+    if (k >= npx) return;
+    int ys, ye;
+    window(y, SR, nrows, ys, ye);
+    float acc[RP][4];
+#pragma unroll
+    for (int m = 0; m < RP; ++m)
+#pragma unroll
+        for (int t = 0; t < 4; ++t) acc[m][t] = 0.0f;
+    if (p0 >= SR && p0 + RP + SR <= ncols) {
+        // every window of the block is centred: column j of the strip is slot j - m of pixel m
+#pragma unroll
+        for (int r = 0; r < WN; ++r) {
+            const float* src = data + ((int64_t)(ys + r) * ncols + (p0 - SR)) * npx + k;
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+                const float4 v = __ldg((const float4*)(src + (int64_t)j * npx));
+#pragma unroll
+                for (int m = 0; m < RP; ++m) {
+                    if (j - m >= 0 && j - m < WN) {
+                        const float wv = ws[m * WS + r * WN + (j - m)];
+                        acc[m][0] = wadd(acc[m][0], v.x, wv);
+                        acc[m][1] = wadd(acc[m][1], v.y, wv);
+                        acc[m][2] = wadd(acc[m][2], v.z, wv);
+                        acc[m][3] = wadd(acc[m][3], v.w, wv);
+                    }
+                }
+            }
+        }
+    } else {
+        // windows shifted inward at the scan's left / right edge: window starts from window()
+        int xs[RP];
+#pragma unroll
+        for (int m = 0; m < RP; ++m) {
+            int xe;
+            window(m < np ? p0 + m : p0 + np - 1, SR, ncols, xs[m], xe);
+        }
+        const int c0 = xs[0], c1 = xs[np - 1] + 2 * SR;  // window starts do not decrease with m
+#pragma unroll
+        for (int r = 0; r < WN; ++r) {
+            const float* src = data + (int64_t)(ys + r) * ncols * npx + k;
+            for (int c = c0; c <= c1; ++c) {
+                const float4 v = __ldg((const float4*)(src + (int64_t)c * npx));
+#pragma unroll
+                for (int m = 0; m < RP; ++m) {
+                    const int d = c - xs[m];
+                    if (m < np && d >= 0 && d < WN) {
+                        const float wv = ws[m * WS + r * WN + d];
+                        acc[m][0] = wadd(acc[m][0], v.x, wv);
+                        acc[m][1] = wadd(acc[m][1], v.y, wv);
+                        acc[m][2] = wadd(acc[m][2], v.z, wv);
+                        acc[m][3] = wadd(acc[m][3], v.w, wv);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < RP; ++m)
+        if (m < np) store4<O>(out + (int64_t)(y * ncols + p0 + m) * npx + k, acc[m]);
+}
+
+// The weighted window sum of the pair path: the register-blocked kernel where it applies
+// (radius 1-3, npx a multiple of 4, 16-byte aligned buffers), else the tiled kernel.
+template <typename O>
+void launch_average(dim3 tgrid, dim3 tblock, size_t tsmem, cudaStream_t st, const float* data, int nrows, int ncols,
+                    int npx, const float* w, int sr, O* out) {
+    const bool rb = sr >= 1 && sr <= 3 && npx % 4 == 0 && (uintptr_t)data % 16 == 0 && (uintptr_t)out % 16 == 0 &&
+                    nrows <= 65535 && (ncols + kRbPix - 1) / kRbPix <= 65535;  // grid y / z limits
+    if (!rb) {
+        launch_average_tiled<float, O>(tgrid, tblock, tsmem, st, data, nrows, ncols, npx, w, sr, out);
+        return;
+    }
+    const dim3 grid((unsigned)((npx / 4 + kRbThreads - 1) / kRbThreads), (unsigned)((ncols + kRbPix - 1) / kRbPix),
+                    (unsigned)nrows);
+    switch (sr) {
+        case 1: k_nlpar_average_rb<O, 1><<<grid, kRbThreads, 0, st>>>(data, nrows, ncols, npx, w, out); break;
+        case 2: k_nlpar_average_rb<O, 2><<<grid, kRbThreads, 0, st>>>(data, nrows, ncols, npx, w, out); break;
+        default: k_nlpar_average_rb<O, 3><<<grid, kRbThreads, 0, st>>>(data, nrows, ncols, npx, w, out); break;
+    }
+}
+
 // ---- pair kernels: each unordered pair's distance computed once ---------------------------
 // The squared difference of a pair is symmetric bit for bit ((a - b)^2 == (b - a)^2 in float,
 // and the saturation test is symmetric), so pixel p's distance to neighbour q is the same
@@ -1084,12 +1200,11 @@ int ebsd_nlpar_pairs_out(const float* d_data, int32_t nrows, int32_t ncols, int3
         if ((rc = launch_status()) != EBSD_OK) return rc;
     }
     if (out_dtype == EBSD_U8)
-        launch_average_tiled<float, uint8_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (uint8_t*)d_out);
+        launch_average<uint8_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (uint8_t*)d_out);
     else if (out_dtype == EBSD_U16)
-        launch_average_tiled<float, uint16_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr,
-                                              (uint16_t*)d_out);
+        launch_average<uint16_t>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (uint16_t*)d_out);
     else
-        launch_average_tiled<float, float>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (float*)d_out);
+        launch_average<float>(tgrid, tblock, asm_, st, d_data, nrows, ncols, npx, w, sr, (float*)d_out);
     return launch_status();
 }
 

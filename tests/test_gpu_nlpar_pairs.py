@@ -1,5 +1,7 @@
 """NLPAR with each unordered pair's distance summed once (ebsd_nlpar_pairs_out) against the
-per-slot kernels (ebsd_nlpar_sigma + ebsd_nlpar_out), through the C ABI.
+per-slot kernels (ebsd_nlpar_sigma + ebsd_nlpar_out), through the C ABI.  The pair path's
+weighted average is the register-blocked kernel (pattern sizes a multiple of 4 pixels), the
+per-slot path's the tiled kernel, so the comparison also pins the one against the other.
 
 A pair's squared difference is symmetric bit for bit, so the two paths must agree exactly:
 sigma, and the averaged patterns (float32, uint8 or uint16), for search radii 1-3, with and
@@ -17,17 +19,19 @@ from pyebsdindex_gb300 import synthetic as syn
 
 pytestmark = pytest.mark.gpu
 
-CASES = [  # nrows, ncols, sr, saturation_protect, dthresh, centre offset, output type
+CASES = [  # nrows, ncols, sr, saturation_protect, dthresh, centre offset, output type[, pattern side]
     (9, 40, 3, True, 0.0, False, "f32"),
     (12, 70, 2, False, 0.5, False, "u8"),
     (7, 33, 1, True, 0.0, True, "f32"),
     (13, 36, 3, True, 0.3, True, "u16"),
     (8, 7, 3, True, 0.0, False, "f32"),
+    (10, 45, 3, True, 0.0, False, "u8", 31),  # 961 pixels: not a multiple of 4 (the tiled average)
+    (9, 61, 3, True, 0.0, False, "u8", 80),   # the bench's pattern size, interior and edge tiles
 ]
 
 
-def _scan(nr, nc, seed):
-    pats, _ = syn.voronoi_scan(nr, nc, ngrains=6, h=32, w=32, seed=seed, peak_range=(40.0, 220.0))
+def _scan(nr, nc, seed, side=32):
+    pats, _ = syn.voronoi_scan(nr, nc, ngrains=6, h=side, w=side, seed=seed, peak_range=(40.0, 220.0))
     pats = pats.astype(np.float32)
     rng = np.random.default_rng(seed)
     sat = rng.random(pats.shape) < 0.002  # a few saturated pixels
@@ -38,11 +42,12 @@ def _scan(nr, nc, seed):
 @pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}_sr{c[2]}_{c[6]}" for c in CASES])
 def test_pair_sums_equal_per_slot_kernels(cuda, case):
     import torch
-    nr, nc, sr, sat, dth, use_off, odt = case
+    nr, nc, sr, sat, dth, use_off, odt = case[:7]
+    side = case[7] if len(case) > 7 else 32
     lib = nlp._bind()
-    x = torch.from_numpy(_scan(nr, nc, seed=nr * 100 + nc)).to(cuda).contiguous()
+    x = torch.from_numpy(_scan(nr, nc, seed=nr * 100 + nc, side=side)).to(cuda).contiguous()
     npix, npx = x.shape
-    ind = torch.from_numpy(np.nonzero(syn.circular_mask(32, 32).ravel())[0].astype(np.int32)).to(cuda)
+    ind = torch.from_numpy(np.nonzero(syn.circular_mask(side, side).ravel())[0].astype(np.int32)).to(cuda)
     dmax = float(x.max().item())
     code, tdt = {"f32": (_lib.EBSD_F32, torch.float32), "u8": (_lib.EBSD_U8, torch.uint8),
                  "u16": (_lib.EBSD_U16, torch.int16)}[odt]
