@@ -1,7 +1,9 @@
 """NLPAR with each unordered pair's distance summed once (ebsd_nlpar_pairs_out) against the
 per-slot kernels (ebsd_nlpar_sigma + ebsd_nlpar_out), through the C ABI.  The pair path's
-weighted average is the register-blocked kernel (pattern sizes a multiple of 4 pixels), the
-per-slot path's the tiled kernel, so the comparison also pins the one against the other.
+pair sums and weighted average are the register-blocked kernels (128 scan pixels of a row per
+pair block, its chunks with and without saturated values; patterns of a multiple of 4 pixels
+for the average), the per-slot path's the per-slot and tiled kernels, so the comparison also
+pins the one against the other.
 
 A pair's squared difference is symmetric bit for bit, so the two paths must agree exactly:
 sigma, and the averaged patterns (float32, uint8 or uint16), for search radii 1-3, with and
@@ -27,25 +29,33 @@ CASES = [  # nrows, ncols, sr, saturation_protect, dthresh, centre offset, outpu
     (8, 7, 3, True, 0.0, False, "f32"),
     (10, 45, 3, True, 0.0, False, "u8", 31),  # 961 pixels: not a multiple of 4 (the tiled average)
     (9, 61, 3, True, 0.0, False, "u8", 80),   # the bench's pattern size, interior and edge tiles
+    (6, 150, 3, True, 0.2, True, "f32"),      # rows wider than one block of the pair kernel
+    (5, 270, 2, True, 0.0, False, "u8"),
+    (8, 140, 1, False, 0.0, False, "f32"),
+    (7, 160, 3, True, 0.0, False, "u8", 32, 2e-6),  # one saturated value: chunks with and without
 ]
 
 
-def _scan(nr, nc, seed, side=32):
+def _scan(nr, nc, seed, side=32, satfrac=0.002):
     pats, _ = syn.voronoi_scan(nr, nc, ngrains=6, h=side, w=side, seed=seed, peak_range=(40.0, 220.0))
     pats = pats.astype(np.float32)
     rng = np.random.default_rng(seed)
-    sat = rng.random(pats.shape) < 0.002  # a few saturated pixels
+    sat = rng.random(pats.shape) < satfrac  # a few saturated pixels
+    if not sat.any():
+        sat.flat[rng.integers(sat.size)] = True
     pats[sat] = pats.max()
     return pats.reshape(nr * nc, -1)
 
 
-@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}_sr{c[2]}_{c[6]}" for c in CASES])
+@pytest.mark.parametrize("case", CASES, ids=[f"{c[0]}x{c[1]}_sr{c[2]}_{c[6]}" + ("_sat1" if len(c) > 8 else "")
+                                             for c in CASES])
 def test_pair_sums_equal_per_slot_kernels(cuda, case):
     import torch
     nr, nc, sr, sat, dth, use_off, odt = case[:7]
     side = case[7] if len(case) > 7 else 32
+    satfrac = case[8] if len(case) > 8 else 0.002
     lib = nlp._bind()
-    x = torch.from_numpy(_scan(nr, nc, seed=nr * 100 + nc, side=side)).to(cuda).contiguous()
+    x = torch.from_numpy(_scan(nr, nc, seed=nr * 100 + nc, side=side, satfrac=satfrac)).to(cuda).contiguous()
     npix, npx = x.shape
     ind = torch.from_numpy(np.nonzero(syn.circular_mask(side, side).ravel())[0].astype(np.int32)).to(cuda)
     dmax = float(x.max().item())
