@@ -29,7 +29,7 @@ CASES = [  # nrows, ncols, sr, saturation_protect, dthresh, centre offset, outpu
     (8, 7, 3, True, 0.0, False, "f32"),
     (10, 45, 3, True, 0.0, False, "u8", 31),  # 961 pixels: not a multiple of 4 (the tiled average)
     (9, 61, 3, True, 0.0, False, "u8", 80),   # the bench's pattern size, interior and edge tiles
-    (6, 150, 3, True, 0.2, True, "f32"),      # rows wider than one block of the pair kernel
+    (7, 150, 3, True, 0.2, True, "f32"),      # rows wider than one block of the pair kernel
     (5, 270, 2, True, 0.0, False, "u8"),
     (8, 140, 1, False, 0.0, False, "f32"),
     (7, 160, 3, True, 0.0, False, "u8", 32, 2e-6),  # one saturated value: chunks with and without
