@@ -613,197 +613,6 @@ __global__ void __launch_bounds__(kTileX * kPairTy) k_nlpar_pairs(
     if (near) sigp[pix * 4 + sk] = make_float2(ds, ns);
 }
 
-// Pair sums register-blocked along the scan row (radius SR fixed).  A block takes 128
-// neighbouring pixels of scan row y -- 32 groups of four (threadIdx.x) -- and one forward row
-// dy = threadIdx.y (0..SR): each thread keeps the sums of its four pixels' pairs in that row
-// (dx = 1..SR for dy = 0, -SR..SR otherwise) and reads, per masked pattern value, its four
-// pixels' values and the 4 + 2 SR values of the neighbour row once, each of which serves up to
-// 2 SR + 1 pairs.  Warp r stages row y + r of each chunk of 32 masked values, columns swizzled
-// by residue mod 4 so that a warp's reads of one column offset hit 32 consecutive positions.  A
-// chunk with no value at or above the saturation levels (the common case) adds every
-// difference square and counts the chunk whole; otherwise every term is tested as
-// k_nlpar_pairs tests it.  The sums run over the masked values in order with pair_ssd's
-// arithmetic, so they equal k_nlpar_pairs' bit for bit (the counts are exact integers).
-constexpr int kPrbPix = 4, kPrbCols = 32 * kPrbPix;
-
-template <int SR>
-__host__ __device__ constexpr int prb_npos() { return 4 * ((kPrbCols + 2 * SR + 3) / 4); }
-
-template <int SR, bool kSig>
-__global__ void __launch_bounds__(32 * (SR + 1)) k_nlpar_pairs_rb(
-        const float* __restrict__ data, int nrows, int ncols, int npx, const int32_t* __restrict__ ind, int nind,
-        float mxval, float mxsig, float2* __restrict__ pairs, float2* __restrict__ sigp) {
-    constexpr int NCX = kPrbCols + 2 * SR;  // staged columns p0 - SR .. p0 + 128 + SR - 1
-    constexpr int NQ = (NCX + 3) / 4;       // positions per residue class
-    constexpr int NPOS = prb_npos<SR>();
-    constexpr int WN = 2 * SR + 1;
-    constexpr int NV = kPrbPix + 2 * SR;    // neighbour-row values a thread reads per pattern value
-    extern __shared__ float sm[];           // [SR + 1][NPOS][kSP]
-    const int g = threadIdx.x, dy = threadIdx.y;
-    const int y = blockIdx.y, p0 = blockIdx.x * kPrbCols;
-    const int nF = SR * (2 * SR + 1) + SR;
-    float d[kPrbPix][WN], ds[kPrbPix][3];
-    int n[kPrbPix][WN], ns[kPrbPix][3];
-#pragma unroll
-    for (int i = 0; i < kPrbPix; ++i) {
-#pragma unroll
-        for (int j = 0; j < WN; ++j) {
-            d[i][j] = 0.0f;
-            n[i][j] = 0;
-        }
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            ds[i][j] = 0.0f;
-            ns[i][j] = 0;
-        }
-    }
-    int nfast = 0;  // values of the chunks in which every term counts
-    // this thread's reads: row 0 (its pixels, slots SR..SR+3) and row dy (slots 0..NV-1, or the
-    // forward slots SR+1..2SR+3 of row 0 for dy = 0); slot s of group g is column 4 g + s
-    const float* rowself = sm + (size_t)g * kSP;
-    const float* rownb = sm + ((size_t)dy * NPOS + g) * kSP;
-    for (int q0 = 0; q0 < nind; q0 += kChunk) {
-        const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
-        const int k = g < qn ? __ldg(ind + q0 + g) : 0;
-        __syncthreads();  // the previous chunk has been consumed
-        // warp dy stages row y + dy: lane g holds masked value q0 + g of every column
-        int bad = 0, badS = 0;
-        {
-            const int row = y + dy;
-            float* srow = sm + (size_t)dy * NPOS * kSP + g;
-            const bool rok = g < qn && row < nrows;
-            const float* src = data + ((int64_t)row * ncols + (p0 - SR)) * npx + k;
-#pragma unroll 4
-            for (int l = 0; l < NCX; ++l) {
-                const int col = p0 - SR + l;
-                float v = 0.0f;
-                if (rok && col >= 0 && col < ncols) {
-                    v = __ldg(src + (int64_t)l * npx);
-                    bad |= !(v < mxval);
-                    if (kSig) badS |= !(v < mxsig);
-                }
-                srow[((l & 3) * NQ + (l >> 2)) * kSP] = v;
-            }
-        }
-        const int any_bad = __syncthreads_or(bad);
-        const int any_bad_sig = kSig ? __syncthreads_or(badS) : 0;
-        const bool slow = any_bad != 0 || any_bad_sig != 0;
-        if (!slow) {
-            nfast += qn;
-            for (int qq = 0; qq < qn; ++qq) {
-                float xs[kPrbPix];
-#pragma unroll
-                for (int i = 0; i < kPrbPix; ++i) xs[i] = rowself[(((SR + i) & 3) * NQ + ((SR + i) >> 2)) * kSP + qq];
-                if (dy == 0) {
-                    float v[SR + kPrbPix - 1];  // row-0 slots SR+1 .. 2 SR+3
-#pragma unroll
-                    for (int s = 0; s < SR + kPrbPix - 1; ++s)
-                        v[s] = rowself[(((SR + 1 + s) & 3) * NQ + ((SR + 1 + s) >> 2)) * kSP + qq];
-#pragma unroll
-                    for (int i = 0; i < kPrbPix; ++i)
-#pragma unroll
-                        for (int dx = 1; dx <= SR; ++dx) {
-                            const float t = __fsub_rn(xs[i], v[i + dx - 1]);
-                            const float tt = __fmul_rn(t, t);
-                            d[i][dx - 1] = __fadd_rn(d[i][dx - 1], tt);
-                            if (kSig && dx == 1) ds[i][0] = __fadd_rn(ds[i][0], tt);
-                        }
-                } else {
-                    float v[NV];
-#pragma unroll
-                    for (int s = 0; s < NV; ++s) v[s] = rownb[((s & 3) * NQ + (s >> 2)) * kSP + qq];
-#pragma unroll
-                    for (int i = 0; i < kPrbPix; ++i)
-#pragma unroll
-                        for (int j = 0; j < WN; ++j) {
-                            const float t = __fsub_rn(xs[i], v[i + j]);
-                            const float tt = __fmul_rn(t, t);
-                            d[i][j] = __fadd_rn(d[i][j], tt);
-                            if (kSig && dy == 1 && j >= SR - 1 && j <= SR + 1)
-                                ds[i][j - SR + 1] = __fadd_rn(ds[i][j - SR + 1], tt);
-                        }
-                }
-            }
-        } else {
-            // some value at or above a saturation level: pair_ssd's test for every term
-            for (int qq = 0; qq < qn; ++qq) {
-                float xs[kPrbPix];
-#pragma unroll
-                for (int i = 0; i < kPrbPix; ++i) xs[i] = rowself[(((SR + i) & 3) * NQ + ((SR + i) >> 2)) * kSP + qq];
-                if (dy == 0) {
-                    float v[SR + kPrbPix - 1];
-#pragma unroll
-                    for (int s = 0; s < SR + kPrbPix - 1; ++s)
-                        v[s] = rowself[(((SR + 1 + s) & 3) * NQ + ((SR + 1 + s) >> 2)) * kSP + qq];
-#pragma unroll
-                    for (int i = 0; i < kPrbPix; ++i)
-#pragma unroll
-                        for (int dx = 1; dx <= SR; ++dx) {
-                            const float yv = v[i + dx - 1];
-                            const float t = __fsub_rn(xs[i], yv);
-                            const float tt = __fmul_rn(t, t);
-                            if (yv < mxval && xs[i] < mxval) {
-                                d[i][dx - 1] = __fadd_rn(d[i][dx - 1], tt);
-                                ++n[i][dx - 1];
-                            }
-                            if (kSig && dx == 1 && yv < mxsig && xs[i] < mxsig) {
-                                ds[i][0] = __fadd_rn(ds[i][0], tt);
-                                ++ns[i][0];
-                            }
-                        }
-                } else {
-                    float v[NV];
-#pragma unroll
-                    for (int s = 0; s < NV; ++s) v[s] = rownb[((s & 3) * NQ + (s >> 2)) * kSP + qq];
-#pragma unroll
-                    for (int i = 0; i < kPrbPix; ++i)
-#pragma unroll
-                        for (int j = 0; j < WN; ++j) {
-                            const float yv = v[i + j];
-                            const float t = __fsub_rn(xs[i], yv);
-                            const float tt = __fmul_rn(t, t);
-                            if (yv < mxval && xs[i] < mxval) {
-                                d[i][j] = __fadd_rn(d[i][j], tt);
-                                ++n[i][j];
-                            }
-                            if (kSig && dy == 1 && j >= SR - 1 && j <= SR + 1 && yv < mxsig && xs[i] < mxsig) {
-                                ds[i][j - SR + 1] = __fadd_rn(ds[i][j - SR + 1], tt);
-                                ++ns[i][j - SR + 1];
-                            }
-                        }
-                }
-            }
-        }
-    }
-    // the pairs whose neighbour lies in the scan, at their forward index
-    if (y + dy >= nrows) return;
-#pragma unroll
-    for (int i = 0; i < kPrbPix; ++i) {
-        const int x = p0 + kPrbPix * g + i;
-        if (x >= ncols) break;
-        const int64_t pix = (int64_t)y * ncols + x;
-        if (dy == 0) {
-#pragma unroll
-            for (int dx = 1; dx <= SR; ++dx)
-                if (x + dx < ncols) pairs[pix * nF + (dx - 1)] = make_float2(d[i][dx - 1], (float)(nfast + n[i][dx - 1]));
-            if (kSig && x + 1 < ncols) sigp[pix * 4] = make_float2(ds[i][0], (float)(nfast + ns[i][0]));
-        } else {
-#pragma unroll
-            for (int j = 0; j < WN; ++j) {
-                const int dx = j - SR;
-                if (x + dx >= 0 && x + dx < ncols)
-                    pairs[pix * nF + SR + (dy - 1) * WN + j] = make_float2(d[i][j], (float)(nfast + n[i][j]));
-            }
-            if (kSig && dy == 1) {
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    if (x + j - 1 >= 0 && x + j - 1 < ncols)
-                        sigp[pix * 4 + 1 + j] = make_float2(ds[i][j], (float)(nfast + ns[i][j]));
-            }
-        }
-    }
-}
-
 // sigma_numba (nn = 1) from the pair sums: min over the clipped 3x3 neighbourhood of
 // SSD / (2 n) for SSD >= 1e-3 (the count starts at 1e-12, which the first add absorbs).
 __global__ void k_nlpar_sigma_pairs(const float2* __restrict__ sigp, int nrows, int ncols, float* __restrict__ sigma) {
@@ -1060,18 +869,6 @@ size_t edge_rows_smem(int sr, int ncols) {
     return (size_t)(2 * sr + 1) * ncx * kSP * sizeof(float);
 }
 size_t edge_cols_smem(int sr) { return (size_t)(kTileX + 2 * sr) * (2 * sr + 1) * kSP * sizeof(float); }
-
-template <int SR, bool kSig>
-int launch_pairs_rb(cudaStream_t st, const float* data, int nrows, int ncols, int npx, const int32_t* ind, int nind,
-                    float mxval, float mxsig, float2* pairs, float2* sigp) {
-    const size_t smem = (size_t)(SR + 1) * prb_npos<SR>() * kSP * sizeof(float);
-    if (smem > 48 * 1024)
-        EBSD_CUDA_TRY(cudaFuncSetAttribute(k_nlpar_pairs_rb<SR, kSig>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem));
-    const dim3 grid((unsigned)((ncols + kPrbCols - 1) / kPrbCols), (unsigned)nrows), block(32, SR + 1);
-    k_nlpar_pairs_rb<SR, kSig><<<grid, block, smem, st>>>(data, nrows, ncols, npx, ind, nind, mxval, mxsig, pairs, sigp);
-    return launch_status();
-}
 
 size_t pairs_smem(int sr, int ncols) {
     const int ncx = std::min(ncols, kTileX + 2 * sr);
@@ -1359,35 +1156,22 @@ int ebsd_nlpar_pairs_out(const float* d_data, int32_t nrows, int32_t ncols, int3
     float2* pairs = (float2*)(d_work + ((npix * winsz + 1) & ~(int64_t)1));
     float2* sigp = pairs + npix * nF;
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = EBSD_OK;
-    if (nrows <= 65535) {
-        // the register-blocked pair sums
-        switch (sr * 2 + (compute_sigma ? 1 : 0)) {
-            case 2: rc = launch_pairs_rb<1, false>(st, d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, pairs, sigp); break;
-            case 3: rc = launch_pairs_rb<1, true>(st, d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, pairs, sigp); break;
-            case 4: rc = launch_pairs_rb<2, false>(st, d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, pairs, sigp); break;
-            case 5: rc = launch_pairs_rb<2, true>(st, d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, pairs, sigp); break;
-            case 6: rc = launch_pairs_rb<3, false>(st, d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, pairs, sigp); break;
-            default: rc = launch_pairs_rb<3, true>(st, d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, pairs, sigp); break;
-        }
-    } else {
-        const dim3 pgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), pblock(kTileX, kPairTy);
-        const int mpf = (nF + kPairTy - 1) / kPairTy;
+    const dim3 pgrid((unsigned)((ncols + kTileX - 1) / kTileX), (unsigned)nrows), pblock(kTileX, kPairTy);
+    const int mpf = (nF + kPairTy - 1) / kPairTy;
 #define EBSD_PAIRS(M, SG)                                                                                     \
     k_nlpar_pairs<M, SG><<<pgrid, pblock, psm, st>>>(d_data, nrows, ncols, npx, d_indices, nind, mxval, mxsig, sr, \
                                                      pairs, sigp)
-        if (compute_sigma) {
-            if (mpf == 1) EBSD_PAIRS(1, true);
-            else if (mpf == 2) EBSD_PAIRS(2, true);
-            else EBSD_PAIRS(3, true);
-        } else {
-            if (mpf == 1) EBSD_PAIRS(1, false);
-            else if (mpf == 2) EBSD_PAIRS(2, false);
-            else EBSD_PAIRS(3, false);
-        }
-#undef EBSD_PAIRS
-        rc = launch_status();
+    if (compute_sigma) {
+        if (mpf == 1) EBSD_PAIRS(1, true);
+        else if (mpf == 2) EBSD_PAIRS(2, true);
+        else EBSD_PAIRS(3, true);
+    } else {
+        if (mpf == 1) EBSD_PAIRS(1, false);
+        else if (mpf == 2) EBSD_PAIRS(2, false);
+        else EBSD_PAIRS(3, false);
     }
+#undef EBSD_PAIRS
+    int rc = launch_status();
     if (rc != EBSD_OK) return rc;
     if (compute_sigma) {
         k_nlpar_sigma_pairs<<<(unsigned)((npix + 255) / 256), 256, 0, st>>>(sigp, nrows, ncols, d_sigma);

@@ -1,9 +1,7 @@
 """NLPAR with each unordered pair's distance summed once (ebsd_nlpar_pairs_out) against the
 per-slot kernels (ebsd_nlpar_sigma + ebsd_nlpar_out), through the C ABI.  The pair path's
-pair sums and weighted average are the register-blocked kernels (128 scan pixels of a row per
-pair block, its chunks with and without saturated values; patterns of a multiple of 4 pixels
-for the average), the per-slot path's the per-slot and tiled kernels, so the comparison also
-pins the one against the other.
+weighted average is the register-blocked kernel (patterns of a multiple of 4 pixels), the
+per-slot path's the tiled kernel, so the comparison also pins the one against the other.
 
 A pair's squared difference is symmetric bit for bit, so the two paths must agree exactly:
 sigma, and the averaged patterns (float32, uint8 or uint16), for search radii 1-3, with and
@@ -29,10 +27,10 @@ CASES = [  # nrows, ncols, sr, saturation_protect, dthresh, centre offset, outpu
     (8, 7, 3, True, 0.0, False, "f32"),
     (10, 45, 3, True, 0.0, False, "u8", 31),  # 961 pixels: not a multiple of 4 (the tiled average)
     (9, 61, 3, True, 0.0, False, "u8", 80),   # the bench's pattern size, interior and edge tiles
-    (7, 150, 3, True, 0.2, True, "f32"),      # rows wider than one block of the pair kernel
+    (7, 150, 3, True, 0.2, True, "f32"),      # wider scans: several blocks per row
     (5, 270, 2, True, 0.0, False, "u8"),
     (8, 140, 1, False, 0.0, False, "f32"),
-    (7, 160, 3, True, 0.0, False, "u8", 32, 2e-6),  # one saturated value: chunks with and without
+    (7, 160, 3, True, 0.0, False, "u8", 32, 2e-6),  # saturation at a single value
 ]
 
 
