@@ -582,12 +582,37 @@ __global__ void __launch_bounds__(kTileX * kPairTy) k_nlpar_pairs(
         const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
         const int k = tx < qn ? __ldg(ind + q0 + tx) : 0;
         __syncthreads();  // the previous chunk has been consumed
+        int bad = 0, bad_sig = 0;  // a staged value at or above a saturation level
         for (int r = 0; r < nr; ++r) {
             const float* prow = data + ((int64_t)(y + r) * ncols + cx0) * npx + k;
             float* srow = S + r * ncx * kSP + tx;
-            for (int cc = ty; cc < ncx; cc += kPairTy) srow[cc * kSP] = tx < qn ? __ldg(prow + (int64_t)cc * npx) : 0.0f;
+            for (int cc = ty; cc < ncx; cc += kPairTy) {
+                const float v = tx < qn ? __ldg(prow + (int64_t)cc * npx) : 0.0f;
+                bad |= !(v < mxval);
+                if (kSig) bad_sig |= !(v < mxsig);
+                srow[cc * kSP] = v;
+            }
         }
-        __syncthreads();
+        const int any_bad = __syncthreads_or(bad);
+        const int any_bad_sig = kSig ? __syncthreads_or(bad_sig) : 0;
+        if (any_bad == 0 && any_bad_sig == 0) {
+            // every term of the chunk counts: the squares added without the tests, the chunk
+            // counted whole (the counts are exact integers either way)
+            for (int qq = 0; qq < qn; ++qq) {
+                const float xv = S[self * kSP + qq];
+#pragma unroll
+                for (int j = 0; j < MPF; ++j) {
+                    const float t = __fsub_rn(xv, S[slot[j] * kSP + qq]);
+                    const float tt = __fmul_rn(t, t);
+                    d[j] = __fadd_rn(d[j], tt);
+                    if (kSig && j == 0 && near) ds = __fadd_rn(ds, tt);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < MPF; ++j) n[j] = __fadd_rn(n[j], (float)qn);
+            if (kSig && near) ns = __fadd_rn(ns, (float)qn);
+            continue;
+        }
         for (int qq = 0; qq < qn; ++qq) {
             const float xv = S[self * kSP + qq];
 #pragma unroll
