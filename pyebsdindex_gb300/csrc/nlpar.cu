@@ -578,43 +578,20 @@ __global__ void __launch_bounds__(kTileX * kPairTy) k_nlpar_pairs(
         d[j] = 0.0f;
         n[j] = 0.0f;
     }
-    // two staging buffers: the copies of chunk c + 1 (cp.async, zero-filled past the chunk's
-    // values) are in flight while chunk c is summed
-    const int bufsz = nr * ncx * kSP;  // buffer b at sm + b * bufsz
-    auto stage = [&](int q0, float* dst) {
+    for (int q0 = 0; q0 < nind; q0 += kChunk) {
         const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
         const int k = tx < qn ? __ldg(ind + q0 + tx) : 0;
-        const unsigned bytes = tx < qn ? 4u : 0u;
+        __syncthreads();  // the previous chunk has been consumed
+        int bad = 0, bad_sig = 0;  // a staged value at or above a saturation level
         for (int r = 0; r < nr; ++r) {
             const float* prow = data + ((int64_t)(y + r) * ncols + cx0) * npx + k;
-            float* srow = dst + r * ncx * kSP + tx;
+            float* srow = S + r * ncx * kSP + tx;
             for (int cc = ty; cc < ncx; cc += kPairTy) {
-                const unsigned sa = (unsigned)__cvta_generic_to_shared(srow + cc * kSP);
-                const float* src = tx < qn ? prow + (int64_t)cc * npx : data;
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(sa), "l"(src), "r"(bytes) : "memory");
+                const float v = tx < qn ? __ldg(prow + (int64_t)cc * npx) : 0.0f;
+                bad |= !(v < mxval);
+                if (kSig) bad_sig |= !(v < mxsig);
+                srow[cc * kSP] = v;
             }
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    if (nind > 0) stage(0, sm);
-    for (int q0 = 0, c = 0; q0 < nind; q0 += kChunk, ++c) {
-        const int qn = nind - q0 < kChunk ? nind - q0 : kChunk;
-        float* const S = sm + (c & 1) * bufsz;
-        if (q0 + kChunk < nind) {
-            // the other buffer was released by the barrier that ended the previous chunk
-            stage(q0 + kChunk, sm + ((c + 1) & 1) * bufsz);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
-        int bad = 0, bad_sig = 0;  // one of this thread's staged values at or above a saturation level
-        if (tx < qn) {
-            for (int r = 0; r < nr; ++r)
-                for (int cc = ty; cc < ncx; cc += kPairTy) {
-                    const float v = S[(r * ncx + cc) * kSP + tx];
-                    bad |= !(v < mxval);
-                    if (kSig) bad_sig |= !(v < mxsig);
-                }
         }
         const int any_bad = __syncthreads_or(bad);
         const int any_bad_sig = kSig ? __syncthreads_or(bad_sig) : 0;
@@ -634,26 +611,25 @@ __global__ void __launch_bounds__(kTileX * kPairTy) k_nlpar_pairs(
 #pragma unroll
             for (int j = 0; j < MPF; ++j) n[j] = __fadd_rn(n[j], (float)qn);
             if (kSig && near) ns = __fadd_rn(ns, (float)qn);
-        } else {
-            for (int qq = 0; qq < qn; ++qq) {
-                const float xv = S[self * kSP + qq];
+            continue;
+        }
+        for (int qq = 0; qq < qn; ++qq) {
+            const float xv = S[self * kSP + qq];
 #pragma unroll
-                for (int j = 0; j < MPF; ++j) {
-                    const float yv = S[slot[j] * kSP + qq];
-                    if (yv < mxval && xv < mxval) {  // pair_ssd's order: count, difference, square
-                        n[j] = __fadd_rn(n[j], 1.0f);
-                        const float t = __fsub_rn(xv, yv);
-                        d[j] = __fadd_rn(d[j], __fmul_rn(t, t));
-                    }
-                    if (kSig && j == 0 && near && yv < mxsig && xv < mxsig) {
-                        ns = __fadd_rn(ns, 1.0f);
-                        const float t = __fsub_rn(xv, yv);
-                        ds = __fadd_rn(ds, __fmul_rn(t, t));
-                    }
+            for (int j = 0; j < MPF; ++j) {
+                const float yv = S[slot[j] * kSP + qq];
+                if (yv < mxval && xv < mxval) {  // pair_ssd's order: count, difference, square
+                    n[j] = __fadd_rn(n[j], 1.0f);
+                    const float t = __fsub_rn(xv, yv);
+                    d[j] = __fadd_rn(d[j], __fmul_rn(t, t));
+                }
+                if (kSig && j == 0 && near && yv < mxsig && xv < mxsig) {
+                    ns = __fadd_rn(ns, 1.0f);
+                    const float t = __fsub_rn(xv, yv);
+                    ds = __fadd_rn(ds, __fmul_rn(t, t));
                 }
             }
         }
-        __syncthreads();  // this buffer is free for the chunk after next
     }
     const int64_t pix = (int64_t)y * ncols + x;
 #pragma unroll
@@ -921,7 +897,7 @@ size_t edge_cols_smem(int sr) { return (size_t)(kTileX + 2 * sr) * (2 * sr + 1) 
 
 size_t pairs_smem(int sr, int ncols) {
     const int ncx = std::min(ncols, kTileX + 2 * sr);
-    return 2 * (size_t)(sr + 1) * ncx * kSP * sizeof(float);  // two staging buffers
+    return (size_t)(sr + 1) * ncx * kSP * sizeof(float);
 }
 
 size_t tiled_smem(int sr, int ncols, size_t elem, bool weights) {
