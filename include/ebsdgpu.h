@@ -470,6 +470,13 @@ int ebsd_linop_create(int64_t nrows, int64_t ncols, const int64_t* rowptr, const
 /* y[b] = A x[b] for b < n (n <= 65535); fp64 = 1 uses double values and double x / y. */
 int ebsd_linop_apply(ebsd_linop_t op, int fp64, const void* d_x, int64_t n, void* d_y, void* stream);
 
+/* The same with the patterns along the fast axis: x^T [ncols][ldx] and y^T [nrows][ldy] hold
+ * pattern b in column b (b < n <= ldx, ldy).  Results equal ebsd_linop_apply's bit for bit;
+ * the operator's rows are read once per 32 patterns and the reads of x^T are coalesced, which
+ * is the layout a batch of thousands of patterns wants. */
+int ebsd_linop_apply_cols(ebsd_linop_t op, int fp64, const void* d_xT, int64_t ldx, int64_t n, void* d_yT,
+                          int64_t ldy, void* stream);
+
 int ebsd_linop_destroy(ebsd_linop_t op);
 
 /* NLPAR window weights of nlpar_nb (nlpar_cpu.py:866-927) exposed for differentiation:

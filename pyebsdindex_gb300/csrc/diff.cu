@@ -42,6 +42,28 @@ __global__ void k_csr_gather(const int64_t* __restrict__ rowptr, const int32_t* 
     y[b * nrows + row] = acc;
 }
 
+// The same products with the patterns along the fast axis: x^T [ncols][ldx], y^T [nrows][ldy]
+// hold pattern b in column b.  A warp takes one operator row for 32 patterns (lanes): each
+// nonzero's column of x^T is one coalesced load, and the row's entries are read once per 32
+// patterns.  Each output adds its row's terms in CSR order with fused multiply-adds, as
+// k_csr_gather, so the results are the same bit for bit.
+template <typename T>
+__global__ void __launch_bounds__(256) k_csr_gather_cols(const int64_t* __restrict__ rowptr,
+                                                         const int32_t* __restrict__ col,
+                                                         const T* __restrict__ val, const T* __restrict__ xT,
+                                                         int64_t ldx, T* __restrict__ yT, int64_t ldy,
+                                                         int64_t nrows, int64_t n) {
+    const int64_t row = (int64_t)blockIdx.x * 8 + threadIdx.y;
+    const int64_t b = (int64_t)blockIdx.y * 32 + threadIdx.x;
+    if (row >= nrows || b >= n) return;
+    const int64_t e1 = __ldg(rowptr + row + 1);
+    T acc = (T)0;
+#pragma unroll 4
+    for (int64_t e = __ldg(rowptr + row); e < e1; ++e)
+        acc = fma(__ldg(val + e), __ldg(xT + (int64_t)__ldg(col + e) * ldx + b), acc);
+    yT[row * ldy + b] = acc;
+}
+
 __device__ __forceinline__ void window(int i, int sr, int n, int& start, int& end) {
     int a = i - sr > 0 ? i - sr : 0;
     int b = i + sr - (n - 1) > 0 ? i + sr - (n - 1) : 0;
@@ -564,6 +586,22 @@ int ebsd_linop_apply(ebsd_linop_t op, int fp64, const void* d_x, int64_t n, void
         k_csr_gather<float><<<grid, 256, 0, (cudaStream_t)stream>>>(op->rowptr, op->col, op->val,
                                                                    (const float*)d_x, (float*)d_y,
                                                                    op->nrows, op->ncols);
+    return launch_status();
+}
+
+int ebsd_linop_apply_cols(ebsd_linop_t op, int fp64, const void* d_xT, int64_t ldx, int64_t n, void* d_yT,
+                          int64_t ldy, void* stream) {
+    if (!op || n < 0 || (n > 0 && (!d_xT || !d_yT)) || ldx < n || ldy < n || (n + 31) / 32 > 65535) return EBSD_E_ARG;
+    if (n == 0) return EBSD_OK;
+    if ((op->nrows + 7) / 8 > 0x7fffffff) return EBSD_E_ARG;
+    if (cudaSetDevice(op->device) != cudaSuccess) return EBSD_E_DEVICE;
+    const dim3 grid((unsigned)((op->nrows + 7) / 8), (unsigned)((n + 31) / 32)), block(32, 8);
+    if (fp64)
+        k_csr_gather_cols<double><<<grid, block, 0, (cudaStream_t)stream>>>(
+            op->rowptr, op->col, op->val64, (const double*)d_xT, ldx, (double*)d_yT, ldy, op->nrows, n);
+    else
+        k_csr_gather_cols<float><<<grid, block, 0, (cudaStream_t)stream>>>(
+            op->rowptr, op->col, op->val, (const float*)d_xT, ldx, (float*)d_yT, ldy, op->nrows, n);
     return launch_status();
 }
 

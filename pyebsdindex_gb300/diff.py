@@ -42,6 +42,7 @@ def _bind():
         P = C.c_void_p
         lib.ebsd_linop_create.argtypes = [C.c_int64, C.c_int64, P, P, P, C.c_int, C.POINTER(P)]
         lib.ebsd_linop_apply.argtypes = [P, C.c_int, P, C.c_int64, P, P]
+        lib.ebsd_linop_apply_cols.argtypes = [P, C.c_int, P, C.c_int64, C.c_int64, P, C.c_int64, P]
         lib.ebsd_linop_destroy.argtypes = [P]
         lib.ebsd_nlpar_weights.argtypes = [P, C.c_int32, C.c_int32, C.c_int32, P, C.c_int32, C.c_float, C.c_float,
                                            C.c_int32, C.c_float, P, C.c_int, P, P, P]
@@ -61,7 +62,8 @@ def _bind():
         lib.ebsd_nlpar_apply64.argtypes = lib.ebsd_nlpar_apply.argtypes
         lib.ebsd_nlpar_apply_t64.argtypes = lib.ebsd_nlpar_apply_t.argtypes
         lib.ebsd_nlpar_lambda_grad64.argtypes = lib.ebsd_nlpar_lambda_grad.argtypes
-        for f in ("ebsd_linop_create", "ebsd_linop_apply", "ebsd_linop_destroy", "ebsd_nlpar_weights",
+        for f in ("ebsd_linop_create", "ebsd_linop_apply", "ebsd_linop_apply_cols", "ebsd_linop_destroy",
+                  "ebsd_nlpar_weights",
                   "ebsd_nlpar_apply", "ebsd_nlpar_apply_t", "ebsd_nlpar_lambda_grad", "ebsd_nlpar_apply64",
                   "ebsd_nlpar_apply_t64", "ebsd_nlpar_lambda_grad64", "ebsd_blur1d", "ebsd_softargmax",
                   "ebsd_nlpar_sigma_arg", "ebsd_nlpar_weights_d", "ebsd_nlpar_weights_grad"):
@@ -159,6 +161,24 @@ class LinOp:
         self.handle = h
 
     def __call__(self, x):
+        """y = A x for a batch x [n, ncols] (float32 / float64 CUDA tensor) -> y [n, nrows], run
+        with the patterns along the fast axis (``ebsd_linop_apply_cols``): a batch held as the
+        transpose of a contiguous [ncols, n] tensor -- e.g. another LinOp's result -- is read
+        where it lies, and y is returned as the transpose of a contiguous [nrows, n] tensor."""
+        import torch
+        n = x.shape[0]
+        xT = x.t()
+        if not xT.is_contiguous():
+            xT = xT.contiguous()
+        yT = torch.empty((self.shape[0], n), dtype=x.dtype, device=x.device)
+        _lib.check(self._lib.ebsd_linop_apply_cols(self.handle, int(x.dtype == torch.float64), xT.data_ptr(), n, n,
+                                                   yT.data_ptr(), n, torch.cuda.current_stream(x.device).cuda_stream),
+                   "ebsd_linop_apply_cols")
+        return yT.t()
+
+    def apply_rows(self, x):
+        """The same product on a pattern-major batch x [n, ncols] (``ebsd_linop_apply``, one
+        thread per output row and pattern) -> contiguous y [n, nrows]; equal bit for bit."""
         import torch
         x = x.contiguous()
         n = x.shape[0]
@@ -194,7 +214,7 @@ def _linop_fn():
 
         @staticmethod
         def backward(ctx, g):
-            return ctx.opT(g.contiguous()), None, None
+            return ctx.opT(g), None, None
 
     return LinOpFn
 
@@ -422,7 +442,7 @@ class BandSharpness:
                            self.dthresh, self.sat)
         z = self._bg.apply(y.contiguous(), bg_sigma, self.bg_radius, self.H, self.W)
         r = self._lin.apply(z.contiguous(), self.R, self.RT)
-        c = self._lin.apply(r.contiguous(), self.M, self.MT)
+        c = self._lin.apply(r, self.M, self.MT)  # r stays in the operators' pattern-minor layout
         J = self._sa.apply(c.contiguous(), self.cells, self.tau)
         return y, z, r, c, J
 

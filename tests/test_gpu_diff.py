@@ -244,3 +244,23 @@ def test_radon_adjoint_is_the_transpose_on_device(cuda):
     lhs = (obj.M(r) * g).sum()
     rhs = (r * obj.MT(g)).sum()
     assert abs(float(lhs - rhs)) <= 1e-10 * abs(float(lhs))
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_pattern_minor_operator_equals_pattern_major(cuda, dtype):
+    """The sparse Radon / LoG operators with the patterns along the fast axis (what the
+    objective runs) give the pattern-major kernel's products bit for bit, for a batch that is
+    not a multiple of 32, a contiguous input and another operator's transposed output."""
+    import torch
+    _, obj, x = _setup(cuda)
+    td = getattr(torch, dtype)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    xb = torch.rand((45, x.shape[1]), generator=g, dtype=td).to(cuda) * 100.0
+    for op in (obj.R, obj.RT):
+        xin = xb if op is obj.R else torch.rand((45, obj.R.shape[0]), generator=g, dtype=td).to(cuda)
+        a = op(xin)
+        b = op.apply_rows(xin)
+        assert a.shape == b.shape and torch.equal(a, b), op.shape
+    r = obj.R(xb)  # a transposed view, read in place by the next operator
+    assert not r.is_contiguous() and r.t().is_contiguous()
+    assert torch.equal(obj.M(r), obj.M.apply_rows(r.contiguous()))
