@@ -306,28 +306,44 @@ __global__ void k_softargmax(const T* __restrict__ c, int64_t ncell, const int32
 __global__ void k_sigma_arg(const float* __restrict__ data, int nrows, int ncols, int npx,
                             const int32_t* __restrict__ ind, int nind, float mxval, float* __restrict__ sig2,
                             int* __restrict__ arg, float* __restrict__ nsig) {
-    const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= nrows * ncols) return;
-    const int j = pix / ncols, i = pix - (pix / ncols) * ncols;
-    float best = 1e24f, bn = 0.0f;
-    int ba = -1;
-    for (int k = 0; k < 9; ++k) {
-        if (k == 4) continue;
-        const int jn = j + k / 3 - 1, inn = i + k % 3 - 1;
-        if (jn < 0 || jn >= nrows || inn < 0 || inn >= ncols) continue;
-        const int nb = inn + ncols * jn;
-        float d2, n2;
-        pair_ssd(data + (int64_t)pix * npx, data + (int64_t)nb * npx, ind, nind, mxval, d2, n2);
-        n2 = __fadd_rn(n2, 1.0e-12f);
-        if (d2 >= 1.e-3f) {
-            const float s0 = __fdiv_rn(d2, __fmul_rn(n2, 2.0f));
-            if (s0 < best) { best = s0; ba = nb; bn = n2; }
+    // eight lanes per scan pixel, one per neighbour of the 3x3 neighbourhood in raster order
+    // (the centre skipped); each lane sums its pair in pair_ssd's order, then the pixel's first
+    // lane takes the minimum in raster order (strict <, the first of equal values), as a
+    // sequential scan of the eight pairs would
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int pix = t >> 3, slot = t & 7;
+    const int npix = nrows * ncols;
+    const int kk = slot < 4 ? slot : slot + 1;  // 3x3 index, the centre (4) skipped
+    float s0 = 1e24f, n2 = 0.0f;
+    int nb = -1;
+    if (pix < npix) {
+        const int j = pix / ncols, i = pix - (pix / ncols) * ncols;
+        const int jn = j + kk / 3 - 1, inn = i + kk % 3 - 1;
+        if (jn >= 0 && jn < nrows && inn >= 0 && inn < ncols) {
+            nb = inn + ncols * jn;
+            float d2;
+            pair_ssd(data + (int64_t)pix * npx, data + (int64_t)nb * npx, ind, nind, mxval, d2, n2);
+            n2 = __fadd_rn(n2, 1.0e-12f);
+            if (d2 >= 1.e-3f) s0 = __fdiv_rn(d2, __fmul_rn(n2, 2.0f));
+            else nb = -1;
         }
     }
-    const float sg = sqrtf(best);
-    sig2[pix] = __fmul_rn(sg, sg);
-    arg[pix] = ba;
-    nsig[pix] = bn;
+    const int lane = threadIdx.x & 31, base = lane & ~7;
+    float best = 1e24f, bn = 0.0f;
+    int ba = -1;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const float v = __shfl_sync(0xffffffffu, s0, base + k);
+        const float vn = __shfl_sync(0xffffffffu, n2, base + k);
+        const int vb = __shfl_sync(0xffffffffu, nb, base + k);
+        if (vb >= 0 && v < best) { best = v; ba = vb; bn = vn; }
+    }
+    if (pix < npix && slot == 0) {
+        const float sg = sqrtf(best);
+        sig2[pix] = __fmul_rn(sg, sg);
+        arg[pix] = ba;
+        nsig[pix] = bn;
+    }
 }
 
 // Window weights with the pieces of their derivative (one block per scan pixel, one thread per
@@ -467,20 +483,29 @@ __global__ void k_nlpar_gamma(const double* __restrict__ beta, int nrows, int nc
 // dJ/dx_q[k] from the weights' dependence on the patterns: the pair SSDs of q's own window, of
 // the windows that hold q, and the noise sigma's minimising pair (q's own, and those of the
 // 3x3 neighbours whose minimum pairs with q).  Masked pixels only, each pair's saturation test.
+// d/dx of the weights' pattern dependence, one block per scan pixel q, its threads over the
+// pattern values k.  The terms that reach q -- its own window slots (the pair distances it
+// enters as the centre), the windows of the pixels whose windows hold q, and the noise sigma
+// of q and of the neighbours whose sigma pairs end at q -- are listed once per block with
+// their coefficients (2 alpha, gamma / n), then every value k adds coef * (x_q - x_n) for the
+// terms whose two values pass the saturation test of their kind.  Sums in the pixel's order;
+// float patterns accumulate in float (the coefficients rounded once), double in double.
 template <typename T>
-__global__ void k_nlpar_dx(const T* __restrict__ x, int nrows, int ncols, int npx, int sr,
-                           const uint8_t* __restrict__ pmask, float mxw, float mxs, const double* __restrict__ alpha,
-                           const double* __restrict__ gamma, const int* __restrict__ arg,
-                           const float* __restrict__ nsig, T* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
-    if (k >= npx) return;
-    double acc = 0.0;
-    if (pmask[k]) {
-        const int winsz = (2 * sr + 1) * (2 * sr + 1), wx = 2 * sr + 1;
+__global__ void __launch_bounds__(128) k_nlpar_dx(const T* __restrict__ x, int nrows, int ncols, int npx, int sr,
+                                                  const uint8_t* __restrict__ pmask, float mxw, float mxs,
+                                                  const double* __restrict__ alpha, const double* __restrict__ gamma,
+                                                  const int* __restrict__ arg, const float* __restrict__ nsig,
+                                                  T* __restrict__ out) {
+    extern __shared__ unsigned char dxsm[];
+    const int q = blockIdx.x;
+    const int winsz = (2 * sr + 1) * (2 * sr + 1), wx = 2 * sr + 1;
+    const int maxt = winsz + (4 * sr + 1) * (4 * sr + 1) + 9;
+    T* co = (T*)dxsm;                        // [maxt] coefficients
+    int* nbs = (int*)(co + maxt);           // [maxt] the other pixel; bit 31: a sigma term
+    __shared__ int nterm;
+    if (threadIdx.x == 0) {
+        int t = 0;
         const int jq = q / ncols, iq = q - (q / ncols) * ncols;
-        const double xq = (double)x[(int64_t)q * npx + k];
-        const bool qw = xq < (double)mxw, qs = xq < (double)mxs;
         {
             int xs, xe, ys, ye;
             window(iq, sr, ncols, xs, xe);
@@ -489,8 +514,8 @@ __global__ void k_nlpar_dx(const T* __restrict__ x, int nrows, int ncols, int np
             for (int c = 0; c < winsz; ++c) {
                 const int nb = (xs + c % wq) + ncols * (ys + c / wq);
                 if (nb == q) continue;
-                const double xc = (double)x[(int64_t)nb * npx + k];
-                if (qw && xc < (double)mxw) acc += 2.0 * alpha[(int64_t)q * winsz + c] * (xq - xc);
+                co[t] = (T)(2.0 * alpha[(int64_t)q * winsz + c]);
+                nbs[t++] = nb;
             }
         }
         const int j0 = jq - 2 * sr < 0 ? 0 : jq - 2 * sr, j1 = jq + 2 * sr > nrows - 1 ? nrows - 1 : jq + 2 * sr;
@@ -505,15 +530,15 @@ __global__ void k_nlpar_dx(const T* __restrict__ x, int nrows, int ncols, int np
                 if (iq < xs || iq >= xe) continue;
                 const int p = ip + ncols * jp;
                 if (p == q) continue;
-                const double xp = (double)x[(int64_t)p * npx + k];
-                if (qw && xp < (double)mxw) acc += 2.0 * alpha[(int64_t)p * winsz + (jq - ys) * wx + (iq - xs)] * (xq - xp);
+                co[t] = (T)(2.0 * alpha[(int64_t)p * winsz + (jq - ys) * wx + (iq - xs)]);
+                nbs[t++] = p;
             }
         }
         // noise sigma: sigma_p^2 = SSD(p, arg_p) / (2 n_p)
         const int aq = arg[q];
         if (aq >= 0) {
-            const double xa = (double)x[(int64_t)aq * npx + k];
-            if (qs && xa < (double)mxs) acc += gamma[q] * (xq - xa) / (double)nsig[q];
+            co[t] = (T)(gamma[q] / (double)nsig[q]);
+            nbs[t++] = aq | (int)0x80000000u;
         }
         for (int dj = -1; dj <= 1; ++dj)
             for (int di = -1; di <= 1; ++di) {
@@ -521,11 +546,28 @@ __global__ void k_nlpar_dx(const T* __restrict__ x, int nrows, int ncols, int np
                 if ((dj == 0 && di == 0) || jn < 0 || jn >= nrows || in_ < 0 || in_ >= ncols) continue;
                 const int p = in_ + ncols * jn;
                 if (arg[p] != q) continue;
-                const double xp = (double)x[(int64_t)p * npx + k];
-                if (qs && xp < (double)mxs) acc += gamma[p] * (xq - xp) / (double)nsig[p];
+                co[t] = (T)(gamma[p] / (double)nsig[p]);
+                nbs[t++] = p | (int)0x80000000u;
             }
+        nterm = t;
     }
-    out[(int64_t)q * npx + k] = (T)acc;
+    __syncthreads();
+    const int nt = nterm;
+    const T* xq_row = x + (int64_t)q * npx;
+    for (int k = threadIdx.x; k < npx; k += blockDim.x) {
+        T acc = (T)0;
+        if (pmask[k]) {
+            const T xq = xq_row[k];
+            const bool qw = xq < (T)mxw, qs = xq < (T)mxs;
+            for (int t = 0; t < nt; ++t) {
+                const int e = nbs[t];
+                const bool sigma_term = e < 0;
+                const T xn = x[(int64_t)(e & 0x7fffffff) * npx + k];
+                if (sigma_term ? (qs && xn < (T)mxs) : (qw && xn < (T)mxw)) acc += co[t] * (xq - xn);
+            }
+        }
+        out[(int64_t)q * npx + k] = acc;
+    }
 }
 
 }  // namespace
@@ -669,8 +711,8 @@ int ebsd_nlpar_sigma_arg(const float* d_data, int32_t nrows, int32_t ncols, int3
         return EBSD_E_ARG;
     const float mxval = saturation_protect ? datamax * 0.9961f : datamax + 1.0f;
     const int npix = nrows * ncols;
-    k_sigma_arg<<<(unsigned)((npix + 127) / 128), 128, 0, (cudaStream_t)stream>>>(d_data, nrows, ncols, npx, d_indices,
-                                                                             nind, mxval, d_sig2, d_arg, d_nsig);
+    k_sigma_arg<<<(unsigned)(((int64_t)npix * 8 + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+        d_data, nrows, ncols, npx, d_indices, nind, mxval, d_sig2, d_arg, d_nsig);
     return launch_status();
 }
 
@@ -710,9 +752,10 @@ int ebsd_nlpar_weights_grad(int fp64, const void* d_g, const void* d_x, int32_t 
     k_nlpar_coef<<<(unsigned)((npix + 127) / 128), 128, 0, st>>>(G, d_w, d_m, d_dS, d_dsig, npix, winsz, lam, alpha,
                                                                  beta, d_glam);
     k_nlpar_gamma<<<(unsigned)((npix + 127) / 128), 128, 0, st>>>(beta, nrows, ncols, sr, gamma);
-    dim3 grid((unsigned)((npx + 127) / 128), (unsigned)npix);
-    if (fp64) k_nlpar_dx<double><<<grid, 128, 0, st>>>((const double*)d_x, nrows, ncols, npx, sr, d_pmask, mxw, mxs, alpha, gamma, d_arg, d_nsig, (double*)d_gx);
-    else k_nlpar_dx<float><<<grid, 128, 0, st>>>((const float*)d_x, nrows, ncols, npx, sr, d_pmask, mxw, mxs, alpha, gamma, d_arg, d_nsig, (float*)d_gx);
+    const size_t maxt = (size_t)winsz + (size_t)(4 * sr + 1) * (4 * sr + 1) + 9;
+    const size_t dsm = maxt * ((fp64 ? sizeof(double) : sizeof(float)) + sizeof(int));
+    if (fp64) k_nlpar_dx<double><<<(unsigned)npix, 128, dsm, st>>>((const double*)d_x, nrows, ncols, npx, sr, d_pmask, mxw, mxs, alpha, gamma, d_arg, d_nsig, (double*)d_gx);
+    else k_nlpar_dx<float><<<(unsigned)npix, 128, dsm, st>>>((const float*)d_x, nrows, ncols, npx, sr, d_pmask, mxw, mxs, alpha, gamma, d_arg, d_nsig, (float*)d_gx);
     return launch_status();
 }
 
