@@ -219,10 +219,16 @@ __global__ void k_blur1d(const T* __restrict__ in, T* __restrict__ out, int64_t 
     const int L = axis == 0 ? H : W, o = axis == 0 ? y : x, stride = axis == 0 ? W : 1;
     const T* base = in + p * H * W + (axis == 0 ? x : y * W);
     T acc = (T)0;
-    for (int t = -r; t <= r; ++t) {
-        int q = o + t;
-        q = q < 0 ? -q : (q >= L ? 2 * (L - 1) - q : q);
-        acc = fma(__ldg(taps + t + r), __ldg(base + (int64_t)q * stride), acc);
+    if (o >= r && o + r < L) {
+        // the window lies inside the line: no reflection (the same taps in the same order)
+        const T* b0 = base + (int64_t)(o - r) * stride;
+        for (int t = 0; t <= 2 * r; ++t) acc = fma(__ldg(taps + t), __ldg(b0 + (int64_t)t * stride), acc);
+    } else {
+        for (int t = -r; t <= r; ++t) {
+            int q = o + t;
+            q = q < 0 ? -q : (q >= L ? 2 * (L - 1) - q : q);
+            acc = fma(__ldg(taps + t + r), __ldg(base + (int64_t)q * stride), acc);
+        }
     }
     out[idx] = acc;
 }
@@ -253,6 +259,8 @@ __global__ void k_blur1d_t(const T* __restrict__ v, T* __restrict__ out, int64_t
 template <typename T>
 __global__ void k_softargmax(const T* __restrict__ c, int64_t ncell, const int32_t* __restrict__ cells, int ncm,
                              double inv_tau, double* __restrict__ Jp, T* __restrict__ grad) {
+    // float patterns take the exponentials in float (their arguments formed in double), double
+    // patterns in double; the sums are double either way
     __shared__ double red[64];
     const int64_t p = blockIdx.x;
     const T* cp = c + p * ncell;
@@ -269,10 +277,14 @@ __global__ void k_softargmax(const T* __restrict__ c, int64_t ncell, const int32
     }
     __syncthreads();
     mx = red[63];
+    auto expo = [&](double v) -> double {
+        if (sizeof(T) == 4) return (double)expf((float)(v * inv_tau - mx));
+        return exp(v * inv_tau - mx);
+    };
     double s0 = 0.0, s1 = 0.0;
     for (int k = tid; k < ncm; k += blockDim.x) {
         const double v = (double)cp[cells[k]];
-        const double e = exp(v * inv_tau - mx);
+        const double e = expo(v);
         s0 += e;
         s1 += e * v;
     }
@@ -295,7 +307,7 @@ __global__ void k_softargmax(const T* __restrict__ c, int64_t ncell, const int32
     T* gp = grad + p * ncell;
     for (int k = tid; k < ncm; k += blockDim.x) {
         const double v = (double)cp[cells[k]];
-        const double si = exp(v * inv_tau - mx) / S0;
+        const double si = expo(v) / S0;
         gp[cells[k]] = (T)(si * (1.0 + (v - J) * inv_tau));
     }
 }
