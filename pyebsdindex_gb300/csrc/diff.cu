@@ -434,7 +434,20 @@ __global__ void k_nlpar_dots(const T* __restrict__ g, const T* __restrict__ x, i
         const int nb = (xs + c % wx) + ncols * (ys + c / wx);
         const T* xc = x + (int64_t)nb * npx;
         double acc = 0.0;
-        for (int k = lane; k < npx; k += 32) acc += (double)__ldg(gp + k) * (double)__ldg(xc + k);
+        if (sizeof(T) == 4) {
+            // float patterns: each lane's products summed in float with Kahan's compensation
+            // (off the slow FP64 pipe), the lanes' sums combined in double
+            float sum = 0.0f, comp = 0.0f;
+            for (int k = lane; k < npx; k += 32) {
+                const float y = __fsub_rn(__fmul_rn((float)__ldg(gp + k), (float)__ldg(xc + k)), comp);
+                const float t = __fadd_rn(sum, y);
+                comp = __fsub_rn(__fsub_rn(t, sum), y);
+                sum = t;
+            }
+            acc = (double)sum - (double)comp;
+        } else {
+            for (int k = lane; k < npx; k += 32) acc += (double)__ldg(gp + k) * (double)__ldg(xc + k);
+        }
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) G[(int64_t)p * winsz + c] = acc;
     }
