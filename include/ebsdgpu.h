@@ -195,8 +195,10 @@ int ebsd_plan_get_tile(ebsd_plan_t plan, ebsd_tile_info* info);
  * 0 the rule (one tile when it fits); slabs = the slab count for the slab tables, in
  * [slabs_min, slabs_max], or 0 for the widest.  The slab tables also serve
  * ebsd_find_bands_mixed.  EBSD_E_UNSUPPORTED for a shape the plan cannot take.  Waits for
- * the device when it rebuilds the slab tables.  For callers that tuned offline; records do not
- * depend on the choice. */
+ * the device when it rebuilds the slab tables, and frees the old ones: a CUDA graph captured
+ * with the old slab count must be captured again (ebsd_plan_autotune and EBSD_FUSED_F16 on a
+ * slab plan re-lay the tables too).  For callers that tuned offline; records do not depend on
+ * the choice. */
 int ebsd_plan_set_tile(ebsd_plan_t plan, int tile, int slabs);
 
 /* Band detection that allocates nothing -- no counterpart in the reference, which always

@@ -206,7 +206,8 @@ class DevicePlan:
 
     def set_tile(self, tile: int, slabs: int = 0):
         """Pin the Radon tile shape: ``tile`` 1 one tile, 2 theta slabs, 0 the rule; ``slabs``
-        the slab count (0 = the widest that fit)."""
+        the slab count (0 = the widest that fit).  A new slab count rebuilds the slab tables
+        (the device is synchronised and the old tables freed): capture CUDA graphs after it."""
         check(self._lib.ebsd_plan_set_tile(self.handle, int(tile), int(slabs)), "ebsd_plan_set_tile")
 
     def set_host_input(self, mode: int):
