@@ -119,7 +119,8 @@ class GPUFindBands:
         FP16 storage on a plan that runs in theta slabs needs room for its theta-max rows beside
         the 16-bit tile, which the widest slabs may not leave (240x240: 10 slabs instead of 9):
         the slab tables are then re-laid to the widest slabs that take it, and FP32 calls run
-        those slabs too until ``set_tile`` changes them."""
+        those slabs too until ``set_tile`` changes them (CUDA graphs captured before a re-layout
+        are captured again: the old tables are freed)."""
         m = self.default_method if method is None else method
         if m == "fused16" and dtype in (None, _lib.EBSD_U8, _lib.EBSD_U16) and not plan.supported(m, dtype):
             info = plan.get_tile()
