@@ -36,3 +36,29 @@ def test_compare_records_identical_and_empty():
     none = {k: v[:0] for k, v in ref.items()}
     e = compare_records(none, none)
     assert e["bands"] == 0 and e["peak_frac"] == 1.0
+
+
+def test_cubic_misorientation_and_orientation_agreement():
+    from pyebsdindex_gb300.accuracy import _cubic_rotations, _qprod, cubic_misorientation_deg, orientation_agreement
+    g = _cubic_rotations()
+    assert g.shape == (24, 4) and np.allclose(np.linalg.norm(g, axis=1), 1.0)
+    # a group: every product of two elements is an element (up to sign)
+    prod = _qprod(g[:, None, :], g[None, :, :]).reshape(-1, 4)
+    assert np.abs(np.abs(prod @ g.T).max(axis=1) - 1.0).max() < 1e-12
+    rng = np.random.default_rng(4)
+    q = rng.normal(size=(50, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    # symmetry-equivalent orientations (either frame) are 0 apart; a 1 degree turn is 1 degree
+    assert cubic_misorientation_deg(q, _qprod(q, g[rng.integers(0, 24, 50)])).max() < 1e-5
+    assert cubic_misorientation_deg(q, _qprod(g[rng.integers(0, 24, 50)], q)).max() < 1e-5
+    turn = np.array([np.cos(np.radians(0.5)), 0.0, np.sin(np.radians(0.5)), 0.0])
+    np.testing.assert_allclose(cubic_misorientation_deg(q[:5], _qprod(q[:5], turn[None])), 1.0, atol=1e-6)
+    # agreement: only patterns both sides index (>= 3 matched bands) count
+    q2 = q.copy()
+    q2[0] = _qprod(q[:1], turn[None])[0]
+    nm = np.full(50, 5)
+    nm_ref = nm.copy()
+    nm_ref[1] = 2
+    a = orientation_agreement(q2, nm, q, nm_ref, tol_deg=0.01)
+    assert a["both_indexed"] == 49 and abs(a["within_tol"] - 48 / 49) < 1e-12
+    assert abs(a["mis_max_deg"] - 1.0) < 1e-6 and a["indexed_ref"] == 49 / 50
