@@ -314,10 +314,6 @@ def gaussian_taps(sigma, radius):
     return k.contiguous(), dk.contiguous()
 
 
-def gaussian_kernel1d(sigma, radius):
-    return gaussian_taps(sigma, radius)[0]
-
-
 def _blur(lib, x, taps, r, H, W, axis, adjoint=False):
     import torch
     out = torch.empty_like(x)
