@@ -139,29 +139,44 @@ __global__ void k_nlpar_weights2(const float* __restrict__ data, int nrows, int 
 
 // out[q][k] = sum over scan pixels p whose window holds q of w[p][slot] * g[p][k].
 template <typename T>
-__global__ void k_nlpar_apply_t(const T* __restrict__ g, int nrows, int ncols, int npx,
-                                const T* __restrict__ w, int sr, T* __restrict__ out) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    int q = blockIdx.y;
-    if (k >= npx) return;
-    int jq = q / ncols, iq = q - (q / ncols) * ncols;
-    int winsz = (2 * sr + 1) * (2 * sr + 1), wx = 2 * sr + 1;
-    T acc = (T)0;
-    int j0 = jq - 2 * sr < 0 ? 0 : jq - 2 * sr, j1 = jq + 2 * sr > nrows - 1 ? nrows - 1 : jq + 2 * sr;
-    int i0 = iq - 2 * sr < 0 ? 0 : iq - 2 * sr, i1 = iq + 2 * sr > ncols - 1 ? ncols - 1 : iq + 2 * sr;
-    for (int jp = j0; jp <= j1; ++jp) {
-        int ys, ye;
-        window(jp, sr, nrows, ys, ye);
-        if (jq < ys || jq >= ye) continue;
-        for (int ip = i0; ip <= i1; ++ip) {
-            int xs, xe;
-            window(ip, sr, ncols, xs, xe);
-            if (iq < xs || iq >= xe) continue;
-            int p = ip + ncols * jp;
-            int c = (jq - ys) * wx + (iq - xs);
-            acc = fma(__ldg(w + (int64_t)p * winsz + c), __ldg(g + (int64_t)p * npx + k), acc);
+__global__ void __launch_bounds__(256) k_nlpar_apply_t(const T* __restrict__ g, int nrows, int ncols, int npx,
+                                                       const T* __restrict__ w, int sr, T* __restrict__ out) {
+    // one scan pixel q per blockIdx.y: the windows that hold q (pixel p, slot c) are listed
+    // once per block in the scan order of the sum, then each pattern value k adds
+    // w[p][c] g[p][k] over the list with fused multiply-adds
+    extern __shared__ unsigned char atsm[];
+    const int q = blockIdx.y;
+    const int winsz = (2 * sr + 1) * (2 * sr + 1), wx = 2 * sr + 1;
+    const int maxt = (4 * sr + 1) * (4 * sr + 1);
+    T* wt = (T*)atsm;                 // [maxt] weights
+    int* pt = (int*)(wt + maxt);      // [maxt] pixels
+    __shared__ int nterm;
+    if (threadIdx.x == 0) {
+        const int jq = q / ncols, iq = q - (q / ncols) * ncols;
+        const int j0 = jq - 2 * sr < 0 ? 0 : jq - 2 * sr, j1 = jq + 2 * sr > nrows - 1 ? nrows - 1 : jq + 2 * sr;
+        const int i0 = iq - 2 * sr < 0 ? 0 : iq - 2 * sr, i1 = iq + 2 * sr > ncols - 1 ? ncols - 1 : iq + 2 * sr;
+        int t = 0;
+        for (int jp = j0; jp <= j1; ++jp) {
+            int ys, ye;
+            window(jp, sr, nrows, ys, ye);
+            if (jq < ys || jq >= ye) continue;
+            for (int ip = i0; ip <= i1; ++ip) {
+                int xs, xe;
+                window(ip, sr, ncols, xs, xe);
+                if (iq < xs || iq >= xe) continue;
+                const int p = ip + ncols * jp;
+                wt[t] = w[(int64_t)p * winsz + (jq - ys) * wx + (iq - xs)];
+                pt[t++] = p;
+            }
         }
+        nterm = t;
     }
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npx) return;
+    const int nt = nterm;
+    T acc = (T)0;
+    for (int t = 0; t < nt; ++t) acc = fma(wt[t], __ldg(g + (int64_t)pt[t] * npx + k), acc);
     out[(int64_t)q * npx + k] = acc;
 }
 
@@ -788,7 +803,8 @@ int ebsd_nlpar_apply_t(const float* d_g, int32_t nrows, int32_t ncols, int32_t n
                        float* d_out, void* stream) {
     if (!d_g || !d_w || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10) return EBSD_E_ARG;
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
-    k_nlpar_apply_t<float><<<grid, 256, 0, (cudaStream_t)stream>>>(d_g, nrows, ncols, npx, d_w, sr, d_out);
+    k_nlpar_apply_t<float><<<grid, 256, (size_t)(4 * sr + 1) * (4 * sr + 1) * (sizeof(float) + sizeof(int)),
+                             (cudaStream_t)stream>>>(d_g, nrows, ncols, npx, d_w, sr, d_out);
     return launch_status();
 }
 
@@ -796,7 +812,8 @@ int ebsd_nlpar_apply_t64(const double* d_g, int32_t nrows, int32_t ncols, int32_
                          int32_t sr, double* d_out, void* stream) {
     if (!d_g || !d_w || !d_out || nrows <= 0 || ncols <= 0 || npx <= 0 || sr < 0 || sr > 10) return EBSD_E_ARG;
     dim3 grid((unsigned)((npx + 255) / 256), (unsigned)(nrows * ncols));
-    k_nlpar_apply_t<double><<<grid, 256, 0, (cudaStream_t)stream>>>(d_g, nrows, ncols, npx, d_w, sr, d_out);
+    k_nlpar_apply_t<double><<<grid, 256, (size_t)(4 * sr + 1) * (4 * sr + 1) * (sizeof(double) + sizeof(int)),
+                              (cudaStream_t)stream>>>(d_g, nrows, ncols, npx, d_w, sr, d_out);
     return launch_status();
 }
 
